@@ -1,0 +1,117 @@
+"""Seeded synthetic polygon systems (the inputs the hot path runs on).
+
+The reference publishes no benchmark inputs, so systems are generated the way
+its own generator and setters shape them (pyCudaPolygon/polygonMixins/
+polygonUtils.py:52-89 for star polygons around a centre, pyCudaPolygon.py:
+182-203 for the 50:50 bidisperse split with the small half first):
+
+  * centre ~ U[0,1)^2, rotation ~ U[0, 2 pi)
+  * vertex k at angle theta + 2 pi k / n, radius R_p (1 + 0.1 u_k), u ~ U[-1,1]
+    (counter-clockwise, positive area)
+  * first half of the polygons small, second half 1.4x larger radius
+  * one global scale so that the sum of the shoelace areas equals phi
+  * positions wrapped into [0, 1)
+  * targetAreas = initial areas, targetEdgeLengths = perimeter / n (one
+    scalar per polygon, as the reference stores it, model.cpp:553)
+  * maxEdgeLength = the longest actual edge (pyCudaPolygon.py:166-179)
+
+Everything is FP64 numpy; positions are interleaved x, y per vertex.
+"""
+from dataclasses import dataclass
+
+import numpy as np
+
+
+@dataclass
+class PolygonSystem:
+    positions: np.ndarray        # float64 [2V], interleaved, in [0, 1)
+    n_array: np.ndarray          # int32 [P]
+    start_indices: np.ndarray    # int32 [P+1]
+    target_areas: np.ndarray     # float64 [P]
+    target_edge_lengths: np.ndarray  # float64 [P]
+    max_edge_length: float
+    phi: float
+
+    @property
+    def num_vertices(self):
+        return int(self.start_indices[-1])
+
+    @property
+    def num_polygons(self):
+        return int(self.n_array.size)
+
+
+def _shoelace(xy):
+    x, y = xy[:, 0], xy[:, 1]
+    return 0.5 * (np.dot(x, np.roll(y, -1)) - np.dot(np.roll(x, -1), y))
+
+
+def make_system(num_polygons, n, phi, seed, ratio=1.4, jitter=0.1):
+    """Generate one system.  `n` is an int (uniform) or an int array [P]."""
+    rng = np.random.default_rng(seed)
+    P = int(num_polygons)
+    n_array = np.full(P, int(n), dtype=np.int32) if np.isscalar(n) else \
+        np.asarray(n, dtype=np.int32).copy()
+    assert n_array.size == P and np.all(n_array >= 3)
+    centres = rng.random((P, 2))
+    theta0 = rng.random(P) * 2.0 * np.pi
+    radius = np.ones(P)
+    radius[P // 2:] = ratio
+    shapes = []
+    for p in range(P):
+        k = np.arange(n_array[p])
+        u = rng.uniform(-1.0, 1.0, n_array[p])
+        ang = theta0[p] + 2.0 * np.pi * k / n_array[p]
+        r = radius[p] * (1.0 + jitter * u)
+        shapes.append(np.stack([r * np.cos(ang), r * np.sin(ang)], axis=1))
+    total = sum(_shoelace(s) for s in shapes)
+    scale = np.sqrt(phi / total)
+    V = int(n_array.sum())
+    pos = np.zeros((V, 2))
+    start = np.concatenate([[0], np.cumsum(n_array)]).astype(np.int32)
+    areas = np.zeros(P)
+    perims = np.zeros(P)
+    for p in range(P):
+        local = shapes[p] * scale
+        areas[p] = _shoelace(local)
+        perims[p] = np.sum(np.linalg.norm(np.roll(local, -1, axis=0) - local, axis=1))
+        pos[start[p]:start[p + 1]] = np.mod(local + centres[p], 1.0)
+    pos = np.mod(pos, 1.0)
+    # longest actual edge under the minimum image (pyCudaPolygon.py:166-179)
+    nxt = np.arange(V) + 1
+    nxt[start[1:] - 1] = start[:-1]
+    d = pos[nxt] - pos
+    d = (d + 1.5) % 1.0 - 0.5
+    max_edge = float(np.max(np.sqrt(np.sum(d * d, axis=1))))
+    return PolygonSystem(positions=pos.reshape(-1).copy(), n_array=n_array,
+                         start_indices=start, target_areas=areas,
+                         target_edge_lengths=perims / n_array,
+                         max_edge_length=max_edge, phi=float(phi))
+
+
+def batched_specs(num_systems, seed, p_range=(64, 1024), n_range=(12, 48),
+                  phi_range=(0.80, 0.92)):
+    """Per-system (P, n array, phi, seed) for the many-systems workload:
+    P ~ U{64..1024}, n per polygon ~ U{12..48}, phi ~ U[0.80, 0.92]."""
+    rng = np.random.default_rng(seed)
+    specs = []
+    for s in range(num_systems):
+        P = int(rng.integers(p_range[0], p_range[1] + 1))
+        n = rng.integers(n_range[0], n_range[1] + 1, size=P).astype(np.int32)
+        phi = float(rng.uniform(*phi_range))
+        specs.append((P, n, phi, int(rng.integers(0, 2**31 - 1))))
+    return specs
+
+
+def load_into(model, system, model_type="normal"):
+    """Configure a reference-API model object (the pybind `Model`, or any
+    object with the same method names) with a generated system."""
+    model.setNumVertices(system.num_vertices)
+    model.setStartIndices(system.start_indices)
+    model.setPositions(system.positions)
+    model.setTargetAreas(system.target_areas)
+    model.setTargetEdgeLengths(system.target_edge_lengths)
+    model.setMaxEdgeLength(system.max_edge_length)
+    model.setModelEnum(model_type)
+    model.initializeNeighborCells()
+    return model

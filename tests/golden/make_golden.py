@@ -1,0 +1,210 @@
+"""Regenerate the golden fixtures in tests/golden/ from the reference.
+
+Run in a container where the reference tree is mounted (default
+/root/reference, or $PCP_REFERENCE).  The fixtures it writes are committed, so
+nothing at test time reads the reference:
+
+  testsaver.json    the reference's own saved two-pentagon state
+                    (tests/testSaver/state.npy, scalars.dat) and the neighbour
+                    known answer of tests/neighborTesting.ipynb (cells 6, 9,
+                    14: vertex 1 crosses 7 and 8, unchanged by a global shift)
+  getdf.json        the reference's Python getDf (pyCudaPolygon.py:348-393)
+                    on seeded non-degenerate edge pairs
+  projection.json   the reference's getConstrainedForcePython
+                    (pyCudaPolygon.py:441-487) on seeded polygon sets with
+                    a random force
+  com_area.json     getCentersOfMass (pyCudaPolygon.py:325-338) and the
+                    unwrapped shoelace of setAreas (pyCudaPolygon.py:114-125)
+  pybind_methods.json  the method names the reference binds on `Model`
+                    (src/pybindWrapper.cpp:25-107)
+
+The reference's model module imports matplotlib, tqdm and its compiled
+`libpyCudaPolygon`; small stand-ins are put on sys.path for the import only.
+The Python twins used here touch no compiled code.
+"""
+import importlib
+import json
+import os
+import re
+import sys
+import types
+
+import numpy as np
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+REF = os.environ.get("PCP_REFERENCE", "/root/reference")
+
+
+def _import_reference_model():
+    """Import pyCudaPolygon/pyCudaPolygon.py with stand-ins for its imports."""
+    mpl = types.ModuleType("matplotlib")
+    plt = types.ModuleType("matplotlib.pyplot")
+    mpl.pyplot = plt
+    sys.modules.setdefault("matplotlib", mpl)
+    sys.modules.setdefault("matplotlib.pyplot", plt)
+    if "tqdm" not in sys.modules:
+        try:
+            importlib.import_module("tqdm")
+        except ImportError:
+            tq = types.ModuleType("tqdm")
+            tq.tqdm = lambda *a, **k: None
+            sys.modules["tqdm"] = tq
+    lib = types.ModuleType("libpyCudaPolygon")
+
+    class Model:  # base class placeholder; the twins below use no methods of it
+        def __init__(self, *a, **k):
+            pass
+
+    class _Enum:
+        pass
+
+    lib.Model = Model
+    lib.modelEnum = _Enum
+    lib.minimizerEnum = _Enum
+    sys.modules["libpyCudaPolygon"] = lib
+    link = types.ModuleType("pyCudaPolygonLink")
+    link.libpyCudaPolygon = lib
+    sys.modules["pyCudaPolygonLink"] = link
+    pkg_dir = os.path.join(REF, "pyCudaPolygon")
+    sys.path.insert(0, pkg_dir)
+    try:
+        mod = importlib.import_module("pyCudaPolygon")
+    finally:
+        sys.path.remove(pkg_dir)
+    return mod
+
+
+class _FakeState:
+    """Minimal stand-in exposing the getters the Python twins call."""
+
+    def __init__(self, positions, start):
+        self._pos = np.asarray(positions, dtype=np.float64)
+        self._start = np.asarray(start, dtype=np.int64)
+
+    def getStartIndices(self):
+        return list(self._start)
+
+    def getnArray(self):
+        return np.diff(self._start)
+
+    def getPositions(self):
+        return self._pos.copy()
+
+    def getNumPolygons(self):
+        return len(self._start) - 1
+
+
+def _star_polygons(rng, ns, radius=0.04):
+    pos = []
+    for n in ns:
+        c = rng.random(2)
+        th = rng.random() * 2 * np.pi
+        k = np.arange(n)
+        r = radius * (1 + 0.1 * rng.uniform(-1, 1, n))
+        a = th + 2 * np.pi * k / n
+        pts = np.stack([c[0] + r * np.cos(a), c[1] + r * np.sin(a)], axis=1) % 1.0
+        pos.append(pts)
+    pos = np.concatenate(pos)
+    start = np.concatenate([[0], np.cumsum(ns)])
+    return pos.reshape(-1), start
+
+
+def main():
+    ref = _import_reference_model()
+    Model = ref.model
+    rng = np.random.default_rng(20240611)
+
+    # ---- testSaver fixture + neighbour known answer ----
+    st = np.load(os.path.join(REF, "tests", "testSaver", "state.npy"))
+    scal = open(os.path.join(REF, "tests", "testSaver", "scalars.dat")).read()
+    nv = int(re.search(r"numVertices:\t(\d+)", scal).group(1))
+    n_array = st[:-2 * nv].astype(int).tolist()
+    pos = st[-2 * nv:].tolist()
+    json.dump({
+        "source": "tests/testSaver/state.npy, tests/testSaver/scalars.dat",
+        "n_array": n_array, "positions": pos,
+        "max_edge_length_saved": float(re.search(r"maxEdgeLength:\t([0-9.eE+-]+)", scal).group(1)),
+        "notebook_max_edge_length": 0.25,
+        "expected_neighbors": {"1": [7, 8]},
+        "expected_inside": {"1": [True, False]},
+        "answer_source": "tests/neighborTesting.ipynb cells 6, 9 and 14 ({1: [7, 8]}, "
+                         "also after the global shift (pos - mean(pos)) % 1)",
+    }, open(os.path.join(HERE, "testsaver.json"), "w"), indent=1)
+
+    # ---- getDf twin ----
+    cases = []
+    for _ in range(64):
+        while True:
+            vi = rng.random(2)
+            di = rng.uniform(-0.02, 0.02, 2)
+            dj = rng.uniform(-0.02, 0.02, 2)
+            vj = (vi + rng.uniform(-0.01, 0.01, 2)) % 1.0
+            w = dj[0] * di[1] - dj[1] * di[0]
+            if w * w > 1e-6 * np.dot(di, di) * np.dot(dj, dj):
+                break
+        vzi = (vi + di) % 1.0
+        vzj = (vj + dj) % 1.0
+        df = Model.getDf(None, vi, vzi, vj, vzj)
+        cases.append({"vi": vi.tolist(), "vzi": vzi.tolist(), "vj": vj.tolist(),
+                      "vzj": vzj.tolist(), "df": np.asarray(df).tolist()})
+    json.dump({"source": "pyCudaPolygon/pyCudaPolygon.py:348-393 (model.getDf)",
+               "cases": cases}, open(os.path.join(HERE, "getdf.json"), "w"))
+
+    # ---- constrained force projection twin ----
+    proj = []
+    for case in range(12):
+        P = int(rng.integers(1, 6))
+        ns = rng.integers(3, 40, size=P) if case % 2 else np.full(P, int(rng.integers(3, 40)))
+        positions, start = _star_polygons(rng, ns)
+        force = rng.normal(size=positions.size)
+        fake = _FakeState(positions, start)
+        out = Model.getConstrainedForcePython(fake, force)
+        proj.append({"positions": positions.tolist(), "start": start.tolist(),
+                     "force": force.tolist(), "projected": np.asarray(out).tolist()})
+    json.dump({"source": "pyCudaPolygon/pyCudaPolygon.py:441-487 "
+                         "(model.getConstrainedForcePython)", "cases": proj},
+              open(os.path.join(HERE, "projection.json"), "w"))
+
+    # ---- centre of mass and shoelace twins ----
+    comcases = []
+    for case in range(8):
+        P = int(rng.integers(1, 8))
+        ns = rng.integers(3, 40, size=P)
+        positions, start = _star_polygons(rng, ns)
+        fake = _FakeState(positions, start)
+        com = Model.getCentersOfMass(fake)
+        # setAreas' unwrapped shoelace (pyCudaPolygon.py:114-125), per polygon
+        areas = []
+        pxy = positions.reshape(-1, 2)
+        for p in range(P):
+            poly = pxy[start[p]:start[p + 1]].copy()
+            refv = poly[0].copy()
+            for j in range(1, len(poly)):
+                d = poly[j] - refv
+                d = d - np.round(d)
+                poly[j] = refv + d
+            x, y = poly[:, 0], poly[:, 1]
+            areas.append(0.5 * abs(np.dot(x, np.roll(y, -1)) - np.dot(np.roll(x, -1), y)))
+        comcases.append({"positions": positions.tolist(), "start": start.tolist(),
+                         "com": np.asarray(com).tolist(), "areas": areas})
+    json.dump({"source": "pyCudaPolygon/pyCudaPolygon.py:325-338 (getCentersOfMass), "
+                         ":114-125 (setAreas shoelace)", "cases": comcases},
+              open(os.path.join(HERE, "com_area.json"), "w"))
+
+    # ---- pybind method table ----
+    src = open(os.path.join(REF, "src", "pybindWrapper.cpp")).read()
+    names = []
+    for nm in re.findall(r'\.def\("([A-Za-z0-9_]+)"', src):
+        if nm not in names:
+            names.append(nm)
+    enums = {}
+    for enum_name, body in re.findall(r'enum_<[^>]+>\(m, "(\w+)"\)((?:\s*\.value\([^)]*\))+)', src):
+        enums[enum_name] = re.findall(r'\.value\("(\w+)"', body)
+    json.dump({"source": "src/pybindWrapper.cpp:12-108", "methods": names,
+               "enums": enums}, open(os.path.join(HERE, "pybind_methods.json"), "w"),
+              indent=1)
+    print("wrote fixtures to", HERE)
+
+
+if __name__ == "__main__":
+    main()
