@@ -1,0 +1,240 @@
+/*
+ * pcp_gb300.h -- C ABI of the GB300-native (sm_103a) polygon overlap path.
+ *
+ * Library: libpcp_gb300.so (built in-tree by pycudapolygon_gb300/build.py).
+ * Every function returns an int status (PCP_OK == 0) and never exits the
+ * process; pcp_last_error() gives the message of the last failure on the
+ * calling thread.  No function allocates device memory except
+ * pcp_model_create and the pcp_model_set_* / pcp_model_initialize_*
+ * functions that size the model's buffers (as the reference's setters do).
+ *
+ * Two layers, each replacing one seam of camdennis/pyCudaPolygon:
+ *
+ *  1. pcp_model_*  -- a handle per simulated system.  Each call is one method
+ *     of the reference's `class Model` (src/model.hpp:18-107) as bound by
+ *     pybind11 (src/pybindWrapper.cpp:25-107); the citation above each
+ *     declaration names the method it replaces.  Host arrays cross by copy,
+ *     as the reference's std::vector setters and getters do.  The pybind11
+ *     module `libpyCudaPolygon` built beside this library is a thin wrapper
+ *     over this layer with the reference's exact method table.
+ *
+ *  2. pcp_* kernels -- stateless launchers on caller-owned device buffers
+ *     (plain pointers + sizes + a cudaStream_t passed as void*).  Each one
+ *     replaces an `extern "C"` wrapper of src/model.cu that the reference's
+ *     C++ host code declares at src/model.cpp:17-56.
+ *
+ * Data layout (identical to the reference): positions and forces are
+ * interleaved FP64 [x0, y0, x1, y1, ...] in the unit periodic box; polygon p
+ * owns vertices [startIndices[p], startIndices[p+1]) in counter-clockwise
+ * order; contact records are packed uint64 keys
+ * (sj << 48 | si << 32 | i << 16 | j, src/kernels.cuh:861-874).
+ */
+#ifndef PCP_GB300_H
+#define PCP_GB300_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+enum {
+    PCP_OK = 0,
+    PCP_ERR_ARG = 1,       /* bad argument or size */
+    PCP_ERR_CUDA = 2,      /* a CUDA runtime call failed */
+    PCP_ERR_CAPACITY = 3,  /* a per-pair or per-polygon size limit was exceeded */
+    PCP_ERR_LIMIT = 4,     /* more than 65535 polygons or vertices per polygon */
+    PCP_ERR_STATE = 5,     /* call order (e.g. no startIndices yet) */
+    PCP_ERR_NUMERIC = 6    /* a kernel met non-finite input it cannot process */
+};
+
+/* simControlStruct::modelEnum (src/enumTypes.h:6) */
+enum { PCP_MODEL_NORMAL = 0, PCP_MODEL_EDGE_ONLY = 1, PCP_MODEL_AREA_ONLY = 2,
+       PCP_MODEL_SOFT_BODY = 3, PCP_MODEL_ABNORMAL = 4, PCP_MODEL_HYBRID = 5 };
+/* minimizerEnum (src/enumTypes.h:9) */
+enum { PCP_MINIMIZER_GD = 0, PCP_MINIMIZER_FIRE = 1 };
+
+/* Message of the last failed call on this thread ("" if none). */
+const char* pcp_last_error(void);
+/* Library version string. */
+const char* pcp_version(void);
+
+/* ======================================================================
+ * 1. Model handle API
+ * ====================================================================== */
+typedef struct pcp_model pcp_model;
+
+/* Model::Model(int) (model.cpp:60-101) */
+int pcp_model_create(int size, pcp_model** out);
+/* Model::~Model (model.cpp:103-160) */
+int pcp_model_destroy(pcp_model* m);
+/* Stream the model launches on (NULL = the legacy default stream). */
+int pcp_model_set_stream(pcp_model* m, void* cuda_stream);
+
+/* ---- setters ---- */
+/* Model::setNumVertices (model.cpp:600-628) */
+int pcp_model_set_num_vertices(pcp_model* m, int n);
+/* Model::setPositions (model.cpp:522-528): len must be 2*numVertices, else
+ * the reference prints and ignores the call; here PCP_ERR_ARG is returned
+ * after the same message. */
+int pcp_model_set_positions(pcp_model* m, const double* host, int len);
+/* Model::setForces (model.cpp:530-535) */
+int pcp_model_set_forces(pcp_model* m, const double* host, int len);
+/* Model::setStartIndices (model.cpp:537-598) */
+int pcp_model_set_start_indices(pcp_model* m, const int* host, int len);
+/* Model::setTargetAreas (model.cpp:634-636) */
+int pcp_model_set_target_areas(pcp_model* m, const double* host, int len);
+/* Model::setTargetEdgeLengths (model.cpp:630-632) */
+int pcp_model_set_target_edge_lengths(pcp_model* m, const double* host, int len);
+/* Model::setMaxEdgeLength (model.cpp:513-516): boxSize = floor(1/l) */
+int pcp_model_set_max_edge_length(pcp_model* m, double l);
+/* Model::setModelEnum (model.cpp:518-520) */
+int pcp_model_set_model_enum(pcp_model* m, int model_enum);
+/* Model::setStiffness / setCompressibility (model.cpp:638-644) */
+int pcp_model_set_stiffness(pcp_model* m, double k);
+int pcp_model_set_compressibility(pcp_model* m, double c);
+int pcp_model_get_stiffness(pcp_model* m, double* out);
+int pcp_model_get_compressibility(pcp_model* m, double* out);
+
+/* ---- initialisers and updaters ---- */
+/* Model::initializeNeighborCells (model.cpp:176-229): topology */
+int pcp_model_initialize_neighbor_cells(pcp_model* m);
+/* Model::updatePolygonGeometry (model.cpp:313-315; model.cu:113-163) */
+int pcp_model_update_polygon_geometry(pcp_model* m);
+/* Model::updateNeighborCells (model.cpp:252-254; model.cu:308-385) */
+int pcp_model_update_neighbor_cells(pcp_model* m);
+/* Model::updateNeighbors (model.cpp:256-307; model.cu:393-411): finds every
+ * edge-edge crossing the reference's 3x3 cell scan finds */
+int pcp_model_update_neighbors(pcp_model* m);
+/* Model::updateValidAndCounts (model.cpp:309-311) */
+int pcp_model_update_valid_and_counts(pcp_model* m);
+/* Model::updateCompactedIntersections (model.cpp:347-349) */
+int pcp_model_update_compacted_intersections(pcp_model* m);
+/* Model::updateOutersections (model.cpp:351-361) */
+int pcp_model_update_outersections(pcp_model* m);
+/* Model::updateForceEnergy (model.cpp:363-395) */
+int pcp_model_update_force_energy(pcp_model* m);
+/* Model::projectForce (model.cpp:337-344; model.cu:165-206) */
+int pcp_model_project_force(pcp_model* m);
+/* Model::shakeProject (model.cpp:317-322; model.cu:619-636) */
+int pcp_model_shake_project(pcp_model* m, int n_iter, double tol, int* iters_out);
+/* xpbdProjectCUDA (model.cu:209-278); not bound by the reference */
+int pcp_model_xpbd_project(pcp_model* m, int n_iter, double tol, int* iters_out);
+/* Model::updatePositions (model.cpp:397-399) */
+int pcp_model_update_positions(pcp_model* m, double dt);
+/* Model::resetVelocities (model.cpp:401-403) */
+int pcp_model_reset_velocities(pcp_model* m);
+/* Model::resetAreas (model.cpp:507-509) */
+int pcp_model_reset_areas(pcp_model* m);
+/* Model::saveTentativePositions (model.cpp:328-330) */
+int pcp_model_save_tentative_positions(pcp_model* m);
+/* Model::getMaxEffectiveForce (model.cpp:332-335) */
+int pcp_model_get_max_effective_force(pcp_model* m, double dt, int minimizer, double* out);
+/* Model::sortKeys (model.cpp:238-240) */
+int pcp_model_sort_keys(pcp_model* m, int end_bit);
+/* Model::updateOverlapArea (model.cpp:824-847) */
+int pcp_model_update_overlap_area(pcp_model* m, int point_density);
+
+/* Model::minimizeFIREStep (model.cpp:405-486); out = {E, dt, alpha, nPos} */
+int pcp_model_fire_step(pcp_model* m, double dt, double alpha, int n_pos, double dt_max,
+                        double alpha_start, double f_alpha, double f_inc, double f_dec,
+                        int n_min, int shake_iter, double out[4]);
+/* Model::minimizeFIRE (model.cpp:488-504); out = {E, dt, steps}.  Runs the
+ * steps as CUDA-graph launches with the stop test on the device. */
+int pcp_model_minimize_fire(pcp_model* m, double max_force_threshold, double dt_init,
+                            int max_steps, double dt_max, double alpha_start, double f_alpha,
+                            double f_inc, double f_dec, int n_min, int shake_iter,
+                            double out[3]);
+
+/* ---- getters (model.cpp:654-893); arrays are copied into caller memory ---- */
+int pcp_model_get_num_vertices(pcp_model* m, int* out);
+int pcp_model_get_num_polygons(pcp_model* m, int* out);
+int pcp_model_get_num_intersections(pcp_model* m, int* out);
+int pcp_model_get_max_neighbors(pcp_model* m, int* out);
+int pcp_model_get_box_size(pcp_model* m, int* out);
+int pcp_model_get_model_enum(pcp_model* m, int* out);
+int pcp_model_get_last_shake_iters(pcp_model* m, int* out);
+int pcp_model_get_energy(pcp_model* m, double* out);
+int pcp_model_get_max_unbalanced_force(pcp_model* m, double* out);
+int pcp_model_get_max_edge_length(pcp_model* m, double* out);
+int pcp_model_get_overlap_area(pcp_model* m, double* out);
+/* The array getters take the capacity of `out` in elements and fail with
+ * PCP_ERR_ARG when it is too small; *len_out receives the element count. */
+int pcp_model_get_positions(pcp_model* m, double* out, int cap, int* len_out);
+int pcp_model_get_forces(pcp_model* m, double* out, int cap, int* len_out);
+int pcp_model_get_velocities(pcp_model* m, double* out, int cap, int* len_out);
+int pcp_model_get_areas(pcp_model* m, double* out, int cap, int* len_out);
+int pcp_model_get_com(pcp_model* m, double* out, int cap, int* len_out);
+int pcp_model_get_perimeters(pcp_model* m, double* out, int cap, int* len_out);
+int pcp_model_get_edge_lengths(pcp_model* m, double* out, int cap, int* len_out);
+int pcp_model_get_constraints(pcp_model* m, double* out, int cap, int* len_out);
+int pcp_model_get_target_areas(pcp_model* m, double* out, int cap, int* len_out);
+int pcp_model_get_target_edge_lengths(pcp_model* m, double* out, int cap, int* len_out);
+int pcp_model_get_start_indices(pcp_model* m, int* out, int cap, int* len_out);
+int pcp_model_get_shape_id(pcp_model* m, int* out, int cap, int* len_out);
+int pcp_model_get_neighbor_cells(pcp_model* m, int* out, int cap, int* len_out);
+int pcp_model_get_neighbor_indices(pcp_model* m, int* out, int cap, int* len_out);
+int pcp_model_get_box_counts(pcp_model* m, int* out, int cap, int* len_out);
+int pcp_model_get_neighbors(pcp_model* m, int* out, int cap, int* len_out);
+int pcp_model_get_num_neighbors(pcp_model* m, int* out, int cap, int* len_out);
+int pcp_model_get_inside_flag(pcp_model* m, uint8_t* out, int cap, int* len_out);
+int pcp_model_get_shape_counts(pcp_model* m, int* out, int cap, int* len_out);
+int pcp_model_get_intersections(pcp_model* m, uint64_t* out, int cap, int* len_out);
+int pcp_model_get_outersections(pcp_model* m, uint64_t* out, int cap, int* len_out);
+int pcp_model_get_tu(pcp_model* m, double* out, int cap, int* len_out);
+int pcp_model_get_ut(pcp_model* m, double* out, int cap, int* len_out);
+int pcp_model_get_keys(pcp_model* m, uint32_t* out, int cap, int* len_out);
+int pcp_model_get_intersections_counter(pcp_model* m, int* out, int cap, int* len_out);
+
+/* Device views of the model's state (valid until the next resize); for
+ * zero-copy use from CUDA-aware callers.  Interleaved FP64 [2*numVertices]. */
+int pcp_model_device_positions(pcp_model* m, double** out);
+int pcp_model_device_forces(pcp_model* m, double** out);
+/* Number of polygon pairs the last contact search examined (pair evals). */
+int pcp_model_get_pair_count(pcp_model* m, long long* out);
+/* Kernel launches issued by the model since creation (for accounting). */
+int pcp_model_get_launch_count(pcp_model* m, long long* out);
+
+/* ======================================================================
+ * 2. Stateless kernels on caller-owned device buffers (stream = cudaStream_t)
+ * ====================================================================== */
+
+/* topology: updateShapeIdKernel + computeNextPrevKernel
+ * (model.cu:77-81, 387-391; kernels.cuh:127-135, 652-659) */
+int pcp_topology(const int* d_start, int num_polygons, int num_vertices,
+                 int* d_shape_id, int* d_next, int* d_prev, void* stream);
+
+/* updatePolygonGeometryCUDA (model.cu:113-163).  One warp per polygon;
+ * outputs areas, centres of mass (wrapped), perimeters, edge lengths, the
+ * three normalised constraint vectors [6V] and the longest edge. */
+int pcp_polygon_geometry(const double* d_pos, const int* d_start, int num_polygons,
+                         int num_vertices, double* d_edge_lengths, double* d_areas,
+                         double* d_com_x, double* d_com_y, double* d_perimeters,
+                         double* d_constraints, double* d_max_edge_length, void* stream);
+
+/* updateNeighborCellsKernel (kernels.cuh:661-707): cell of each edge midpoint */
+int pcp_neighbor_cells(const double* d_pos, const int* d_start, const int* d_shape_id,
+                       int num_vertices, int box_size, int* d_cell_location, void* stream);
+
+/* projectForceCUDA (model.cu:165-206): removes from each polygon's force the
+ * span of its edge-length gradients and of its (normalised) area gradient
+ * d_constraints[6k+0..1].  Any n per polygon. */
+int pcp_project_force(const double* d_pos, const int* d_start, int num_polygons,
+                      const double* d_constraints, double* d_force, void* stream);
+
+/* shakeProjectCUDA (model.cu:619-636): projects each polygon onto
+ * |edge| = targetEdgeLength[p], area = targetArea[p]; *d_max_iters receives
+ * the largest iteration count (failure when >= max_iter). */
+int pcp_shake_project(double* d_pos, const int* d_start, int num_polygons,
+                      const double* d_target_edge_lengths, const double* d_target_areas,
+                      int max_iter, double tol, int* d_max_iters, void* stream);
+
+/* updatePositionsKernel (kernels.cuh:1433-1438): x = frac(x + dt F) */
+int pcp_update_positions(double* d_pos, const double* d_force, int num_vertices,
+                         double dt, void* stream);
+
+#ifdef __cplusplus
+}
+#endif
+#endif

@@ -1,0 +1,798 @@
+// contacts.cu -- contact search and overlap energy/force on GB300 (sm_103a).
+//
+// Replaces the reference's edge-level cell list + per-edge narrow phase +
+// compaction + two radix sorts + outersection search + exterior/interior
+// kernels (camdennis/pyCudaPolygon src/kernels.cuh:661-1424, src/model.cu:
+// 308-551, src/model.cpp:252-372) by:
+//
+//   prepass      one warp per polygon: exact FP64 edge vectors, FP32 copies of
+//                the ring with its edge-midpoint cells, bounding circle
+//   broad phase  polygon grid built by counting sort (histogram, prefix sum,
+//                scatter) on cell key; candidate pairs a <= b whose bounding
+//                circles overlap (a == b covers self-crossings)
+//   narrow phase one warp per candidate pair, both rings staged in shared
+//                memory by cp.async.bulk (TMA) with an mbarrier, double
+//                buffered across the warp's pairs; a conservative FP32 box
+//                test and the reference's cell-adjacency rule filter edge
+//                pairs; survivors get the reference's exact FP64 crossing
+//                test (no FMA contraction) in full-warp batches; the pair's
+//                crossings are matched to their exits (outersections) in
+//                shared memory and written out as packed records
+//   force        one thread per record: exterior terms and the interior
+//                chain of whole edges, FP64, forces by atomics
+//
+// The crossing set equals the reference's whenever its cell scan would see
+// the pair: polygons whose bounding circles do not overlap cannot have
+// crossing edges, and the reference's own 3x3 cell rule is applied to every
+// edge pair.  Records are bit-identical; their order is restored to the
+// reference's (si, i, j, sj) order only when a getter asks for them.
+#include <cuda_runtime.h>
+#include <math.h>
+#include <stdint.h>
+
+#include "pcp_common.cuh"
+#include "pcp_internal.h"
+
+namespace pcp {
+
+static inline int nblocks(long long n, int threads) {
+    long long b = (n + threads - 1) / threads;
+    if (b < 1) b = 1;
+    return (int)b;
+}
+
+// ------------------------------------------------------------ prepass ----
+// Reset of the contact counters (everything in Ctrl before `energy`).
+__global__ void k_reset_contacts(Ctrl* __restrict__ ctrl, const int* gate) {
+    if (gate_closed(gate)) return;
+    int* w = reinterpret_cast<int*>(ctrl);
+    int n = (int)(offsetof(Ctrl, energy) / sizeof(int));
+    for (int i = threadIdx.x; i < n; i += blockDim.x) w[i] = 0;
+}
+
+__global__ void __launch_bounds__(256)
+k_prepass(const double2* __restrict__ pos, const int* __restrict__ start,
+          const int* __restrict__ cellLocation, int P, double2* __restrict__ edgeVec,
+          float4* __restrict__ vtx, float4* __restrict__ polyInfo, int* __restrict__ polyFlags,
+          int* __restrict__ unsafeList, Ctrl* __restrict__ ctrl, const int* gate) {
+    if (gate_closed(gate)) return;
+    int p = blockIdx.x * (blockDim.x / 32) + threadIdx.x / 32;
+    int lane = threadIdx.x & 31;
+    if (p >= P) return;
+    int st = start[p], en = start[p + 1];
+    int n = en - st;
+    if (n <= 0) {   // empty polygon: no edges, never a candidate
+        if (lane == 0) { polyInfo[p] = make_float4(0.f, 0.f, 0.f, 0.f); polyFlags[p] = 0; }
+        return;
+    }
+    double2 q0 = pos[st];
+    float f0x = (float)q0.x, f0y = (float)q0.y;
+    float mnx = 0.f, mxx = 0.f, mny = 0.f, mxy = 0.f, emax = 0.f;
+    bool bad = false;
+    for (int kl = lane; kl < n; kl += 32) {
+        int k = st + kl;
+        int nx = (kl + 1 == n) ? st : k + 1;
+        double2 pk = pos[k], pn = pos[nx];
+        // r = wrap(p_next - p) exactly as updateNeighborsKernel (kernels.cuh:724-725)
+        edgeVec[k] = make_double2(wrap(pn.x - pk.x), wrap(pn.y - pk.y));
+        float fx = (float)pk.x, fy = (float)pk.y;
+        vtx[k] = make_float4(fx, fy, __int_as_float(cellLocation[k]), 0.f);
+        float lx = wrapf(fx - f0x), ly = wrapf(fy - f0y);
+        float nxl = wrapf((float)pn.x - fx), nyl = wrapf((float)pn.y - fy);
+        if (!(isfinite(lx) && isfinite(ly) && isfinite(nxl) && isfinite(nyl))) bad = true;
+        mnx = fminf(mnx, lx); mxx = fmaxf(mxx, lx);
+        mny = fminf(mny, ly); mxy = fmaxf(mxy, ly);
+        emax = fmaxf(emax, sqrtf(nxl * nxl + nyl * nyl));
+    }
+    mnx = warp_minf(mnx); mxx = warp_maxf(mxx);
+    mny = warp_minf(mny); mxy = warp_maxf(mxy);
+    emax = warp_maxf(emax);
+    bad = __any_sync(PCP_FULL, bad);
+    if (lane == 0) {
+        float cx = f0x + 0.5f * (mnx + mxx), cy = f0y + 0.5f * (mny + mxy);
+        cx -= floorf(cx); cy -= floorf(cy);
+        float w = mxx - mnx, h = mxy - mny;
+        float R = 0.5f * sqrtf(w * w + h * h) * 1.0001f + 4e-6f;
+        bool safe = !bad && isfinite(R) && R < 0.1f && n >= 3;
+        polyInfo[p] = make_float4(cx, cy, R, emax);
+        polyFlags[p] = safe ? 1 : 0;
+        if (safe) atomic_max_nonneg_f(&ctrl->Rmax, R);
+        else unsafeList[atomicAdd(&ctrl->numUnsafe, 1)] = p;
+    }
+}
+
+// -------------------------------------------------------- broad phase ----
+__device__ __forceinline__ int grid_dim_from(float Rmax) {
+    float side = 2.0f * Rmax * 1.001f + 1e-4f;
+    int G = (int)floorf(1.0f / side);
+    if (!(G >= 1)) G = 1;
+    if (G > kGridMax) G = kGridMax;
+    return G;
+}
+__device__ __forceinline__ int grid_cell(float c, int G) {
+    int i = (int)floorf(c * (float)G);
+    if (i < 0) i = 0;
+    if (i >= G) i = G - 1;
+    return i;
+}
+
+__global__ void k_grid_count(const float4* __restrict__ polyInfo, const int* __restrict__ flags,
+                             int P, int* __restrict__ gridCount, Ctrl* __restrict__ ctrl,
+                             const int* gate) {
+    if (gate_closed(gate)) return;
+    int G = grid_dim_from(ctrl->Rmax);
+    int p = blockIdx.x * blockDim.x + threadIdx.x;
+    if (p == 0) ctrl->G = G;
+    if (p >= P || !flags[p]) return;
+    float4 c = polyInfo[p];
+    atomicAdd(&gridCount[grid_cell(c.y, G) * G + grid_cell(c.x, G)], 1);
+}
+
+// exclusive scan of the G*G counts in one block (G*G <= 65536)
+__global__ void __launch_bounds__(1024)
+k_grid_scan(int* __restrict__ gridCount, int* __restrict__ gridStart, int* __restrict__ gridFill,
+            Ctrl* __restrict__ ctrl, const int* gate) {
+    if (gate_closed(gate)) return;
+    __shared__ int warpSums[32];
+    int G = ctrl->G;
+    int N = G * G;
+    int per = (N + blockDim.x - 1) / blockDim.x;
+    int b0 = threadIdx.x * per;
+    int local = 0;
+    for (int i = 0; i < per; ++i) {
+        int idx = b0 + i;
+        if (idx < N) local += gridCount[idx];
+    }
+    int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+    int incl = local;
+    for (int o = 1; o < 32; o <<= 1) {
+        int t = __shfl_up_sync(PCP_FULL, incl, o);
+        if (lane >= o) incl += t;
+    }
+    if (lane == 31) warpSums[w] = incl;
+    __syncthreads();
+    if (w == 0) {
+        int v = lane < (int)(blockDim.x >> 5) ? warpSums[lane] : 0;
+        int s = v;
+        for (int o = 1; o < 32; o <<= 1) {
+            int t = __shfl_up_sync(PCP_FULL, s, o);
+            if (lane >= o) s += t;
+        }
+        warpSums[lane] = s - v;
+    }
+    __syncthreads();
+    int run = warpSums[w] + incl - local;
+    for (int i = 0; i < per; ++i) {
+        int idx = b0 + i;
+        if (idx < N) {
+            gridStart[idx] = run;
+            run += gridCount[idx];
+            gridFill[idx] = 0;
+            gridCount[idx] = 0;    // ready for the next search
+        }
+    }
+    if (threadIdx.x == blockDim.x - 1) gridStart[N] = run;
+}
+
+__global__ void k_grid_scatter(const float4* __restrict__ polyInfo, const int* __restrict__ flags,
+                               int P, const int* __restrict__ gridStart, int* __restrict__ gridFill,
+                               int* __restrict__ sortedPoly, const Ctrl* __restrict__ ctrl,
+                               const int* gate) {
+    if (gate_closed(gate)) return;
+    int p = blockIdx.x * blockDim.x + threadIdx.x;
+    if (p >= P || !flags[p]) return;
+    int G = ctrl->G;
+    float4 c = polyInfo[p];
+    int cell = grid_cell(c.y, G) * G + grid_cell(c.x, G);
+    sortedPoly[gridStart[cell] + atomicAdd(&gridFill[cell], 1)] = p;
+}
+
+__device__ __forceinline__ void emit_pair(int a, int b, int2* pairs, int cap, Ctrl* ctrl) {
+    int slot = atomicAdd(&ctrl->numPairs, 1);
+    if (slot < cap) pairs[slot] = make_int2(a, b);
+    else atomicOr(&ctrl->flags, kFlagPairOverflow);
+}
+
+__global__ void k_candidates(const float4* __restrict__ polyInfo, const int* __restrict__ flags,
+                             const int* __restrict__ start, int P,
+                             const int* __restrict__ gridStart,
+                             const int* __restrict__ sortedPoly, int2* __restrict__ pairs,
+                             int capPairs, Ctrl* __restrict__ ctrl, const int* gate) {
+    if (gate_closed(gate)) return;
+    int i = blockIdx.x * blockDim.x + threadIdx.x;
+    unsigned long long evals = 0;
+    if (i < P && start[i + 1] > start[i]) {
+        int n = start[i + 1] - start[i];
+        if (n >= 4) emit_pair(i, i, pairs, capPairs, ctrl);
+        if (!flags[i]) {
+            // not well formed: paired with everyone (safe partners below i, all above)
+            for (int j = 0; j < P; ++j) {
+                if (j == i) continue;
+                if (j > i || flags[j]) { emit_pair(j < i ? j : i, j < i ? i : j, pairs, capPairs, ctrl); ++evals; }
+            }
+        } else {
+            int G = ctrl->G;
+            float4 ci = polyInfo[i];
+            int gx = grid_cell(ci.x, G), gy = grid_cell(ci.y, G);
+            int seen[9];
+            int ns = 0;
+            for (int dx = -1; dx <= 1; ++dx) {
+                int nx = gx + dx;
+                if (nx < 0) nx += G; else if (nx >= G) nx -= G;
+                for (int dy = -1; dy <= 1; ++dy) {
+                    int ny = gy + dy;
+                    if (ny < 0) ny += G; else if (ny >= G) ny -= G;
+                    int cell = ny * G + nx;
+                    bool dup = false;
+                    for (int t = 0; t < ns; ++t) dup |= (seen[t] == cell);
+                    if (dup) continue;
+                    seen[ns++] = cell;
+                    for (int q = gridStart[cell]; q < gridStart[cell + 1]; ++q) {
+                        int j = sortedPoly[q];
+                        if (j <= i) continue;
+                        float4 cj = polyInfo[j];
+                        float ddx = wrapf(cj.x - ci.x), ddy = wrapf(cj.y - ci.y);
+                        float rr = ci.z + cj.z + 1e-5f;
+                        if (ddx * ddx + ddy * ddy <= rr * rr) {
+                            emit_pair(i, j, pairs, capPairs, ctrl);
+                            ++evals;
+                        }
+                    }
+                }
+            }
+        }
+    }
+    for (int o = 16; o > 0; o >>= 1) evals += __shfl_xor_sync(PCP_FULL, evals, o);
+    if ((threadIdx.x & 31) == 0 && evals) atomicAdd(&ctrl->pairEvals, evals);
+}
+
+// -------------------------------------------------------- narrow phase ----
+
+// mbarrier / bulk-copy helpers (PTX ISA: mbarrier, cp.async.bulk)
+__device__ __forceinline__ uint32_t smem_u32(const void* p) {
+    return (uint32_t)__cvta_generic_to_shared(p);
+}
+__device__ __forceinline__ void mbar_init(unsigned long long* bar, int count) {
+    asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" :: "r"(smem_u32(bar)), "r"(count) : "memory");
+}
+__device__ __forceinline__ void fence_barrier_init() {
+    asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+}
+__device__ __forceinline__ void mbar_arrive_expect(unsigned long long* bar, uint32_t bytes) {
+    asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;"
+                 :: "r"(smem_u32(bar)), "r"(bytes) : "memory");
+}
+__device__ __forceinline__ void bulk_g2s(void* dst, const void* src, uint32_t bytes,
+                                         unsigned long long* bar) {
+    asm volatile(
+        "cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1], %2, [%3];"
+        :: "r"(smem_u32(dst)), "l"(src), "r"(bytes), "r"(smem_u32(bar)) : "memory");
+}
+__device__ __forceinline__ bool mbar_try_wait(unsigned long long* bar, uint32_t parity) {
+    uint32_t ok;
+    asm volatile(
+        "{\n .reg .pred p;\n"
+        " mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n"
+        " selp.u32 %0, 1, 0, p;\n}"
+        : "=r"(ok) : "r"(smem_u32(bar)), "r"(parity) : "memory");
+    return ok != 0;
+}
+// Bounded wait: gives up after ~2^24 polls (far beyond any copy's latency)
+// and reports it through the control block instead of hanging the GPU.
+__device__ __forceinline__ bool mbar_wait_bounded(unsigned long long* bar, uint32_t parity,
+                                                  Ctrl* ctrl) {
+    for (int it = 0; it < (1 << 24); ++it)
+        if (mbar_try_wait(bar, parity)) return true;
+    atomicOr(&ctrl->flags, kFlagCapacity);
+    atomicExch(&ctrl->errorCode, 100);
+    return false;
+}
+
+struct PairCtx {
+    int a, b;         // polygons (a <= b)
+    int stA, stB, nA, nB;
+    bool self;
+};
+
+__device__ __forceinline__ unsigned long long pack_key(int sj, int si, int i, int j) {
+    return ((unsigned long long)(uint16_t)sj << 48) | ((unsigned long long)(uint16_t)si << 32) |
+           ((unsigned long long)(uint16_t)i << 16) | (unsigned long long)(uint16_t)j;
+}
+
+// Process one staged pair with one warp.  ringA/ringB hold (x, y, cell) of
+// the two rings as float; aabb is scratch for A's edge boxes.  Returns the
+// number of records in recKey/recTU, or -1 when they do not fit.
+__device__ int narrow_pair(const PairCtx& pc, const float4* ringA, const float4* ringB,
+                           float4* aabb, int* queue, unsigned long long* recKey, float2* recTU,
+                           int recCap, int B, const double2* __restrict__ pos,
+                           const double2* __restrict__ edgeVec, const float4* __restrict__ polyInfo) {
+    const int lane = threadIdx.x & 31;
+    const int nA = pc.nA, nB = pc.nB;
+    const float f0x = ringA[0].x, f0y = ringA[0].y;
+    // margin: FP32 coordinate error plus the FP64 predicate's slack for long,
+    // nearly parallel edges (|denom| >= 1e-12 bounds its error in t and u)
+    const float LA = polyInfo[pc.a].w, LB = polyInfo[pc.b].w;
+    const float m = 4e-6f + 1e-3f * LA * LB;
+    for (int a = lane; a < nA; a += 32) {
+        float4 v0 = ringA[a], v1 = ringA[(a + 1 == nA) ? 0 : a + 1];
+        float x0 = wrapf(v0.x - f0x), y0 = wrapf(v0.y - f0y);
+        float x1 = wrapf(v1.x - f0x), y1 = wrapf(v1.y - f0y);
+        aabb[a] = make_float4(fminf(x0, x1) - m, fmaxf(x0, x1) + m, fminf(y0, y1) - m,
+                              fmaxf(y0, y1) + m);
+    }
+    __syncwarp();
+    // this lane's B edges (up to 4 for rings of <= 128 vertices; more on the
+    // block path through the outer loop)
+    int qn = 0;
+    int rec = 0;
+    bool overflow = false;
+    auto run_batch = [&](int cnt) {
+        bool hit = false;
+        unsigned long long key = 0;
+        float2 tuf = make_float2(0.f, 0.f);
+        if (lane < cnt) {
+            int e = queue[lane];
+            int ea = e & 0xFFFF, eb = (e >> 16) & 0xFFFF;
+            int id1 = pc.stA + ea, nid = pc.stB + eb;
+            Crossing c = cross_exact(pos[id1], edgeVec[id1], pos[nid], edgeVec[nid]);
+            if (c.hit) {
+                hit = true;
+                if (c.denom > 0) {   // kernels.cuh:796-799, 862-867
+                    key = pack_key(pc.a, pc.b, eb, ea);
+                    tuf = make_float2((float)c.tt, (float)c.uu);
+                } else {             // kernels.cuh:800-804, 868-873
+                    key = pack_key(pc.b, pc.a, ea, eb);
+                    tuf = make_float2((float)c.uu, (float)c.tt);
+                }
+            }
+        }
+        unsigned mask = __ballot_sync(PCP_FULL, hit);
+        int cnt2 = __popc(mask);
+        if (rec + cnt2 > recCap) { overflow = true; return; }
+        if (hit) {
+            int slot = rec + __popc(mask & ((1u << lane) - 1u));
+            recKey[slot] = key;
+            recTU[slot] = tuf;
+        }
+        rec += cnt2;
+    };
+    for (int b0 = 0; b0 < nB && !overflow; b0 += 32) {
+        int b = b0 + lane;
+        bool bval = b < nB;
+        float bx0 = 0, bx1 = 0, by0 = 0, by1 = 0;
+        int cb = 0;
+        if (bval) {
+            float4 w0 = ringB[b], w1 = ringB[(b + 1 == nB) ? 0 : b + 1];
+            float x0 = wrapf(w0.x - f0x), y0 = wrapf(w0.y - f0y);
+            float x1 = wrapf(w1.x - f0x), y1 = wrapf(w1.y - f0y);
+            bx0 = fminf(x0, x1); bx1 = fmaxf(x0, x1);
+            by0 = fminf(y0, y1); by1 = fmaxf(y0, y1);
+            cb = __float_as_int(w0.z);
+        }
+        for (int a = 0; a < nA && !overflow; ++a) {
+            float4 bb = aabb[a];
+            int ca = __float_as_int(ringA[a].z);
+            bool ok = bval;
+            if (pc.self) {
+                // id1 < nid, not adjacent (kernels.cuh:766-775)
+                ok = ok && b > a + 1 && !(a == 0 && b == nA - 1);
+            }
+            // reject only when the boxes are certainly apart (NaN keeps the pair)
+            ok = ok && !(bx0 > bb.y || bx1 < bb.x || by0 > bb.w || by1 < bb.z);
+            ok = ok && cells_adjacent(ca, cb, B);
+            unsigned mk = __ballot_sync(PCP_FULL, ok);
+            if (mk) {
+                if (ok) queue[qn + __popc(mk & ((1u << lane) - 1u))] = a | (b << 16);
+                qn += __popc(mk);
+                __syncwarp();
+                if (qn >= 32) {
+                    run_batch(32);
+                    __syncwarp();
+                    int rest = qn - 32;
+                    int v = lane < rest ? queue[32 + lane] : 0;
+                    __syncwarp();
+                    if (lane < rest) queue[lane] = v;
+                    qn = rest;
+                    __syncwarp();
+                }
+            }
+        }
+    }
+    if (!overflow && qn > 0) run_batch(qn);
+    __syncwarp();
+    return overflow ? -1 : rec;
+}
+
+// Match each crossing to its exit in the same pair (updateOutersectionsKernel,
+// kernels.cuh:981-1065): among records of the reverse group (sj' = si,
+// si' = sj) skip those on the same edge that are not ahead (l == i and
+// t >= u), take the smallest cyclic edge distance d = (l - i) mod n_si, then
+// the smallest u, then the smallest key (first in the reference's sorted
+// scan).  Writes the pair's records to global memory.
+__device__ void match_and_write(const PairCtx& pc, int R, const unsigned long long* recKey,
+                                const float2* recTU, Ctrl* ctrl, ContactWS& ws) {
+    const int lane = threadIdx.x & 31;
+    int base = 0;
+    if (lane == 0) base = atomicAdd(&ctrl->numRecords, R);
+    base = __shfl_sync(PCP_FULL, base, 0);
+    if (base + R > ws.capRecords) {
+        if (lane == 0) atomicOr(&ctrl->flags, kFlagRecordOverflow);
+        return;
+    }
+    unsigned long long kmax = 0;
+    for (int r = lane; r < R; r += 32) {
+        unsigned long long key = recKey[r];
+        int sj = (int)(key >> 48), si = (int)((key >> 32) & 0xFFFF);
+        int i = (int)((key >> 16) & 0xFFFF);
+        int ni = (si == pc.a) ? pc.nA : pc.nB;
+        float tVal = recTU[r].y;
+        unsigned long long grp = ((unsigned long long)si << 16) | (unsigned long long)sj;
+        bool groupSeen = false;
+        int best = -1, bestD = 0;
+        float bestU = 0.f;
+        unsigned long long bestK = 0;
+        for (int c = 0; c < R; ++c) {
+            unsigned long long kc = recKey[c];
+            if ((kc >> 32) != grp) continue;
+            groupSeen = true;
+            int l = (int)(kc & 0xFFFF);
+            float uVal = recTU[c].x;
+            if (l == i && tVal >= uVal) continue;
+            int d = (l - i + ni) % ni;
+            bool better = best < 0 || d < bestD || (d == bestD && (uVal < bestU ||
+                          (uVal == bestU && kc < bestK)));
+            if (better) { best = c; bestD = d; bestU = uVal; bestK = kc; }
+        }
+        int g = base + r;
+        ws.recKey[g] = key;
+        ws.recTU[g] = recTU[r];
+        if (best >= 0) {
+            ws.recOuter[g] = recKey[best];
+            ws.recUT[g] = recTU[best];
+        } else {
+            ws.recOuter[g] = key;
+            ws.recUT[g] = recTU[r];
+            if (!groupSeen) {
+                int f = atomicAdd(&ctrl->numFix, 1);
+                if (f < ws.capFix) ws.fixList[f] = g;
+                else atomicOr(&ctrl->flags, kFlagFixOverflow);
+            }
+        }
+        kmax = key > kmax ? key : kmax;
+    }
+    for (int o = 16; o > 0; o >>= 1) {
+        unsigned long long t = __shfl_xor_sync(PCP_FULL, kmax, o);
+        kmax = t > kmax ? t : kmax;
+    }
+    if (lane == 0 && R > 0) atomicMax(&ctrl->maxKey, kmax);
+}
+
+__device__ __forceinline__ PairCtx make_ctx(int2 pr, const int* __restrict__ start) {
+    PairCtx pc;
+    pc.a = pr.x; pc.b = pr.y;
+    pc.stA = start[pr.x]; pc.nA = start[pr.x + 1] - pc.stA;
+    pc.stB = start[pr.y]; pc.nB = start[pr.y + 1] - pc.stB;
+    pc.self = pr.x == pr.y;
+    return pc;
+}
+
+struct alignas(16) WarpSmem {
+    float4 ring[2][2 * kFastRing];
+    float4 aabb[kFastRing];
+    unsigned long long recKey[kFastRecords];
+    float2 recTU[kFastRecords];
+    int queue[64];
+    unsigned long long bar[2];
+};
+constexpr int kNarrowWarps = 4;
+
+__device__ __forceinline__ void push_slow(int q, Ctrl* ctrl, ContactWS& ws) {
+    int s = atomicAdd(&ctrl->numSlow, 1);
+    if (s < ws.capSlow) ws.slowList[s] = q;
+    else atomicOr(&ctrl->flags, kFlagSlowOverflow);
+}
+
+__global__ void __launch_bounds__(32 * kNarrowWarps)
+k_narrow(const double2* __restrict__ pos, const int* __restrict__ start, int B,
+         ContactWS ws, Ctrl* __restrict__ ctrl, const int* gate) {
+    if (gate_closed(gate)) return;
+    extern __shared__ __align__(128) unsigned char smem_raw[];
+    WarpSmem& S = reinterpret_cast<WarpSmem*>(smem_raw)[threadIdx.x / 32];
+    const int lane = threadIdx.x & 31;
+    const int numPairs = min(ctrl->numPairs, ws.capPairs);
+    if (lane == 0) {
+        mbar_init(&S.bar[0], 1);
+        mbar_init(&S.bar[1], 1);
+        fence_barrier_init();
+    }
+    __syncwarp();
+    uint32_t phase[2] = {0u, 0u};
+    // claim the first pair and start its copy
+    int q = 0;
+    if (lane == 0) q = atomicAdd(&ctrl->pairCursor, 1);
+    q = __shfl_sync(PCP_FULL, q, 0);
+    auto issue = [&](int qq, int stage) -> bool {
+        // returns true when a copy was issued for pair qq into `stage`
+        if (qq >= numPairs) return false;
+        PairCtx pc = make_ctx(ws.pairs[qq], start);
+        if (pc.nA > kFastRing || pc.nB > kFastRing || pc.nA < 3 || pc.nB < 3) return false;
+        if (lane == 0) {
+            // order this warp's earlier generic reads of the buffer before the
+            // async-proxy writes that refill it
+            asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+            uint32_t bytesA = 16u * (uint32_t)pc.nA;
+            uint32_t bytesB = pc.self ? 0u : 16u * (uint32_t)pc.nB;
+            mbar_arrive_expect(&S.bar[stage], bytesA + bytesB);
+            bulk_g2s(&S.ring[stage][0], ws.vtx + pc.stA, bytesA, &S.bar[stage]);
+            if (!pc.self) bulk_g2s(&S.ring[stage][kFastRing], ws.vtx + pc.stB, bytesB, &S.bar[stage]);
+        }
+        return true;
+    };
+    int stage = 0;
+    bool inflight = issue(q, stage);
+    while (q < numPairs) {
+        int qn = 0;
+        if (lane == 0) qn = atomicAdd(&ctrl->pairCursor, 1);
+        qn = __shfl_sync(PCP_FULL, qn, 0);
+        PairCtx pc = make_ctx(ws.pairs[q], start);
+        if (!inflight) {
+            // too large (or degenerate) for the warp path: hand to the block path
+            if (lane == 0 && pc.nA >= 1 && pc.nB >= 1) push_slow(q, ctrl, ws);
+            inflight = issue(qn, stage);
+            q = qn;
+            continue;
+        }
+        // prefetch the next pair into the other buffer while this one is processed
+        int other = stage ^ 1;
+        bool nextInflight = issue(qn, other);
+        if (!mbar_wait_bounded(&S.bar[stage], phase[stage], ctrl)) {
+            // the copy never landed: wait (bounded) for the prefetch too, then stop
+            if (nextInflight) mbar_wait_bounded(&S.bar[other], phase[other], ctrl);
+            return;
+        }
+        phase[stage] ^= 1u;
+        const float4* ringA = &S.ring[stage][0];
+        const float4* ringB = pc.self ? ringA : &S.ring[stage][kFastRing];
+        int R = narrow_pair(pc, ringA, ringB, S.aabb, S.queue, S.recKey, S.recTU, kFastRecords,
+                            B, pos, ws.edgeVec, ws.polyInfo);
+        if (R < 0) {
+            if (lane == 0) push_slow(q, ctrl, ws);
+        } else if (R > 0) {
+            match_and_write(pc, R, S.recKey, S.recTU, ctrl, ws);
+        }
+        __syncwarp();
+        stage = other;
+        inflight = nextInflight;
+        q = qn;
+    }
+}
+
+// Block path: one warp per block, rings loaded with plain loads into a large
+// dynamic shared-memory area; for polygons above kFastRing vertices and for
+// pairs with more than kFastRecords crossings.
+__global__ void __launch_bounds__(32)
+k_narrow_slow(const double2* __restrict__ pos, const int* __restrict__ start, int B,
+              ContactWS ws, Ctrl* __restrict__ ctrl, const int* gate) {
+    if (gate_closed(gate)) return;
+    extern __shared__ __align__(128) unsigned char smem_raw[];
+    float4* ring = reinterpret_cast<float4*>(smem_raw);                 // kSlowRing
+    float4* aabb = ring + kSlowRing;                                      // kSlowRing
+    unsigned long long* recKey = reinterpret_cast<unsigned long long*>(aabb + kSlowRing);
+    float2* recTU = reinterpret_cast<float2*>(recKey + kSlowRecords);
+    int* queue = reinterpret_cast<int*>(recTU + kSlowRecords);
+    const int lane = threadIdx.x & 31;
+    int numSlow = min(ctrl->numSlow, ws.capSlow);
+    for (;;) {
+        int s = 0;
+        if (lane == 0) s = atomicAdd(&ctrl->slowCursor, 1);
+        s = __shfl_sync(PCP_FULL, s, 0);
+        if (s >= numSlow) break;
+        int q = ws.slowList[s];
+        PairCtx pc = make_ctx(ws.pairs[q], start);
+        int tot = pc.self ? pc.nA : pc.nA + pc.nB;
+        if (pc.nA < 1 || pc.nB < 1) continue;
+        if (tot > kSlowRing || pc.nA > 65535 || pc.nB > 65535) {
+            if (lane == 0) atomicOr(&ctrl->flags, kFlagCapacity);
+            continue;
+        }
+        for (int t = lane; t < pc.nA; t += 32) ring[t] = ws.vtx[pc.stA + t];
+        if (!pc.self)
+            for (int t = lane; t < pc.nB; t += 32) ring[pc.nA + t] = ws.vtx[pc.stB + t];
+        __syncwarp();
+        const float4* ringB = pc.self ? ring : ring + pc.nA;
+        int R = narrow_pair(pc, ring, ringB, aabb, queue, recKey, recTU, kSlowRecords, B, pos,
+                            ws.edgeVec, ws.polyInfo);
+        if (R < 0) {
+            if (lane == 0) atomicOr(&ctrl->flags, kFlagCapacity);
+        } else if (R > 0) {
+            match_and_write(pc, R, recKey, recTU, ctrl, ws);
+        }
+        __syncwarp();
+    }
+}
+
+// A crossing whose reverse group is empty: the reference's binary search
+// (kernels.cuh:993-1000) stops at the last record when every key is below
+// sij, and that record is then tried as the partner.  Reproduced here.
+__global__ void k_fixup(const int* __restrict__ start, ContactWS ws, Ctrl* __restrict__ ctrl,
+                        const int* gate) {
+    if (gate_closed(gate)) return;
+    int nf = min(ctrl->numFix, ws.capFix);
+    if (nf == 0) return;
+    int I = min(ctrl->numRecords, ws.capRecords);
+    unsigned long long kmax = ctrl->maxKey;
+    // locate the record holding the largest key (keys are unique)
+    __shared__ int s_idx;
+    if (threadIdx.x == 0) s_idx = -1;
+    __syncthreads();
+    for (int g = threadIdx.x; g < I; g += blockDim.x)
+        if (ws.recKey[g] == kmax) s_idx = g;
+    __syncthreads();
+    int mi = s_idx;
+    if (mi < 0) return;
+    float2 tuMax = ws.recTU[mi];
+    for (int f = threadIdx.x; f < nf; f += blockDim.x) {
+        int g = ws.fixList[f];
+        unsigned long long key = ws.recKey[g];
+        int sj = (int)(key >> 48), si = (int)((key >> 32) & 0xFFFF);
+        int i = (int)((key >> 16) & 0xFFFF);
+        unsigned long long sij = ((unsigned long long)si << 48) | ((unsigned long long)sj << 32);
+        if (!(sij > kmax)) continue;
+        int l = (int)(kmax & 0xFFFF);
+        float tVal = ws.recTU[g].y;
+        if (l == i && tVal >= tuMax.x) continue;
+        (void)start;
+        ws.recOuter[g] = kmax;
+        ws.recUT[g] = tuMax;
+    }
+}
+
+// ---------------------------------------------------------------- force ----
+__device__ __forceinline__ void add_f(double2* F, int v, double fx, double fy) {
+    double* f = reinterpret_cast<double*>(F) + 2 * (size_t)v;
+    atomicAdd(f, fx);
+    atomicAdd(f + 1, fy);
+}
+
+// updateForceEnergyExteriorKernel (kernels.cuh:1067-1273) and, per record,
+// the interior chain of updateForceEnergyInteriorKernel (kernels.cuh:
+// 1354-1424): whole edges of si strictly between the entry edge i and the
+// exit edge l, each taken relative to the record's own entry point.
+__global__ void __launch_bounds__(256)
+k_overlap_force(const double2* __restrict__ pos, const int* __restrict__ start,
+                const int* __restrict__ next, int V, ContactWS ws, Ctrl* __restrict__ ctrl,
+                double2* __restrict__ force, const int* gate) {
+    if (gate_closed(gate)) return;
+    int I = min(ctrl->numRecords, ws.capRecords);
+    double eLocal = 0.0;
+    for (int r = blockIdx.x * blockDim.x + threadIdx.x; r < I; r += gridDim.x * blockDim.x) {
+        unsigned long long inter = ws.recKey[r], outer = ws.recOuter[r];
+        if (inter == outer) continue;
+        int s1 = (int)((inter >> 32) & 0xFFFF), s2 = (int)(inter >> 48);
+        int iLoc = (int)((inter >> 16) & 0xFFFF), jLoc = (int)(inter & 0xFFFF);
+        int kLoc = (int)((outer >> 16) & 0xFFFF), lLoc = (int)(outer & 0xFFFF);
+        int start1 = start[s1], start2 = start[s2];
+        int i = start1 + iLoc, j = start2 + jLoc, k = start2 + kLoc, l = start1 + lLoc;
+        if (i >= V || j >= V || k >= V || l >= V) {
+            atomicOr(&ctrl->flags, kFlagNonFinite);
+            continue;
+        }
+        int zi = next[i], zj = next[j], zk = next[k], zl = next[l];
+        double2 pi = pos[i], pj = pos[j], pk = pos[k], pl = pos[l];
+        double2 pzi = pos[zi], pzj = pos[zj], pzk = pos[zk], pzl = pos[zl];
+        double2 r1 = make_double2(wrap(pzi.x - pi.x), wrap(pzi.y - pi.y));
+        double2 r2 = make_double2(wrap(pzk.x - pk.x), wrap(pzk.y - pk.y));
+        double t1 = (double)ws.recTU[r].y;
+        double t2 = (double)ws.recUT[r].y;
+        double2 fij = make_double2(wrap(pi.x + t1 * r1.x), wrap(pi.y + t1 * r1.y));
+        double2 fkl = make_double2(wrap(pk.x + t2 * r2.x), wrap(pk.y + t2 * r2.y));
+        double2 sp = fij;
+        double e = 0.0;
+        double2 o[4];
+        if (i == l) {
+            double2 g1, g2;
+            e += h_g12(fij, fkl, sp, g1, g2);
+            gDf(pi, pzi, pj, pzj, g1, o);
+            add_f(force, i, -o[0].x, -o[0].y);
+            add_f(force, zi, -o[1].x, -o[1].y);
+            add_f(force, j, -o[2].x, -o[2].y);
+            add_f(force, zj, -o[3].x, -o[3].y);
+            gDf(pk, pzk, pi, pzi, g2, o);
+            add_f(force, k, -o[0].x, -o[0].y);
+            add_f(force, zk, -o[1].x, -o[1].y);
+            add_f(force, i, -o[2].x, -o[2].y);
+            add_f(force, zi, -o[3].x, -o[3].y);
+        } else {
+            double2 g1a, g2a, g1b, g2b;
+            e += h_g12(fij, pzi, sp, g1a, g2a);
+            e += h_g12(pl, fkl, sp, g1b, g2b);
+            gDf(pi, pzi, pj, pzj, g1a, o);
+            add_f(force, i, -o[0].x, -o[0].y);
+            add_f(force, j, -o[2].x, -o[2].y);
+            add_f(force, zi, -(o[1].x + g2a.x), -(o[1].y + g2a.y));
+            add_f(force, zj, -o[3].x, -o[3].y);
+            gDf(pk, pzk, pl, pzl, g2b, o);
+            add_f(force, l, -(g1b.x + o[2].x), -(g1b.y + o[2].y));
+            add_f(force, k, -o[0].x, -o[0].y);
+            add_f(force, zl, -o[3].x, -o[3].y);
+            add_f(force, zk, -o[1].x, -o[1].y);
+        }
+        // interior chain
+        int n1 = start[s1 + 1] - start1;
+        if (n1 > 0) {
+            int lDist = ((lLoc - iLoc) % n1 + n1) % n1;
+            for (int step = 1; step < lDist; ++step) {
+                int mLoc = iLoc + step;
+                if (mLoc >= n1) mLoc -= n1;
+                int mv = start1 + mLoc;
+                int nv = next[mv];
+                double2 g1, g2;
+                e += h_g12(pos[mv], pos[nv], sp, g1, g2);
+                add_f(force, mv, -g1.x, -g1.y);
+                add_f(force, nv, -g2.x, -g2.y);
+            }
+        }
+        eLocal += e;
+    }
+    eLocal = warp_sum(eLocal);
+    if ((threadIdx.x & 31) == 0 && eLocal != 0.0) atomicAdd(&ctrl->energy, eLocal / 2.0);
+}
+
+// ------------------------------------------------------------ launchers ----
+static const size_t kSlowSmem = (size_t)kSlowRing * 32 + (size_t)kSlowRecords * 16 + 64 * 4;
+
+// Opt the narrow-phase kernels into their shared-memory sizes; called once
+// per process before any launch or graph capture.
+cudaError_t contacts_init() {
+    static bool done = false;
+    if (done) return cudaSuccess;
+    cudaError_t e = cudaFuncSetAttribute(k_narrow, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                         (int)(sizeof(WarpSmem) * kNarrowWarps));
+    if (e != cudaSuccess) return e;
+    e = cudaFuncSetAttribute(k_narrow_slow, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                             (int)kSlowSmem);
+    if (e != cudaSuccess) return e;
+    done = true;
+    return cudaSuccess;
+}
+
+cudaError_t launch_contacts(const double2* pos, const int* start, const int* shapeId,
+                            const int* cellLocation, int P, int V, int B, ContactWS& ws,
+                            Ctrl* ctrl, const int* gate, cudaStream_t st) {
+    (void)shapeId; (void)V;
+    k_reset_contacts<<<1, 64, 0, st>>>(ctrl, gate);
+    if (P <= 0) return cudaGetLastError();
+    if (B < 1) B = 1;
+    k_prepass<<<nblocks(P, 8), 256, 0, st>>>(pos, start, cellLocation, P, ws.edgeVec, ws.vtx,
+                                             ws.polyInfo, ws.polyFlags, ws.unsafeList, ctrl, gate);
+    k_grid_count<<<nblocks(P, 256), 256, 0, st>>>(ws.polyInfo, ws.polyFlags, P, ws.gridCount,
+                                                  ctrl, gate);
+    k_grid_scan<<<1, 1024, 0, st>>>(ws.gridCount, ws.gridStart, ws.gridFill, ctrl, gate);
+    k_grid_scatter<<<nblocks(P, 256), 256, 0, st>>>(ws.polyInfo, ws.polyFlags, P, ws.gridStart,
+                                                    ws.gridFill, ws.sortedPoly, ctrl, gate);
+    k_candidates<<<nblocks(P, 128), 128, 0, st>>>(ws.polyInfo, ws.polyFlags, start, P,
+                                                  ws.gridStart, ws.sortedPoly, ws.pairs,
+                                                  ws.capPairs, ctrl, gate);
+    size_t smem = sizeof(WarpSmem) * kNarrowWarps;
+    size_t smemSlow = kSlowSmem;
+    int grid = sm_count() * 4;
+    k_narrow<<<grid, 32 * kNarrowWarps, smem, st>>>(pos, start, B, ws, ctrl, gate);
+    k_narrow_slow<<<sm_count(), 32, smemSlow, st>>>(pos, start, B, ws, ctrl, gate);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_contacts_finish(const int* start, ContactWS& ws, Ctrl* ctrl,
+                                   const int* gate, cudaStream_t st) {
+    k_fixup<<<1, 1024, 0, st>>>(start, ws, ctrl, gate);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_overlap_force(const double2* pos, const int* start, const int* next,
+                                 int V, ContactWS& ws, Ctrl* ctrl, double2* force,
+                                 const int* gate, cudaStream_t st) {
+    int grid = sm_count() * 8;
+    k_overlap_force<<<grid, 256, 0, st>>>(pos, start, next, V, ws, ctrl, force, gate);
+    return cudaGetLastError();
+}
+
+}  // namespace pcp

@@ -1,0 +1,1374 @@
+// model.cpp -- host side of the GB300 polygon path: the model object behind
+// the pcp_model_* C ABI (include/pcp_gb300.h) and the stateless pcp_*
+// launchers.  It mirrors the reference's `class Model` (camdennis/
+// pyCudaPolygon src/model.hpp, src/model.cpp) method by method, but
+//   * never calls exit(): every failure is a status code + message;
+//   * allocates once per size change (no per-call cudaMalloc/cudaFree);
+//   * runs a FIRE step as one CUDA-graph launch with every scalar of the
+//     reference's host loop (dt, alpha, nPos, E_pre, rollback decisions)
+//     kept on the device, and one small device-to-host read per step;
+//   * keeps contact records grouped by polygon pair and only restores the
+//     reference's sorted (si, i, j, sj) order when a getter asks for it.
+#include <cuda_runtime.h>
+
+#include <algorithm>
+#include <cmath>
+#include <cstdarg>
+#include <cstdio>
+#include <cstring>
+#include <numeric>
+#include <string>
+#include <vector>
+
+#include "pcp_gb300.h"
+#include "pcp_internal.h"
+
+using namespace pcp;
+
+namespace pcp {
+cudaError_t launch_fire_reset(Ctrl* c, const int* gate, cudaStream_t st);
+}
+
+namespace {
+
+thread_local std::string g_err;
+
+int fail(int code, const char* fmt, ...) {
+    char buf[512];
+    va_list ap;
+    va_start(ap, fmt);
+    vsnprintf(buf, sizeof(buf), fmt, ap);
+    va_end(ap);
+    g_err = buf;
+    return code;
+}
+
+#define CK(call)                                                                         \
+    do {                                                                                 \
+        cudaError_t _e = (call);                                                         \
+        if (_e != cudaSuccess)                                                           \
+            return fail(PCP_ERR_CUDA, "%s: %s (%s:%d)", #call, cudaGetErrorString(_e),   \
+                        __FILE__, __LINE__);                                             \
+    } while (0)
+
+template <typename T>
+cudaError_t dalloc(T** p, size_t n) {
+    if (*p) { cudaFree(*p); *p = nullptr; }
+    if (n == 0) n = 1;
+    cudaError_t e = cudaMalloc((void**)p, n * sizeof(T));
+    if (e == cudaSuccess) e = cudaMemset(*p, 0, n * sizeof(T));
+    return e;
+}
+template <typename T>
+void dfree(T** p) {
+    if (*p) { cudaFree(*p); *p = nullptr; }
+}
+
+}  // namespace
+
+struct pcp_model {
+    // host-side parameters
+    int modelType = PCP_MODEL_NORMAL;
+    int V = 0, P = 0;
+    int boxSize = 2;
+    double maxEdgeLengthSet = 0.5;
+    int maxNeighbors = 100;
+    int numIntersections = 0;
+    double stiffness = 0.0, compressibility = 0.0;
+    int lastShakeIters = 0;
+    int pointDensity = -1;
+    double overlapArea = 0.0;
+    bool topology = false;
+    std::vector<int> startHost;
+    cudaStream_t stream = nullptr;
+    long long launches = 0;
+    unsigned long long generation = 1;
+
+    // device state
+    double2 *pos = nullptr, *force = nullptr, *vel = nullptr;
+    double2 *posTMP = nullptr, *posTMP2 = nullptr, *posTent = nullptr;
+    double2 *velSnap = nullptr, *forceSnap = nullptr;
+    double *edgeLengths = nullptr, *constraints = nullptr, *scratch = nullptr;
+    double *areas = nullptr, *comX = nullptr, *comY = nullptr, *perimeters = nullptr;
+    double *targetAreas = nullptr, *targetEdge = nullptr;
+    double *maxEdge = nullptr, *dtmp = nullptr, *xpbdDev = nullptr;
+    int *start = nullptr, *shapeId = nullptr, *next = nullptr, *prev = nullptr;
+    int *cellLocation = nullptr, *shakeIters = nullptr;
+    int *mcCounter = nullptr, *mcNbIdx = nullptr, *mcBoxStarts = nullptr;
+    unsigned long long* mcSum = nullptr;
+    Ctrl* ctrl = nullptr;
+    Ctrl* ctrlHost = nullptr;   // pinned mirror
+    ContactWS ws;
+
+    // host views of the contact records
+    enum View { VIEW_NONE, VIEW_COMPACT, VIEW_FINAL } view = VIEW_NONE;
+    bool recordsCached = false;
+    std::vector<unsigned long long> hKey, hOuter;   // records in the current view
+    std::vector<float2> hTU, hUT;
+    std::vector<uint32_t> hKeys;                    // permutation of the last sort
+    bool neighborsCached = false;
+    std::vector<int> hNeighbors, hNumNeighbors, hShapeCounts;
+    std::vector<uint8_t> hInside;
+
+    // FIRE graph
+    cudaGraphExec_t fireExec = nullptr;
+    unsigned long long fireGen = 0;
+    int fireShakeIter = -1, fireModel = -1, fireB = -1;
+
+    ~pcp_model() { release(); }
+
+    void release() {
+        if (fireExec) { cudaGraphExecDestroy(fireExec); fireExec = nullptr; }
+        dfree(&pos); dfree(&force); dfree(&vel); dfree(&posTMP); dfree(&posTMP2); dfree(&posTent);
+        dfree(&velSnap); dfree(&forceSnap);
+        dfree(&edgeLengths); dfree(&constraints); dfree(&scratch);
+        dfree(&areas); dfree(&comX); dfree(&comY); dfree(&perimeters);
+        dfree(&targetAreas); dfree(&targetEdge); dfree(&maxEdge); dfree(&dtmp); dfree(&xpbdDev);
+        dfree(&start); dfree(&shapeId); dfree(&next); dfree(&prev); dfree(&cellLocation);
+        dfree(&shakeIters); dfree(&mcCounter); dfree(&mcNbIdx); dfree(&mcBoxStarts); dfree(&mcSum);
+        dfree(&ctrl);
+        if (ctrlHost) { cudaFreeHost(ctrlHost); ctrlHost = nullptr; }
+        free_ws();
+    }
+    void free_ws() {
+        dfree(&ws.edgeVec); dfree(&ws.vtx); dfree(&ws.polyInfo); dfree(&ws.polyFlags);
+        dfree(&ws.gridCount); dfree(&ws.gridStart); dfree(&ws.gridFill); dfree(&ws.sortedPoly);
+        dfree(&ws.unsafeList); dfree(&ws.pairs); dfree(&ws.recKey); dfree(&ws.recOuter);
+        dfree(&ws.recTU); dfree(&ws.recUT); dfree(&ws.fixList); dfree(&ws.slowList);
+    }
+    void invalidate() {
+        recordsCached = false;
+        neighborsCached = false;
+    }
+};
+
+namespace {
+
+int alloc_vertex(pcp_model* m) {
+    size_t V = (size_t)m->V;
+    CK(dalloc(&m->pos, V)); CK(dalloc(&m->force, V)); CK(dalloc(&m->vel, V));
+    CK(dalloc(&m->posTMP, V)); CK(dalloc(&m->posTMP2, V)); CK(dalloc(&m->posTent, V));
+    CK(dalloc(&m->velSnap, V)); CK(dalloc(&m->forceSnap, V));
+    CK(dalloc(&m->edgeLengths, V)); CK(dalloc(&m->constraints, 6 * V));
+    CK(dalloc(&m->scratch, (size_t)kScratchPerVertex * V));
+    m->generation++;
+    m->topology = false;
+    return PCP_OK;
+}
+
+int alloc_ws(pcp_model* m, int capPairs, int capRecords) {
+    ContactWS& w = m->ws;
+    w.V = m->V; w.P = m->P;
+    w.capPairs = capPairs; w.capRecords = capRecords;
+    w.capFix = std::max(1024, capRecords / 16);
+    w.capSlow = std::max(1024, capPairs / 4);
+    size_t V = (size_t)m->V, P = (size_t)std::max(m->P, 1);
+    CK(dalloc(&w.edgeVec, V)); CK(dalloc(&w.vtx, V));
+    CK(dalloc(&w.polyInfo, P)); CK(dalloc(&w.polyFlags, P));
+    CK(dalloc(&w.gridCount, (size_t)kGridMax * kGridMax));
+    CK(dalloc(&w.gridStart, (size_t)kGridMax * kGridMax + 1));
+    CK(dalloc(&w.gridFill, (size_t)kGridMax * kGridMax));
+    CK(dalloc(&w.sortedPoly, P)); CK(dalloc(&w.unsafeList, P));
+    CK(dalloc(&w.pairs, (size_t)capPairs));
+    CK(dalloc(&w.recKey, (size_t)capRecords)); CK(dalloc(&w.recOuter, (size_t)capRecords));
+    CK(dalloc(&w.recTU, (size_t)capRecords)); CK(dalloc(&w.recUT, (size_t)capRecords));
+    CK(dalloc(&w.fixList, (size_t)w.capFix)); CK(dalloc(&w.slowList, (size_t)w.capSlow));
+    m->generation++;
+    return PCP_OK;
+}
+
+int sync(pcp_model* m) {
+    CK(cudaStreamSynchronize(m->stream));
+    return PCP_OK;
+}
+
+int read_ctrl(pcp_model* m) {
+    CK(cudaMemcpyAsync(m->ctrlHost, m->ctrl, sizeof(Ctrl), cudaMemcpyDeviceToHost, m->stream));
+    return sync(m);
+}
+
+int need_topology(pcp_model* m) {
+    if (m->P <= 0 || m->startHost.empty())
+        return fail(PCP_ERR_STATE, "setStartIndices has not been called");
+    if (!m->topology) return fail(PCP_ERR_STATE, "initializeNeighborCells has not been called");
+    return PCP_OK;
+}
+
+// contact search with the reference's resize-and-retry (model.cpp:256-307):
+// capacities grow until the search fits, so no crossing is ever dropped
+int run_contacts(pcp_model* m) {
+    for (int attempt = 0; attempt < 8; ++attempt) {
+        CK(launch_contacts(m->pos, m->start, m->shapeId, m->cellLocation, m->P, m->V, m->boxSize,
+                           m->ws, m->ctrl, nullptr, m->stream));
+        m->launches += 7;
+        int rc = read_ctrl(m);
+        if (rc) return rc;
+        unsigned fl = m->ctrlHost->flags;
+        if (fl & kFlagCapacity)
+            return fail(PCP_ERR_CAPACITY,
+                        "a polygon pair exceeds the contact kernel limits (%d vertices, %d "
+                        "crossings per pair)", kSlowRing, kSlowRecords);
+        if (!(fl & (kFlagPairOverflow | kFlagRecordOverflow | kFlagSlowOverflow |
+                    kFlagFixOverflow)))
+            return PCP_OK;
+        int np = std::max(m->ws.capPairs, m->ctrlHost->numPairs) * 2 + 1024;
+        int nr = std::max(m->ws.capRecords, m->ctrlHost->numRecords) * 2 + 4096;
+        int rc2 = alloc_ws(m, np, nr);
+        if (rc2) return rc2;
+    }
+    return fail(PCP_ERR_CAPACITY, "contact buffers could not be sized");
+}
+
+// ---- host views of the records ----------------------------------------
+
+int fetch_records(pcp_model* m, std::vector<unsigned long long>& key,
+                  std::vector<unsigned long long>& outer, std::vector<float2>& tu,
+                  std::vector<float2>& ut) {
+    int rc = read_ctrl(m);
+    if (rc) return rc;
+    int I = std::min(m->ctrlHost->numRecords, m->ws.capRecords);
+    key.resize(I); outer.resize(I); tu.resize(I); ut.resize(I);
+    if (I > 0) {
+        CK(cudaMemcpy(key.data(), m->ws.recKey, I * sizeof(unsigned long long), cudaMemcpyDeviceToHost));
+        CK(cudaMemcpy(outer.data(), m->ws.recOuter, I * sizeof(unsigned long long), cudaMemcpyDeviceToHost));
+        CK(cudaMemcpy(tu.data(), m->ws.recTU, I * sizeof(float2), cudaMemcpyDeviceToHost));
+        CK(cudaMemcpy(ut.data(), m->ws.recUT, I * sizeof(float2), cudaMemcpyDeviceToHost));
+    }
+    return PCP_OK;
+}
+
+// lower (id1) and higher (nid) vertex of a record and its inside flag
+// (inverse of the packing at kernels.cuh:861-874)
+inline void record_vertices(const std::vector<int>& st, unsigned long long key, int& id1,
+                            int& nid, bool& inside) {
+    int sj = (int)(key >> 48), si = (int)((key >> 32) & 0xFFFF);
+    int i = (int)((key >> 16) & 0xFFFF), j = (int)(key & 0xFFFF);
+    inside = (sj < si) || (sj == si && j < i);
+    if (inside) { id1 = st[sj] + j; nid = st[si] + i; }
+    else { id1 = st[si] + i; nid = st[sj] + j; }
+}
+
+// rank of cell c2 in the 3x3 scan order of updateNeighborsKernel around c1
+// (kernels.cuh:737-757): dx outer, dy inner, repeated cells skipped
+int visit_rank(int c1, int c2, int B) {
+    int bx = c1 % B, by = c1 / B;
+    int seen[9], ns = 0;
+    for (int dx = -1; dx <= 1; dx++) {
+        int nx = bx + dx;
+        if (nx < 0) nx += B; else if (nx >= B) nx -= B;
+        for (int dy = -1; dy <= 1; dy++) {
+            int ny = by + dy;
+            if (ny < 0) ny += B; else if (ny >= B) ny -= B;
+            int nb = ny * B + nx;
+            bool dup = false;
+            for (int t = 0; t < ns; t++) dup |= seen[t] == nb;
+            if (dup) continue;
+            seen[ns++] = nb;
+            if (nb == c2) return ns - 1;
+        }
+    }
+    return 9;
+}
+
+// Records in the compaction order of the reference (by id1, then slot):
+// slots fill in cell-scan order, and inside a cell by vertex id.
+int build_compact(pcp_model* m, std::vector<size_t>& order,
+                  const std::vector<unsigned long long>& key, std::vector<int>& id1s,
+                  std::vector<int>& nids, std::vector<uint8_t>& ins) {
+    size_t I = key.size();
+    std::vector<int> cells(m->V);
+    if (m->V > 0)
+        CK(cudaMemcpy(cells.data(), m->cellLocation, m->V * sizeof(int), cudaMemcpyDeviceToHost));
+    id1s.resize(I); nids.resize(I); ins.resize(I);
+    std::vector<long long> sortKey(I);
+    int B = std::max(1, m->boxSize);
+    for (size_t r = 0; r < I; ++r) {
+        int a, b; bool in;
+        record_vertices(m->startHost, key[r], a, b, in);
+        id1s[r] = a; nids[r] = b; ins[r] = in ? 1 : 0;
+        int rank = (a < m->V && b < m->V) ? visit_rank(cells[a], cells[b], B) : 9;
+        sortKey[r] = ((long long)a << 36) | ((long long)rank << 32) | (long long)(unsigned)b;
+    }
+    order.resize(I);
+    std::iota(order.begin(), order.end(), 0);
+    std::sort(order.begin(), order.end(), [&](size_t x, size_t y) { return sortKey[x] < sortKey[y]; });
+    return PCP_OK;
+}
+
+// Canonical final order (model.cpp:354-360): keys sorted, then stably by the
+// low 48 bits, i.e. ascending (si, i, j) with ties in ascending sj.
+void final_order(const std::vector<unsigned long long>& key, std::vector<size_t>& order) {
+    order.resize(key.size());
+    std::iota(order.begin(), order.end(), 0);
+    std::sort(order.begin(), order.end(), [&](size_t a, size_t b) {
+        unsigned long long la = key[a] & 0xFFFFFFFFFFFFull, lb = key[b] & 0xFFFFFFFFFFFFull;
+        if (la != lb) return la < lb;
+        return key[a] < key[b];
+    });
+}
+
+int ensure_records(pcp_model* m) {
+    if (m->recordsCached) return PCP_OK;
+    std::vector<unsigned long long> key, outer;
+    std::vector<float2> tu, ut;
+    int rc = fetch_records(m, key, outer, tu, ut);
+    if (rc) return rc;
+    std::vector<size_t> order;
+    if (m->view == pcp_model::VIEW_COMPACT) {
+        std::vector<int> a, b;
+        std::vector<uint8_t> in;
+        rc = build_compact(m, order, key, a, b, in);
+        if (rc) return rc;
+    } else {
+        final_order(key, order);
+    }
+    size_t I = key.size();
+    m->hKey.resize(I); m->hOuter.resize(I); m->hTU.resize(I); m->hUT.resize(I);
+    for (size_t r = 0; r < I; ++r) {
+        m->hKey[r] = key[order[r]];
+        m->hOuter[r] = outer[order[r]];
+        m->hTU[r] = tu[order[r]];
+        m->hUT[r] = ut[order[r]];
+    }
+    // permutation of the reference's last sort (bits [0,48) over the 64-bit order)
+    std::vector<size_t> o64(I);
+    std::iota(o64.begin(), o64.end(), 0);
+    std::sort(o64.begin(), o64.end(), [&](size_t a, size_t b) { return key[a] < key[b]; });
+    std::vector<uint32_t> perm(I);
+    std::iota(perm.begin(), perm.end(), 0u);
+    std::stable_sort(perm.begin(), perm.end(), [&](uint32_t a, uint32_t b) {
+        return (key[o64[a]] & 0xFFFFFFFFFFFFull) < (key[o64[b]] & 0xFFFFFFFFFFFFull);
+    });
+    m->hKeys = perm;
+    m->recordsCached = true;
+    return PCP_OK;
+}
+
+// per-vertex slot arrays of updateNeighborsKernel (kernels.cuh:792-811)
+int ensure_neighbors(pcp_model* m) {
+    if (m->neighborsCached) return PCP_OK;
+    std::vector<unsigned long long> key, outer;
+    std::vector<float2> tu, ut;
+    int rc = fetch_records(m, key, outer, tu, ut);
+    if (rc) return rc;
+    std::vector<size_t> order;
+    std::vector<int> a, b;
+    std::vector<uint8_t> in;
+    rc = build_compact(m, order, key, a, b, in);
+    if (rc) return rc;
+    std::vector<int> count(m->V, 0);
+    for (size_t r = 0; r < key.size(); ++r) if (a[r] < m->V) count[a[r]]++;
+    int need = 0;
+    for (int c : count) need = std::max(need, c);
+    if (need > m->maxNeighbors) {
+        fprintf(stderr, "Warning: neighbor buffer overflow: maxNeighbors=%d required=%d. "
+                        "Resizing and retrying.\n", m->maxNeighbors, need);
+        m->maxNeighbors = std::max(m->maxNeighbors * 2 + 1, need);
+    }
+    int M = m->maxNeighbors;
+    m->hNeighbors.assign((size_t)m->V * M, 0);
+    m->hInside.assign((size_t)m->V * M, 0);
+    m->hNumNeighbors.assign(m->V, 0);
+    m->hShapeCounts.assign(m->P, 0);
+    for (size_t t = 0; t < order.size(); ++t) {
+        size_t r = order[t];
+        int v = a[r];
+        if (v >= m->V) continue;
+        int s = m->hNumNeighbors[v]++;
+        if (s < M) {
+            m->hNeighbors[(size_t)v * M + s] = b[r];
+            m->hInside[(size_t)v * M + s] = in[r];
+        }
+        int si = (int)((key[r] >> 32) & 0xFFFF);
+        if (si < m->P) m->hShapeCounts[si]++;
+    }
+    m->neighborsCached = true;
+    return PCP_OK;
+}
+
+template <typename T>
+int copy_out(const T* src, int n, T* out, int cap, int* len_out) {
+    if (len_out) *len_out = n;
+    if (!out) return PCP_OK;
+    if (cap < n) return fail(PCP_ERR_ARG, "output buffer holds %d elements, %d needed", cap, n);
+    if (n > 0) memcpy(out, src, (size_t)n * sizeof(T));
+    return PCP_OK;
+}
+
+template <typename T>
+int copy_dev_out(pcp_model* m, const T* dsrc, int n, T* out, int cap, int* len_out) {
+    if (len_out) *len_out = n;
+    if (!out) return PCP_OK;
+    if (cap < n) return fail(PCP_ERR_ARG, "output buffer holds %d elements, %d needed", cap, n);
+    int rc = sync(m);
+    if (rc) return rc;
+    if (n > 0) CK(cudaMemcpy(out, dsrc, (size_t)n * sizeof(T), cudaMemcpyDeviceToHost));
+    return PCP_OK;
+}
+
+int upload(pcp_model* m, void* dst, const void* src, size_t bytes) {
+    if (bytes == 0) return PCP_OK;
+    CK(cudaMemcpyAsync(dst, src, bytes, cudaMemcpyHostToDevice, m->stream));
+    return sync(m);
+}
+
+// ---- the force evaluation (Model::updateForceEnergy, model.cpp:363-395) ----
+int force_energy(pcp_model* m, const int* gate) {
+    CK(launch_zero_force(m->force, m->V, m->ctrl, gate, m->stream));
+    m->launches++;
+    int t = m->modelType;
+    bool overlap = (t == PCP_MODEL_NORMAL || t == PCP_MODEL_HYBRID);
+    bool edge = (t == PCP_MODEL_SOFT_BODY || t == PCP_MODEL_EDGE_ONLY || t == PCP_MODEL_HYBRID);
+    bool area = (t == PCP_MODEL_SOFT_BODY || t == PCP_MODEL_AREA_ONLY || t == PCP_MODEL_HYBRID);
+    if (overlap) {
+        CK(launch_overlap_force(m->pos, m->start, m->next, m->V, m->ws, m->ctrl, m->force, gate,
+                                m->stream));
+        m->launches++;
+    }
+    if (edge) {
+        CK(launch_soft_edge(m->pos, m->targetEdge, m->edgeLengths, m->next, m->prev, m->shapeId,
+                            m->V, m->stiffness, reinterpret_cast<double*>(m->force),
+                            &m->ctrl->energy, gate, m->stream));
+        m->launches++;
+    }
+    if (area) {
+        CK(launch_soft_area(m->pos, m->shapeId, m->next, m->prev, m->areas, m->targetAreas,
+                            m->start, m->V, m->compressibility, reinterpret_cast<double*>(m->force),
+                            &m->ctrl->energy, gate, m->stream));
+        m->launches++;
+    }
+    return PCP_OK;
+}
+
+int geometry(pcp_model* m, const int* gate) {
+    CK(launch_geometry(m->pos, m->start, m->P, m->V, m->edgeLengths, m->areas, m->comX, m->comY,
+                       m->perimeters, m->constraints, m->maxEdge, gate, m->stream));
+    m->launches += 2;
+    return PCP_OK;
+}
+
+// ---- FIRE step graph ------------------------------------------------------
+int record_fire_step(pcp_model* m) {
+    const int* gA = &m->ctrl->active;
+    const int* gRetry = &m->ctrl->retryGate;
+    const int* gRb = &m->ctrl->rbGate;
+    cudaStream_t st = m->stream;
+    bool needsI = (m->modelType == PCP_MODEL_NORMAL || m->modelType == PCP_MODEL_HYBRID);
+    bool rigid = (m->modelType == PCP_MODEL_NORMAL);
+    int V = m->V;
+    CK(launch_fire_reset(m->ctrl, gA, st));
+    CK(cudaMemcpyAsync(m->velSnap, m->vel, V * sizeof(double2), cudaMemcpyDeviceToDevice, st));
+    CK(cudaMemcpyAsync(m->forceSnap, m->force, V * sizeof(double2), cudaMemcpyDeviceToDevice, st));
+    CK(launch_fire_begin(m->pos, m->vel, m->force, m->posTMP2, V, m->ctrl, gA, st));
+    if (needsI) {
+        CK(launch_neighbor_cells(m->pos, m->start, m->shapeId, V, m->boxSize, m->cellLocation, gA, st));
+        CK(launch_contacts(m->pos, m->start, m->shapeId, m->cellLocation, m->P, V, m->boxSize,
+                           m->ws, m->ctrl, gA, st));
+        if (rigid && m->fireShakeIter > 0) {
+            CK(cudaMemcpyAsync(m->posTMP, m->pos, V * sizeof(double2), cudaMemcpyDeviceToDevice, st));
+            CK(launch_shake(m->pos, m->start, m->P, m->targetEdge, m->targetAreas, m->fireShakeIter,
+                            1e-15, &m->ctrl->shakeIters1, m->scratch, V, gA, st));
+            CK(launch_fire_shake_check(m->ctrl, 1, gA, st));
+            CK(launch_shake(m->pos, m->start, m->P, m->targetEdge, m->targetAreas,
+                            m->fireShakeIter * 10, 1e-15, &m->ctrl->shakeIters2, m->scratch, V,
+                            gRetry, st));
+            CK(launch_fire_shake_check(m->ctrl, 2, gA, st));
+            CK(launch_fire_after_shake(m->pos, m->vel, m->posTMP2, m->posTMP, V, m->ctrl, gA, st));
+        }
+    }
+    int rc = geometry(m, gA);
+    if (rc) return rc;
+    if (needsI) CK(launch_contacts_finish(m->start, m->ws, m->ctrl, gA, st));
+    rc = force_energy(m, gA);
+    if (rc) return rc;
+    if (rigid) {
+        CK(launch_project(m->pos, m->start, m->P, m->constraints, m->force, m->scratch, V, m->ctrl,
+                          gA, m->vel, st));
+    } else {
+        CK(launch_fire_velocity(m->vel, m->force, V, m->ctrl, gA, st));
+    }
+    // energy-increase rollback (model.cpp:450-470), gated on rbGate
+    CK(launch_fire_rollback(m->pos, m->vel, m->force, m->posTMP2, V, m->ctrl, gRb, st));
+    rc = geometry(m, gRb);
+    if (rc) return rc;
+    if (needsI) {
+        CK(launch_neighbor_cells(m->pos, m->start, m->shapeId, V, m->boxSize, m->cellLocation, gRb, st));
+        CK(launch_contacts(m->pos, m->start, m->shapeId, m->cellLocation, m->P, V, m->boxSize,
+                           m->ws, m->ctrl, gRb, st));
+        CK(launch_contacts_finish(m->start, m->ws, m->ctrl, gRb, st));
+    }
+    rc = force_energy(m, gRb);
+    if (rc) return rc;
+    if (rigid) {
+        CK(launch_project(m->pos, m->start, m->P, m->constraints, m->force, m->scratch, V, m->ctrl,
+                          gRb, m->vel, st));
+    } else {
+        CK(launch_fire_maxf(m->force, V, m->ctrl, gRb, st));
+    }
+    CK(launch_fire_finish(m->vel, m->force, V, m->ctrl, gA, st));
+    return PCP_OK;
+}
+
+int build_fire_graph(pcp_model* m, int shakeIter) {
+    if (m->fireExec && m->fireGen == m->generation && m->fireShakeIter == shakeIter &&
+        m->fireModel == m->modelType && m->fireB == m->boxSize)
+        return PCP_OK;
+    if (m->fireExec) { cudaGraphExecDestroy(m->fireExec); m->fireExec = nullptr; }
+    m->fireShakeIter = shakeIter;
+    cudaStream_t cap = nullptr;
+    CK(cudaStreamCreateWithFlags(&cap, cudaStreamNonBlocking));
+    cudaStream_t saved = m->stream;
+    m->stream = cap;
+    cudaGraph_t g = nullptr;
+    cudaError_t e = cudaStreamBeginCapture(cap, cudaStreamCaptureModeThreadLocal);
+    int rc = PCP_OK;
+    if (e == cudaSuccess) {
+        rc = record_fire_step(m);
+        e = cudaStreamEndCapture(cap, &g);
+    }
+    m->stream = saved;
+    cudaStreamDestroy(cap);
+    if (rc) { if (g) cudaGraphDestroy(g); return rc; }
+    if (e != cudaSuccess) return fail(PCP_ERR_CUDA, "graph capture failed: %s", cudaGetErrorString(e));
+    e = cudaGraphInstantiate(&m->fireExec, g, 0);
+    cudaGraphDestroy(g);
+    if (e != cudaSuccess) return fail(PCP_ERR_CUDA, "graph instantiate failed: %s", cudaGetErrorString(e));
+    m->fireGen = m->generation;
+    m->fireModel = m->modelType;
+    m->fireB = m->boxSize;
+    return PCP_OK;
+}
+
+struct FireParams {
+    double dt, alpha, dtMax, alphaStart, fAlpha, fInc, fDec, threshold;
+    int nPos, nMin, shakeIter, stepLimit;
+};
+
+// write the step parameters into the device control block
+int set_fire_params(pcp_model* m, const FireParams& f, bool resetRun) {
+    int rc = read_ctrl(m);
+    if (rc) return rc;
+    Ctrl& c = *m->ctrlHost;
+    c.dt = f.dt; c.alpha = f.alpha; c.nPos = f.nPos;
+    c.dtMax = f.dtMax; c.alphaStart = f.alphaStart; c.fAlpha = f.fAlpha; c.fInc = f.fInc;
+    c.fDec = f.fDec; c.nMin = f.nMin; c.shakeIter = f.shakeIter; c.threshold = f.threshold;
+    c.active = 1;
+    if (resetRun) { c.converged = 0; c.stepsDone = 0; }
+    c.stepLimit = f.stepLimit;
+    CK(cudaMemcpyAsync(m->ctrl, m->ctrlHost, sizeof(Ctrl), cudaMemcpyHostToDevice, m->stream));
+    return sync(m);
+}
+
+// A contact buffer overflowed inside a FIRE step: the step stopped itself
+// (k_fire_scalars clears `active`).  Grow the buffers, put back the state
+// the step started from and let the caller run it again.
+int recover_fire(pcp_model* m, bool& redo) {
+    redo = false;
+    Ctrl c = *m->ctrlHost;
+    if (c.flags & kFlagCapacity)
+        return fail(PCP_ERR_CAPACITY, "a polygon pair exceeds the contact kernel limits");
+    if (!c.needsRecovery) return PCP_OK;
+    redo = true;
+    int np = std::max(m->ws.capPairs, c.numPairs) * 2 + 1024;
+    int nr = std::max(m->ws.capRecords, c.numRecords) * 2 + 4096;
+    int rc = alloc_ws(m, np, nr);
+    if (rc) return rc;
+    size_t b = (size_t)m->V * sizeof(double2);
+    CK(cudaMemcpyAsync(m->pos, m->posTMP2, b, cudaMemcpyDeviceToDevice, m->stream));
+    CK(cudaMemcpyAsync(m->vel, m->velSnap, b, cudaMemcpyDeviceToDevice, m->stream));
+    CK(cudaMemcpyAsync(m->force, m->forceSnap, b, cudaMemcpyDeviceToDevice, m->stream));
+    c.energy = c.ePre;
+    c.dt = c.snapDt; c.alpha = c.snapAlpha; c.nPos = c.snapNPos;
+    c.flags = 0; c.needsRecovery = 0; c.active = 1;
+    *m->ctrlHost = c;
+    CK(cudaMemcpyAsync(m->ctrl, m->ctrlHost, sizeof(Ctrl), cudaMemcpyHostToDevice, m->stream));
+    rc = sync(m);
+    if (rc) return rc;
+    return build_fire_graph(m, m->fireShakeIter);
+}
+
+int fire_step_once(pcp_model* m, const FireParams& fp, double out[4]) {
+    int rc = build_fire_graph(m, fp.shakeIter);
+    if (rc) return rc;
+    rc = set_fire_params(m, fp, true);
+    if (rc) return rc;
+    for (int attempt = 0; attempt < 6; ++attempt) {
+        CK(cudaGraphLaunch(m->fireExec, m->stream));
+        m->launches += 1;
+        rc = read_ctrl(m);
+        if (rc) return rc;
+        bool redo = false;
+        rc = recover_fire(m, redo);
+        if (rc) return rc;
+        if (!redo) {
+            const Ctrl& c = *m->ctrlHost;
+            out[0] = c.outE; out[1] = c.dt; out[2] = c.alpha; out[3] = c.nPos;
+            m->lastShakeIters = c.shakeLast;
+            m->numIntersections = c.numRecords;
+            m->view = pcp_model::VIEW_FINAL;
+            m->invalidate();
+            return PCP_OK;
+        }
+    }
+    return fail(PCP_ERR_CAPACITY, "FIRE step: contact buffers could not be sized");
+}
+
+}  // namespace
+
+// =========================================================================
+// C ABI
+// =========================================================================
+extern "C" {
+
+const char* pcp_last_error(void) { return g_err.c_str(); }
+const char* pcp_version(void) { return "pcp_gb300 0.1 (sm_103a)"; }
+
+#define CHECK_M(m) do { if (!(m)) return fail(PCP_ERR_ARG, "null model"); } while (0)
+
+int pcp_model_create(int size, pcp_model** out) {
+    if (!out) return fail(PCP_ERR_ARG, "null output");
+    *out = nullptr;
+    if (size < 0) return fail(PCP_ERR_ARG, "negative size");
+    CK(cudaFree(0));
+    pcp_model* m = new pcp_model();
+    m->V = size;
+    int rc = alloc_vertex(m);
+    if (!rc) {
+        cudaError_t e = dalloc(&m->ctrl, 1);
+        if (e == cudaSuccess) e = cudaMallocHost((void**)&m->ctrlHost, sizeof(Ctrl));
+        if (e == cudaSuccess) memset(m->ctrlHost, 0, sizeof(Ctrl));
+        if (e == cudaSuccess) e = dalloc(&m->maxEdge, 1);
+        if (e == cudaSuccess) e = dalloc(&m->dtmp, 1);
+        if (e == cudaSuccess) e = dalloc(&m->shakeIters, 1);
+        if (e == cudaSuccess) e = dalloc(&m->mcSum, 1);
+        if (e != cudaSuccess) rc = fail(PCP_ERR_CUDA, "allocation failed: %s", cudaGetErrorString(e));
+    }
+    if (!rc) {
+        cudaError_t e = contacts_init();
+        if (e != cudaSuccess) rc = fail(PCP_ERR_CUDA, "kernel setup failed: %s", cudaGetErrorString(e));
+    }
+    if (rc) { delete m; return rc; }
+    sm_count();
+    *out = m;
+    return PCP_OK;
+}
+
+int pcp_model_destroy(pcp_model* m) {
+    if (!m) return PCP_OK;
+    if (m->stream) cudaStreamSynchronize(m->stream);
+    else cudaDeviceSynchronize();
+    delete m;
+    return PCP_OK;
+}
+
+int pcp_model_set_stream(pcp_model* m, void* s) {
+    CHECK_M(m);
+    m->stream = (cudaStream_t)s;
+    return PCP_OK;
+}
+
+int pcp_model_set_num_vertices(pcp_model* m, int n) {
+    CHECK_M(m);
+    if (n < 0) return fail(PCP_ERR_ARG, "negative vertex count");
+    int rc = sync(m);
+    if (rc) return rc;
+    m->V = n;
+    m->invalidate();
+    return alloc_vertex(m);
+}
+
+int pcp_model_set_positions(pcp_model* m, const double* host, int len) {
+    CHECK_M(m);
+    if (len != 2 * m->V) {
+        printf("Update numVertices before setting the positions\n");   // model.cpp:524
+        fflush(stdout);
+        return fail(PCP_ERR_ARG, "positions hold %d values, 2*numVertices = %d", len, 2 * m->V);
+    }
+    return upload(m, m->pos, host, (size_t)len * sizeof(double));
+}
+
+int pcp_model_set_forces(pcp_model* m, const double* host, int len) {
+    CHECK_M(m);
+    if (len > 2 * m->V) len = 2 * m->V;
+    return upload(m, m->force, host, (size_t)len * sizeof(double));
+}
+
+int pcp_model_set_start_indices(pcp_model* m, const int* host, int len) {
+    CHECK_M(m);
+    if (len < 1) return fail(PCP_ERR_ARG, "startIndices needs at least one entry");
+    int P = len - 1;
+    if (P > 65535) return fail(PCP_ERR_LIMIT, "%d polygons; the packed records hold 65535", P);
+    for (int p = 0; p < P; ++p) {
+        if (host[p + 1] < host[p]) return fail(PCP_ERR_ARG, "startIndices must not decrease");
+        if (host[p + 1] - host[p] > 65535)
+            return fail(PCP_ERR_LIMIT, "polygon %d has more than 65535 vertices", p);
+    }
+    if (host[0] < 0) return fail(PCP_ERR_ARG, "startIndices[0] < 0");
+    int rc = sync(m);
+    if (rc) return rc;
+    m->P = P;
+    m->startHost.assign(host, host + len);
+    size_t Pn = (size_t)std::max(P, 1);
+    CK(dalloc(&m->start, (size_t)len));
+    CK(dalloc(&m->areas, Pn)); CK(dalloc(&m->comX, Pn)); CK(dalloc(&m->comY, Pn));
+    CK(dalloc(&m->perimeters, Pn)); CK(dalloc(&m->targetAreas, Pn)); CK(dalloc(&m->targetEdge, Pn));
+    CK(dalloc(&m->xpbdDev, 2 * Pn));
+    CK(cudaMemcpy(m->start, host, (size_t)len * sizeof(int), cudaMemcpyHostToDevice));
+    m->generation++;
+    m->topology = false;
+    m->invalidate();
+    return PCP_OK;
+}
+
+int pcp_model_set_target_areas(pcp_model* m, const double* host, int len) {
+    CHECK_M(m);
+    if (len > m->P) len = m->P;
+    return upload(m, m->targetAreas, host, (size_t)len * sizeof(double));
+}
+
+int pcp_model_set_target_edge_lengths(pcp_model* m, const double* host, int len) {
+    CHECK_M(m);
+    if (len > m->P) len = m->P;
+    return upload(m, m->targetEdge, host, (size_t)len * sizeof(double));
+}
+
+int pcp_model_set_max_edge_length(pcp_model* m, double l) {
+    CHECK_M(m);
+    double b = std::floor(1.0 / l);
+    if (!(b >= 1.0)) b = 1.0;
+    if (b > 1e7) b = 1e7;   // boxSize*boxSize must stay an int
+    m->boxSize = (int)b;
+    m->maxEdgeLengthSet = l;
+    // the reference copies the value into its device maxEdgeLength (model.cpp:515)
+    CK(cudaMemcpy(m->maxEdge, &l, sizeof(double), cudaMemcpyHostToDevice));
+    return PCP_OK;
+}
+
+int pcp_model_set_model_enum(pcp_model* m, int e) {
+    CHECK_M(m);
+    if (e < 0 || e > 5) return fail(PCP_ERR_ARG, "unknown model enum %d", e);
+    m->modelType = e;
+    return PCP_OK;
+}
+
+int pcp_model_set_stiffness(pcp_model* m, double k) { CHECK_M(m); m->stiffness = k; return PCP_OK; }
+int pcp_model_set_compressibility(pcp_model* m, double c) { CHECK_M(m); m->compressibility = c; return PCP_OK; }
+int pcp_model_get_stiffness(pcp_model* m, double* out) { CHECK_M(m); *out = m->stiffness; return PCP_OK; }
+int pcp_model_get_compressibility(pcp_model* m, double* out) { CHECK_M(m); *out = m->compressibility; return PCP_OK; }
+
+int pcp_model_initialize_neighbor_cells(pcp_model* m) {
+    CHECK_M(m);
+    if (m->P <= 0 || m->startHost.empty())
+        return fail(PCP_ERR_STATE, "setStartIndices has not been called");
+    if (m->startHost.back() > m->V)
+        return fail(PCP_ERR_ARG, "startIndices end at %d but the model has %d vertices",
+                    m->startHost.back(), m->V);
+    int rc = sync(m);
+    if (rc) return rc;
+    size_t V = (size_t)m->V;
+    CK(dalloc(&m->shapeId, V)); CK(dalloc(&m->next, V)); CK(dalloc(&m->prev, V));
+    CK(dalloc(&m->cellLocation, V));
+    int capPairs = 16 * m->P + 4096;
+    int capRecords = 8 * m->V + 16384;
+    rc = alloc_ws(m, capPairs, capRecords);
+    if (rc) return rc;
+    CK(launch_topology(m->start, m->P, m->V, m->shapeId, m->next, m->prev, m->stream));
+    m->launches++;
+    rc = sync(m);
+    if (rc) return rc;
+    m->topology = true;
+    m->numIntersections = 0;
+    m->view = pcp_model::VIEW_NONE;
+    m->invalidate();
+    // reset the record counters
+    memset(m->ctrlHost, 0, sizeof(Ctrl));
+    CK(cudaMemcpy(m->ctrl, m->ctrlHost, sizeof(Ctrl), cudaMemcpyHostToDevice));
+    return PCP_OK;
+}
+
+int pcp_model_update_polygon_geometry(pcp_model* m) {
+    CHECK_M(m);
+    int rc = need_topology(m);
+    if (rc) return rc;
+    return geometry(m, nullptr);
+}
+
+int pcp_model_update_neighbor_cells(pcp_model* m) {
+    CHECK_M(m);
+    int rc = need_topology(m);
+    if (rc) return rc;
+    CK(launch_neighbor_cells(m->pos, m->start, m->shapeId, m->V, m->boxSize, m->cellLocation,
+                             nullptr, m->stream));
+    m->launches++;
+    m->neighborsCached = false;
+    return PCP_OK;
+}
+
+int pcp_model_update_neighbors(pcp_model* m) {
+    CHECK_M(m);
+    int rc = need_topology(m);
+    if (rc) return rc;
+    rc = run_contacts(m);
+    m->view = pcp_model::VIEW_COMPACT;
+    m->invalidate();
+    return rc;
+}
+
+int pcp_model_update_valid_and_counts(pcp_model* m) {
+    CHECK_M(m);
+    int rc = read_ctrl(m);
+    if (rc) return rc;
+    m->numIntersections = m->ctrlHost->numRecords;
+    return PCP_OK;
+}
+
+int pcp_model_update_compacted_intersections(pcp_model* m) {
+    CHECK_M(m);
+    int rc = read_ctrl(m);
+    if (rc) return rc;
+    m->numIntersections = m->ctrlHost->numRecords;
+    m->view = pcp_model::VIEW_COMPACT;
+    m->recordsCached = false;
+    return PCP_OK;
+}
+
+int pcp_model_update_outersections(pcp_model* m) {
+    CHECK_M(m);
+    int rc = need_topology(m);
+    if (rc) return rc;
+    CK(launch_contacts_finish(m->start, m->ws, m->ctrl, nullptr, m->stream));
+    m->launches++;
+    rc = read_ctrl(m);
+    if (rc) return rc;
+    m->numIntersections = m->ctrlHost->numRecords;
+    m->view = pcp_model::VIEW_FINAL;
+    m->recordsCached = false;
+    return PCP_OK;
+}
+
+int pcp_model_update_force_energy(pcp_model* m) {
+    CHECK_M(m);
+    int rc = need_topology(m);
+    if (rc) return rc;
+    return force_energy(m, nullptr);
+}
+
+int pcp_model_project_force(pcp_model* m) {
+    CHECK_M(m);
+    int rc = need_topology(m);
+    if (rc) return rc;
+    CK(launch_project(m->pos, m->start, m->P, m->constraints, m->force, m->scratch, m->V, nullptr,
+                      nullptr, nullptr, m->stream));
+    m->launches++;
+    return PCP_OK;
+}
+
+int pcp_model_shake_project(pcp_model* m, int n_iter, double tol, int* iters_out) {
+    CHECK_M(m);
+    int rc = need_topology(m);
+    if (rc) return rc;
+    int it = 0;
+    if (m->P > 0 && n_iter > 0) {
+        CK(cudaMemsetAsync(m->shakeIters, 0, sizeof(int), m->stream));
+        CK(launch_shake(m->pos, m->start, m->P, m->targetEdge, m->targetAreas, n_iter, tol,
+                        m->shakeIters, m->scratch, m->V, nullptr, m->stream));
+        m->launches++;
+        CK(cudaMemcpyAsync(&it, m->shakeIters, sizeof(int), cudaMemcpyDeviceToHost, m->stream));
+        rc = sync(m);
+        if (rc) return rc;
+    }
+    m->lastShakeIters = it;
+    if (iters_out) *iters_out = it;
+    return PCP_OK;
+}
+
+int pcp_model_xpbd_project(pcp_model* m, int n_iter, double tol, int* iters_out) {
+    CHECK_M(m);
+    int rc = need_topology(m);
+    if (rc) return rc;
+    int iter = 0;
+    std::vector<double> dev(2 * (size_t)m->P);
+    for (; iter < n_iter; ++iter) {
+        CK(launch_xpbd_iteration(m->pos, m->start, m->P, m->targetEdge, m->targetAreas, m->xpbdDev,
+                                 m->stream));
+        m->launches++;
+        if (tol > 0) {
+            rc = sync(m);
+            if (rc) return rc;
+            CK(cudaMemcpy(dev.data(), m->xpbdDev, dev.size() * sizeof(double), cudaMemcpyDeviceToHost));
+            double me = 0, ma = 0;
+            for (int p = 0; p < m->P; ++p) { me = std::max(me, dev[2 * p]); ma = std::max(ma, dev[2 * p + 1]); }
+            if (me < tol && ma < tol) break;
+        }
+    }
+    rc = sync(m);
+    if (iters_out) *iters_out = iter;
+    return rc;
+}
+
+int pcp_model_update_positions(pcp_model* m, double dt) {
+    CHECK_M(m);
+    CK(launch_update_positions(reinterpret_cast<double*>(m->pos), reinterpret_cast<const double*>(m->force),
+                               m->V, dt, m->stream));
+    m->launches++;
+    return PCP_OK;
+}
+
+int pcp_model_reset_velocities(pcp_model* m) {
+    CHECK_M(m);
+    CK(cudaMemsetAsync(m->vel, 0, (size_t)m->V * sizeof(double2), m->stream));
+    return PCP_OK;
+}
+
+int pcp_model_reset_areas(pcp_model* m) {
+    CHECK_M(m);
+    int rc = need_topology(m);
+    if (rc) return rc;
+    CK(launch_reset_areas(reinterpret_cast<double*>(m->pos), m->shapeId, m->areas, m->targetAreas,
+                          m->comX, m->comY, m->V, m->stream));
+    m->launches++;
+    return PCP_OK;
+}
+
+int pcp_model_save_tentative_positions(pcp_model* m) {
+    CHECK_M(m);
+    CK(cudaMemcpyAsync(m->posTent, m->pos, (size_t)m->V * sizeof(double2), cudaMemcpyDeviceToDevice,
+                       m->stream));
+    return PCP_OK;
+}
+
+int pcp_model_get_max_effective_force(pcp_model* m, double dt, int minimizer, double* out) {
+    CHECK_M(m);
+    double scale = (minimizer == PCP_MINIMIZER_GD) ? (1.0 / dt) : (2.0 / (dt * dt));
+    CK(launch_max_effective_force(reinterpret_cast<const double*>(m->pos),
+                                  reinterpret_cast<const double*>(m->posTent),
+                                  reinterpret_cast<const double*>(m->force), m->V, scale, m->dtmp,
+                                  m->stream));
+    m->launches++;
+    CK(cudaMemcpyAsync(out, m->dtmp, sizeof(double), cudaMemcpyDeviceToHost, m->stream));
+    return sync(m);
+}
+
+int pcp_model_sort_keys(pcp_model* m, int end_bit) {
+    CHECK_M(m);
+    int rc = ensure_records(m);
+    if (rc) return rc;
+    size_t I = m->hKey.size();
+    unsigned long long mask = end_bit >= 64 ? ~0ull : ((1ull << std::max(end_bit, 0)) - 1ull);
+    std::vector<uint32_t> perm(I);
+    std::iota(perm.begin(), perm.end(), 0u);
+    std::stable_sort(perm.begin(), perm.end(), [&](uint32_t a, uint32_t b) {
+        return (m->hKey[a] & mask) < (m->hKey[b] & mask);
+    });
+    std::vector<unsigned long long> k2(I);
+    for (size_t i = 0; i < I; ++i) k2[i] = m->hKey[perm[i]];
+    m->hKey.swap(k2);
+    m->hKeys = perm;
+    return PCP_OK;
+}
+
+int pcp_model_update_overlap_area(pcp_model* m, int pd) {
+    CHECK_M(m);
+    int rc = need_topology(m);
+    if (rc) return rc;
+    if (pd <= 0) return fail(PCP_ERR_ARG, "point density must be positive");
+    // vertex-level sorted cell list (model.cu:308-385) for the Monte-Carlo scan
+    std::vector<int> cells(m->V);
+    rc = sync(m);
+    if (rc) return rc;
+    CK(cudaMemcpy(cells.data(), m->cellLocation, m->V * sizeof(int), cudaMemcpyDeviceToHost));
+    int B = std::max(1, m->boxSize), nb = B * B;
+    std::vector<int> cnt(nb + 1, 0), idx(m->V);
+    for (int i = 0; i < m->V; ++i) cnt[std::min(std::max(cells[i], 0), nb - 1) + 1]++;
+    for (int c = 0; c < nb; ++c) cnt[c + 1] += cnt[c];
+    std::vector<int> starts(cnt.begin(), cnt.end() - 1);
+    std::vector<int> fill = starts;
+    for (int i = 0; i < m->V; ++i) idx[fill[std::min(std::max(cells[i], 0), nb - 1)]++] = i;
+    CK(dalloc(&m->mcNbIdx, (size_t)m->V));
+    CK(dalloc(&m->mcBoxStarts, (size_t)nb));
+    CK(cudaMemcpy(m->mcNbIdx, idx.data(), m->V * sizeof(int), cudaMemcpyHostToDevice));
+    CK(cudaMemcpy(m->mcBoxStarts, starts.data(), nb * sizeof(int), cudaMemcpyHostToDevice));
+    if (pd != m->pointDensity) {
+        CK(dalloc(&m->mcCounter, (size_t)pd * pd));
+        m->pointDensity = pd;
+    }
+    CK(launch_overlap_area_mc(m->pos, m->start, m->shapeId, m->mcNbIdx, m->mcBoxStarts, m->V, B,
+                              pd, m->mcCounter, m->mcSum, m->stream));
+    m->launches++;
+    unsigned long long s = 0;
+    CK(cudaMemcpyAsync(&s, m->mcSum, sizeof(s), cudaMemcpyDeviceToHost, m->stream));
+    rc = sync(m);
+    if (rc) return rc;
+    m->overlapArea = (double)s / ((double)pd * (double)pd);
+    return PCP_OK;
+}
+
+int pcp_model_fire_step(pcp_model* m, double dt, double alpha, int n_pos, double dt_max,
+                        double alpha_start, double f_alpha, double f_inc, double f_dec, int n_min,
+                        int shake_iter, double out[4]) {
+    CHECK_M(m);
+    int rc = need_topology(m);
+    if (rc) return rc;
+    FireParams fp{dt, alpha, dt_max, alpha_start, f_alpha, f_inc, f_dec, -1.0,
+                  n_pos, n_min, shake_iter, 0};
+    return fire_step_once(m, fp, out);
+}
+
+int pcp_model_minimize_fire(pcp_model* m, double thr, double dt0, int max_steps, double dt_max,
+                            double alpha_start, double f_alpha, double f_inc, double f_dec,
+                            int n_min, int shake_iter, double out[3]) {
+    CHECK_M(m);
+    int rc = need_topology(m);
+    if (rc) return rc;
+    // Model::minimizeFIRE (model.cpp:488-504)
+    rc = pcp_model_reset_velocities(m);
+    if (rc) return rc;
+    rc = geometry(m, nullptr);
+    if (rc) return rc;
+    rc = force_energy(m, nullptr);
+    if (rc) return rc;
+    bool rigid = m->modelType == PCP_MODEL_NORMAL;
+    if (rigid) {
+        rc = pcp_model_project_force(m);
+        if (rc) return rc;
+    }
+    FireParams fp{dt0, alpha_start, dt_max, alpha_start, f_alpha, f_inc, f_dec, thr,
+                  0, n_min, shake_iter, max_steps};
+    rc = build_fire_graph(m, shake_iter);
+    if (rc) return rc;
+    rc = set_fire_params(m, fp, true);
+    if (rc) return rc;
+    if (max_steps <= 0) {
+        out[0] = m->ctrlHost->energy; out[1] = dt0; out[2] = 0;
+        return PCP_OK;
+    }
+    // Steps are launched in chunks; a step that finds the stop test true (or
+    // the step limit) clears `active`, and every later launch is a no-op.
+    const int chunk = 32;
+    int recoveries = 0;
+    for (;;) {
+        int left = max_steps - m->ctrlHost->stepsDone;
+        int todo = std::min(chunk, left);
+        if (todo <= 0) break;
+        for (int s = 0; s < todo; ++s) CK(cudaGraphLaunch(m->fireExec, m->stream));
+        m->launches += todo;
+        rc = read_ctrl(m);
+        if (rc) return rc;
+        bool redo = false;
+        rc = recover_fire(m, redo);
+        if (rc) return rc;
+        if (redo) {
+            if (++recoveries > 16) return fail(PCP_ERR_CAPACITY, "contact buffers could not be sized");
+            continue;
+        }
+        if (!m->ctrlHost->active) break;
+    }
+    const Ctrl& c = *m->ctrlHost;
+    m->lastShakeIters = c.shakeLast;
+    m->numIntersections = c.numRecords;
+    m->view = pcp_model::VIEW_FINAL;
+    m->invalidate();
+    out[0] = c.converged ? c.outE : c.energy;
+    out[1] = c.dt;
+    out[2] = c.stepsDone;
+    return PCP_OK;
+}
+
+// ---- scalar getters ----
+int pcp_model_get_num_vertices(pcp_model* m, int* out) { CHECK_M(m); *out = m->V; return PCP_OK; }
+int pcp_model_get_num_polygons(pcp_model* m, int* out) { CHECK_M(m); *out = m->P; return PCP_OK; }
+int pcp_model_get_num_intersections(pcp_model* m, int* out) { CHECK_M(m); *out = m->numIntersections; return PCP_OK; }
+int pcp_model_get_max_neighbors(pcp_model* m, int* out) {
+    CHECK_M(m);
+    if (m->topology && m->view != pcp_model::VIEW_NONE) {
+        int rc = ensure_neighbors(m);
+        if (rc) return rc;
+    }
+    *out = m->maxNeighbors;
+    return PCP_OK;
+}
+int pcp_model_get_box_size(pcp_model* m, int* out) { CHECK_M(m); *out = m->boxSize; return PCP_OK; }
+int pcp_model_get_model_enum(pcp_model* m, int* out) { CHECK_M(m); *out = m->modelType; return PCP_OK; }
+int pcp_model_get_last_shake_iters(pcp_model* m, int* out) { CHECK_M(m); *out = m->lastShakeIters; return PCP_OK; }
+int pcp_model_get_energy(pcp_model* m, double* out) {
+    CHECK_M(m);
+    int rc = read_ctrl(m);
+    if (rc) return rc;
+    *out = m->ctrlHost->energy;
+    return PCP_OK;
+}
+int pcp_model_get_max_unbalanced_force(pcp_model* m, double* out) {
+    CHECK_M(m);
+    CK(launch_max_abs(reinterpret_cast<const double*>(m->force), 2 * m->V, m->dtmp, m->stream));
+    m->launches++;
+    CK(cudaMemcpyAsync(out, m->dtmp, sizeof(double), cudaMemcpyDeviceToHost, m->stream));
+    return sync(m);
+}
+int pcp_model_get_max_edge_length(pcp_model* m, double* out) {
+    CHECK_M(m);
+    CK(cudaMemcpyAsync(out, m->maxEdge, sizeof(double), cudaMemcpyDeviceToHost, m->stream));
+    return sync(m);
+}
+int pcp_model_get_overlap_area(pcp_model* m, double* out) { CHECK_M(m); *out = m->overlapArea; return PCP_OK; }
+
+// ---- array getters ----
+int pcp_model_get_positions(pcp_model* m, double* out, int cap, int* len) {
+    CHECK_M(m); return copy_dev_out(m, reinterpret_cast<const double*>(m->pos), 2 * m->V, out, cap, len);
+}
+int pcp_model_get_forces(pcp_model* m, double* out, int cap, int* len) {
+    CHECK_M(m); return copy_dev_out(m, reinterpret_cast<const double*>(m->force), 2 * m->V, out, cap, len);
+}
+int pcp_model_get_velocities(pcp_model* m, double* out, int cap, int* len) {
+    CHECK_M(m); return copy_dev_out(m, reinterpret_cast<const double*>(m->vel), 2 * m->V, out, cap, len);
+}
+int pcp_model_get_areas(pcp_model* m, double* out, int cap, int* len) {
+    CHECK_M(m); return copy_dev_out(m, (const double*)m->areas, m->P, out, cap, len);
+}
+int pcp_model_get_com(pcp_model* m, double* out, int cap, int* len) {
+    CHECK_M(m);
+    if (len) *len = 2 * m->P;
+    if (!out) return PCP_OK;
+    if (cap < 2 * m->P) return fail(PCP_ERR_ARG, "output buffer too small");
+    int rc = copy_dev_out(m, (const double*)m->comX, m->P, out, cap, nullptr);
+    if (rc) return rc;
+    return copy_dev_out(m, (const double*)m->comY, m->P, out + m->P, cap - m->P, nullptr);
+}
+int pcp_model_get_perimeters(pcp_model* m, double* out, int cap, int* len) {
+    CHECK_M(m); return copy_dev_out(m, (const double*)m->perimeters, m->P, out, cap, len);
+}
+int pcp_model_get_edge_lengths(pcp_model* m, double* out, int cap, int* len) {
+    CHECK_M(m); return copy_dev_out(m, (const double*)m->edgeLengths, m->V, out, cap, len);
+}
+int pcp_model_get_constraints(pcp_model* m, double* out, int cap, int* len) {
+    CHECK_M(m); return copy_dev_out(m, (const double*)m->constraints, 6 * m->V, out, cap, len);
+}
+int pcp_model_get_target_areas(pcp_model* m, double* out, int cap, int* len) {
+    CHECK_M(m); return copy_dev_out(m, (const double*)m->targetAreas, m->P, out, cap, len);
+}
+int pcp_model_get_target_edge_lengths(pcp_model* m, double* out, int cap, int* len) {
+    CHECK_M(m); return copy_dev_out(m, (const double*)m->targetEdge, m->P, out, cap, len);
+}
+int pcp_model_get_start_indices(pcp_model* m, int* out, int cap, int* len) {
+    CHECK_M(m); return copy_out(m->startHost.data(), (int)m->startHost.size(), out, cap, len);
+}
+int pcp_model_get_shape_id(pcp_model* m, int* out, int cap, int* len) {
+    CHECK_M(m);
+    int rc = need_topology(m);
+    if (rc) return rc;
+    return copy_dev_out(m, (const int*)m->shapeId, m->V, out, cap, len);
+}
+int pcp_model_get_neighbor_cells(pcp_model* m, int* out, int cap, int* len) {
+    CHECK_M(m);
+    int rc = need_topology(m);
+    if (rc) return rc;
+    return copy_dev_out(m, (const int*)m->cellLocation, m->V, out, cap, len);
+}
+
+static int sorted_cells(pcp_model* m, std::vector<int>& idx, std::vector<int>& starts) {
+    int rc = sync(m);
+    if (rc) return rc;
+    std::vector<int> cells(m->V);
+    if (m->V) CK(cudaMemcpy(cells.data(), m->cellLocation, m->V * sizeof(int), cudaMemcpyDeviceToHost));
+    int B = std::max(1, m->boxSize), nb = B * B;
+    // stable sort of vertex ids by cell + lower bound per cell (model.cu:308-377)
+    idx.resize(m->V);
+    std::iota(idx.begin(), idx.end(), 0);
+    std::stable_sort(idx.begin(), idx.end(), [&](int a, int b) { return cells[a] < cells[b]; });
+    starts.assign(nb, 0);
+    for (int c = 0; c < nb; ++c)
+        starts[c] = (int)(std::lower_bound(idx.begin(), idx.end(), c,
+                                           [&](int v, int cc) { return cells[v] < cc; }) - idx.begin());
+    return PCP_OK;
+}
+
+int pcp_model_get_neighbor_indices(pcp_model* m, int* out, int cap, int* len) {
+    CHECK_M(m);
+    int rc = need_topology(m);
+    if (rc) return rc;
+    std::vector<int> idx, starts;
+    rc = sorted_cells(m, idx, starts);
+    if (rc) return rc;
+    return copy_out(idx.data(), (int)idx.size(), out, cap, len);
+}
+int pcp_model_get_box_counts(pcp_model* m, int* out, int cap, int* len) {
+    CHECK_M(m);
+    int rc = need_topology(m);
+    if (rc) return rc;
+    std::vector<int> idx, starts;
+    rc = sorted_cells(m, idx, starts);
+    if (rc) return rc;
+    return copy_out(starts.data(), (int)starts.size(), out, cap, len);
+}
+int pcp_model_get_neighbors(pcp_model* m, int* out, int cap, int* len) {
+    CHECK_M(m);
+    int rc = need_topology(m);
+    if (rc) return rc;
+    rc = ensure_neighbors(m);
+    if (rc) return rc;
+    return copy_out(m->hNeighbors.data(), (int)m->hNeighbors.size(), out, cap, len);
+}
+int pcp_model_get_num_neighbors(pcp_model* m, int* out, int cap, int* len) {
+    CHECK_M(m);
+    int rc = need_topology(m);
+    if (rc) return rc;
+    rc = ensure_neighbors(m);
+    if (rc) return rc;
+    return copy_out(m->hNumNeighbors.data(), (int)m->hNumNeighbors.size(), out, cap, len);
+}
+int pcp_model_get_inside_flag(pcp_model* m, uint8_t* out, int cap, int* len) {
+    CHECK_M(m);
+    int rc = need_topology(m);
+    if (rc) return rc;
+    rc = ensure_neighbors(m);
+    if (rc) return rc;
+    return copy_out(m->hInside.data(), (int)m->hInside.size(), out, cap, len);
+}
+int pcp_model_get_shape_counts(pcp_model* m, int* out, int cap, int* len) {
+    CHECK_M(m);
+    int rc = need_topology(m);
+    if (rc) return rc;
+    rc = ensure_neighbors(m);
+    if (rc) return rc;
+    return copy_out(m->hShapeCounts.data(), (int)m->hShapeCounts.size(), out, cap, len);
+}
+
+static int records_or_empty(pcp_model* m) {
+    if (!m->topology || m->view == pcp_model::VIEW_NONE) {
+        m->hKey.clear(); m->hOuter.clear(); m->hTU.clear(); m->hUT.clear(); m->hKeys.clear();
+        return PCP_OK;
+    }
+    return ensure_records(m);
+}
+
+int pcp_model_get_intersections(pcp_model* m, uint64_t* out, int cap, int* len) {
+    CHECK_M(m);
+    int rc = records_or_empty(m);
+    if (rc) return rc;
+    return copy_out(reinterpret_cast<const uint64_t*>(m->hKey.data()), (int)m->hKey.size(), out, cap, len);
+}
+int pcp_model_get_outersections(pcp_model* m, uint64_t* out, int cap, int* len) {
+    CHECK_M(m);
+    int rc = records_or_empty(m);
+    if (rc) return rc;
+    return copy_out(reinterpret_cast<const uint64_t*>(m->hOuter.data()), (int)m->hOuter.size(), out, cap, len);
+}
+static int tu_out(const std::vector<float2>& v, double* out, int cap, int* len) {
+    int n = 2 * (int)v.size();
+    if (len) *len = n;
+    if (!out) return PCP_OK;
+    if (cap < n) return fail(PCP_ERR_ARG, "output buffer too small");
+    for (size_t i = 0; i < v.size(); ++i) { out[2 * i] = (double)v[i].x; out[2 * i + 1] = (double)v[i].y; }
+    return PCP_OK;
+}
+int pcp_model_get_tu(pcp_model* m, double* out, int cap, int* len) {
+    CHECK_M(m);
+    int rc = records_or_empty(m);
+    if (rc) return rc;
+    return tu_out(m->hTU, out, cap, len);
+}
+int pcp_model_get_ut(pcp_model* m, double* out, int cap, int* len) {
+    CHECK_M(m);
+    int rc = records_or_empty(m);
+    if (rc) return rc;
+    return tu_out(m->hUT, out, cap, len);
+}
+int pcp_model_get_keys(pcp_model* m, uint32_t* out, int cap, int* len) {
+    CHECK_M(m);
+    int rc = records_or_empty(m);
+    if (rc) return rc;
+    return copy_out(m->hKeys.data(), (int)m->hKeys.size(), out, cap, len);
+}
+int pcp_model_get_intersections_counter(pcp_model* m, int* out, int cap, int* len) {
+    CHECK_M(m);
+    int n = m->pointDensity > 0 ? m->pointDensity * m->pointDensity : 0;
+    if (n == 0) { if (len) *len = 0; return PCP_OK; }
+    return copy_dev_out(m, (const int*)m->mcCounter, n, out, cap, len);
+}
+
+int pcp_model_device_positions(pcp_model* m, double** out) {
+    CHECK_M(m); *out = reinterpret_cast<double*>(m->pos); return PCP_OK;
+}
+int pcp_model_device_forces(pcp_model* m, double** out) {
+    CHECK_M(m); *out = reinterpret_cast<double*>(m->force); return PCP_OK;
+}
+int pcp_model_get_pair_count(pcp_model* m, long long* out) {
+    CHECK_M(m);
+    int rc = read_ctrl(m);
+    if (rc) return rc;
+    *out = (long long)m->ctrlHost->pairEvals;
+    return PCP_OK;
+}
+int pcp_model_get_launch_count(pcp_model* m, long long* out) {
+    CHECK_M(m); *out = m->launches; return PCP_OK;
+}
+
+// ---- stateless launchers ----
+int pcp_topology(const int* d_start, int P, int V, int* d_shape_id, int* d_next, int* d_prev,
+                 void* stream) {
+    CK(launch_topology(d_start, P, V, d_shape_id, d_next, d_prev, (cudaStream_t)stream));
+    return PCP_OK;
+}
+
+int pcp_polygon_geometry(const double* d_pos, const int* d_start, int P, int V,
+                         double* d_edge_lengths, double* d_areas, double* d_com_x, double* d_com_y,
+                         double* d_perimeters, double* d_constraints, double* d_max_edge,
+                         void* stream) {
+    CK(launch_geometry(reinterpret_cast<const double2*>(d_pos), d_start, P, V, d_edge_lengths,
+                       d_areas, d_com_x, d_com_y, d_perimeters, d_constraints, d_max_edge, nullptr,
+                       (cudaStream_t)stream));
+    return PCP_OK;
+}
+
+int pcp_neighbor_cells(const double* d_pos, const int* d_start, const int* d_shape_id, int V,
+                       int B, int* d_cell, void* stream) {
+    CK(launch_neighbor_cells(reinterpret_cast<const double2*>(d_pos), d_start, d_shape_id, V, B,
+                             d_cell, nullptr, (cudaStream_t)stream));
+    return PCP_OK;
+}
+
+// The stateless projection and SHAKE launchers need per-vertex scratch; the
+// caller's stream gets a scratch buffer of kScratchPerVertex doubles per
+// vertex that is allocated on first use and kept until the process ends.
+static double* stateless_scratch(int V) {
+    static double* buf = nullptr;
+    static size_t cap = 0;
+    size_t need = (size_t)kScratchPerVertex * (size_t)std::max(V, 1);
+    if (need > cap) {
+        if (buf) cudaFree(buf);
+        buf = nullptr;
+        if (cudaMalloc((void**)&buf, need * sizeof(double)) != cudaSuccess) { cap = 0; return nullptr; }
+        cap = need;
+    }
+    return buf;
+}
+
+int pcp_project_force(const double* d_pos, const int* d_start, int P, const double* d_constraints,
+                      double* d_force, void* stream) {
+    int V = 0;
+    if (P > 0) CK(cudaMemcpy(&V, d_start + P, sizeof(int), cudaMemcpyDeviceToHost));
+    double* s = stateless_scratch(V);
+    if (!s) return fail(PCP_ERR_CUDA, "scratch allocation failed");
+    CK(launch_project(reinterpret_cast<const double2*>(d_pos), d_start, P, d_constraints,
+                      reinterpret_cast<double2*>(d_force), s, V, nullptr, nullptr, nullptr,
+                      (cudaStream_t)stream));
+    return PCP_OK;
+}
+
+int pcp_shake_project(double* d_pos, const int* d_start, int P, const double* d_tl,
+                      const double* d_ta, int max_iter, double tol, int* d_max_iters, void* stream) {
+    int V = 0;
+    if (P > 0) CK(cudaMemcpy(&V, d_start + P, sizeof(int), cudaMemcpyDeviceToHost));
+    double* s = stateless_scratch(V);
+    if (!s) return fail(PCP_ERR_CUDA, "scratch allocation failed");
+    CK(cudaMemsetAsync(d_max_iters, 0, sizeof(int), (cudaStream_t)stream));
+    CK(launch_shake(reinterpret_cast<double2*>(d_pos), d_start, P, d_tl, d_ta, max_iter, tol,
+                    d_max_iters, s, V, nullptr, (cudaStream_t)stream));
+    return PCP_OK;
+}
+
+int pcp_update_positions(double* d_pos, const double* d_force, int V, double dt, void* stream) {
+    CK(launch_update_positions(d_pos, d_force, V, dt, (cudaStream_t)stream));
+    return PCP_OK;
+}
+
+}  // extern "C"

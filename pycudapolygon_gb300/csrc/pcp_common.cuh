@@ -1,0 +1,220 @@
+// pcp_common.cuh -- shared device code for the GB300 (sm_103a) polygon kernels.
+//
+// FP64 arithmetic here restates the reference's device functions
+// (camdennis/pyCudaPolygon src/kernels.cuh); the crossing predicate is
+// evaluated without fused multiply-adds so that its decisions and its
+// float-rounded (t, u) agree bit for bit with the FP64 restatement.
+#pragma once
+
+#include <cuda_runtime.h>
+#include <stdint.h>
+
+#include "pcp_gb300.h"
+
+#define PCP_WARP 32
+#define PCP_FULL 0xffffffffu
+
+namespace pcp {
+
+// ---------------------------------------------------------------- wraps ----
+
+// wrap (kernels.cuh:115-119): minimum image into [-0.5, 0.5).
+__device__ __forceinline__ double wrap(double x) {
+    double y = x + 1.5;
+    y = y - floor(y);
+    return y - 0.5;
+}
+
+__device__ __forceinline__ double2 wrap2(double2 v) {
+    return make_double2(wrap(v.x), wrap(v.y));
+}
+
+// FP32 minimum image for the conservative prefilters (range [-0.5, 0.5]).
+__device__ __forceinline__ float wrapf(float x) { return x - rintf(x); }
+
+// The reference's `while` wrap loops into [0,1) (kernels.cuh:670-699).  For
+// positions inside [0,1] they take at most one pass; the cap only stops
+// corrupt input from spinning (the reference would not return there).
+__device__ __forceinline__ double loop_wrap_unit(double x) {
+    int it = 0;
+    while (x < 0.0 && it < 64) { x += 1.0; ++it; }
+    while (x >= 1.0 && it < 128) { x -= 1.0; ++it; }
+    if (it >= 64 && isfinite(x) && (x < 0.0 || x >= 1.0)) x = x - floor(x);
+    return x;
+}
+
+// (int)floor(v * B) clamped into [0, B) like kernels.cuh:700-704; NaN -> 0.
+__device__ __forceinline__ int cell_coord(double v, int B) {
+    double f = floor(v * (double)B);
+    if (!(f >= 0.0)) return 0;
+    if (f >= (double)B) return B - 1;
+    return (int)f;
+}
+
+// Cell of the midpoint of the edge that starts at vertex idx
+// (updateNeighborCellsKernel, kernels.cuh:661-707).
+__device__ __forceinline__ int midpoint_cell(const double2* __restrict__ pos,
+                                             const int* __restrict__ start,
+                                             const int* __restrict__ shapeId,
+                                             int size, int idx, int B) {
+    int v2 = idx + 1;
+    if (idx == size - 1 || shapeId[idx] != shapeId[idx + 1]) v2 = start[shapeId[idx]];
+    double2 a = pos[idx], b = pos[v2];
+    double x = b.x - a.x + 0.5;
+    double y = b.y - a.y + 0.5;
+    x = loop_wrap_unit(x);
+    y = loop_wrap_unit(y);
+    x -= 0.5; y -= 0.5;
+    x /= 2.0; y /= 2.0;
+    x += a.x; y += a.y;
+    x = loop_wrap_unit(x);
+    y = loop_wrap_unit(y);
+    return cell_coord(y, B) * B + cell_coord(x, B);
+}
+
+// Cells visited by updateNeighborsKernel's 3x3 stencil (kernels.cuh:737-762):
+// every cell for B < 3, otherwise cyclic distance <= 1 on both axes.  The
+// relation is symmetric, so it can be tested from either edge.
+__device__ __forceinline__ bool cells_adjacent(int c1, int c2, int B) {
+    if (B < 3) return true;
+    int x1 = c1 % B, y1 = c1 / B, x2 = c2 % B, y2 = c2 / B;
+    int dx = x1 - x2; if (dx < 0) dx = -dx;
+    int dy = y1 - y2; if (dy < 0) dy = -dy;
+    return (dx <= 1 || dx == B - 1) && (dy <= 1 || dy == B - 1);
+}
+
+// ------------------------------------------------------ exact predicate ----
+
+// Crossing test of updateNeighborsKernel (kernels.cuh:778-807) with the edge
+// vectors precomputed as r = wrap(p2 - p), s = wrap(q2 - q).  No contraction:
+// every product and difference is rounded separately.
+struct Crossing { double tt, uu, denom; bool hit; };
+
+__device__ __forceinline__ Crossing cross_exact(double2 p, double2 r, double2 q, double2 s) {
+    Crossing c;
+    double gx = wrap(__dsub_rn(q.x, p.x));
+    double gy = wrap(__dsub_rn(q.y, p.y));
+    c.denom = __dsub_rn(__dmul_rn(r.x, s.y), __dmul_rn(r.y, s.x));
+    c.hit = false;
+    c.tt = 0.0; c.uu = 0.0;
+    if (fabs(c.denom) < 1e-12) return c;
+    double nt = __dsub_rn(__dmul_rn(gx, s.y), __dmul_rn(gy, s.x));
+    double nu = __dsub_rn(__dmul_rn(gx, r.y), __dmul_rn(gy, r.x));
+    c.tt = __ddiv_rn(nt, c.denom);
+    c.uu = __ddiv_rn(nu, c.denom);
+    c.hit = (c.tt > 0.0 && c.tt < 1.0 && c.uu > 0.0 && c.uu < 1.0);
+    return c;
+}
+
+// ---------------------------------------------------- energy functions ----
+
+// h (kernels.cuh:139-146)
+__device__ __forceinline__ double h_term(double2 p1, double2 p2, double2 sp) {
+    double r1x = wrap(p1.x - sp.x), r1y = wrap(p1.y - sp.y);
+    double r2x = wrap(p2.x - sp.x), r2y = wrap(p2.y - sp.y);
+    double dy = wrap(r2y - r1y);
+    return (r1x + r2x) * dy;
+}
+
+// g12 (kernels.cuh:148-159): g1 = (dy, -(r1x+r2x)), g2 = (dy, r1x+r2x)
+__device__ __forceinline__ void g12(double2 p1, double2 p2, double2 sp, double2& g1, double2& g2) {
+    double r1x = wrap(p1.x - sp.x);
+    double r2x = wrap(p2.x - sp.x);
+    double dy = wrap(p2.y - p1.y);
+    g1 = make_double2(dy, -(r1x + r2x));
+    g2 = make_double2(dy, r1x + r2x);
+}
+
+// h and g12 together (they share r1x, r2x).
+__device__ __forceinline__ double h_g12(double2 p1, double2 p2, double2 sp, double2& g1, double2& g2) {
+    double r1x = wrap(p1.x - sp.x), r1y = wrap(p1.y - sp.y);
+    double r2x = wrap(p2.x - sp.x), r2y = wrap(p2.y - sp.y);
+    double dyh = wrap(r2y - r1y);
+    double dyg = wrap(p2.y - p1.y);
+    double sx = r1x + r2x;
+    g1 = make_double2(dyg, -sx);
+    g2 = make_double2(dyg, sx);
+    return sx * dyh;
+}
+
+// getDf (kernels.cuh:161-222): Jacobian of f = vi + u (vzi - vi), the point
+// where edge (vi, vzi) meets edge (vj, vzj), with respect to (vi, vzi, vj,
+// vzj).  Only its contractions with a row vector g are needed; this returns
+// the four 2-vectors gT df restricted to each vertex:  out[p] = (g . df[:,2p],
+// g . df[:,2p+1]).  Zero for near-parallel or degenerate edges.
+__device__ __forceinline__ void gDf(double2 vi, double2 vzi, double2 vj, double2 vzj,
+                                    double2 g, double2 out[4]) {
+    double djx = wrap(vzj.x - vj.x), djy = wrap(vzj.y - vj.y);
+    double dix = wrap(vzi.x - vi.x), diy = wrap(vzi.y - vi.y);
+    double dijx = wrap(vj.x - vi.x), dijy = wrap(vj.y - vi.y);
+    double w = djx * diy - djy * dix;
+    double diN = dix * dix + diy * diy;
+    double djN = djx * djx + djy * djy;
+    if (w * w < 1e-12 * diN * djN || diN < 1e-28 || djN < 1e-28) {
+        out[0] = out[1] = out[2] = out[3] = make_double2(0.0, 0.0);
+        return;
+    }
+    double k = djx * dijy - djy * dijx;
+    double iw = 1.0 / w;
+    double u = k * iw;
+    // du/d(vertex p, component b) = (dk[p][b] - u dw[p][b]) / w
+    double gd = g.x * dix + g.y * diy;       // g . di
+    // vi: dk=(djy,-djx), dw=(djy,-djx)
+    double du0x = (djy - u * djy) * iw, du0y = (-djx + u * djx) * iw;
+    // vzi: dk=0, dw=(-djy, djx)
+    double du1x = (u * djy) * iw, du1y = (-u * djx) * iw;
+    // vj: dk=(-dijy-djy, djx+dijx), dw=(-diy, dix)
+    double du2x = ((-dijy - djy) + u * diy) * iw, du2y = ((djx + dijx) - u * dix) * iw;
+    // vzj: dk=(dijy,-dijx), dw=(diy,-dix)
+    double du3x = (dijy - u * diy) * iw, du3y = (-dijx + u * dix) * iw;
+    out[0] = make_double2(gd * du0x + g.x * (1.0 - u), gd * du0y + g.y * (1.0 - u));
+    out[1] = make_double2(gd * du1x + g.x * u, gd * du1y + g.y * u);
+    out[2] = make_double2(gd * du2x, gd * du2y);
+    out[3] = make_double2(gd * du3x, gd * du3y);
+}
+
+// ------------------------------------------------------- warp helpers ----
+
+__device__ __forceinline__ double warp_sum(double v) {
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(PCP_FULL, v, o);
+    return v;
+}
+__device__ __forceinline__ float warp_maxf(float v) {
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) v = fmaxf(v, __shfl_xor_sync(PCP_FULL, v, o));
+    return v;
+}
+__device__ __forceinline__ float warp_minf(float v) {
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) v = fminf(v, __shfl_xor_sync(PCP_FULL, v, o));
+    return v;
+}
+__device__ __forceinline__ double warp_maxd(double v) {
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) v = fmax(v, __shfl_xor_sync(PCP_FULL, v, o));
+    return v;
+}
+__device__ __forceinline__ int warp_sumi(int v) {
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(PCP_FULL, v, o);
+    return v;
+}
+
+// max of non-negative doubles through their bit patterns (NaN ignored).
+__device__ __forceinline__ void atomic_max_nonneg(double* addr, double v) {
+    if (!(v >= 0.0)) return;
+    atomicMax(reinterpret_cast<unsigned long long*>(addr), (unsigned long long)__double_as_longlong(v));
+}
+__device__ __forceinline__ void atomic_max_nonneg_f(float* addr, float v) {
+    if (!(v >= 0.0f)) return;
+    atomicMax(reinterpret_cast<int*>(addr), __float_as_int(v));
+}
+
+// Gate: kernels of the device-resident FIRE step run only when the flag they
+// are given is set (null = always run).
+__device__ __forceinline__ bool gate_closed(const int* gate) {
+    return gate != nullptr && *(volatile const int*)gate == 0;
+}
+
+}  // namespace pcp

@@ -1,0 +1,175 @@
+// pcp_internal.h -- internal launchers and device-state layout shared by the
+// .cu translation units and the host-side model (model.cpp).
+#pragma once
+
+#include <cuda_runtime.h>
+#include <stdint.h>
+
+#include "pcp_gb300.h"
+
+namespace pcp {
+
+// Largest polygon the warp-per-pair contact kernel stages in shared memory;
+// bigger polygons (and pairs with more crossings than a warp buffers) take
+// the block-per-pair path, which handles up to kSlowRing vertices per pair.
+constexpr int kFastRing = 128;
+constexpr int kFastRecords = 64;
+constexpr int kSlowRing = 2048;
+constexpr int kSlowRecords = 2048;
+// Largest polygon the thread-per-polygon projection / SHAKE kernels accept.
+constexpr int kMaxPolyN = 256;
+// Broad-phase grid cap per axis.
+constexpr int kGridMax = 256;
+
+// Device control block of one model (contact search counters, FIRE scalars).
+struct Ctrl {
+    // ---- contact search (zeroed at the start of each search) ----
+    int numPairs;
+    int pairCursor;
+    int numRecords;
+    int numFix;
+    int numSlow;
+    int slowCursor;
+    int numUnsafe;
+    int G;                 // broad-phase grid cells per axis
+    unsigned int flags;    // kFlag* bits
+    float Rmax;            // largest bounding radius of a well-formed polygon
+    unsigned long long maxKey;
+    // ---- energy / force ----
+    double energy;
+    double maxF;           // max |force component| after the last projection
+    // ---- FIRE scalars (the reference keeps these on the host) ----
+    double dt, alpha;
+    double ePre;
+    double P, vv, ff;
+    double dtMax, alphaStart, fAlpha, fInc, fDec;
+    double threshold;
+    double outE;           // energy the step returns
+    int nPos, nMin, shakeIter;
+    int shakeIters1, shakeIters2;
+    int shakeLast;         // iterations of the last SHAKE call
+    int needRetry;
+    int retryGate;         // gate: second SHAKE attempt
+    int shakeFailed;
+    int rollback;          // the energy-increase rollback was taken
+    int rbGate;            // gate: rollback path
+    int proceed;           // the step's FIRE velocity update ran
+    int active;            // gate: the minimisation is still running
+    int converged;
+    int stepsDone;
+    int stepLimit;
+    int errorCode;
+    int needsRecovery;     // a contact buffer overflowed during a FIRE step
+    int snapNPos;
+    double snapDt, snapAlpha;   // FIRE scalars at the start of the step
+    unsigned long long pairEvals;   // cumulative candidate pairs (a < b) examined
+};
+
+enum : unsigned int {
+    kFlagPairOverflow = 1u,
+    kFlagRecordOverflow = 2u,
+    kFlagSlowOverflow = 4u,
+    kFlagFixOverflow = 8u,
+    kFlagCapacity = 16u,    // a pair exceeds even the block-per-pair limits
+    kFlagNonFinite = 32u,
+};
+
+// Contact-search workspace (device memory owned by the model).
+struct ContactWS {
+    int V = 0, P = 0;
+    int capPairs = 0, capRecords = 0, capFix = 0, capSlow = 0;
+    double2* edgeVec = nullptr;     // [V] wrap(p_next - p)
+    float4* vtx = nullptr;          // [V] (x, y) as float, cell, 0
+    float4* polyInfo = nullptr;     // [P] centre x, y, radius, longest edge
+    int* polyFlags = nullptr;       // [P] 1 = well formed (safe for the culls)
+    int* gridCount = nullptr;       // [G*G] (G <= kGridMax)
+    int* gridStart = nullptr;       // [G*G + 1]
+    int* gridFill = nullptr;        // [G*G]
+    int* sortedPoly = nullptr;      // [P]
+    int* unsafeList = nullptr;      // [P]
+    int2* pairs = nullptr;          // [capPairs] candidate pairs a <= b
+    unsigned long long* recKey = nullptr;    // [capRecords]
+    unsigned long long* recOuter = nullptr;  // [capRecords]
+    float2* recTU = nullptr;        // [capRecords] (tu.x, tu.y) rounded to float
+    float2* recUT = nullptr;        // [capRecords]
+    int* fixList = nullptr;         // [capFix] records whose partner group is empty
+    int* slowList = nullptr;        // [capSlow] pair indices for the block path
+};
+
+// --- launchers (all asynchronous on `st`) ---
+cudaError_t launch_topology(const int* start, int P, int V, int* shapeId, int* next, int* prev,
+                            cudaStream_t st);
+cudaError_t launch_geometry(const double2* pos, const int* start, int P, int V,
+                            double* edgeLengths, double* areas, double* comX, double* comY,
+                            double* perimeters, double* constraints, double* maxEdge,
+                            const int* gate, cudaStream_t st);
+cudaError_t launch_neighbor_cells(const double2* pos, const int* start, const int* shapeId,
+                                  int V, int B, int* cellLocation, const int* gate,
+                                  cudaStream_t st);
+cudaError_t launch_update_positions(double* pos, const double* force, int V, double dt,
+                                    cudaStream_t st);
+cudaError_t launch_reset_areas(double* pos, const int* shapeId, const double* areas,
+                               const double* targetAreas, const double* comX,
+                               const double* comY, int V, cudaStream_t st);
+cudaError_t launch_max_abs(const double* x, int n, double* out, cudaStream_t st);
+cudaError_t launch_max_effective_force(const double* pos, const double* posTent,
+                                       const double* force, int V, double scale,
+                                       double* out, cudaStream_t st);
+cudaError_t launch_soft_edge(const double2* pos, const double* targetEdgeLengths,
+                             const double* edgeLengths, const int* next, const int* prev,
+                             const int* shapeId, int V, double stiffness, double* force,
+                             double* energy, const int* gate, cudaStream_t st);
+cudaError_t launch_soft_area(const double2* pos, const int* shapeId, const int* next,
+                             const int* prev, const double* areas, const double* targetAreas,
+                             const int* start, int V, double compressibility, double* force,
+                             double* energy, const int* gate, cudaStream_t st);
+cudaError_t launch_overlap_area_mc(const double2* pos, const int* start, const int* shapeId,
+                                   const int* neighborIndices, const int* boxStarts, int V,
+                                   int B, int pointDensity, int* counter,
+                                   unsigned long long* sum, cudaStream_t st);
+
+// contacts
+cudaError_t contacts_init();
+cudaError_t launch_contacts(const double2* pos, const int* start, const int* shapeId,
+                            const int* cellLocation, int P, int V, int B, ContactWS& ws,
+                            Ctrl* ctrl, const int* gate, cudaStream_t st);
+cudaError_t launch_contacts_finish(const int* start, ContactWS& ws, Ctrl* ctrl,
+                                   const int* gate, cudaStream_t st);
+cudaError_t launch_overlap_force(const double2* pos, const int* start, const int* next,
+                                 int V, ContactWS& ws, Ctrl* ctrl, double2* force,
+                                 const int* gate, cudaStream_t st);
+
+// constraints
+cudaError_t launch_project(const double2* pos, const int* start, int P,
+                           const double* constraints, double2* force, double* scratch, int V,
+                           Ctrl* fireCtrl, const int* gate, double2* vel, cudaStream_t st);
+cudaError_t launch_shake(double2* pos, const int* start, int P, const double* targetEdge,
+                         const double* targetArea, int maxIter, double tol, int* maxItersOut,
+                         double* scratch, int V, const int* gate, cudaStream_t st);
+// scratch doubles per vertex needed by launch_project / launch_shake
+constexpr int kScratchPerVertex = 17;
+cudaError_t launch_xpbd_iteration(double2* pos, const int* start, int P,
+                                  const double* targetEdge, const double* targetArea,
+                                  double* devOut, cudaStream_t st);
+
+// FIRE pieces (device-resident scalars in Ctrl)
+cudaError_t launch_fire_reset(Ctrl* c, const int* gate, cudaStream_t st);
+cudaError_t launch_fire_begin(double2* pos, double2* vel, const double2* force, double2* save,
+                              int V, Ctrl* c, const int* gate, cudaStream_t st);
+cudaError_t launch_fire_shake_check(Ctrl* c, int which, const int* gate, cudaStream_t st);
+cudaError_t launch_fire_after_shake(double2* pos, double2* vel, const double2* save,
+                                    const double2* verlet, int V, Ctrl* c, const int* gate,
+                                    cudaStream_t st);
+cudaError_t launch_fire_rollback(double2* pos, double2* vel, double2* force, const double2* save,
+                                 int V, Ctrl* c, const int* gate, cudaStream_t st);
+cudaError_t launch_zero_force(double2* force, int V, Ctrl* c, const int* gate, cudaStream_t st);
+cudaError_t launch_fire_velocity(double2* vel, const double2* force, int V, Ctrl* c,
+                                 const int* gate, cudaStream_t st);
+cudaError_t launch_fire_maxf(const double2* force, int V, Ctrl* c, const int* gate,
+                             cudaStream_t st);
+cudaError_t launch_fire_finish(double2* vel, const double2* force, int V, Ctrl* c,
+                               const int* gate, cudaStream_t st);
+
+int sm_count();
+
+}  // namespace pcp

@@ -103,15 +103,18 @@ def batched_specs(num_systems, seed, p_range=(64, 1024), n_range=(12, 48),
     return specs
 
 
-def load_into(model, system, model_type="normal"):
+def load_into(model, system, model_type=None):
     """Configure a reference-API model object (the pybind `Model`, or any
-    object with the same method names) with a generated system."""
+    object with the same method names) with a generated system.  The cell
+    size is set after initializeNeighborCells, so the Python wrapper's reset
+    to 0.5 (pyCudaPolygon.py:54-57) does not undo it."""
     model.setNumVertices(system.num_vertices)
     model.setStartIndices(system.start_indices)
     model.setPositions(system.positions)
     model.setTargetAreas(system.target_areas)
     model.setTargetEdgeLengths(system.target_edge_lengths)
-    model.setMaxEdgeLength(system.max_edge_length)
-    model.setModelEnum(model_type)
+    if model_type is not None:
+        model.setModelEnum(model_type)
     model.initializeNeighborCells()
+    model.setMaxEdgeLength(system.max_edge_length)
     return model

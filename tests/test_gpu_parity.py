@@ -1,0 +1,292 @@
+"""Parity of the CUDA path (through the reference-facing Model API, which calls
+the C ABI) with the CPU oracle on identical seeded inputs.
+
+Tolerances (stated by the benchmark spec for this path): contact lists bit-exact;
+areas relative 1e-12; forces 1e-10 relative to the largest force component;
+energies 1e-12 relative.
+"""
+import json
+import os
+
+import numpy as np
+import pytest
+
+pytestmark = pytest.mark.gpu
+
+torch = pytest.importorskip("torch")
+if not torch.cuda.is_available():
+    pytest.skip("needs a CUDA GPU", allow_module_level=True)
+
+import pycudapolygon_gb300 as pg  # noqa: E402
+from pycudapolygon_gb300.systems import load_into, make_system  # noqa: E402
+from oracle import oracle as orc  # noqa: E402
+
+pg.build()
+lib = pg.load_module()
+
+FORCE_RTOL = 1e-10
+AREA_RTOL = 1e-12
+ENERGY_RTOL = 1e-12
+
+
+def pair(system):
+    g = load_into(lib.Model(system.num_vertices), system)
+    o = load_into(orc.OracleModel(system.num_vertices), system)
+    return g, o
+
+
+def contacts(m):
+    m.updatePolygonGeometry()
+    m.updateNeighborCells()
+    m.updateNeighbors()
+    m.updateOutersections()
+
+
+def assert_records_equal(g, o):
+    assert g.getNumIntersections() == o.getNumIntersections()
+    np.testing.assert_array_equal(np.asarray(g.getIntersections(), dtype=np.uint64),
+                                  o.getIntersections())
+    np.testing.assert_array_equal(np.asarray(g.getOutersections(), dtype=np.uint64),
+                                  o.getOutersections())
+    np.testing.assert_array_equal(np.asarray(g.getTU()), o.getTU())
+    np.testing.assert_array_equal(np.asarray(g.getUT()), o.getUT())
+
+
+def assert_forces_close(gf, of):
+    gf = np.asarray(gf)
+    scale = max(np.abs(of).max(), 1e-300)
+    assert np.abs(gf - of).max() <= FORCE_RTOL * scale, np.abs(gf - of).max() / scale
+
+
+SYSTEMS = {
+    "small_64x16": dict(num_polygons=64, n=16, phi=0.85, seed=1),
+    "mid_256x24": dict(num_polygons=256, n=24, phi=0.87, seed=7),
+    "tri_quads": dict(num_polygons=40, n=4, phi=0.9, seed=3),
+    "varn_200": dict(num_polygons=200, n=np.random.default_rng(5).integers(12, 49, 200), phi=0.86, seed=11),
+}
+
+
+@pytest.fixture(params=list(SYSTEMS))
+def system(request):
+    return make_system(**SYSTEMS[request.param])
+
+
+# ------------------------------------------------------------------ known answer
+def test_testsaver_known_answer():
+    fx = json.load(open(os.path.join(os.path.dirname(__file__), "golden", "testsaver.json")))
+    pos = np.asarray(fx["positions"])
+    n_array = np.asarray(fx["n_array"])
+    for shift in (False, True):
+        p = pos.reshape(-1, 2)
+        p = ((p - p.mean(axis=0)) % 1.0).reshape(-1) if shift else pos
+        m = lib.Model(10)
+        m.setNumVertices(10)
+        m.setStartIndices(np.concatenate([[0], np.cumsum(n_array)]).astype(np.int32))
+        m.setPositions(p)
+        m.setMaxEdgeLength(0.25)
+        m.initializeNeighborCells()
+        m.setMaxEdgeLength(0.5)
+        m.updateNeighborCells()
+        m.updateNeighbors()
+        nb = np.asarray(m.getNeighbors()).reshape(10, -1)
+        cnt = np.asarray(m.getNumNeighbors())
+        got = {i: nb[i, :cnt[i]].tolist() for i in range(10) if cnt[i]}
+        assert got == {1: [7, 8]}
+        ins = np.asarray(m.getInsideFlag()).reshape(10, -1)
+        assert ins[1, :2].tolist() == [True, False]
+
+
+# ------------------------------------------------------------------ geometry
+def test_geometry_parity(system):
+    g, o = pair(system)
+    g.updatePolygonGeometry()
+    o.updatePolygonGeometry()
+    np.testing.assert_allclose(g.getAreas(), o.getAreas(), rtol=AREA_RTOL)
+    np.testing.assert_allclose(g.getPerimeters(), o.getPerimeters(), rtol=1e-12)
+    np.testing.assert_allclose(g.getEdgeLengths(), o.getEdgeLengths(), rtol=1e-12)
+    d = (np.asarray(g.getCOM()) - o.getCOM() + 0.5) % 1.0 - 0.5
+    assert np.abs(d).max() < 1e-13
+    np.testing.assert_allclose(g.getConstraints(), o.getConstraints(), rtol=1e-10, atol=1e-13)
+    assert g.getMaxEdgeLength() == pytest.approx(o.getMaxEdgeLength(), rel=1e-13)
+
+
+# ------------------------------------------------------------------ contacts
+@pytest.mark.parametrize("box", ["system", 2, 1, 7])
+def test_contact_records_bit_exact(system, box):
+    g, o = pair(system)
+    if box != "system":
+        g.setMaxEdgeLength(1.0 / box)
+        o.setMaxEdgeLength(1.0 / box)
+    contacts(g)
+    contacts(o)
+    assert o.getNumIntersections() > 0 or system.num_polygons < 50
+    assert_records_equal(g, o)
+    np.testing.assert_array_equal(g.getNeighborCells(), o.getNeighborCells())
+    np.testing.assert_array_equal(g.getNeighborIndices(), o.getNeighborIndices())
+    np.testing.assert_array_equal(g.getBoxCounts(), o.getBoxCounts())
+
+
+def test_neighbor_slots_bit_exact(system):
+    g, o = pair(system)
+    contacts(g)
+    contacts(o)
+    nb_o, ins_o = o.getNeighborSlots()
+    cnt_o = o.getNumNeighbors()
+    np.testing.assert_array_equal(g.getNumNeighbors(), cnt_o)
+    M = g.getMaxNeighbors()
+    assert M == o.getMaxNeighbors()
+    nb_g = np.asarray(g.getNeighbors()).reshape(-1, M)
+    ins_g = np.asarray(g.getInsideFlag()).reshape(-1, M)
+    for v in np.nonzero(cnt_o)[0]:
+        c = cnt_o[v]
+        assert nb_g[v, :c].tolist() == nb_o[v, :c].tolist()
+        assert ins_g[v, :c].astype(bool).tolist() == ins_o[v, :c].astype(bool).tolist()
+
+
+def test_contacts_unchanged_by_stale_cells(system):
+    """updateNeighbors uses the cells of the last updateNeighborCells, as the
+    reference does, even when positions moved in between."""
+    g, o = pair(system)
+    for m in (g, o):
+        m.updatePolygonGeometry()
+        m.updateNeighborCells()
+        m.updateForceEnergy()
+        m.updatePositions(1e-3)
+        m.updateNeighbors()
+        m.updateOutersections()
+    assert_records_equal(g, o)
+
+
+# ------------------------------------------------------------------ force / energy
+def test_overlap_force_energy_parity(system):
+    g, o = pair(system)
+    for m in (g, o):
+        contacts(m)
+        m.updateForceEnergy()
+    e_o = o.getEnergy()
+    assert g.getEnergy() == pytest.approx(e_o, rel=ENERGY_RTOL, abs=1e-300)
+    assert_forces_close(g.getForces(), o.getForces())
+    assert g.getMaxUnbalancedForce() == pytest.approx(o.getMaxUnbalancedForce(), rel=1e-10)
+
+
+def test_projection_parity(system):
+    g, o = pair(system)
+    for m in (g, o):
+        contacts(m)
+        m.updateForceEnergy()
+        m.projectForce()
+    assert_forces_close(g.getForces(), o.getForces())
+
+
+def test_soft_body_parity(system):
+    # targets moved off the current shape so that the springs carry real force
+    ta = system.target_areas * 1.1
+    tl = system.target_edge_lengths * 0.95
+    for mt, k, c in [(3, 1.0, 1.0), (1, 2.0, 0.0), (2, 0.0, 3.0), (5, 1.0, 1.0)]:
+        g, o = pair(system)
+        g.setModelEnum(lib.modelEnum(mt))
+        o.setModelEnum(mt)
+        for m in (g, o):
+            m.setTargetAreas(ta)
+            m.setTargetEdgeLengths(tl)
+            m.setStiffness(k)
+            m.setCompressibility(c)
+            contacts(m)
+            m.updateForceEnergy()
+        assert g.getEnergy() == pytest.approx(o.getEnergy(), rel=1e-11)
+        assert_forces_close(g.getForces(), o.getForces())
+
+
+# ------------------------------------------------------------------ constraints
+def test_shake_parity(system):
+    g, o = pair(system)
+    it_g = g.shakeProject(100, 1e-15)
+    it_o = o.shakeProject(100, 1e-15)
+    assert abs(it_g - it_o) <= 1
+    assert it_g < 100
+    d = (np.asarray(g.getPositions()) - o.getPositions() + 0.5) % 1.0 - 0.5
+    assert np.abs(d).max() < 1e-12
+    g.updatePolygonGeometry()
+    np.testing.assert_allclose(g.getAreas(), system.target_areas, rtol=1e-10)
+    el = np.asarray(g.getEdgeLengths())
+    np.testing.assert_allclose(el, np.repeat(system.target_edge_lengths, system.n_array),
+                               rtol=1e-10)
+
+
+def test_xpbd_parity(system):
+    g, o = pair(system)
+    ig = g.xpbdProject(5, 0.0)
+    io = o.xpbdProject(5, 0.0)
+    assert ig == io == 5
+    d = (np.asarray(g.getPositions()) - o.getPositions() + 0.5) % 1.0 - 0.5
+    assert np.abs(d).max() < 1e-12
+
+
+# ------------------------------------------------------------------ FIRE
+def test_fire_steps_parity():
+    s = make_system(64, 16, 0.85, seed=2)
+    g, o = pair(s)
+    for m in (g, o):
+        m.shakeProject(200, 1e-15)
+        contacts(m)
+        m.updateForceEnergy()
+        m.projectForce()
+    st_g = (1e-3, 0.1, 0)
+    st_o = (1e-3, 0.1, 0)
+    for step in range(30):
+        rg = g.minimizeFIREStep(*st_g)
+        ro = o.minimizeFIREStep(*st_o)
+        assert rg[0] == pytest.approx(ro[0], rel=1e-9, abs=1e-14), step
+        assert rg[1] == pytest.approx(ro[1], rel=1e-12), step
+        assert rg[3] == ro[3], step
+        assert g.getLastShakeIters() == pytest.approx(o.getLastShakeIters(), abs=1)
+        st_g = rg[1:]
+        st_o = ro[1:]
+    d = (np.asarray(g.getPositions()) - o.getPositions() + 0.5) % 1.0 - 0.5
+    assert np.abs(d).max() < 1e-9
+
+
+def test_minimize_fire_matches_step_loop():
+    """Model::minimizeFIRE (graph loop with the stop test on the device) walks
+    the same trajectory as repeated minimizeFIREStep calls."""
+    s = make_system(64, 16, 0.85, seed=4)
+    a = load_into(lib.Model(s.num_vertices), s)
+    b = load_into(lib.Model(s.num_vertices), s)
+    for m in (a, b):
+        m.shakeProject(200, 1e-15)
+        contacts(m)
+    ea, dta, steps = a.minimizeFIRE(1e-10, 1e-3, 40)
+    b.resetVelocities()
+    b.updatePolygonGeometry()
+    b.updateForceEnergy()
+    b.projectForce()
+    st = (1e-3, 0.1, 0)
+    for _ in range(40):
+        r = b.minimizeFIREStep(*st)
+        st = r[1:]
+    assert steps == 40
+    assert dta == pytest.approx(st[0], rel=1e-12)
+    assert a.getEnergy() == pytest.approx(b.getEnergy(), rel=1e-9)
+
+
+def test_large_system_contacts_and_force():
+    """4096 polygons of 32 vertices (131,072 vertices): bit-exact records and
+    force parity for one evaluation."""
+    s = make_system(4096, 32, 0.88, seed=42)
+    g, o = pair(s)
+    for m in (g, o):
+        contacts(m)
+        m.updateForceEnergy()
+    assert_records_equal(g, o)
+    assert g.getEnergy() == pytest.approx(o.getEnergy(), rel=ENERGY_RTOL)
+    assert_forces_close(g.getForces(), o.getForces())
+
+
+def test_wrong_position_length_is_ignored_like_reference(capfd):
+    s = make_system(8, 6, 0.5, seed=0)
+    g = load_into(lib.Model(s.num_vertices), s)
+    before = np.asarray(g.getPositions()).copy()
+    g.setPositions(np.zeros(3))
+    out = capfd.readouterr().out
+    assert "Update numVertices" in out
+    np.testing.assert_array_equal(g.getPositions(), before)
