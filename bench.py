@@ -1,0 +1,419 @@
+#!/usr/bin/env python3
+"""Benchmark of the pyCudaPolygon hot path on GB300.
+
+Workload (one "step"): one FIRE step of the plain method at scale -- 4096
+polygons of 32 vertices (131,072 vertices), 50:50 bidisperse radii 1.4,
+packing fraction 0.88, seeded synthetic system -- with the reference's full
+step: Verlet update, edge-midpoint cells, contact search (broad phase, narrow
+phase, exit matching), SHAKE (5 iterations, retry x10), overlap energy and
+force, constraint projection, energy-rollback test and FIRE velocity update.
+
+metric  pair evals/s: candidate polygon pairs (a < b, overlapping bounding
+        circles) taken through the narrow phase, exit matching and force per
+        second.  `value` is measured with the system resident in HBM, L2 flushed
+        (256 MiB write) before every timed step, CUDA events around each step.
+e2e     the same metric through the C ABI with host buffers: positions copied
+        from pinned host memory in, the step, positions copied back, per step.
+
+--impl reference times the CPU restatement of the reference (oracle/, C with
+OpenMP on all host cores) on the same workload; the reference itself is CUDA
+code that does not build as shipped and has no CPU implementation.
+"""
+import argparse
+import json
+import os
+import statistics
+import subprocess
+import sys
+import threading
+import time
+
+import numpy as np
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+METRIC = "pair evals/s"
+UNIT = "pair evals/s"
+N_POLY, N_VERT, PHI = 4096, 32, 0.88
+WORKLOAD = ("plain FIRE step at scale: 4096 polygons x 32 vertices (131072 vertices), "
+            "phi 0.88, cell list + narrow phase + outersections + overlap force + "
+            "constraint projection + SHAKE (5, retry 50)")
+FIRE_ARGS = dict(dtMax=0.1, alphaStart=0.1, fAlpha=0.99, fInc=1.1, fDec=0.5, nMin=5, shakeIter=5)
+
+
+def dist_env():
+    ws = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    return ws, rank, local
+
+
+# ------------------------------------------------------------------ clocks
+class ClockSampler:
+    """nvidia-smi clocks and throttle reasons sampled during the timed region."""
+    Q = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+         "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+         "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, index):
+        self.index = index
+        self.proc = None
+        self.lines = []
+
+    def __enter__(self):
+        try:
+            self.proc = subprocess.Popen(
+                ["nvidia-smi", "-i", str(self.index), "--query-gpu=" + self.Q,
+                 "--format=csv,noheader,nounits", "-lms", "200"],
+                stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+            self.t = threading.Thread(target=self._read, daemon=True)
+            self.t.start()
+        except (OSError, FileNotFoundError):
+            self.proc = None
+        return self
+
+    def _read(self):
+        for line in self.proc.stdout:
+            self.lines.append(line.strip())
+
+    def __exit__(self, *a):
+        if self.proc:
+            self.proc.terminate()
+            try:
+                self.proc.wait(timeout=5)
+            except subprocess.TimeoutExpired:
+                self.proc.kill()
+
+    def summary(self):
+        sm, mx, reasons = [], None, set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for ln in self.lines:
+            f = [x.strip() for x in ln.split(",")]
+            if len(f) < 9:
+                continue
+            try:
+                sm.append(float(f[1]))
+                mx = float(f[2])
+            except ValueError:
+                continue
+            for nm, v in zip(names, f[5:9]):
+                if v.lower() in ("active", "1"):
+                    reasons.add(nm)
+        return {"sm_mhz": statistics.median(sm) if sm else None, "sm_max_mhz": mx,
+                "reasons": sorted(reasons), "samples": len(sm)}
+
+
+# ------------------------------------------------------------------ workload
+def make_workload(seed):
+    from pycudapolygon_gb300.systems import make_system
+    return make_system(N_POLY, N_VERT, PHI, seed=seed)
+
+
+def candidate_pairs(positions, start):
+    """Pairs (a < b) with overlapping bounding circles: the pair count of the
+    narrow phase (same circle rule and padding as the broad phase)."""
+    xy = positions.reshape(-1, 2)
+    P = len(start) - 1
+    cx, cy, R = np.zeros(P), np.zeros(P), np.zeros(P)
+    for p in range(P):
+        ring = xy[start[p]:start[p + 1]]
+        rel = (ring - ring[0] + 0.5) % 1.0 - 0.5
+        lo, hi = rel.min(axis=0), rel.max(axis=0)
+        c = (ring[0] + 0.5 * (lo + hi)) % 1.0
+        cx[p], cy[p] = c
+        R[p] = 0.5 * np.hypot(*(hi - lo)) * 1.0001 + 4e-6
+    count = 0
+    for p in range(P - 1):
+        dx = (cx[p + 1:] - cx[p] + 0.5) % 1.0 - 0.5
+        dy = (cy[p + 1:] - cy[p] + 0.5) % 1.0 - 0.5
+        rr = R[p] + R[p + 1:] + 1e-5
+        count += int(np.count_nonzero(dx * dx + dy * dy <= rr * rr))
+    return count
+
+
+def prepare_gpu(seed):
+    import pycudapolygon_gb300 as pg
+    from pycudapolygon_gb300.systems import load_into
+    pg.build()
+    lib = pg.load_module()
+    s = make_workload(seed)
+    m = load_into(lib.Model(s.num_vertices), s)
+    m.shakeProject(200, 1e-15)          # start on the constraint manifold
+    m.updatePolygonGeometry()
+    m.updateNeighborCells()
+    m.updateNeighbors()
+    m.updateOutersections()
+    m.fireSetup(-1.0, 1e-3, 0, **FIRE_ARGS)
+    return lib, m, s
+
+
+# ------------------------------------------------------------------ GPU arm
+def run_gpu(args, ws, rank, local):
+    import torch
+    torch.cuda.set_device(local)
+    dist = None
+    if ws > 1:
+        import torch.distributed as dist
+        dist.init_process_group("nccl")
+    lib, m, s = prepare_gpu(args.seed + rank)
+    flush = torch.empty(256 << 20, dtype=torch.uint8, device="cuda")
+    for _ in range(args.warmup):
+        flush.fill_(1)
+        m.fireContinue(1)
+    st = m.fireStatus()
+    if st[8]:
+        raise RuntimeError("contact buffers grew during warm-up; rerun")
+    ev = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True))
+          for _ in range(args.steps)]
+    pairs0 = m.getPairCount()
+    launches0 = m.getLaunchCount()
+    torch.cuda.synchronize()
+    if dist:
+        dist.barrier()
+    with ClockSampler(local) as clk:
+        for i in range(args.steps):
+            flush.fill_(i & 255)
+            ev[i][0].record()
+            m.fireContinue(1)
+            ev[i][1].record()
+        torch.cuda.synchronize()
+    if dist:
+        dist.barrier()
+    st = m.fireStatus()
+    if st[8]:
+        raise RuntimeError("contact buffers grew inside the timed region; rerun")
+    ms = sum(a.elapsed_time(b) for a, b in ev)
+    pairs = m.getPairCount() - pairs0
+    launches = m.getLaunchCount() - launches0
+    if dist:
+        t = torch.tensor([ms, float(pairs)], dtype=torch.float64, device="cuda")
+        tmax = t.clone()
+        dist.all_reduce(tmax, op=dist.ReduceOp.MAX)
+        dist.all_reduce(t, op=dist.ReduceOp.SUM)
+        ms, pairs = float(tmax[0]), float(t[1])
+    value = pairs / (ms / 1e3)
+    result = {
+        "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": ws, "steps": args.steps,
+        "warmup": args.warmup, "ms_per_step": ms / args.steps, "higher_is_better": True,
+        "scaling": "weak", "vs_baseline": None, "dtype": "f64",
+        "data": "synthetic (seeded bidisperse star polygons; the reference publishes no inputs)",
+        "config": {"workload": WORKLOAD, "polygons": N_POLY, "vertices_per_polygon": N_VERT,
+                   "phi": PHI, "parallelism": "replicas" if ws > 1 else "single",
+                   "l2": "flushed before every timed step (256 MiB write)",
+                   "pair_evals_per_step": pairs / max(1, args.steps) / ws,
+                   "fire": "dt0 1e-3, dtMax 0.1, alpha0 0.1, fAlpha 0.99, fInc 1.1, fDec 0.5, "
+                           "nMin 5, shakeIter 5"},
+        "clocks": clk.summary(),
+        "gpu_launches": int(launches),
+        "fire_state": {"energy": st[0], "dt": st[1], "max_force": st[4], "steps": st[5]},
+    }
+    if rank == 0 and not args.no_roofline:
+        result["roofline"], result["fp64"] = roofline(m, s, torch, flush, args)
+    if rank == 0 and not args.no_e2e:
+        result["e2e"] = e2e(args, s)
+    if rank == 0 and not args.no_cpu:
+        result["cpu_baseline"] = cpu_baseline(args, s, pairs / max(1, args.steps) / ws)
+    if dist:
+        dist.destroy_process_group()
+    if rank == 0:
+        print(json.dumps(result))
+
+
+def roofline(m, s, torch, flush, args):
+    """Dominant kernel: the narrow phase (warp per candidate pair).  Algorithmic
+    bytes per launch: 16 (n_a + n_b) + 24 per candidate pair (both FP64 rings
+    and the pair entry) over the pairs it examines, self pairs counted once."""
+    peaks = {}
+    try:
+        peaks = json.load(open(os.path.join(ROOT, "MEASURED_PEAKS.json")))
+    except (OSError, ValueError):
+        pass
+    hbm = peaks.get("hbm_gbs")
+    src = "measured"
+    if not hbm:
+        hbm, src = 6800.0, "fallback"
+    reps = 20
+    times = []
+    m.updateNeighborCells()
+    for _ in range(reps):
+        m.contactsStage(0)
+        flush.fill_(3)
+        a = torch.cuda.Event(enable_timing=True)
+        b = torch.cuda.Event(enable_timing=True)
+        a.record()
+        m.contactsStage(1)
+        b.record()
+        torch.cuda.synchronize()
+        times.append(a.elapsed_time(b))
+    m.contactsStage(2)
+    ms = statistics.median(times)
+    n = N_VERT
+    P = N_POLY
+    cross = m.getPairCount()  # cumulative; the per-search count comes from the geometry
+    pairs = candidate_pairs(np.asarray(m.getPositions()), s.start_indices)
+    bytes_launch = pairs * (16 * 2 * n + 24) + P * (16 * n + 24)
+    achieved = bytes_launch / (ms / 1e3) / 1e9
+    traffic = None
+    prof = os.path.join(ROOT, "profiles", "narrow_phase_traffic.json")
+    if os.path.exists(prof):
+        try:
+            traffic = json.load(open(prof)).get("dram_bytes_per_launch")
+        except (OSError, ValueError):
+            traffic = None
+    roof = {"bound": "hbm", "achieved": achieved, "peak": hbm, "unit": "GB/s",
+            "frac": achieved / hbm, "traffic": traffic, "peak_source": src + " (MEASURED_PEAKS.json hbm_gbs)",
+            "kernel": "k_narrow + k_narrow_slow (contact stage 1)",
+            "launch_ms": ms, "algorithmic_bytes": bytes_launch, "pairs": pairs}
+    fp64 = None
+    p64 = os.path.join(ROOT, "profiles", "fp64_peak.json")
+    if os.path.exists(p64):
+        try:
+            fp64 = json.load(open(p64))
+        except (OSError, ValueError):
+            fp64 = None
+    del cross
+    return roof, fp64
+
+
+def e2e(args, s):
+    """Same metric through the C ABI with host buffers (pinned), per step:
+    positions in, one FIRE step, positions out."""
+    import torch
+
+    from pycudapolygon_gb300 import cabi
+    from pycudapolygon_gb300.systems import make_system  # noqa: F401
+    c = cabi.CModel(s.num_vertices)
+    c.set_num_vertices(s.num_vertices)
+    c.set_start_indices(s.start_indices)
+    c.set_positions(s.positions)
+    c.set_target_areas(s.target_areas)
+    c.set_target_edge_lengths(s.target_edge_lengths)
+    c.initialize_neighbor_cells()
+    c.set_max_edge_length(s.max_edge_length)
+    c.shake_project(200)
+    c.update_polygon_geometry()
+    c.update_neighbor_cells()
+    c.update_neighbors()
+    c.update_outersections()
+    c.update_force_energy()
+    c.project_force()
+    host = torch.empty(2 * s.num_vertices, dtype=torch.float64, pin_memory=True).numpy()
+    c.get_positions_into(host)
+    flush = torch.empty(256 << 20, dtype=torch.uint8, device="cuda")
+    dt, alpha, npos = 1e-3, 0.1, 0
+    for _ in range(args.warmup):
+        _, dt, alpha, npos = c.fire_step(dt, alpha, npos)
+    c.get_positions_into(host)
+    p0 = c.pair_count()
+    total = 0.0
+    steps = max(3, args.steps // 2)
+    for i in range(steps):
+        flush.fill_(i & 255)
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        c.set_positions(host)
+        _, dt, alpha, npos = c.fire_step(dt, alpha, npos)
+        c.get_positions_into(host)
+        total += time.perf_counter() - t0
+    pairs = c.pair_count() - p0
+    ctrl_bytes = 512
+    c.close()
+    return {"value": pairs / total, "unit": UNIT,
+            "h2d_bytes_per_step": 16 * s.num_vertices + ctrl_bytes,
+            "d2h_bytes_per_step": 16 * s.num_vertices + ctrl_bytes,
+            "steps": steps, "ms_per_step": total / steps * 1e3,
+            "path": "C ABI (pcp_model_set_positions, pcp_model_fire_step, "
+                    "pcp_model_get_positions), pinned host buffers, wall clock"}
+
+
+# ------------------------------------------------------------------ CPU legs
+def cpu_threads():
+    try:
+        return len(os.sched_getaffinity(0))
+    except AttributeError:
+        return os.cpu_count() or 1
+
+
+def run_cpu_steps(s, steps, warmup, threads):
+    """The CPU oracle (restatement of the reference) doing FIRE steps on the
+    same system; returns (seconds, pair evals, steps)."""
+    from oracle import oracle as orc
+    from pycudapolygon_gb300.systems import load_into
+    orc.set_threads(threads)
+    o = load_into(orc.OracleModel(s.num_vertices), s)
+    o.shakeProject(200, 1e-15)
+    o.updatePolygonGeometry()
+    o.updateNeighborCells()
+    o.updateNeighbors()
+    o.updateOutersections()
+    o.updateForceEnergy()
+    o.projectForce()
+    dt, alpha, npos = 1e-3, 0.1, 0
+    for _ in range(warmup):
+        _, dt, alpha, npos = o.minimizeFIREStep(dt, alpha, npos)
+    # the pair count moves slowly along a FIRE run: count it at both ends
+    first = candidate_pairs(o.getPositions(), s.start_indices)
+    total = 0.0
+    for _ in range(steps):
+        t0 = time.perf_counter()
+        _, dt, alpha, npos = o.minimizeFIREStep(dt, alpha, npos)
+        total += time.perf_counter() - t0
+    last = candidate_pairs(o.getPositions(), s.start_indices)
+    return total, 0.5 * (first + last) * steps, steps
+
+
+def cpu_baseline(args, s, gpu_pairs_per_step):
+    threads = cpu_threads()
+    secs, pairs, steps = run_cpu_steps(s, args.cpu_steps, 1, threads)
+    return {"value": pairs / secs, "unit": UNIT, "cores": threads, "kind": "port",
+            "sample": "%d FIRE steps of the same 4096x32 system (after 1 warm-up step) "
+                      "by the C oracle with OpenMP, %.1f s" % (steps, secs)}
+
+
+def run_reference(args, ws, rank):
+    if rank != 0:
+        return
+    s = make_workload(args.seed)
+    threads = cpu_threads()
+    secs, pairs, steps = run_cpu_steps(s, max(1, args.steps), max(0, min(args.warmup, 3)), threads)
+    value = pairs / secs
+    print(json.dumps({
+        "impl": "reference", "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": ws,
+        "steps": steps, "warmup": min(args.warmup, 3), "ms_per_step": secs / steps * 1e3,
+        "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64",
+        "data": "synthetic (seeded bidisperse star polygons)",
+        "config": {"workload": WORKLOAD, "polygons": N_POLY, "vertices_per_polygon": N_VERT,
+                   "phi": PHI},
+        "cpu_baseline": {"value": value, "unit": UNIT, "cores": threads, "kind": "port",
+                         "sample": "%d FIRE steps of the workload by the C restatement of the "
+                                   "reference (oracle/), OpenMP on %d threads" % (steps, threads)},
+        "e2e": {"value": value, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+        "note": "the reference is CUDA-only and does not build as shipped (FIRE.h and shake.h "
+                "are missing); its algorithm is timed through the CPU restatement",
+    }))
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=50)
+    ap.add_argument("--warmup", type=int, default=5)
+    ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
+    ap.add_argument("--seed", type=int, default=2024)
+    ap.add_argument("--cpu-steps", type=int, default=100)
+    ap.add_argument("--no-e2e", action="store_true")
+    ap.add_argument("--no-cpu", action="store_true")
+    ap.add_argument("--no-roofline", action="store_true")
+    args = ap.parse_args()
+    if args.warmup < 3 and args.impl == "gb300":
+        args.warmup = 3
+    ws, rank, local = dist_env()
+    if args.impl == "reference":
+        run_reference(args, ws, rank)
+        return
+    run_gpu(args, ws, rank, local)
+
+
+if __name__ == "__main__":
+    main()

@@ -147,6 +147,32 @@ int pcp_model_minimize_fire(pcp_model* m, double max_force_threshold, double dt_
                             double f_inc, double f_dec, int n_min, int shake_iter,
                             double out[3]);
 
+/* Device-resident FIRE driver (the loop of Model::minimizeFIRE, model.cpp:
+ * 488-504, and of the Python minimizeFIRELoop, pyCudaPolygon.py:653-672,
+ * without a host round trip per step).
+ * pcp_model_fire_setup: reset velocities, evaluate force (+ projection for the
+ *   normal model) and load the FIRE parameters; max_force_threshold is the
+ *   stop test, max_steps the step limit (<= 0: none).
+ * pcp_model_fire_continue: enqueue n_steps step-graph launches on the model's
+ *   stream and return at once; steps after the stop test or the limit are
+ *   no-ops on the device.
+ * pcp_model_fire_status: wait for the stream; out = {E, dt, alpha, nPos,
+ *   max|F|, steps done, converged, last SHAKE iterations}.  A contact buffer
+ *   that overflowed during a step is grown here and the step is rolled back
+ *   to its start; *redo_out is then 1 and the caller continues. */
+int pcp_model_fire_setup(pcp_model* m, double max_force_threshold, double dt_init,
+                         int max_steps, double dt_max, double alpha_start, double f_alpha,
+                         double f_inc, double f_dec, int n_min, int shake_iter);
+int pcp_model_fire_continue(pcp_model* m, int n_steps);
+int pcp_model_fire_status(pcp_model* m, double out[8], int* redo_out);
+
+/* The contact search (update of the crossing records) split into its stages,
+ * enqueued without waiting: 0 = per-polygon prepass and broad phase
+ * (bounding circles, grid counting sort, candidate pairs), 1 = narrow phase
+ * (warp-per-pair kernel and its block fallback), 2 = exit matching fix-up.
+ * Overflow is only detected by pcp_model_update_neighbors. */
+int pcp_model_contacts_stage(pcp_model* m, int stage);
+
 /* ---- getters (model.cpp:654-893); arrays are copied into caller memory ---- */
 int pcp_model_get_num_vertices(pcp_model* m, int* out);
 int pcp_model_get_num_polygons(pcp_model* m, int* out);

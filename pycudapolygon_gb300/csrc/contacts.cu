@@ -758,11 +758,13 @@ cudaError_t contacts_init() {
 
 cudaError_t launch_contacts(const double2* pos, const int* start, const int* shapeId,
                             const int* cellLocation, int P, int V, int B, ContactWS& ws,
-                            Ctrl* ctrl, const int* gate, cudaStream_t st) {
+                            Ctrl* ctrl, const int* gate, cudaStream_t st, int stages) {
+    // stages: bit 0 = reset + prepass + broad phase, bit 1 = narrow phase
     (void)shapeId; (void)V;
+    if (B < 1) B = 1;
+    if (stages & 1) {
     k_reset_contacts<<<1, 64, 0, st>>>(ctrl, gate);
     if (P <= 0) return cudaGetLastError();
-    if (B < 1) B = 1;
     k_prepass<<<nblocks(P, 8), 256, 0, st>>>(pos, start, cellLocation, P, ws.edgeVec, ws.vtx,
                                              ws.polyInfo, ws.polyFlags, ws.unsafeList, ctrl, gate);
     k_grid_count<<<nblocks(P, 256), 256, 0, st>>>(ws.polyInfo, ws.polyFlags, P, ws.gridCount,
@@ -773,11 +775,13 @@ cudaError_t launch_contacts(const double2* pos, const int* start, const int* sha
     k_candidates<<<nblocks(P, 128), 128, 0, st>>>(ws.polyInfo, ws.polyFlags, start, P,
                                                   ws.gridStart, ws.sortedPoly, ws.pairs,
                                                   ws.capPairs, ctrl, gate);
-    size_t smem = sizeof(WarpSmem) * kNarrowWarps;
-    size_t smemSlow = kSlowSmem;
-    int grid = sm_count() * 4;
-    k_narrow<<<grid, 32 * kNarrowWarps, smem, st>>>(pos, start, B, ws, ctrl, gate);
-    k_narrow_slow<<<sm_count(), 32, smemSlow, st>>>(pos, start, B, ws, ctrl, gate);
+    }
+    if ((stages & 2) && P > 0) {
+        size_t smem = sizeof(WarpSmem) * kNarrowWarps;
+        int grid = sm_count() * 4;
+        k_narrow<<<grid, 32 * kNarrowWarps, smem, st>>>(pos, start, B, ws, ctrl, gate);
+        k_narrow_slow<<<sm_count(), 32, kSlowSmem, st>>>(pos, start, B, ws, ctrl, gate);
+    }
     return cudaGetLastError();
 }
 

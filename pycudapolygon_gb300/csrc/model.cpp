@@ -114,6 +114,7 @@ struct pcp_model {
     cudaGraphExec_t fireExec = nullptr;
     unsigned long long fireGen = 0;
     int fireShakeIter = -1, fireModel = -1, fireB = -1;
+    int fireKernelNodes = 0;   // kernel launches one FIRE step graph makes
 
     ~pcp_model() { release(); }
 
@@ -200,7 +201,7 @@ int run_contacts(pcp_model* m) {
     for (int attempt = 0; attempt < 8; ++attempt) {
         CK(launch_contacts(m->pos, m->start, m->shapeId, m->cellLocation, m->P, m->V, m->boxSize,
                            m->ws, m->ctrl, nullptr, m->stream));
-        m->launches += 7;
+        m->launches += 8;
         int rc = read_ctrl(m);
         if (rc) return rc;
         unsigned fl = m->ctrlHost->flags;
@@ -518,6 +519,7 @@ int build_fire_graph(pcp_model* m, int shakeIter) {
     cudaStream_t cap = nullptr;
     CK(cudaStreamCreateWithFlags(&cap, cudaStreamNonBlocking));
     cudaStream_t saved = m->stream;
+    long long savedLaunches = m->launches;   // captured launches are not launches
     m->stream = cap;
     cudaGraph_t g = nullptr;
     cudaError_t e = cudaStreamBeginCapture(cap, cudaStreamCaptureModeThreadLocal);
@@ -527,9 +529,22 @@ int build_fire_graph(pcp_model* m, int shakeIter) {
         e = cudaStreamEndCapture(cap, &g);
     }
     m->stream = saved;
+    m->launches = savedLaunches;
     cudaStreamDestroy(cap);
     if (rc) { if (g) cudaGraphDestroy(g); return rc; }
     if (e != cudaSuccess) return fail(PCP_ERR_CUDA, "graph capture failed: %s", cudaGetErrorString(e));
+    {
+        size_t nn = 0;
+        cudaGraphGetNodes(g, nullptr, &nn);
+        std::vector<cudaGraphNode_t> nodes(nn);
+        if (nn) cudaGraphGetNodes(g, nodes.data(), &nn);
+        int k = 0;
+        for (size_t i = 0; i < nn; ++i) {
+            cudaGraphNodeType t;
+            if (cudaGraphNodeGetType(nodes[i], &t) == cudaSuccess && t == cudaGraphNodeTypeKernel) ++k;
+        }
+        m->fireKernelNodes = k;
+    }
     e = cudaGraphInstantiate(&m->fireExec, g, 0);
     cudaGraphDestroy(g);
     if (e != cudaSuccess) return fail(PCP_ERR_CUDA, "graph instantiate failed: %s", cudaGetErrorString(e));
@@ -594,7 +609,7 @@ int fire_step_once(pcp_model* m, const FireParams& fp, double out[4]) {
     if (rc) return rc;
     for (int attempt = 0; attempt < 6; ++attempt) {
         CK(cudaGraphLaunch(m->fireExec, m->stream));
-        m->launches += 1;
+        m->launches += m->fireKernelNodes;
         rc = read_ctrl(m);
         if (rc) return rc;
         bool redo = false;
@@ -1051,7 +1066,7 @@ int pcp_model_minimize_fire(pcp_model* m, double thr, double dt0, int max_steps,
         int todo = std::min(chunk, left);
         if (todo <= 0) break;
         for (int s = 0; s < todo; ++s) CK(cudaGraphLaunch(m->fireExec, m->stream));
-        m->launches += todo;
+        m->launches += (long long)todo * m->fireKernelNodes;
         rc = read_ctrl(m);
         if (rc) return rc;
         bool redo = false;
@@ -1071,6 +1086,75 @@ int pcp_model_minimize_fire(pcp_model* m, double thr, double dt0, int max_steps,
     out[0] = c.converged ? c.outE : c.energy;
     out[1] = c.dt;
     out[2] = c.stepsDone;
+    return PCP_OK;
+}
+
+int pcp_model_fire_setup(pcp_model* m, double thr, double dt0, int max_steps, double dt_max,
+                         double alpha_start, double f_alpha, double f_inc, double f_dec,
+                         int n_min, int shake_iter) {
+    CHECK_M(m);
+    int rc = need_topology(m);
+    if (rc) return rc;
+    rc = pcp_model_reset_velocities(m);
+    if (rc) return rc;
+    rc = geometry(m, nullptr);
+    if (rc) return rc;
+    rc = force_energy(m, nullptr);
+    if (rc) return rc;
+    if (m->modelType == PCP_MODEL_NORMAL) {
+        rc = pcp_model_project_force(m);
+        if (rc) return rc;
+    }
+    FireParams fp{dt0, alpha_start, dt_max, alpha_start, f_alpha, f_inc, f_dec, thr,
+                  0, n_min, shake_iter, max_steps > 0 ? max_steps : 0};
+    rc = build_fire_graph(m, shake_iter);
+    if (rc) return rc;
+    return set_fire_params(m, fp, true);
+}
+
+int pcp_model_fire_continue(pcp_model* m, int n_steps) {
+    CHECK_M(m);
+    if (!m->fireExec) return fail(PCP_ERR_STATE, "pcp_model_fire_setup has not been called");
+    for (int s = 0; s < n_steps; ++s) CK(cudaGraphLaunch(m->fireExec, m->stream));
+    m->launches += (long long)n_steps * m->fireKernelNodes;
+    return PCP_OK;
+}
+
+int pcp_model_fire_status(pcp_model* m, double out[8], int* redo_out) {
+    CHECK_M(m);
+    int rc = read_ctrl(m);
+    if (rc) return rc;
+    bool redo = false;
+    rc = recover_fire(m, redo);
+    if (rc) return rc;
+    if (redo_out) *redo_out = redo ? 1 : 0;
+    const Ctrl& c = *m->ctrlHost;
+    out[0] = c.converged ? c.outE : c.energy;
+    out[1] = c.dt; out[2] = c.alpha; out[3] = c.nPos; out[4] = c.maxF;
+    out[5] = c.stepsDone; out[6] = c.converged; out[7] = c.shakeLast;
+    m->lastShakeIters = c.shakeLast;
+    m->numIntersections = c.numRecords;
+    m->view = pcp_model::VIEW_FINAL;
+    m->invalidate();
+    return PCP_OK;
+}
+
+int pcp_model_contacts_stage(pcp_model* m, int stage) {
+    CHECK_M(m);
+    int rc = need_topology(m);
+    if (rc) return rc;
+    if (stage == 0 || stage == 1) {
+        CK(launch_contacts(m->pos, m->start, m->shapeId, m->cellLocation, m->P, m->V, m->boxSize,
+                           m->ws, m->ctrl, nullptr, m->stream, stage == 0 ? 1 : 2));
+        m->launches += stage == 0 ? 6 : 2;
+    } else if (stage == 2) {
+        CK(launch_contacts_finish(m->start, m->ws, m->ctrl, nullptr, m->stream));
+        m->launches += 1;
+    } else {
+        return fail(PCP_ERR_ARG, "unknown contact stage %d", stage);
+    }
+    m->view = pcp_model::VIEW_FINAL;
+    m->invalidate();
     return PCP_OK;
 }
 

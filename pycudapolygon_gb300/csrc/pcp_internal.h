@@ -132,7 +132,7 @@ cudaError_t launch_overlap_area_mc(const double2* pos, const int* start, const i
 cudaError_t contacts_init();
 cudaError_t launch_contacts(const double2* pos, const int* start, const int* shapeId,
                             const int* cellLocation, int P, int V, int B, ContactWS& ws,
-                            Ctrl* ctrl, const int* gate, cudaStream_t st);
+                            Ctrl* ctrl, const int* gate, cudaStream_t st, int stages = 3);
 cudaError_t launch_contacts_finish(const int* start, ContactWS& ws, Ctrl* ctrl,
                                    const int* gate, cudaStream_t st);
 cudaError_t launch_overlap_force(const double2* pos, const int* start, const int* next,

@@ -111,6 +111,25 @@ public:
         return {out[0], out[1], (int)out[2]};
     }
 
+    void fireSetup(double thr, double dt, int maxSteps, double dtMax, double alphaStart,
+                   double fAlpha, double fInc, double fDec, int nMin, int shakeIter) {
+        py::gil_scoped_release nogil;
+        check(pcp_model_fire_setup(m_, thr, dt, maxSteps, dtMax, alphaStart, fAlpha, fInc, fDec,
+                                   nMin, shakeIter));
+    }
+    void fireContinue(int n) { check(pcp_model_fire_continue(m_, n)); }
+    py::tuple fireStatus() {
+        double out[8];
+        int redo = 0;
+        {
+            py::gil_scoped_release nogil;
+            check(pcp_model_fire_status(m_, out, &redo));
+        }
+        return py::make_tuple(out[0], out[1], out[2], (int)out[3], out[4], (long long)out[5],
+                              out[6] != 0.0, (int)out[7], redo != 0);
+    }
+    void contactsStage(int s) { check(pcp_model_contacts_stage(m_, s)); }
+
     // scalar getters
     int getNumVertices() { int v; check(pcp_model_get_num_vertices(m_, &v)); return v; }
     int getNumPolygons() { int v; check(pcp_model_get_num_polygons(m_, &v)); return v; }
@@ -283,5 +302,12 @@ PYBIND11_MODULE(libpyCudaPolygon, m) {
         .def("devicePositions", &Model::devicePositions)
         .def("deviceForces", &Model::deviceForces)
         .def("handle", &Model::handlePtr)
-        .def("setStream", &Model::setStream);
+        .def("setStream", &Model::setStream)
+        .def("fireSetup", &Model::fireSetup, py::arg("maxForceThreshold"), py::arg("dtInit"),
+             py::arg("maxSteps"), py::arg("dtMax") = 0.1, py::arg("alphaStart") = 0.1,
+             py::arg("fAlpha") = 0.99, py::arg("fInc") = 1.1, py::arg("fDec") = 0.5,
+             py::arg("nMin") = 5, py::arg("shakeIter") = 5)
+        .def("fireContinue", &Model::fireContinue)
+        .def("fireStatus", &Model::fireStatus)
+        .def("contactsStage", &Model::contactsStage);
 }
