@@ -1014,136 +1014,146 @@ void orc_project_force(orc_model* m) {
 /* model.cu:616-636: one polygon per block, constraints = n edge lengths     */
 /* (scalar target per polygon) + 1 area, an (n+1)x(n+1) matrix per polygon,  */
 /* returns the largest iteration count over polygons; failure = count >=     */
-/* maxIter.  Restatement (matrix SHAKE, Newton in the multipliers):          */
-/*   sigma_k = |e_k| - L (k < n),  sigma_n = A - A0,                          */
-/*   x <- x + G_ref^T dl,  (G(x) G_ref^T) dl = -sigma(x),                     */
-/* where G_ref is the constraint Jacobian at the positions SHAKE starts     */
-/* from, e_k = wrap(x_{k+1} - x_k) and A is the shoelace of                  */
-/* updatePolygonGeometryKernel.  Each iteration first checks                 */
-/* max|sigma| < tol; the count is the number of updates made.               */
+/* maxIter.  Restatement (matrix SHAKE, Newton in the multipliers, the       */
+/* correction solved in single precision):                                   */
+/*   s_k = (|e_k|^2 - L^2)/2, e_k = wrap(x_{k+1} - x_k);  s_A = A - A0;       */
+/*   stop when max(max_k |s_k|/L, |s_A|) < tol;                               */
+/*   x <- x + G_ref^T l,  (G(x) G_ref^T) l = -s,                              */
+/* G_ref the constraint gradients where SHAKE starts (rows -+e_k, grad A).    */
+/* The matrix is a cyclic tridiagonal block bordered by the area row and      */
+/* column; it is formed in float and solved by parallel cyclic reduction      */
+/* (after a Sherman-Morrison split of the cyclic corners), exactly the steps  */
+/* of the CUDA kernel, row by row.  Residuals and updates are double.        */
 /* ------------------------------------------------------------------------ */
-static double shake_area(const double* x, int n) {
-    /* sum_k (X_k + X_{k+1}) * dy_k / 2 with X relative to vertex 0
-     * (kernels.cuh:327-332) */
-    double a = 0.0;
-    for (int k = 0; k < n; ++k) {
-        int kn = (k + 1) % n;
-        double x1 = orc_wrap(x[2 * k] - x[0]);
-        double x2 = orc_wrap(x[2 * kn] - x[0]);
-        double dy = orc_wrap(x[2 * kn + 1] - x[2 * k + 1]);
-        a += dy * (x2 + x1) / 2.0;
-    }
-    return a;
-}
+static int pow2_at_least(int n) { int N = 4; while (N < n) N <<= 1; return N; }
 
-/* rows of G at x: unit edge vectors (2n) and area gradient (2n) */
-static void shake_grads(const double* x, int n, double* eh, double* ag) {
-    for (int k = 0; k < n; ++k) {
-        int kn = (k + 1) % n;
-        double ex = orc_wrap(x[2 * kn] - x[2 * k]);
-        double ey = orc_wrap(x[2 * kn + 1] - x[2 * k + 1]);
-        double len = sqrt(ex * ex + ey * ey);
-        if (len > 0) { eh[2 * k] = ex / len; eh[2 * k + 1] = ey / len; }
-        else { eh[2 * k] = 0; eh[2 * k + 1] = 0; }
-    }
-    for (int k = 0; k < n; ++k) {
-        int kn = (k + 1) % n, kp = (k + n - 1) % n;
-        ag[2 * k] = 0.5 * orc_wrap(x[2 * kn + 1] - x[2 * kp + 1]);
-        ag[2 * k + 1] = 0.5 * orc_wrap(x[2 * kp] - x[2 * kn]);
-    }
-}
-
-/* solve dense N x N (row-major) with partial pivoting; returns 0 if singular */
-static int dense_solve(double* Am, double* b, int N) {
-    for (int c = 0; c < N; ++c) {
-        int piv = c; double best = fabs(Am[c * N + c]);
-        for (int r = c + 1; r < N; ++r) if (fabs(Am[r * N + c]) > best) { best = fabs(Am[r * N + c]); piv = r; }
-        if (!(best > 0.0)) return 0;
-        if (piv != c) {
-            for (int k = 0; k < N; ++k) { double t = Am[c * N + k]; Am[c * N + k] = Am[piv * N + k]; Am[piv * N + k] = t; }
-            double t = b[c]; b[c] = b[piv]; b[piv] = t;
+/* parallel cyclic reduction, sequential form; arrays [2][N], 3 rhs */
+static void pcr3_f(float* pa, float* pb, float* pc, float* p0, float* p1, float* p2, int N) {
+    int cur = 0;
+    for (int d = 1; d < N; d <<= 1) {
+        int nx = cur ^ 1;
+        float *a = pa + cur * N, *b = pb + cur * N, *c = pc + cur * N;
+        float *r0 = p0 + cur * N, *r1 = p1 + cur * N, *r2 = p2 + cur * N;
+        float *a2 = pa + nx * N, *b2 = pb + nx * N, *c2 = pc + nx * N;
+        float *s0 = p0 + nx * N, *s1 = p1 + nx * N, *s2 = p2 + nx * N;
+        for (int i = 0; i < N; ++i) {
+            int im = i - d, ip = i + d;
+            float na = 0.f, nc = 0.f;
+            float nb = b[i], n0 = r0[i], n1 = r1[i], n2 = r2[i];
+            if (im >= 0) {
+                float k1 = a[i] / b[im];
+                na = -k1 * a[im];
+                nb -= k1 * c[im];
+                n0 -= k1 * r0[im]; n1 -= k1 * r1[im]; n2 -= k1 * r2[im];
+            }
+            if (ip < N) {
+                float k2 = c[i] / b[ip];
+                nc = -k2 * c[ip];
+                nb -= k2 * a[ip];
+                n0 -= k2 * r0[ip]; n1 -= k2 * r1[ip]; n2 -= k2 * r2[ip];
+            }
+            a2[i] = na; b2[i] = nb; c2[i] = nc; s0[i] = n0; s1[i] = n1; s2[i] = n2;
         }
-        for (int r = c + 1; r < N; ++r) {
-            double f = Am[r * N + c] / Am[c * N + c];
-            if (f == 0.0) continue;
-            for (int k = c; k < N; ++k) Am[r * N + k] -= f * Am[c * N + k];
-            b[r] -= f * b[c];
-        }
+        cur = nx;
     }
-    for (int r = N - 1; r >= 0; --r) {
-        double s = b[r];
-        for (int k = r + 1; k < N; ++k) s -= Am[r * N + k] * b[k];
-        b[r] = s / Am[r * N + r];
+    float *b = pb + cur * N, *r0 = p0 + cur * N, *r1 = p1 + cur * N, *r2 = p2 + cur * N;
+    for (int i = 0; i < N; ++i) {
+        float ib = 1.0f / b[i];
+        float x0 = r0[i] * ib, x1 = r1[i] * ib, x2 = r2[i] * ib;
+        p0[i] = x0; p1[i] = x1; p2[i] = x2;
     }
-    return 1;
 }
 
 static int shake_polygon(orc_model* m, int p, int maxIter, double tol, double* work) {
     int st = m->startIndices[p], n = m->startIndices[p + 1] - st;
     if (n < 3) return 0;
     double L = m->targetEdgeLengths[p], A0 = m->targetAreas[p];
-    double* x = work;                 /* 2n current */
-    double* ehr = x + 2 * n;          /* 2n ref unit edges */
-    double* agr = ehr + 2 * n;        /* 2n ref area grad */
-    double* eh = agr + 2 * n;         /* 2n cur unit edges */
-    double* ag = eh + 2 * n;          /* 2n cur area grad */
-    double* sig = ag + 2 * n;         /* n+1 */
-    double* Mx = sig + (n + 1);       /* (n+1)^2 */
-    int N = n + 1;
+    double invL = L > 0.0 ? 1.0 / L : 1.0;
+    int N = pow2_at_least(n);
+    double* x = work;              /* 2n */
+    double* r = x + 2 * n;         /* 2n reference edges */
+    double* ar = r + 2 * n;        /* 2n reference area gradient */
+    float* f = (float*)(ar + 2 * n);
+    float *rf = f, *arf = rf + 2 * n, *ef = arf + 2 * n, *acf = ef + 2 * n;
+    float *vr = acf + 2 * n, *lam = vr + n;
+    float *pa = lam + n, *pb = pa + 2 * N, *pc = pb + 2 * N;
+    float *p0 = pc + 2 * N, *p1 = p0 + 2 * N, *p2 = p1 + 2 * N;
     for (int i = 0; i < 2 * n; ++i) x[i] = m->positions[2 * st + i];
-    shake_grads(x, n, ehr, agr);
+    for (int k = 0; k < n; ++k) {
+        int kn = (k + 1) % n, kp = (k + n - 1) % n;
+        r[2 * k] = orc_wrap(x[2 * kn] - x[2 * k]);
+        r[2 * k + 1] = orc_wrap(x[2 * kn + 1] - x[2 * k + 1]);
+        ar[2 * k] = 0.5 * orc_wrap(x[2 * kn + 1] - x[2 * kp + 1]);
+        ar[2 * k + 1] = 0.5 * orc_wrap(x[2 * kp] - x[2 * kn]);
+        rf[2 * k] = (float)r[2 * k]; rf[2 * k + 1] = (float)r[2 * k + 1];
+        arf[2 * k] = (float)ar[2 * k]; arf[2 * k + 1] = (float)ar[2 * k + 1];
+    }
     int it = 0;
     for (; it < maxIter; ++it) {
-        double worst = 0.0;
+        double worst = 0.0, area = 0.0;
+        int nonfinite = 0;
         for (int k = 0; k < n; ++k) {
-            int kn = (k + 1) % n;
-            double ex = orc_wrap(x[2 * kn] - x[2 * k]);
-            double ey = orc_wrap(x[2 * kn + 1] - x[2 * k + 1]);
-            sig[k] = sqrt(ex * ex + ey * ey) - L;
-            if (!(fabs(sig[k]) <= worst)) worst = fabs(sig[k]);
+            int kn = (k + 1) % n, kp = (k + n - 1) % n;
+            double ex = orc_wrap(x[2 * kn] - x[2 * k]), ey = orc_wrap(x[2 * kn + 1] - x[2 * k + 1]);
+            double sk = 0.5 * (ex * ex + ey * ey - L * L);
+            double q = fabs(sk) * invL;
+            if (!(q <= worst)) { worst = q; if (!isfinite(q)) nonfinite = 1; }
+            double X1 = orc_wrap(x[2 * k] - x[0]), X2 = orc_wrap(x[2 * kn] - x[0]);
+            area += ey * (X2 + X1) / 2.0;
+            ef[2 * k] = (float)ex; ef[2 * k + 1] = (float)ey;
+            acf[2 * k] = (float)(0.5 * orc_wrap(x[2 * kn + 1] - x[2 * kp + 1]));
+            acf[2 * k + 1] = (float)(0.5 * orc_wrap(x[2 * kp] - x[2 * kn]));
+            lam[k] = (float)(-sk);
         }
-        sig[n] = shake_area(x, n) - A0;
-        if (!(fabs(sig[n]) <= worst)) worst = fabs(sig[n]);
+        double sA = area - A0;
+        if (!(fabs(sA) <= worst)) worst = fabs(sA);
+        if (nonfinite || !isfinite(worst)) { it = maxIter; break; }
         if (worst < tol) break;
-        if (!isfinite(worst)) { it = maxIter; break; }
-        shake_grads(x, n, eh, ag);
-        memset(Mx, 0, (size_t)N * N * 8);
-        /* edge rows: G row j has -eh_j at vertex j and +eh_j at vertex j+1 */
-        for (int j = 0; j < n; ++j) {
-            int j1 = (j + 1) % n;
-            for (int c = 0; c < n; ++c) {
-                int c1 = (c + 1) % n;
-                /* column c of G_ref^T: -ehr_c at vertex c, +ehr_c at vertex c+1 */
-                double s = 0.0;
-                if (j == c)  s += eh[2*j] * ehr[2*c] + eh[2*j+1] * ehr[2*c+1];
-                if (j == c1) s -= eh[2*j] * ehr[2*c] + eh[2*j+1] * ehr[2*c+1];
-                if (j1 == c) s -= eh[2*j] * ehr[2*c] + eh[2*j+1] * ehr[2*c+1];
-                if (j1 == c1) s += eh[2*j] * ehr[2*c] + eh[2*j+1] * ehr[2*c+1];
-                Mx[j * N + c] = s;
-            }
-            Mx[j * N + n] = -(eh[2*j] * agr[2*j] + eh[2*j+1] * agr[2*j+1])
-                            + (eh[2*j] * agr[2*j1] + eh[2*j+1] * agr[2*j1+1]);
+        float dc = 0.f;
+        for (int k = 0; k < n; ++k) {
+            int kn = (k + 1) % n, kp = (k + n - 1) % n;
+            float ex = ef[2 * k], ey = ef[2 * k + 1];
+            pb[k] = 2.0f * (ex * rf[2 * k] + ey * rf[2 * k + 1]);
+            pc[k] = -(ex * rf[2 * kn] + ey * rf[2 * kn + 1]);
+            pa[k] = -(ex * rf[2 * kp] + ey * rf[2 * kp + 1]);
+            p0[k] = lam[k];
+            p1[k] = ex * (arf[2 * kn] - arf[2 * k]) + ey * (arf[2 * kn + 1] - arf[2 * k + 1]);
+            p2[k] = 0.f;
+            vr[k] = (acf[2 * kn] - acf[2 * k]) * rf[2 * k] + (acf[2 * kn + 1] - acf[2 * k + 1]) * rf[2 * k + 1];
+            dc += acf[2 * k] * arf[2 * k] + acf[2 * k + 1] * arf[2 * k + 1];
         }
-        for (int c = 0; c < n; ++c) {
-            int c1 = (c + 1) % n;
-            Mx[n * N + c] = -(ag[2*c] * ehr[2*c] + ag[2*c+1] * ehr[2*c+1])
-                            + (ag[2*c1] * ehr[2*c] + ag[2*c1+1] * ehr[2*c+1]);
+        for (int k = n; k < N; ++k) { pa[k] = 0.f; pb[k] = 1.f; pc[k] = 0.f; p0[k] = 0.f; p1[k] = 0.f; p2[k] = 0.f; }
+        float gamma = -pb[0], beta = pa[0], alpha = pc[n - 1];
+        if (!(gamma != 0.f)) { it = maxIter; break; }
+        pb[0] = pb[0] - gamma;
+        pb[n - 1] = pb[n - 1] - alpha * beta / gamma;
+        pa[0] = 0.f; pc[n - 1] = 0.f;
+        p2[0] = gamma; p2[n - 1] = alpha;
+        pcr3_f(pa, pb, pc, p0, p1, p2, N);
+        float den = 1.f + p2[0] + beta * p2[n - 1] / gamma;
+        float fy = (p0[0] + beta * p0[n - 1] / gamma) / den;
+        float fz = (p1[0] + beta * p1[n - 1] / gamma) / den;
+        float vy = 0.f, vz = 0.f;
+        for (int k = 0; k < n; ++k) {
+            float sv = p2[k];
+            float yk = p0[k] - fy * sv, zk = p1[k] - fz * sv;
+            p0[k] = yk; p1[k] = zk;
+            vy += vr[k] * yk; vz += vr[k] * zk;
         }
-        {
-            double s = 0.0;
-            for (int i = 0; i < 2 * n; ++i) s += ag[i] * agr[i];
-            Mx[n * N + n] = s;
+        float mu = (-(float)sA - vy) / (dc - vz);
+        int finite = isfinite(mu);
+        for (int k = 0; k < n; ++k) {
+            lam[k] = p0[k] - mu * p1[k];
+            finite = finite && isfinite(lam[k]);
         }
-        for (int i = 0; i < N; ++i) sig[i] = -sig[i];
-        if (!dense_solve(Mx, sig, N)) { it = maxIter; break; }
-        /* x += G_ref^T dl */
-        for (int c = 0; c < n; ++c) {
-            int c1 = (c + 1) % n;
-            double l = sig[c];
-            x[2 * c] -= l * ehr[2 * c];      x[2 * c + 1] -= l * ehr[2 * c + 1];
-            x[2 * c1] += l * ehr[2 * c];     x[2 * c1 + 1] += l * ehr[2 * c + 1];
+        if (!finite) { it = maxIter; break; }
+        double mu64 = (double)mu;
+        for (int k = 0; k < n; ++k) {
+            int kp = (k + n - 1) % n;
+            double lk = (double)lam[k], lp = (double)lam[kp];
+            x[2 * k] += -lk * r[2 * k] + lp * r[2 * kp] + mu64 * ar[2 * k];
+            x[2 * k + 1] += -lk * r[2 * k + 1] + lp * r[2 * kp + 1] + mu64 * ar[2 * k + 1];
         }
-        for (int i = 0; i < 2 * n; ++i) x[i] += sig[n] * agr[i];
     }
     for (int i = 0; i < 2 * n; ++i) {
         double v = x[i];
@@ -1163,7 +1173,7 @@ int orc_shake_project(orc_model* m, int nIter, double tol) {
     int worst = 0;
     #pragma omp parallel reduction(max:worst)
     {
-        double* work = (double*)xcalloc((size_t)10 * nmax + (size_t)(nmax + 1) * (nmax + 2) + 8, 8);
+        double* work = (double*)xcalloc((size_t)40 * nmax + 64, 8);
         #pragma omp for schedule(dynamic, 16)
         for (int p = 0; p < P; ++p) {
             int it = shake_polygon(m, p, nIter, tol, work);

@@ -23,57 +23,85 @@ static inline int nblk(long long n, int t) {
     return b < 1 ? 1 : (int)b;
 }
 
-// Solve three right-hand sides of a cyclic tridiagonal system
-//   lo[k] x[k-1] + di[k] x[k] + up[k] x[k+1] = d[k]   (indices mod n, n >= 3)
-// by Sherman-Morrison on top of the Thomas algorithm.  All arrays are strided
-// views into per-vertex scratch; d0..d2 are overwritten by the solutions.
-// cp is scratch.  Returns false when a pivot vanishes.
-struct Tri {
-    const double* lo; const double* di; const double* up;
+// Strided view of one per-vertex scratch array: element k of the polygon a
+// thread works on lives at p[k * s].  In shared memory the arrays are laid out
+// [array][k][lane] (s = 32, bank-conflict free); in the global fallback they
+// are indexed by vertex (s = 1).
+struct Arr {
+    double* p;
+    int s;
+    __device__ __forceinline__ double& operator[](int k) const { return p[(size_t)k * s]; }
 };
 
-__device__ bool cyclic_solve3(int n, Tri T, double* d0, double* d1, double* d2, double* cp,
-                              double* zs) {
-    const double gamma = -T.di[0];
-    const double beta = T.lo[0];          // coefficient of x[n-1] in row 0
-    const double alpha = T.up[n - 1];     // coefficient of x[0] in row n-1
+struct Scratch {
+    double* base;
+    size_t arrStride;   // distance between arrays
+    int kStride;        // distance between consecutive vertices
+    __device__ __forceinline__ Arr arr(int a) const { return Arr{base + (size_t)a * arrStride, kStride}; }
+};
+
+// Scratch of the polygon handled by this thread: shared memory when the
+// launch provided it (smemN > 0 vertices per thread), else the global array.
+__device__ __forceinline__ Scratch thread_scratch(double* smem, int smemN, double* global, int V,
+                                                  int st) {
+    if (smemN > 0) return Scratch{smem + (threadIdx.x & 31), (size_t)smemN * 32, 32};
+    return Scratch{global + st, (size_t)V, 1};
+}
+
+// Solve `nr` (1..3) right-hand sides of a cyclic tridiagonal system
+//   lo[k] x[k-1] + di[k] x[k] + up[k] x[k+1] = d[k]   (indices mod n, n >= 3)
+// by Sherman-Morrison on top of the Thomas algorithm.  The right-hand sides
+// are overwritten by the solutions; cp and zs are scratch.  Returns false
+// when a pivot vanishes.
+__device__ bool cyclic_solve(int n, Arr lo, Arr di, Arr up, int nr, Arr d0, Arr d1, Arr d2,
+                             Arr cp, Arr zs) {
+    const double gamma = -di[0];
+    const double beta = lo[0];          // coefficient of x[n-1] in row 0
+    const double alpha = up[n - 1];     // coefficient of x[0] in row n-1
     if (gamma == 0.0) return false;
-    // forward sweep for the modified tridiagonal, 4 right-hand sides
-    // (d0, d1, d2 and the Sherman-Morrison vector u = (gamma, 0.., alpha))
-    double b0 = T.di[0] - gamma;
+    double b0 = di[0] - gamma;
     if (b0 == 0.0) return false;
     double inv = 1.0 / b0;
-    cp[0] = T.up[0] * inv;
-    d0[0] *= inv; d1[0] *= inv; d2[0] *= inv;
+    cp[0] = up[0] * inv;
+    d0[0] *= inv;
+    if (nr > 1) d1[0] *= inv;
+    if (nr > 2) d2[0] *= inv;
     zs[0] = gamma * inv;
+    double cpPrev = cp[0], z0 = d0[0], z1 = nr > 1 ? d1[0] : 0.0, z2 = nr > 2 ? d2[0] : 0.0;
+    double zsPrev = zs[0];
     for (int k = 1; k < n; ++k) {
-        double bk = T.di[k];
+        double bk = di[k];
         if (k == n - 1) bk -= alpha * beta / gamma;
-        double m = bk - T.lo[k] * cp[k - 1];
+        double l = lo[k];
+        double m = bk - l * cpPrev;
         if (m == 0.0) return false;
         double im = 1.0 / m;
-        cp[k] = (k < n - 1) ? T.up[k] * im : 0.0;
-        d0[k] = (d0[k] - T.lo[k] * d0[k - 1]) * im;
-        d1[k] = (d1[k] - T.lo[k] * d1[k - 1]) * im;
-        d2[k] = (d2[k] - T.lo[k] * d2[k - 1]) * im;
+        cpPrev = (k < n - 1) ? up[k] * im : 0.0;
+        cp[k] = cpPrev;
+        z0 = (d0[k] - l * z0) * im; d0[k] = z0;
+        if (nr > 1) { z1 = (d1[k] - l * z1) * im; d1[k] = z1; }
+        if (nr > 2) { z2 = (d2[k] - l * z2) * im; d2[k] = z2; }
         double uk = (k == n - 1) ? alpha : 0.0;
-        zs[k] = (uk - T.lo[k] * zs[k - 1]) * im;
+        zsPrev = (uk - l * zsPrev) * im;
+        zs[k] = zsPrev;
     }
     for (int k = n - 2; k >= 0; --k) {
-        d0[k] -= cp[k] * d0[k + 1];
-        d1[k] -= cp[k] * d1[k + 1];
-        d2[k] -= cp[k] * d2[k + 1];
-        zs[k] -= cp[k] * zs[k + 1];
+        double c = cp[k];
+        z0 = d0[k] - c * z0; d0[k] = z0;
+        if (nr > 1) { z1 = d1[k] - c * z1; d1[k] = z1; }
+        if (nr > 2) { z2 = d2[k] - c * z2; d2[k] = z2; }
+        zsPrev = zs[k] - c * zsPrev; zs[k] = zsPrev;
     }
     double den = 1.0 + zs[0] + beta * zs[n - 1] / gamma;
     if (den == 0.0) return false;
     double f0 = (d0[0] + beta * d0[n - 1] / gamma) / den;
-    double f1 = (d1[0] + beta * d1[n - 1] / gamma) / den;
-    double f2 = (d2[0] + beta * d2[n - 1] / gamma) / den;
+    double f1 = nr > 1 ? (d1[0] + beta * d1[n - 1] / gamma) / den : 0.0;
+    double f2 = nr > 2 ? (d2[0] + beta * d2[n - 1] / gamma) / den : 0.0;
     for (int k = 0; k < n; ++k) {
-        d0[k] -= f0 * zs[k];
-        d1[k] -= f1 * zs[k];
-        d2[k] -= f2 * zs[k];
+        double z = zs[k];
+        d0[k] -= f0 * z;
+        if (nr > 1) d1[k] -= f1 * z;
+        if (nr > 2) d2[k] -= f2 * z;
     }
     return true;
 }
@@ -86,20 +114,23 @@ __device__ bool cyclic_solve3(int n, Tri T, double* d0, double* d1, double* d2, 
 // J column k = -t_k at vertex k, +t_k at vertex k+1 (buildEdgeGradMatrix,
 // kernels.cuh:389-406); J^T J is cyclic tridiagonal with 2 on the diagonal
 // and -t_k.t_{k+1} beside it.  Edges shorter than 1e-14 are left out, as
-// the reference leaves their column zero.
+// the reference leaves their column zero.  One polygon per thread, 32
+// threads per block so that small systems still spread over the SMs.
 //
 // When `fire` is given (device-resident FIRE step) the kernel also applies
 // the FIRE velocity half-kick v += dt/2 F'' and accumulates F.v, |v|^2 and
 // |F|^2 (Model::minimizeFIREStep lines 471-472) if the step is neither a
 // SHAKE failure nor an energy-increase rollback, and always max |F''|.
-struct ProjScratch { double* s; int V; };
+constexpr int kProjArrays = 11;
+constexpr int kConsThreads = 32;
 
-__global__ void __launch_bounds__(128)
+__global__ void __launch_bounds__(kConsThreads)
 k_project(const double2* __restrict__ pos, const int* __restrict__ start, int P,
           const double* __restrict__ constraints, double2* __restrict__ force,
-          double* __restrict__ scratch, int V, Ctrl* fire, double2* __restrict__ vel,
-          const int* gate) {
+          double* __restrict__ scratch, int V, int smemN, int areaFromPositions, Ctrl* fire,
+          double2* __restrict__ vel, const int* gate) {
     if (gate_closed(gate)) return;
+    extern __shared__ double cons_smem[];
     int p = blockIdx.x * blockDim.x + threadIdx.x;
     bool proceed = false;
     double dt = 0.0;
@@ -118,18 +149,30 @@ k_project(const double2* __restrict__ pos, const int* __restrict__ start, int P,
     double sP = 0.0, sV = 0.0, sF = 0.0, mF = 0.0;
     if (p < P) {
         int st = start[p], n = start[p + 1] - st;
+        int useSmem = (n <= smemN) ? smemN : 0;
         if (n >= 3) {
-            // scratch layout per vertex (stride V): tx ty lo di up r0 r1 r2 cp zs
-            double* tx = scratch + 0 * (size_t)V + st;
-            double* ty = scratch + 1 * (size_t)V + st;
-            double* lo = scratch + 2 * (size_t)V + st;
-            double* di = scratch + 3 * (size_t)V + st;
-            double* up = scratch + 4 * (size_t)V + st;
-            double* r0 = scratch + 5 * (size_t)V + st;
-            double* r1 = scratch + 6 * (size_t)V + st;
-            double* r2 = scratch + 7 * (size_t)V + st;
-            double* cp = scratch + 8 * (size_t)V + st;
-            double* zs = scratch + 9 * (size_t)V + st;
+            Scratch S = thread_scratch(cons_smem, useSmem, scratch, V, st);
+            Arr tx = S.arr(0), ty = S.arr(1), lo = S.arr(2), di = S.arr(3), up = S.arr(4);
+            Arr r0 = S.arr(5), r1 = S.arr(6), ac = S.arr(7), cp = S.arr(8), zs = S.arr(9);
+            Arr ad = S.arr(10);   // unit area gradient (x in ac, y in ad)
+            double an = 0.0;
+            for (int k = 0; k < n; ++k) {
+                int kn = (k + 1 == n) ? 0 : k + 1, kp = (k == 0) ? n - 1 : k - 1;
+                double a0, a1;
+                if (areaFromPositions) {
+                    double2 xp = pos[st + kp], xn = pos[st + kn];
+                    a0 = -wrap(xp.y - xn.y); a1 = wrap(xp.x - xn.x);
+                    an += a0 * a0 + a1 * a1;
+                } else {
+                    const double* c = constraints + 6 * (size_t)(st + k);
+                    a0 = c[0]; a1 = c[1];
+                }
+                ac[k] = a0; ad[k] = a1;
+            }
+            if (areaFromPositions && an > 0.0) {
+                double ir = 1.0 / sqrt(an);
+                for (int k = 0; k < n; ++k) { ac[k] *= ir; ad[k] *= ir; }
+            }
             for (int k = 0; k < n; ++k) {
                 int kn = (k + 1 == n) ? 0 : k + 1;
                 double2 a = pos[st + k], b = pos[st + kn];
@@ -138,43 +181,48 @@ k_project(const double2* __restrict__ pos, const int* __restrict__ start, int P,
                 if (len < 1e-14) { tx[k] = 0.0; ty[k] = 0.0; di[k] = 1.0; }
                 else { double il = 1.0 / len; tx[k] = dx * il; ty[k] = dy * il; di[k] = 2.0; }
             }
+            double tx0 = tx[0], ty0 = ty[0];
+            double txk = tx0, tyk = ty0;
+            double2 f0 = force[st];
+            double2 fk = f0;
+            double ck0 = ac[0], ck1 = ad[0];
+            double ak0 = ck0, ak1 = ck1;
             for (int k = 0; k < n; ++k) {
                 int kn = (k + 1 == n) ? 0 : k + 1;
-                double o = -(tx[k] * tx[kn] + ty[k] * ty[kn]);
+                double txn = (kn == 0) ? tx0 : tx[kn], tyn = (kn == 0) ? ty0 : ty[kn];
+                double o = -(txk * txn + tyk * tyn);
                 up[k] = o;
                 lo[kn] = o;
-                double2 f0 = force[st + k], f1 = force[st + kn];
-                r0[k] = tx[k] * (f1.x - f0.x) + ty[k] * (f1.y - f0.y);
-                const double* c0 = constraints + 6 * (size_t)(st + k);
-                const double* c1 = constraints + 6 * (size_t)(st + kn);
-                r1[k] = tx[k] * (c1[0] - c0[0]) + ty[k] * (c1[1] - c0[1]);
-                r2[k] = 0.0;
+                double2 f1 = (kn == 0) ? f0 : force[st + kn];
+                double a0 = (kn == 0) ? ck0 : ac[kn], a1 = (kn == 0) ? ck1 : ad[kn];
+                r0[k] = txk * (f1.x - fk.x) + tyk * (f1.y - fk.y);
+                r1[k] = txk * (a0 - ak0) + tyk * (a1 - ak1);
+                txk = txn; tyk = tyn; fk = f1; ak0 = a0; ak1 = a1;
             }
-            Tri T{lo, di, up};
-            bool ok = cyclic_solve3(n, T, r0, r1, r2, cp, zs);
+            bool ok = cyclic_solve(n, lo, di, up, 2, r0, r1, r1, cp, zs);
             if (ok) {
                 double qF = 0.0, qq = 0.0;
+                // reuse lo/up for F' and cp/zs for q
+                double txp = tx[n - 1], typ = ty[n - 1], l0p = r0[n - 1], l1p = r1[n - 1];
                 for (int k = 0; k < n; ++k) {
-                    int kp = (k == 0) ? n - 1 : k - 1;
+                    double txc = tx[k], tyc = ty[k], l0 = r0[k], l1 = r1[k];
                     // (J x)_k = -x_k t_k + x_{k-1} t_{k-1}
-                    double jlx = -r0[k] * tx[k] + r0[kp] * tx[kp];
-                    double jly = -r0[k] * ty[k] + r0[kp] * ty[kp];
-                    double jmx = -r1[k] * tx[k] + r1[kp] * tx[kp];
-                    double jmy = -r1[k] * ty[k] + r1[kp] * ty[kp];
-                    const double* c0 = constraints + 6 * (size_t)(st + k);
-                    double qx = c0[0] - jmx, qy = c0[1] - jmy;
+                    double jlx = -l0 * txc + l0p * txp, jly = -l0 * tyc + l0p * typ;
+                    double jmx = -l1 * txc + l1p * txp, jmy = -l1 * tyc + l1p * typ;
+                    double q0 = ac[k] - jmx, q1 = ad[k] - jmy;
                     double2 f = force[st + k];
                     double fx = f.x - jlx, fy = f.y - jly;
-                    cp[k] = qx; zs[k] = qy;        // reuse scratch for q
-                    r2[k] = fx; lo[k] = fy;        // and for F'
-                    qF += qx * fx + qy * fy;
-                    qq += qx * qx + qy * qy;
+                    cp[k] = q0; zs[k] = q1;
+                    lo[k] = fx; up[k] = fy;
+                    qF += q0 * fx + q1 * fy;
+                    qq += q0 * q0 + q1 * q1;
+                    txp = txc; typ = tyc; l0p = l0; l1p = l1;
                 }
                 double mag = sqrt(qq);
                 double coef = (mag > 1e-14) ? qF / qq : 0.0;
                 for (int k = 0; k < n; ++k) {
-                    double fx = r2[k] - coef * cp[k];
-                    double fy = lo[k] - coef * zs[k];
+                    double fx = lo[k] - coef * cp[k];
+                    double fy = up[k] - coef * zs[k];
                     force[st + k] = make_double2(fx, fy);
                     mF = fmax(mF, fmax(fabs(fx), fabs(fy)));
                     if (proceed) {
@@ -219,139 +267,547 @@ k_project(const double2* __restrict__ pos, const int* __restrict__ start, int P,
     }
 }
 
-cudaError_t launch_project(const double2* pos, const int* start, int P,
-                           const double* constraints, double2* force, double* scratch, int V,
-                           Ctrl* fireCtrl, const int* gate, double2* vel, cudaStream_t st) {
-    if (P <= 0) return cudaSuccess;
-    k_project<<<nblk(P, 128), 128, 0, st>>>(pos, start, P, constraints, force, scratch, V,
-                                            fireCtrl, vel, gate);
-    return cudaGetLastError();
+// vertices per thread that fit in shared memory for `arrays` scratch arrays
+static int smem_vertices(int nmax, int arrays) {
+    size_t per = (size_t)arrays * kConsThreads * sizeof(double);
+    size_t cap = 200 * 1024;
+    if (nmax <= 0 || (size_t)nmax * per > cap) return 0;
+    return nmax;
 }
 
 // ------------------------------------------------------------------ SHAKE ----
 // shakeProjectCUDA (model.cu:616-636; the kernel itself, src/shake.h, is not
-// in the reference tree).  Restated as matrix SHAKE with Newton steps in the
-// multipliers:  sigma_k = |e_k| - L, sigma_n = A - A0;  x += G_ref^T dl with
-// (G(x) G_ref^T) dl = -sigma(x), G_ref the constraint gradients at entry.
-// G(x) G_ref^T is a cyclic tridiagonal block (edges) bordered by one row and
-// column (area); it is solved through two cyclic tridiagonal solves.  Each
-// iteration first tests max|sigma| < tol; the count is the number of updates.
-__device__ __forceinline__ double poly_area_rel(const double2* x, int n) {
-    // sum (X_k + X_{k+1}) dy_k / 2 relative to vertex 0 (kernels.cuh:327-332)
-    double a = 0.0;
-    double2 p0 = x[0];
-    for (int k = 0; k < n; ++k) {
-        int kn = (k + 1 == n) ? 0 : k + 1;
-        double x1 = wrap(x[k].x - p0.x), x2 = wrap(x[kn].x - p0.x);
-        double dy = wrap(x[kn].y - x[k].y);
-        a += dy * (x2 + x1) / 2.0;
-    }
-    return a;
+// in the reference tree).  Restated as matrix SHAKE, Newton steps in the
+// multipliers with the correction solved in FP32:
+//   s_k = (|e_k|^2 - L^2) / 2  (edge k, e_k = wrap(x_{k+1} - x_k)),
+//   s_A = A - A0               (shoelace of updatePolygonGeometryKernel),
+//   converged when max(max_k |s_k| / L, |s_A|) < tol  (|s_k|/L ~ ||e_k| - L|);
+//   otherwise x += G_ref^T l with (G(x) G_ref^T) l = -s, G_ref the
+//   constraint gradients where SHAKE started (rows -+e_k, grad A).
+// Residuals and the update are FP64 (the tolerance is met in FP64); the
+// matrix (a cyclic tridiagonal block bordered by the area row and column)
+// is formed and solved in FP32 by parallel cyclic reduction with a
+// Sherman-Morrison correction for the cyclic corners.  Each FP32 solve is
+// accurate to ~1e-5 relative, so the iteration still converges in about as
+// many steps as an FP64 Newton iteration while the FP64 work per vertex
+// and iteration drops to ~45 operations.  One warp per polygon.
+__device__ __forceinline__ int pow2_at_least(int n) {
+    int N = 4;
+    while (N < n) N <<= 1;
+    return N;
 }
 
-__global__ void __launch_bounds__(128)
-k_shake(double2* __restrict__ pos, const int* __restrict__ start, int P,
-        const double* __restrict__ targetEdge, const double* __restrict__ targetArea,
-        int maxIter, double tol, int* __restrict__ itersOut, double* __restrict__ scratch,
-        int V, const int* gate) {
+struct ShakeWS {
+    double2 *xs, *r, *ar;
+    float2 *rf, *arf, *ef, *acf;
+    float *vr, *lam;
+    float *pa, *pb, *pc, *p0, *p1, *p2;   // [2][N] each
+};
+
+__device__ __forceinline__ ShakeWS shake_ws(unsigned char* base, int NV, int N) {
+    ShakeWS w;
+    double2* d = reinterpret_cast<double2*>(base);
+    w.xs = d; w.r = d + NV; w.ar = d + 2 * NV;
+    float2* f2 = reinterpret_cast<float2*>(d + 3 * NV);
+    w.rf = f2; w.arf = f2 + NV; w.ef = f2 + 2 * NV; w.acf = f2 + 3 * NV;
+    float* f = reinterpret_cast<float*>(f2 + 4 * NV);
+    w.vr = f; w.lam = f + NV;
+    float* q = f + 2 * NV;
+    w.pa = q; w.pb = q + 2 * N; w.pc = q + 4 * N; w.p0 = q + 6 * N; w.p1 = q + 8 * N; w.p2 = q + 10 * N;
+    return w;
+}
+// bytes of one polygon's workspace (NV vertex slots, N PCR rows); a multiple
+// of 16 whenever NV is even
+__host__ __device__ constexpr size_t shake_ws_bytes(int NV, int N) {
+    return (size_t)NV * (3 * 16 + 4 * 8 + 2 * 4) + (size_t)N * 12 * 4;
+}
+
+// Parallel cyclic reduction of the N rows in buffer 0 of w (three
+// right-hand sides); leaves x = r / b in p0, p1, p2.  One warp, rows strided.
+__device__ void pcr3(ShakeWS& w, int N) {
+    const int lane = threadIdx.x & 31;
+    int cur = 0;
+    for (int d = 1; d < N; d <<= 1) {
+        int nxt = cur ^ 1;
+        const float *a = w.pa + cur * N, *b = w.pb + cur * N, *c = w.pc + cur * N;
+        const float *r0 = w.p0 + cur * N, *r1 = w.p1 + cur * N, *r2 = w.p2 + cur * N;
+        float *a2 = w.pa + nxt * N, *b2 = w.pb + nxt * N, *c2 = w.pc + nxt * N;
+        float *s0 = w.p0 + nxt * N, *s1 = w.p1 + nxt * N, *s2 = w.p2 + nxt * N;
+        for (int i = lane; i < N; i += 32) {
+            int im = i - d, ip = i + d;
+            float na = 0.f, nc = 0.f;
+            float nb = b[i], n0 = r0[i], n1 = r1[i], n2 = r2[i];
+            if (im >= 0) {
+                float k1 = a[i] / b[im];
+                na = -k1 * a[im];
+                nb -= k1 * c[im];
+                n0 -= k1 * r0[im]; n1 -= k1 * r1[im]; n2 -= k1 * r2[im];
+            }
+            if (ip < N) {
+                float k2 = c[i] / b[ip];
+                nc = -k2 * c[ip];
+                nb -= k2 * a[ip];
+                n0 -= k2 * r0[ip]; n1 -= k2 * r1[ip]; n2 -= k2 * r2[ip];
+            }
+            a2[i] = na; b2[i] = nb; c2[i] = nc; s0[i] = n0; s1[i] = n1; s2[i] = n2;
+        }
+        __syncwarp();
+        cur = nxt;
+    }
+    // solutions into buffer 0 (when the final buffer is 1 it is a distinct array)
+    const float *b = w.pb + cur * N, *r0 = w.p0 + cur * N, *r1 = w.p1 + cur * N;
+    const float *r2 = w.p2 + cur * N;
+    for (int i = lane; i < N; i += 32) {
+        float ib = 1.0f / b[i];
+        float x0 = r0[i] * ib, x1 = r1[i] * ib, x2 = r2[i] * ib;
+        w.p0[i] = x0; w.p1[i] = x1; w.p2[i] = x2;
+    }
+    __syncwarp();
+}
+
+__global__ void k_shake(double2* __restrict__ pos, const int* __restrict__ start, int P,
+                        const double* __restrict__ targetEdge,
+                        const double* __restrict__ targetArea, int maxIter, double tol,
+                        int* __restrict__ itersOut, double* __restrict__ scratch, int nmaxSmem,
+                        const int* gate) {
     if (gate_closed(gate)) return;
-    int p = blockIdx.x * blockDim.x + threadIdx.x;
+    extern __shared__ __align__(16) unsigned char shake_smem[];
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    const int wpb = blockDim.x >> 5;
+    int p = blockIdx.x * wpb + warp;
     int it = 0;
     if (p < P) {
         int st = start[p], n = start[p + 1] - st;
         if (n >= 3 && maxIter > 0) {
-            double L = targetEdge[p], A0 = targetArea[p];
-            double2* x = pos + st;
-            double* erx = scratch + 0 * (size_t)V + st;   // reference unit edges
-            double* ery = scratch + 1 * (size_t)V + st;
-            double* arx = scratch + 2 * (size_t)V + st;   // reference area gradient
-            double* ary = scratch + 3 * (size_t)V + st;
-            double* ecx = scratch + 4 * (size_t)V + st;   // current unit edges
-            double* ecy = scratch + 5 * (size_t)V + st;
-            double* lo = scratch + 6 * (size_t)V + st;
-            double* di = scratch + 7 * (size_t)V + st;
-            double* up = scratch + 8 * (size_t)V + st;
-            double* y = scratch + 9 * (size_t)V + st;     // -sigma_e -> T^-1 (-sigma_e)
-            double* w = scratch + 10 * (size_t)V + st;    // border column -> T^-1 w
-            double* dummy = scratch + 11 * (size_t)V + st;
-            double* cp = scratch + 12 * (size_t)V + st;
-            double* zs = scratch + 13 * (size_t)V + st;
-            double* vrow = scratch + 14 * (size_t)V + st; // border row
-            double* acx = scratch + 15 * (size_t)V + st;  // current area gradient
-            double* acy = scratch + 16 * (size_t)V + st;
-            for (int k = 0; k < n; ++k) {
+            ShakeWS w;
+            int N;
+            if (n <= nmaxSmem) {
+                N = pow2_at_least(nmaxSmem);
+                w = shake_ws(shake_smem + (size_t)warp * shake_ws_bytes(nmaxSmem, N), nmaxSmem, N);
+            } else {
+                // per-polygon slice of the global scratch (kScratchPerVertex
+                // doubles per vertex >= shake_ws_bytes(n, 2n) / 8)
+                N = pow2_at_least(n);
+                w = shake_ws(reinterpret_cast<unsigned char*>(scratch + (size_t)kScratchPerVertex * st),
+                             n, N);
+            }
+            const double L = targetEdge[p], A0 = targetArea[p];
+            const double invL = L > 0.0 ? 1.0 / L : 1.0;
+            for (int k = lane; k < n; k += 32) w.xs[k] = pos[st + k];
+            __syncwarp();
+            for (int k = lane; k < n; k += 32) {
                 int kn = (k + 1 == n) ? 0 : k + 1, kp = (k == 0) ? n - 1 : k - 1;
-                double ex = wrap(x[kn].x - x[k].x), ey = wrap(x[kn].y - x[k].y);
-                double len = sqrt(ex * ex + ey * ey);
-                if (len > 0.0) { erx[k] = ex / len; ery[k] = ey / len; }
-                else { erx[k] = 0.0; ery[k] = 0.0; }
-                arx[k] = 0.5 * wrap(x[kn].y - x[kp].y);
-                ary[k] = 0.5 * wrap(x[kp].x - x[kn].x);
+                double2 xk = w.xs[k], xn = w.xs[kn], xp = w.xs[kp];
+                double2 r = make_double2(wrap(xn.x - xk.x), wrap(xn.y - xk.y));
+                double2 a = make_double2(0.5 * wrap(xn.y - xp.y), 0.5 * wrap(xp.x - xn.x));
+                w.r[k] = r; w.ar[k] = a;
+                w.rf[k] = make_float2((float)r.x, (float)r.y);
+                w.arf[k] = make_float2((float)a.x, (float)a.y);
             }
+            __syncwarp();
             for (; it < maxIter; ++it) {
-                double worst = 0.0;
-                for (int k = 0; k < n; ++k) {
-                    int kn = (k + 1 == n) ? 0 : k + 1;
-                    double ex = wrap(x[kn].x - x[k].x), ey = wrap(x[kn].y - x[k].y);
-                    double len = sqrt(ex * ex + ey * ey);
-                    double s = len - L;
-                    y[k] = -s;
-                    if (!(fabs(s) <= worst)) worst = fabs(s);
-                    if (len > 0.0) { ecx[k] = ex / len; ecy[k] = ey / len; }
-                    else { ecx[k] = 0.0; ecy[k] = 0.0; }
-                }
-                double sA = poly_area_rel(x, n) - A0;
-                if (!(fabs(sA) <= worst)) worst = fabs(sA);
-                if (worst < tol) break;
-                if (!isfinite(worst)) { it = maxIter; break; }
-                double dcorner = 0.0;
-                for (int k = 0; k < n; ++k) {
+                // residuals (FP64)
+                double worst = 0.0, area = 0.0;
+                bool nonfinite = false;
+                double x0x = w.xs[0].x;
+                for (int k = lane; k < n; k += 32) {
                     int kn = (k + 1 == n) ? 0 : k + 1, kp = (k == 0) ? n - 1 : k - 1;
-                    acx[k] = 0.5 * wrap(x[kn].y - x[kp].y);
-                    acy[k] = 0.5 * wrap(x[kp].x - x[kn].x);
-                    dcorner += acx[k] * arx[k] + acy[k] * ary[k];
+                    double2 xk = w.xs[k], xn = w.xs[kn], xp = w.xs[kp];
+                    double ex = wrap(xn.x - xk.x), ey = wrap(xn.y - xk.y);
+                    double sk = 0.5 * (ex * ex + ey * ey - L * L);
+                    double q = fabs(sk) * invL;
+                    if (!(q <= worst)) { worst = q; nonfinite |= !isfinite(q); }
+                    double X1 = wrap(xk.x - x0x), X2 = wrap(xn.x - x0x);
+                    area += ey * (X2 + X1) / 2.0;
+                    w.ef[k] = make_float2((float)ex, (float)ey);
+                    w.acf[k] = make_float2((float)(0.5 * wrap(xn.y - xp.y)),
+                                           (float)(0.5 * wrap(xp.x - xn.x)));
+                    w.lam[k] = (float)(-sk);      // right-hand side until the rows are built
                 }
-                for (int j = 0; j < n; ++j) {
-                    int jn = (j + 1 == n) ? 0 : j + 1, jp = (j == 0) ? n - 1 : j - 1;
-                    double cx = ecx[j], cy = ecy[j];
-                    di[j] = 2.0 * (cx * erx[j] + cy * ery[j]);
-                    up[j] = -(cx * erx[jn] + cy * ery[jn]);
-                    lo[j] = -(cx * erx[jp] + cy * ery[jp]);
-                    w[j] = cx * (arx[jn] - arx[j]) + cy * (ary[jn] - ary[j]);
-                    vrow[j] = (acx[jn] - acx[j]) * erx[j] + (acy[jn] - acy[j]) * ery[j];
-                    dummy[j] = 0.0;
+                worst = warp_maxd(worst);
+                area = warp_sum(area);
+                nonfinite = __any_sync(PCP_FULL, nonfinite);
+                double sA = area - A0;
+                if (!(fabs(sA) <= worst)) worst = fabs(sA);
+                if (nonfinite || !isfinite(worst)) { it = maxIter; break; }
+                if (worst < tol) break;
+                __syncwarp();
+                // rows of G(x) G_ref^T (FP32) into PCR buffer 0
+                float dc = 0.f;
+                for (int k = lane; k < n; k += 32) {
+                    int kn = (k + 1 == n) ? 0 : k + 1, kp = (k == 0) ? n - 1 : k - 1;
+                    float2 e = w.ef[k], rk = w.rf[k], rn = w.rf[kn], rp = w.rf[kp];
+                    float2 an = w.arf[kn], ak = w.arf[k], cn = w.acf[kn], ck = w.acf[k];
+                    w.pb[k] = 2.0f * (e.x * rk.x + e.y * rk.y);
+                    w.pc[k] = -(e.x * rn.x + e.y * rn.y);
+                    w.pa[k] = -(e.x * rp.x + e.y * rp.y);
+                    w.p0[k] = w.lam[k];
+                    w.p1[k] = e.x * (an.x - ak.x) + e.y * (an.y - ak.y);
+                    w.p2[k] = 0.f;
+                    w.vr[k] = (cn.x - ck.x) * rk.x + (cn.y - ck.y) * rk.y;
+                    dc += ck.x * ak.x + ck.y * ak.y;
                 }
-                Tri T{lo, di, up};
-                if (!cyclic_solve3(n, T, y, w, dummy, cp, zs)) { it = maxIter; break; }
-                double vy = 0.0, vz = 0.0;
-                for (int j = 0; j < n; ++j) { vy += vrow[j] * y[j]; vz += vrow[j] * w[j]; }
-                double den = dcorner - vz;
-                if (den == 0.0) { it = maxIter; break; }
-                double mu = (-sA - vy) / den;
-                for (int c = 0; c < n; ++c) {
-                    int cn = (c + 1 == n) ? 0 : c + 1;
-                    double l = y[c] - mu * w[c];
-                    x[c].x -= l * erx[c]; x[c].y -= l * ery[c];
-                    x[cn].x += l * erx[c]; x[cn].y += l * ery[c];
+                for (int k = n + lane; k < N; k += 32) {
+                    w.pa[k] = 0.f; w.pb[k] = 1.f; w.pc[k] = 0.f;
+                    w.p0[k] = 0.f; w.p1[k] = 0.f; w.p2[k] = 0.f;
                 }
-                for (int k = 0; k < n; ++k) { x[k].x += mu * arx[k]; x[k].y += mu * ary[k]; }
+                for (int o = 16; o > 0; o >>= 1) dc += __shfl_xor_sync(PCP_FULL, dc, o);
+                __syncwarp();
+                // Sherman-Morrison: move the cyclic corners out of the matrix
+                float gamma = -w.pb[0];
+                float beta = w.pa[0], alpha = w.pc[n - 1];
+                bool bad = !(gamma != 0.f);
+                __syncwarp();
+                if (lane == 0 && !bad) {
+                    w.pb[0] = w.pb[0] - gamma;
+                    w.pb[n - 1] = w.pb[n - 1] - alpha * beta / gamma;
+                    w.pa[0] = 0.f;
+                    w.pc[n - 1] = 0.f;
+                    w.p2[0] = gamma;
+                    w.p2[n - 1] = alpha;
+                }
+                __syncwarp();
+                if (bad) { it = maxIter; break; }
+                pcr3(w, N);
+                float y0 = w.p0[0], yl = w.p0[n - 1], z0 = w.p1[0], zl = w.p1[n - 1];
+                float s0 = w.p2[0], sl = w.p2[n - 1];
+                float den = 1.f + s0 + beta * sl / gamma;
+                float fy = (y0 + beta * yl / gamma) / den;
+                float fz = (z0 + beta * zl / gamma) / den;
+                __syncwarp();
+                float vy = 0.f, vz = 0.f;
+                for (int k = lane; k < n; k += 32) {
+                    float s = w.p2[k];
+                    float yk = w.p0[k] - fy * s, zk = w.p1[k] - fz * s;
+                    w.p0[k] = yk; w.p1[k] = zk;
+                    vy += w.vr[k] * yk; vz += w.vr[k] * zk;
+                }
+                for (int o = 16; o > 0; o >>= 1) {
+                    vy += __shfl_xor_sync(PCP_FULL, vy, o);
+                    vz += __shfl_xor_sync(PCP_FULL, vz, o);
+                }
+                float mu = (-(float)sA - vy) / (dc - vz);
+                bool finite = isfinite(mu);
+                __syncwarp();
+                for (int k = lane; k < n; k += 32) {
+                    float l = w.p0[k] - mu * w.p1[k];
+                    w.lam[k] = l;
+                    finite = finite && isfinite(l);
+                }
+                if (!__all_sync(PCP_FULL, finite)) { it = maxIter; break; }
+                __syncwarp();
+                // x_k += -l_k r_k + l_{k-1} r_{k-1} + mu ar_k   (FP64)
+                double mu64 = (double)mu;
+                for (int k = lane; k < n; k += 32) {
+                    int kp = (k == 0) ? n - 1 : k - 1;
+                    double lk = (double)w.lam[k], lp = (double)w.lam[kp];
+                    double2 rk = w.r[k], rp = w.r[kp], ak = w.ar[k];
+                    double2 x = w.xs[k];
+                    x.x += -lk * rk.x + lp * rp.x + mu64 * ak.x;
+                    x.y += -lk * rk.y + lp * rp.y + mu64 * ak.y;
+                    w.xs[k] = x;
+                }
+                __syncwarp();
             }
-            for (int k = 0; k < n; ++k) {
-                double2 v = x[k];
-                x[k] = make_double2(v.x - floor(v.x), v.y - floor(v.y));
+            for (int k = lane; k < n; k += 32) {
+                double2 v = w.xs[k];
+                pos[st + k] = make_double2(v.x - floor(v.x), v.y - floor(v.y));
             }
         }
     }
-    for (int o = 16; o > 0; o >>= 1) it = max(it, __shfl_xor_sync(PCP_FULL, it, o));
-    if ((threadIdx.x & 31) == 0 && it > 0) atomicMax(itersOut, it);
+    if (lane == 0 && it > 0) atomicMax(itersOut, it);
 }
 
-cudaError_t launch_shake(double2* pos, const int* start, int P, const double* targetEdge,
+cudaError_t launch_shake(double2* pos, const int* start, int P, int nmax, const double* targetEdge,
                          const double* targetArea, int maxIter, double tol, int* maxItersOut,
                          double* scratch, int V, const int* gate, cudaStream_t st) {
+    (void)V;
     if (P <= 0) return cudaSuccess;
-    k_shake<<<nblk(P, 128), 128, 0, st>>>(pos, start, P, targetEdge, targetArea, maxIter, tol,
-                                          maxItersOut, scratch, V, gate);
+    // per-warp workspace in shared memory when it fits (polygons up to ~1000
+    // vertices), else a per-polygon slice of the global scratch
+    int nv = (nmax + 1) & ~1;          // even, so each workspace stays 16-byte aligned
+    int N = 4;
+    while (N < nv) N <<= 1;
+    size_t per = shake_ws_bytes(nv, N);
+    int wpb = 8;
+    while (wpb > 1 && per * wpb > 200 * 1024) wpb >>= 1;
+    int nmaxSmem = nv;
+    if (per * wpb > 200 * 1024) { nmaxSmem = 0; per = 0; wpb = 8; }
+    size_t smem = per * wpb;
+    k_shake<<<nblk(P, wpb), 32 * wpb, smem, st>>>(pos, start, P, targetEdge, targetArea, maxIter,
+                                                   tol, maxItersOut, scratch, nmaxSmem, gate);
+    return cudaGetLastError();
+}
+
+// Warp-per-polygon form of the projection for systems with few polygons
+// (small systems leave most SMs idle with one polygon per thread): per-vertex
+// work runs across the lanes and J^T J is solved by FP64 parallel cyclic
+// reduction (Sherman-Morrison split of the cyclic corners, rows padded to a
+// power of two).  Same mathematics as k_project.
+//
+// areaFromPositions: take the unit area gradient from the positions (the
+// normalised areaComp of updatePolygonGeometryKernel, kernels.cuh:303,313)
+// instead of the constraints array; the device-resident FIRE step uses this
+// because its positions are those the reference's last geometry call saw.
+struct ProjWS {
+    double2 *t, *a, *f, *f2, *q;
+    double *pa, *pb, *pc, *p0, *p1, *p2;   // [2][N] each
+};
+__device__ __forceinline__ ProjWS proj_ws(unsigned char* base, int NV, int N) {
+    ProjWS w;
+    double2* d = reinterpret_cast<double2*>(base);
+    w.t = d; w.a = d + NV; w.f = d + 2 * NV; w.f2 = d + 3 * NV; w.q = d + 4 * NV;
+    double* q = reinterpret_cast<double*>(d + 5 * NV);
+    w.pa = q; w.pb = q + 2 * N; w.pc = q + 4 * N; w.p0 = q + 6 * N; w.p1 = q + 8 * N; w.p2 = q + 10 * N;
+    return w;
+}
+__host__ __device__ constexpr size_t proj_ws_bytes(int NV, int N) {
+    return (size_t)NV * 80 + (size_t)N * 12 * 8;
+}
+
+__device__ void pcr3_d(ProjWS& w, int N) {
+    const int lane = threadIdx.x & 31;
+    int cur = 0;
+    for (int d = 1; d < N; d <<= 1) {
+        int nxt = cur ^ 1;
+        const double *a = w.pa + cur * N, *b = w.pb + cur * N, *c = w.pc + cur * N;
+        const double *r0 = w.p0 + cur * N, *r1 = w.p1 + cur * N, *r2 = w.p2 + cur * N;
+        double *a2 = w.pa + nxt * N, *b2 = w.pb + nxt * N, *c2 = w.pc + nxt * N;
+        double *s0 = w.p0 + nxt * N, *s1 = w.p1 + nxt * N, *s2 = w.p2 + nxt * N;
+        for (int i = lane; i < N; i += 32) {
+            int im = i - d, ip = i + d;
+            double na = 0.0, nc = 0.0;
+            double nb = b[i], n0 = r0[i], n1 = r1[i], n2 = r2[i];
+            if (im >= 0) {
+                double k1 = a[i] / b[im];
+                na = -k1 * a[im];
+                nb -= k1 * c[im];
+                n0 -= k1 * r0[im]; n1 -= k1 * r1[im]; n2 -= k1 * r2[im];
+            }
+            if (ip < N) {
+                double k2 = c[i] / b[ip];
+                nc = -k2 * c[ip];
+                nb -= k2 * a[ip];
+                n0 -= k2 * r0[ip]; n1 -= k2 * r1[ip]; n2 -= k2 * r2[ip];
+            }
+            a2[i] = na; b2[i] = nb; c2[i] = nc; s0[i] = n0; s1[i] = n1; s2[i] = n2;
+        }
+        __syncwarp();
+        cur = nxt;
+    }
+    const double *b = w.pb + cur * N, *r0 = w.p0 + cur * N, *r1 = w.p1 + cur * N;
+    const double *r2 = w.p2 + cur * N;
+    for (int i = lane; i < N; i += 32) {
+        double ib = 1.0 / b[i];
+        double x0 = r0[i] * ib, x1 = r1[i] * ib, x2 = r2[i] * ib;
+        w.p0[i] = x0; w.p1[i] = x1; w.p2[i] = x2;
+    }
+    __syncwarp();
+}
+
+__global__ void k_project_warp(const double2* __restrict__ pos, const int* __restrict__ start,
+                               int P, const double* __restrict__ constraints,
+                               double2* __restrict__ force, double* __restrict__ scratch,
+                               int nmaxSmem, int areaFromPositions, Ctrl* fire,
+                               double2* __restrict__ vel, const int* gate) {
+    if (gate_closed(gate)) return;
+    extern __shared__ __align__(16) unsigned char proj_smem[];
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    const int wpb = blockDim.x >> 5;
+    int p = blockIdx.x * wpb + warp;
+    bool proceed = false;
+    double dt = 0.0;
+    if (fire) {
+        double E = fire->energy, E0 = fire->ePre;
+        bool rb = E > E0 + fmax(fabs(E0) * 1e-10, 1e-14);
+        proceed = !fire->shakeFailed && !rb && fire->rollback == 0;
+        dt = fire->dt;
+        if (blockIdx.x == 0 && threadIdx.x == 0 && fire->rollback == 0) {
+            fire->proceed = proceed ? 1 : 0;
+            fire->rbGate = (!fire->shakeFailed && rb && fire->active) ? 1 : 0;
+        }
+    }
+    double sP = 0.0, sV = 0.0, sF = 0.0, mF = 0.0;
+    if (p < P) {
+        int st = start[p], n = start[p + 1] - st;
+        if (n >= 3) {
+            ProjWS w;
+            int N;
+            if (n <= nmaxSmem) {
+                N = pow2_at_least(nmaxSmem);
+                w = proj_ws(proj_smem + (size_t)warp * proj_ws_bytes(nmaxSmem, N), nmaxSmem, N);
+            } else {
+                N = pow2_at_least(n);
+                w = proj_ws(reinterpret_cast<unsigned char*>(scratch + (size_t)kScratchPerVertex * st),
+                            n, N);
+            }
+            double an = 0.0;
+            for (int k = lane; k < n; k += 32) {
+                int kn = (k + 1 == n) ? 0 : k + 1, kp = (k == 0) ? n - 1 : k - 1;
+                double2 xk = pos[st + k], xn = pos[st + kn];
+                double dx = wrap(xn.x - xk.x), dy = wrap(xn.y - xk.y);
+                double len = sqrt(dx * dx + dy * dy);
+                double2 t = make_double2(0.0, 0.0);
+                bool ok = !(len < 1e-14);
+                if (ok) { double il = 1.0 / len; t = make_double2(dx * il, dy * il); }
+                w.t[k] = t;
+                w.pb[k] = ok ? 2.0 : 1.0;
+                w.f[k] = force[st + k];
+                if (areaFromPositions) {
+                    double2 xp = pos[st + kp];
+                    double a0 = -wrap(xp.y - xn.y), a1 = wrap(xp.x - xn.x);
+                    w.a[k] = make_double2(a0, a1);
+                    an += a0 * a0 + a1 * a1;
+                } else {
+                    const double* c = constraints + 6 * (size_t)(st + k);
+                    w.a[k] = make_double2(c[0], c[1]);
+                }
+            }
+            if (areaFromPositions) {
+                an = warp_sum(an);
+                double ir = an > 0.0 ? 1.0 / sqrt(an) : 1.0;
+                for (int k = lane; k < n; k += 32) {
+                    double2 a = w.a[k];
+                    w.a[k] = make_double2(a.x * ir, a.y * ir);
+                }
+            }
+            __syncwarp();
+            for (int k = lane; k < n; k += 32) {
+                int kn = (k + 1 == n) ? 0 : k + 1, kp = (k == 0) ? n - 1 : k - 1;
+                double2 t = w.t[k], tn = w.t[kn], tp = w.t[kp];
+                double2 f0 = w.f[k], f1 = w.f[kn], a0 = w.a[k], a1 = w.a[kn];
+                w.pc[k] = -(t.x * tn.x + t.y * tn.y);
+                w.pa[k] = -(tp.x * t.x + tp.y * t.y);
+                w.p0[k] = t.x * (f1.x - f0.x) + t.y * (f1.y - f0.y);
+                w.p1[k] = t.x * (a1.x - a0.x) + t.y * (a1.y - a0.y);
+                w.p2[k] = 0.0;
+            }
+            for (int k = n + lane; k < N; k += 32) {
+                w.pa[k] = 0.0; w.pb[k] = 1.0; w.pc[k] = 0.0;
+                w.p0[k] = 0.0; w.p1[k] = 0.0; w.p2[k] = 0.0;
+            }
+            __syncwarp();
+            double gamma = -w.pb[0], beta = w.pa[0], alpha = w.pc[n - 1];
+            __syncwarp();
+            if (lane == 0) {
+                w.pb[0] = w.pb[0] - gamma;
+                w.pb[n - 1] = w.pb[n - 1] - alpha * beta / gamma;
+                w.pa[0] = 0.0; w.pc[n - 1] = 0.0;
+                w.p2[0] = gamma; w.p2[n - 1] = alpha;
+            }
+            __syncwarp();
+            pcr3_d(w, N);
+            double den = 1.0 + w.p2[0] + beta * w.p2[n - 1] / gamma;
+            double f0 = (w.p0[0] + beta * w.p0[n - 1] / gamma) / den;
+            double f1 = (w.p1[0] + beta * w.p1[n - 1] / gamma) / den;
+            __syncwarp();
+            for (int k = lane; k < n; k += 32) {
+                double s = w.p2[k];
+                w.p0[k] -= f0 * s;
+                w.p1[k] -= f1 * s;
+            }
+            __syncwarp();
+            double qF = 0.0, qq = 0.0;
+            for (int k = lane; k < n; k += 32) {
+                int kp = (k == 0) ? n - 1 : k - 1;
+                double2 t = w.t[k], tp = w.t[kp];
+                double l0 = w.p0[k], l0p = w.p0[kp], l1 = w.p1[k], l1p = w.p1[kp];
+                // (J x)_k = -x_k t_k + x_{k-1} t_{k-1}
+                double2 f = w.f[k], a = w.a[k];
+                double fx = f.x - (-l0 * t.x + l0p * tp.x), fy = f.y - (-l0 * t.y + l0p * tp.y);
+                double qx = a.x - (-l1 * t.x + l1p * tp.x), qy = a.y - (-l1 * t.y + l1p * tp.y);
+                w.f2[k] = make_double2(fx, fy);
+                w.q[k] = make_double2(qx, qy);
+                qF += qx * fx + qy * fy;
+                qq += qx * qx + qy * qy;
+            }
+            qF = warp_sum(qF);
+            qq = warp_sum(qq);
+            double coef = (sqrt(qq) > 1e-14) ? qF / qq : 0.0;
+            for (int k = lane; k < n; k += 32) {
+                double2 f1v = w.f2[k], q = w.q[k];
+                double fx = f1v.x - coef * q.x, fy = f1v.y - coef * q.y;
+                force[st + k] = make_double2(fx, fy);
+                mF = fmax(mF, fmax(fabs(fx), fabs(fy)));
+                if (proceed) {
+                    double2 v = vel[st + k];
+                    v.x += 0.5 * dt * fx;
+                    v.y += 0.5 * dt * fy;
+                    vel[st + k] = v;
+                    sP += fx * v.x + fy * v.y;
+                    sV += v.x * v.x + v.y * v.y;
+                    sF += fx * fx + fy * fy;
+                }
+            }
+        } else {
+            for (int k = lane; k < n; k += 32) {
+                double2 f = force[st + k];
+                mF = fmax(mF, fmax(fabs(f.x), fabs(f.y)));
+                if (proceed) {
+                    double2 v = vel[st + k];
+                    v.x += 0.5 * dt * f.x; v.y += 0.5 * dt * f.y;
+                    vel[st + k] = v;
+                    sP += f.x * v.x + f.y * v.y;
+                    sV += v.x * v.x + v.y * v.y;
+                    sF += f.x * f.x + f.y * f.y;
+                }
+            }
+        }
+    }
+    if (fire) {
+        mF = warp_maxd(mF);
+        if (lane == 0) atomic_max_nonneg(&fire->maxF, mF);
+        if (proceed) {
+            sP = warp_sum(sP); sV = warp_sum(sV); sF = warp_sum(sF);
+            if (lane == 0) {
+                atomicAdd(&fire->P, sP);
+                atomicAdd(&fire->vv, sV);
+                atomicAdd(&fire->ff, sF);
+            }
+        }
+    }
+}
+
+cudaError_t constraints_init() {
+    static bool done = false;
+    if (done) return cudaSuccess;
+    cudaError_t e = cudaFuncSetAttribute(k_project, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                         200 * 1024);
+    if (e != cudaSuccess) return e;
+    e = cudaFuncSetAttribute(k_shake, cudaFuncAttributeMaxDynamicSharedMemorySize, 200 * 1024);
+    if (e != cudaSuccess) return e;
+    e = cudaFuncSetAttribute(k_project_warp, cudaFuncAttributeMaxDynamicSharedMemorySize, 200 * 1024);
+    if (e != cudaSuccess) return e;
+    done = true;
+    return cudaSuccess;
+}
+
+// One polygon per thread (J^T J by Thomas) when there are enough polygons to
+// fill the GPU, else one polygon per warp (J^T J by parallel cyclic
+// reduction): 4096 polygons give only 128 warps of thread-per-polygon work.
+cudaError_t launch_project(const double2* pos, const int* start, int P, int nmax,
+                           const double* constraints, double2* force, double* scratch, int V,
+                           int areaFromPositions, Ctrl* fireCtrl, const int* gate, double2* vel,
+                           cudaStream_t st) {
+    if (P <= 0) return cudaSuccess;
+    if (P >= 128 * sm_count()) {
+        int sn = smem_vertices(nmax, kProjArrays);
+        size_t smem = (size_t)sn * kProjArrays * kConsThreads * sizeof(double);
+        k_project<<<nblk(P, kConsThreads), kConsThreads, smem, st>>>(
+            pos, start, P, constraints, force, scratch, V, sn, areaFromPositions, fireCtrl, vel, gate);
+        return cudaGetLastError();
+    }
+    int nv = nmax;
+    int N = 4;
+    while (N < nv) N <<= 1;
+    size_t per = proj_ws_bytes(nv, N);
+    int wpb = 8;
+    while (wpb > 1 && per * wpb > 200 * 1024) wpb >>= 1;
+    int nmaxSmem = nv;
+    if (per * wpb > 200 * 1024) { nmaxSmem = 0; per = 0; wpb = 8; }
+    k_project_warp<<<nblk(P, wpb), 32 * wpb, per * wpb, st>>>(pos, start, P, constraints, force,
+                                                              scratch, nmaxSmem, areaFromPositions,
+                                                              fireCtrl, vel, gate);
     return cudaGetLastError();
 }
 

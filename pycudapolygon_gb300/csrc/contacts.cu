@@ -52,7 +52,7 @@ __global__ void k_reset_contacts(Ctrl* __restrict__ ctrl, const int* gate) {
 
 __global__ void __launch_bounds__(256)
 k_prepass(const double2* __restrict__ pos, const int* __restrict__ start,
-          const int* __restrict__ cellLocation, int P, double2* __restrict__ edgeVec,
+          const int* __restrict__ cellLocation, int P, int B, double2* __restrict__ edgeVec,
           float4* __restrict__ vtx, float4* __restrict__ polyInfo, int* __restrict__ polyFlags,
           int* __restrict__ unsafeList, Ctrl* __restrict__ ctrl, const int* gate) {
     if (gate_closed(gate)) return;
@@ -76,7 +76,10 @@ k_prepass(const double2* __restrict__ pos, const int* __restrict__ start,
         // r = wrap(p_next - p) exactly as updateNeighborsKernel (kernels.cuh:724-725)
         edgeVec[k] = make_double2(wrap(pn.x - pk.x), wrap(pn.y - pk.y));
         float fx = (float)pk.x, fy = (float)pk.y;
-        vtx[k] = make_float4(fx, fy, __int_as_float(cellLocation[k]), 0.f);
+        // cell (x, y) of the edge midpoint as updateNeighborsKernel splits it
+        // with the current box size (kernels.cuh:727-729)
+        int cell = cellLocation[k];
+        vtx[k] = make_float4(fx, fy, __int_as_float(cell % B), __int_as_float(cell / B));
         float lx = wrapf(fx - f0x), ly = wrapf(fy - f0y);
         float nxl = wrapf((float)pn.x - fx), nyl = wrapf((float)pn.y - fy);
         if (!(isfinite(lx) && isfinite(ly) && isfinite(nxl) && isfinite(nyl))) bad = true;
@@ -193,57 +196,89 @@ __device__ __forceinline__ void emit_pair(int a, int b, int2* pairs, int cap, Ct
     else atomicOr(&ctrl->flags, kFlagPairOverflow);
 }
 
-__global__ void k_candidates(const float4* __restrict__ polyInfo, const int* __restrict__ flags,
-                             const int* __restrict__ start, int P,
-                             const int* __restrict__ gridStart,
-                             const int* __restrict__ sortedPoly, int2* __restrict__ pairs,
-                             int capPairs, Ctrl* __restrict__ ctrl, const int* gate) {
+// warp-aggregated emission: one atomic per warp for the lanes with `ok`
+__device__ __forceinline__ void emit_pairs_warp(bool ok, int a, int b, int2* pairs, int cap,
+                                                Ctrl* ctrl) {
+    unsigned mk = __ballot_sync(PCP_FULL, ok);
+    if (!mk) return;
+    int lane = threadIdx.x & 31;
+    int leader = __ffs(mk) - 1;
+    int base = 0;
+    if (lane == leader) base = atomicAdd(&ctrl->numPairs, __popc(mk));
+    base = __shfl_sync(PCP_FULL, base, leader);
+    if (ok) {
+        int slot = base + __popc(mk & ((1u << lane) - 1u));
+        if (slot < cap) pairs[slot] = make_int2(a, b);
+        else atomicOr(&ctrl->flags, kFlagPairOverflow);
+    }
+}
+
+// One warp per polygon i: the lanes walk the polygons of the (up to) nine
+// neighbouring grid cells and keep j > i whose bounding circle meets i's.
+__global__ void __launch_bounds__(256)
+k_candidates(const float4* __restrict__ polyInfo, const int* __restrict__ flags,
+             const int* __restrict__ start, int P, const int* __restrict__ gridStart,
+             const int* __restrict__ sortedPoly, int2* __restrict__ pairs, int capPairs,
+             Ctrl* __restrict__ ctrl, const int* gate) {
     if (gate_closed(gate)) return;
-    int i = blockIdx.x * blockDim.x + threadIdx.x;
+    int i = blockIdx.x * (blockDim.x >> 5) + (threadIdx.x >> 5);
+    int lane = threadIdx.x & 31;
+    if (i >= P) return;
+    int n = start[i + 1] - start[i];
+    if (n <= 0) return;
     unsigned long long evals = 0;
-    if (i < P && start[i + 1] > start[i]) {
-        int n = start[i + 1] - start[i];
-        if (n >= 4) emit_pair(i, i, pairs, capPairs, ctrl);
-        if (!flags[i]) {
-            // not well formed: paired with everyone (safe partners below i, all above)
-            for (int j = 0; j < P; ++j) {
-                if (j == i) continue;
-                if (j > i || flags[j]) { emit_pair(j < i ? j : i, j < i ? i : j, pairs, capPairs, ctrl); ++evals; }
+    if (lane == 0 && n >= 4) emit_pair(i, i, pairs, capPairs, ctrl);
+    if (!flags[i]) {
+        // not well formed: paired with everyone (safe partners below i, all above)
+        for (int j0 = 0; j0 < P; j0 += 32) {
+            int j = j0 + lane;
+            bool ok = j < P && j != i && (j > i || flags[j]) && start[j + 1] > start[j];
+            emit_pairs_warp(ok, j < i ? j : i, j < i ? i : j, pairs, capPairs, ctrl);
+            evals += ok ? 1 : 0;
+        }
+    } else {
+        int G = ctrl->G;
+        float4 ci = polyInfo[i];
+        int gx = grid_cell(ci.x, G), gy = grid_cell(ci.y, G);
+        // the distinct neighbouring cells and their ranges
+        int cs[9], ce[9], nc = 0;
+        for (int dx = -1; dx <= 1; ++dx) {
+            int nx = gx + dx;
+            if (nx < 0) nx += G; else if (nx >= G) nx -= G;
+            for (int dy = -1; dy <= 1; ++dy) {
+                int ny = gy + dy;
+                if (ny < 0) ny += G; else if (ny >= G) ny -= G;
+                int cell = ny * G + nx;
+                int a = gridStart[cell], b = gridStart[cell + 1];
+                // cells are disjoint ranges of sortedPoly; a repeated cell
+                // (G < 3) repeats its range exactly
+                bool dup = false;
+                for (int t = 0; t < nc; ++t) dup |= (cs[t] == a && ce[t] == b);
+                if (dup || b <= a) continue;
+                cs[nc] = a; ce[nc] = b; ++nc;
             }
-        } else {
-            int G = ctrl->G;
-            float4 ci = polyInfo[i];
-            int gx = grid_cell(ci.x, G), gy = grid_cell(ci.y, G);
-            int seen[9];
-            int ns = 0;
-            for (int dx = -1; dx <= 1; ++dx) {
-                int nx = gx + dx;
-                if (nx < 0) nx += G; else if (nx >= G) nx -= G;
-                for (int dy = -1; dy <= 1; ++dy) {
-                    int ny = gy + dy;
-                    if (ny < 0) ny += G; else if (ny >= G) ny -= G;
-                    int cell = ny * G + nx;
-                    bool dup = false;
-                    for (int t = 0; t < ns; ++t) dup |= (seen[t] == cell);
-                    if (dup) continue;
-                    seen[ns++] = cell;
-                    for (int q = gridStart[cell]; q < gridStart[cell + 1]; ++q) {
-                        int j = sortedPoly[q];
-                        if (j <= i) continue;
+        }
+        for (int t = 0; t < nc; ++t) {
+            for (int q0 = cs[t]; q0 < ce[t]; q0 += 32) {
+                int q = q0 + lane;
+                bool ok = false;
+                int j = 0;
+                if (q < ce[t]) {
+                    j = sortedPoly[q];
+                    if (j > i) {
                         float4 cj = polyInfo[j];
                         float ddx = wrapf(cj.x - ci.x), ddy = wrapf(cj.y - ci.y);
                         float rr = ci.z + cj.z + 1e-5f;
-                        if (ddx * ddx + ddy * ddy <= rr * rr) {
-                            emit_pair(i, j, pairs, capPairs, ctrl);
-                            ++evals;
-                        }
+                        ok = ddx * ddx + ddy * ddy <= rr * rr;
                     }
                 }
+                emit_pairs_warp(ok, i, j, pairs, capPairs, ctrl);
+                evals += ok ? 1 : 0;
             }
         }
     }
     for (int o = 16; o > 0; o >>= 1) evals += __shfl_xor_sync(PCP_FULL, evals, o);
-    if ((threadIdx.x & 31) == 0 && evals) atomicAdd(&ctrl->pairEvals, evals);
+    if (lane == 0 && evals) atomicAdd(&ctrl->pairEvals, evals);
 }
 
 // -------------------------------------------------------- narrow phase ----
@@ -299,30 +334,81 @@ __device__ __forceinline__ unsigned long long pack_key(int sj, int si, int i, in
            ((unsigned long long)(uint16_t)i << 16) | (unsigned long long)(uint16_t)j;
 }
 
-// Process one staged pair with one warp.  ringA/ringB hold (x, y, cell) of
-// the two rings as float; aabb is scratch for A's edge boxes.  Returns the
-// number of records in recKey/recTU, or -1 when they do not fit.
+// Process one staged pair with one warp.  ringA/ringB hold (x, y) of the
+// two rings as float and the (x, y) index of each edge's midpoint cell.
+// candA/candB are scratch for the edges that survive the overlap-box cull
+// (capacity >= nA, nB).  Returns the number of records in recKey/recTU, or
+// -1 when they do not fit in recCap.
+//
+// Culls, all conservative (they never drop a pair the FP64 test accepts):
+//  1. overlap box: a crossing point lies in both polygons' bounding boxes,
+//     so only edges whose box meets the intersection of the two polygon
+//     boxes are kept (cross pairs only);
+//  2. edge boxes: FP32 boxes padded by m = 4e-6 + 1e-3 La Lb must meet --
+//     the FP32 coordinates are within 1.2e-7 of the FP64 ones and the FP64
+//     predicate cannot accept a pair farther apart than 3.3e-4 |r| |s|
+//     (its |denom| >= 1e-12 bounds the error of t and u);
+//  3. the reference's 3x3 cell rule on the edge-midpoint cells.
+struct EdgeCand { float4 box; int idx, cx, cy, pad; };
+
 __device__ int narrow_pair(const PairCtx& pc, const float4* ringA, const float4* ringB,
-                           float4* aabb, int* queue, unsigned long long* recKey, float2* recTU,
-                           int recCap, int B, const double2* __restrict__ pos,
-                           const double2* __restrict__ edgeVec, const float4* __restrict__ polyInfo) {
+                           EdgeCand* candA, EdgeCand* candB, int* queue,
+                           unsigned long long* recKey, float2* recTU, int recCap, int B,
+                           const double2* __restrict__ pos, const double2* __restrict__ edgeVec,
+                           const float4* __restrict__ polyInfo) {
     const int lane = threadIdx.x & 31;
+    const unsigned lt = (1u << lane) - 1u;
     const int nA = pc.nA, nB = pc.nB;
     const float f0x = ringA[0].x, f0y = ringA[0].y;
-    // margin: FP32 coordinate error plus the FP64 predicate's slack for long,
-    // nearly parallel edges (|denom| >= 1e-12 bounds its error in t and u)
     const float LA = polyInfo[pc.a].w, LB = polyInfo[pc.b].w;
     const float m = 4e-6f + 1e-3f * LA * LB;
+    // polygon boxes in A's frame
+    float ax0 = 3.f, ax1 = -3.f, ay0 = 3.f, ay1 = -3.f;
     for (int a = lane; a < nA; a += 32) {
-        float4 v0 = ringA[a], v1 = ringA[(a + 1 == nA) ? 0 : a + 1];
-        float x0 = wrapf(v0.x - f0x), y0 = wrapf(v0.y - f0y);
-        float x1 = wrapf(v1.x - f0x), y1 = wrapf(v1.y - f0y);
-        aabb[a] = make_float4(fminf(x0, x1) - m, fmaxf(x0, x1) + m, fminf(y0, y1) - m,
-                              fmaxf(y0, y1) + m);
+        float x = wrapf(ringA[a].x - f0x), y = wrapf(ringA[a].y - f0y);
+        ax0 = fminf(ax0, x); ax1 = fmaxf(ax1, x); ay0 = fminf(ay0, y); ay1 = fmaxf(ay1, y);
     }
+    ax0 = warp_minf(ax0); ax1 = warp_maxf(ax1); ay0 = warp_minf(ay0); ay1 = warp_maxf(ay1);
+    float ox0 = ax0 - m, ox1 = ax1 + m, oy0 = ay0 - m, oy1 = ay1 + m;
+    if (!pc.self) {
+        float bx0 = 3.f, bx1 = -3.f, by0 = 3.f, by1 = -3.f;
+        for (int b = lane; b < nB; b += 32) {
+            float x = wrapf(ringB[b].x - f0x), y = wrapf(ringB[b].y - f0y);
+            bx0 = fminf(bx0, x); bx1 = fmaxf(bx1, x); by0 = fminf(by0, y); by1 = fmaxf(by1, y);
+        }
+        bx0 = warp_minf(bx0); bx1 = warp_maxf(bx1); by0 = warp_minf(by0); by1 = warp_maxf(by1);
+        ox0 = fmaxf(ax0, bx0) - m; ox1 = fminf(ax1, bx1) + m;
+        oy0 = fmaxf(ay0, by0) - m; oy1 = fminf(ay1, by1) + m;
+    }
+    // candidate edges of each ring (edge box padded by m meets the overlap box)
+    auto collect = [&](const float4* ring, int n, EdgeCand* out, float pad) -> int {
+        int cnt = 0;
+        for (int e0 = 0; e0 < n; e0 += 32) {
+            int e = e0 + lane;
+            bool ok = false;
+            EdgeCand c;
+            if (e < n) {
+                float4 v0 = ring[e], v1 = ring[(e + 1 == n) ? 0 : e + 1];
+                float x0 = wrapf(v0.x - f0x), y0 = wrapf(v0.y - f0y);
+                float x1 = wrapf(v1.x - f0x), y1 = wrapf(v1.y - f0y);
+                c.box = make_float4(fminf(x0, x1) - pad, fmaxf(x0, x1) + pad,
+                                    fminf(y0, y1) - pad, fmaxf(y0, y1) + pad);
+                c.idx = e; c.cx = __float_as_int(v0.z); c.cy = __float_as_int(v0.w); c.pad = 0;
+                // keep unless certainly outside the overlap box (NaN keeps it)
+                ok = !(c.box.x > ox1 || c.box.y < ox0 || c.box.z > oy1 || c.box.w < oy0);
+            }
+            unsigned mk = __ballot_sync(PCP_FULL, ok);
+            if (ok) out[cnt + __popc(mk & lt)] = c;
+            cnt += __popc(mk);
+        }
+        return cnt;
+    };
+    int nLA = collect(ringA, nA, candA, m);
+    int nLB = pc.self ? 0 : collect(ringB, nB, candB, 0.f);
     __syncwarp();
-    // this lane's B edges (up to 4 for rings of <= 128 vertices; more on the
-    // block path through the outer loop)
+    const EdgeCand* cb = pc.self ? candA : candB;
+    if (pc.self) nLB = nLA;
+    bool wrapB = B >= 3;
     int qn = 0;
     int rec = 0;
     bool overflow = false;
@@ -350,39 +436,34 @@ __device__ int narrow_pair(const PairCtx& pc, const float4* ringA, const float4*
         int cnt2 = __popc(mask);
         if (rec + cnt2 > recCap) { overflow = true; return; }
         if (hit) {
-            int slot = rec + __popc(mask & ((1u << lane) - 1u));
+            int slot = rec + __popc(mask & lt);
             recKey[slot] = key;
             recTU[slot] = tuf;
         }
         rec += cnt2;
     };
-    for (int b0 = 0; b0 < nB && !overflow; b0 += 32) {
-        int b = b0 + lane;
-        bool bval = b < nB;
-        float bx0 = 0, bx1 = 0, by0 = 0, by1 = 0;
-        int cb = 0;
-        if (bval) {
-            float4 w0 = ringB[b], w1 = ringB[(b + 1 == nB) ? 0 : b + 1];
-            float x0 = wrapf(w0.x - f0x), y0 = wrapf(w0.y - f0y);
-            float x1 = wrapf(w1.x - f0x), y1 = wrapf(w1.y - f0y);
-            bx0 = fminf(x0, x1); bx1 = fmaxf(x0, x1);
-            by0 = fminf(y0, y1); by1 = fmaxf(y0, y1);
-            cb = __float_as_int(w0.z);
-        }
-        for (int a = 0; a < nA && !overflow; ++a) {
-            float4 bb = aabb[a];
-            int ca = __float_as_int(ringA[a].z);
+    for (int t0 = 0; t0 < nLB && !overflow; t0 += 32) {
+        int t = t0 + lane;
+        bool bval = t < nLB;
+        EdgeCand eb;
+        if (bval) eb = cb[t];
+        else { eb.box = make_float4(0.f, 0.f, 0.f, 0.f); eb.idx = 0; eb.cx = 0; eb.cy = 0; }
+        for (int i = 0; i < nLA && !overflow; ++i) {
+            EdgeCand ea = candA[i];
             bool ok = bval;
             if (pc.self) {
                 // id1 < nid, not adjacent (kernels.cuh:766-775)
-                ok = ok && b > a + 1 && !(a == 0 && b == nA - 1);
+                ok = ok && eb.idx > ea.idx + 1 && !(ea.idx == 0 && eb.idx == nA - 1);
             }
-            // reject only when the boxes are certainly apart (NaN keeps the pair)
-            ok = ok && !(bx0 > bb.y || bx1 < bb.x || by0 > bb.w || by1 < bb.z);
-            ok = ok && cells_adjacent(ca, cb, B);
+            ok = ok && !(eb.box.x > ea.box.y || eb.box.y < ea.box.x ||
+                         eb.box.z > ea.box.w || eb.box.w < ea.box.z);
+            if (wrapB) {
+                int dx = abs(ea.cx - eb.cx), dy = abs(ea.cy - eb.cy);
+                ok = ok && (dx <= 1 || dx == B - 1) && (dy <= 1 || dy == B - 1);
+            }
             unsigned mk = __ballot_sync(PCP_FULL, ok);
             if (mk) {
-                if (ok) queue[qn + __popc(mk & ((1u << lane) - 1u))] = a | (b << 16);
+                if (ok) queue[qn + __popc(mk & lt)] = ea.idx | (eb.idx << 16);
                 qn += __popc(mk);
                 __syncwarp();
                 if (qn >= 32) {
@@ -478,7 +559,8 @@ __device__ __forceinline__ PairCtx make_ctx(int2 pr, const int* __restrict__ sta
 
 struct alignas(16) WarpSmem {
     float4 ring[2][2 * kFastRing];
-    float4 aabb[kFastRing];
+    EdgeCand candA[kFastRing];
+    EdgeCand candB[kFastRing];
     unsigned long long recKey[kFastRecords];
     float2 recTU[kFastRecords];
     int queue[64];
@@ -553,8 +635,8 @@ k_narrow(const double2* __restrict__ pos, const int* __restrict__ start, int B,
         phase[stage] ^= 1u;
         const float4* ringA = &S.ring[stage][0];
         const float4* ringB = pc.self ? ringA : &S.ring[stage][kFastRing];
-        int R = narrow_pair(pc, ringA, ringB, S.aabb, S.queue, S.recKey, S.recTU, kFastRecords,
-                            B, pos, ws.edgeVec, ws.polyInfo);
+        int R = narrow_pair(pc, ringA, ringB, S.candA, S.candB, S.queue, S.recKey, S.recTU,
+                            kFastRecords, B, pos, ws.edgeVec, ws.polyInfo);
         if (R < 0) {
             if (lane == 0) push_slow(q, ctrl, ws);
         } else if (R > 0) {
@@ -575,9 +657,9 @@ k_narrow_slow(const double2* __restrict__ pos, const int* __restrict__ start, in
               ContactWS ws, Ctrl* __restrict__ ctrl, const int* gate) {
     if (gate_closed(gate)) return;
     extern __shared__ __align__(128) unsigned char smem_raw[];
-    float4* ring = reinterpret_cast<float4*>(smem_raw);                 // kSlowRing
-    float4* aabb = ring + kSlowRing;                                      // kSlowRing
-    unsigned long long* recKey = reinterpret_cast<unsigned long long*>(aabb + kSlowRing);
+    float4* ring = reinterpret_cast<float4*>(smem_raw);                    // kSlowRing
+    EdgeCand* cand = reinterpret_cast<EdgeCand*>(ring + kSlowRing);          // kSlowRing
+    unsigned long long* recKey = reinterpret_cast<unsigned long long*>(cand + kSlowRing);
     float2* recTU = reinterpret_cast<float2*>(recKey + kSlowRecords);
     int* queue = reinterpret_cast<int*>(recTU + kSlowRecords);
     const int lane = threadIdx.x & 31;
@@ -600,8 +682,9 @@ k_narrow_slow(const double2* __restrict__ pos, const int* __restrict__ start, in
             for (int t = lane; t < pc.nB; t += 32) ring[pc.nA + t] = ws.vtx[pc.stB + t];
         __syncwarp();
         const float4* ringB = pc.self ? ring : ring + pc.nA;
-        int R = narrow_pair(pc, ring, ringB, aabb, queue, recKey, recTU, kSlowRecords, B, pos,
-                            ws.edgeVec, ws.polyInfo);
+        // the two candidate lists share one buffer: A from the front, B behind it
+        int R = narrow_pair(pc, ring, ringB, cand, cand + pc.nA, queue, recKey, recTU,
+                            kSlowRecords, B, pos, ws.edgeVec, ws.polyInfo);
         if (R < 0) {
             if (lane == 0) atomicOr(&ctrl->flags, kFlagCapacity);
         } else if (R > 0) {
@@ -739,7 +822,7 @@ k_overlap_force(const double2* __restrict__ pos, const int* __restrict__ start,
 }
 
 // ------------------------------------------------------------ launchers ----
-static const size_t kSlowSmem = (size_t)kSlowRing * 32 + (size_t)kSlowRecords * 16 + 64 * 4;
+static const size_t kSlowSmem = (size_t)kSlowRing * (16 + 32) + (size_t)kSlowRecords * 16 + 64 * 4;
 
 // Opt the narrow-phase kernels into their shared-memory sizes; called once
 // per process before any launch or graph capture.
@@ -765,14 +848,14 @@ cudaError_t launch_contacts(const double2* pos, const int* start, const int* sha
     if (stages & 1) {
     k_reset_contacts<<<1, 64, 0, st>>>(ctrl, gate);
     if (P <= 0) return cudaGetLastError();
-    k_prepass<<<nblocks(P, 8), 256, 0, st>>>(pos, start, cellLocation, P, ws.edgeVec, ws.vtx,
+    k_prepass<<<nblocks(P, 8), 256, 0, st>>>(pos, start, cellLocation, P, B, ws.edgeVec, ws.vtx,
                                              ws.polyInfo, ws.polyFlags, ws.unsafeList, ctrl, gate);
     k_grid_count<<<nblocks(P, 256), 256, 0, st>>>(ws.polyInfo, ws.polyFlags, P, ws.gridCount,
                                                   ctrl, gate);
     k_grid_scan<<<1, 1024, 0, st>>>(ws.gridCount, ws.gridStart, ws.gridFill, ctrl, gate);
     k_grid_scatter<<<nblocks(P, 256), 256, 0, st>>>(ws.polyInfo, ws.polyFlags, P, ws.gridStart,
                                                     ws.gridFill, ws.sortedPoly, ctrl, gate);
-    k_candidates<<<nblocks(P, 128), 128, 0, st>>>(ws.polyInfo, ws.polyFlags, start, P,
+    k_candidates<<<nblocks(P, 8), 256, 0, st>>>(ws.polyInfo, ws.polyFlags, start, P,
                                                   ws.gridStart, ws.sortedPoly, ws.pairs,
                                                   ws.capPairs, ctrl, gate);
     }

@@ -70,6 +70,7 @@ struct pcp_model {
     // host-side parameters
     int modelType = PCP_MODEL_NORMAL;
     int V = 0, P = 0;
+    int nmax = 0;          // largest polygon
     int boxSize = 2;
     double maxEdgeLengthSet = 0.5;
     int maxNeighbors = 100;
@@ -79,6 +80,7 @@ struct pcp_model {
     int pointDensity = -1;
     double overlapArea = 0.0;
     bool topology = false;
+    bool geometryStale = false;   // geometry of the current positions not yet computed
     std::vector<int> startHost;
     cudaStream_t stream = nullptr;
     long long launches = 0;
@@ -448,6 +450,14 @@ int geometry(pcp_model* m, const int* gate) {
     return PCP_OK;
 }
 
+// Materialise geometry the FIRE graph deferred (it corresponds to the
+// positions the last FIRE step ended with, as in the reference).
+int ensure_geometry(pcp_model* m) {
+    if (!m->geometryStale) return PCP_OK;
+    m->geometryStale = false;
+    return geometry(m, nullptr);
+}
+
 // ---- FIRE step graph ------------------------------------------------------
 int record_fire_step(pcp_model* m) {
     const int* gA = &m->ctrl->active;
@@ -467,31 +477,39 @@ int record_fire_step(pcp_model* m) {
                            m->ws, m->ctrl, gA, st));
         if (rigid && m->fireShakeIter > 0) {
             CK(cudaMemcpyAsync(m->posTMP, m->pos, V * sizeof(double2), cudaMemcpyDeviceToDevice, st));
-            CK(launch_shake(m->pos, m->start, m->P, m->targetEdge, m->targetAreas, m->fireShakeIter,
+            CK(launch_shake(m->pos, m->start, m->P, m->nmax, m->targetEdge, m->targetAreas, m->fireShakeIter,
                             1e-15, &m->ctrl->shakeIters1, m->scratch, V, gA, st));
             CK(launch_fire_shake_check(m->ctrl, 1, gA, st));
-            CK(launch_shake(m->pos, m->start, m->P, m->targetEdge, m->targetAreas,
+            CK(launch_shake(m->pos, m->start, m->P, m->nmax, m->targetEdge, m->targetAreas,
                             m->fireShakeIter * 10, 1e-15, &m->ctrl->shakeIters2, m->scratch, V,
                             gRetry, st));
             CK(launch_fire_shake_check(m->ctrl, 2, gA, st));
             CK(launch_fire_after_shake(m->pos, m->vel, m->posTMP2, m->posTMP, V, m->ctrl, gA, st));
         }
     }
-    int rc = geometry(m, gA);
-    if (rc) return rc;
+    // The normal model reads nothing of the geometry inside the step (the
+    // projection takes the area gradient from the positions), so the
+    // geometry of the final positions is computed when a getter asks for it.
+    int rc = PCP_OK;
+    if (!rigid) {
+        rc = geometry(m, gA);
+        if (rc) return rc;
+    }
     if (needsI) CK(launch_contacts_finish(m->start, m->ws, m->ctrl, gA, st));
     rc = force_energy(m, gA);
     if (rc) return rc;
     if (rigid) {
-        CK(launch_project(m->pos, m->start, m->P, m->constraints, m->force, m->scratch, V, m->ctrl,
-                          gA, m->vel, st));
+        CK(launch_project(m->pos, m->start, m->P, m->nmax, m->constraints, m->force, m->scratch, V, 1,
+                          m->ctrl, gA, m->vel, st));
     } else {
         CK(launch_fire_velocity(m->vel, m->force, V, m->ctrl, gA, st));
     }
     // energy-increase rollback (model.cpp:450-470), gated on rbGate
     CK(launch_fire_rollback(m->pos, m->vel, m->force, m->posTMP2, V, m->ctrl, gRb, st));
-    rc = geometry(m, gRb);
-    if (rc) return rc;
+    if (!rigid) {
+        rc = geometry(m, gRb);
+        if (rc) return rc;
+    }
     if (needsI) {
         CK(launch_neighbor_cells(m->pos, m->start, m->shapeId, V, m->boxSize, m->cellLocation, gRb, st));
         CK(launch_contacts(m->pos, m->start, m->shapeId, m->cellLocation, m->P, V, m->boxSize,
@@ -501,8 +519,8 @@ int record_fire_step(pcp_model* m) {
     rc = force_energy(m, gRb);
     if (rc) return rc;
     if (rigid) {
-        CK(launch_project(m->pos, m->start, m->P, m->constraints, m->force, m->scratch, V, m->ctrl,
-                          gRb, m->vel, st));
+        CK(launch_project(m->pos, m->start, m->P, m->nmax, m->constraints, m->force, m->scratch, V, 1,
+                          m->ctrl, gRb, m->vel, st));
     } else {
         CK(launch_fire_maxf(m->force, V, m->ctrl, gRb, st));
     }
@@ -622,6 +640,7 @@ int fire_step_once(pcp_model* m, const FireParams& fp, double out[4]) {
             m->numIntersections = c.numRecords;
             m->view = pcp_model::VIEW_FINAL;
             m->invalidate();
+            if (m->modelType == PCP_MODEL_NORMAL) m->geometryStale = true;
             return PCP_OK;
         }
     }
@@ -660,6 +679,7 @@ int pcp_model_create(int size, pcp_model** out) {
     }
     if (!rc) {
         cudaError_t e = contacts_init();
+        if (e == cudaSuccess) e = constraints_init();
         if (e != cudaSuccess) rc = fail(PCP_ERR_CUDA, "kernel setup failed: %s", cudaGetErrorString(e));
     }
     if (rc) { delete m; return rc; }
@@ -693,6 +713,7 @@ int pcp_model_set_num_vertices(pcp_model* m, int n) {
 }
 
 int pcp_model_set_positions(pcp_model* m, const double* host, int len) {
+    if (m && m->geometryStale) { int grc = ensure_geometry(m); if (grc) return grc; }
     CHECK_M(m);
     if (len != 2 * m->V) {
         printf("Update numVertices before setting the positions\n");   // model.cpp:524
@@ -723,6 +744,8 @@ int pcp_model_set_start_indices(pcp_model* m, const int* host, int len) {
     if (rc) return rc;
     m->P = P;
     m->startHost.assign(host, host + len);
+    m->nmax = 0;
+    for (int p = 0; p < P; ++p) m->nmax = std::max(m->nmax, host[p + 1] - host[p]);
     size_t Pn = (size_t)std::max(P, 1);
     CK(dalloc(&m->start, (size_t)len));
     CK(dalloc(&m->areas, Pn)); CK(dalloc(&m->comX, Pn)); CK(dalloc(&m->comY, Pn));
@@ -802,6 +825,7 @@ int pcp_model_initialize_neighbor_cells(pcp_model* m) {
 }
 
 int pcp_model_update_polygon_geometry(pcp_model* m) {
+    if (m) m->geometryStale = false;
     CHECK_M(m);
     int rc = need_topology(m);
     if (rc) return rc;
@@ -862,6 +886,7 @@ int pcp_model_update_outersections(pcp_model* m) {
 }
 
 int pcp_model_update_force_energy(pcp_model* m) {
+    if (m && m->geometryStale) { int grc = ensure_geometry(m); if (grc) return grc; }
     CHECK_M(m);
     int rc = need_topology(m);
     if (rc) return rc;
@@ -869,23 +894,26 @@ int pcp_model_update_force_energy(pcp_model* m) {
 }
 
 int pcp_model_project_force(pcp_model* m) {
+    if (m && m->geometryStale) { int grc = ensure_geometry(m); if (grc) return grc; }
     CHECK_M(m);
     int rc = need_topology(m);
     if (rc) return rc;
-    CK(launch_project(m->pos, m->start, m->P, m->constraints, m->force, m->scratch, m->V, nullptr,
+    CK(launch_project(m->pos, m->start, m->P, m->nmax, m->constraints, m->force, m->scratch, m->V, 0,
+                      nullptr,
                       nullptr, nullptr, m->stream));
     m->launches++;
     return PCP_OK;
 }
 
 int pcp_model_shake_project(pcp_model* m, int n_iter, double tol, int* iters_out) {
+    if (m && m->geometryStale) { int grc = ensure_geometry(m); if (grc) return grc; }
     CHECK_M(m);
     int rc = need_topology(m);
     if (rc) return rc;
     int it = 0;
     if (m->P > 0 && n_iter > 0) {
         CK(cudaMemsetAsync(m->shakeIters, 0, sizeof(int), m->stream));
-        CK(launch_shake(m->pos, m->start, m->P, m->targetEdge, m->targetAreas, n_iter, tol,
+        CK(launch_shake(m->pos, m->start, m->P, m->nmax, m->targetEdge, m->targetAreas, n_iter, tol,
                         m->shakeIters, m->scratch, m->V, nullptr, m->stream));
         m->launches++;
         CK(cudaMemcpyAsync(&it, m->shakeIters, sizeof(int), cudaMemcpyDeviceToHost, m->stream));
@@ -898,6 +926,7 @@ int pcp_model_shake_project(pcp_model* m, int n_iter, double tol, int* iters_out
 }
 
 int pcp_model_xpbd_project(pcp_model* m, int n_iter, double tol, int* iters_out) {
+    if (m && m->geometryStale) { int grc = ensure_geometry(m); if (grc) return grc; }
     CHECK_M(m);
     int rc = need_topology(m);
     if (rc) return rc;
@@ -922,6 +951,7 @@ int pcp_model_xpbd_project(pcp_model* m, int n_iter, double tol, int* iters_out)
 }
 
 int pcp_model_update_positions(pcp_model* m, double dt) {
+    if (m && m->geometryStale) { int grc = ensure_geometry(m); if (grc) return grc; }
     CHECK_M(m);
     CK(launch_update_positions(reinterpret_cast<double*>(m->pos), reinterpret_cast<const double*>(m->force),
                                m->V, dt, m->stream));
@@ -936,6 +966,7 @@ int pcp_model_reset_velocities(pcp_model* m) {
 }
 
 int pcp_model_reset_areas(pcp_model* m) {
+    if (m && m->geometryStale) { int grc = ensure_geometry(m); if (grc) return grc; }
     CHECK_M(m);
     int rc = need_topology(m);
     if (rc) return rc;
@@ -1038,6 +1069,7 @@ int pcp_model_minimize_fire(pcp_model* m, double thr, double dt0, int max_steps,
     // Model::minimizeFIRE (model.cpp:488-504)
     rc = pcp_model_reset_velocities(m);
     if (rc) return rc;
+    m->geometryStale = false;
     rc = geometry(m, nullptr);
     if (rc) return rc;
     rc = force_energy(m, nullptr);
@@ -1083,6 +1115,7 @@ int pcp_model_minimize_fire(pcp_model* m, double thr, double dt0, int max_steps,
     m->numIntersections = c.numRecords;
     m->view = pcp_model::VIEW_FINAL;
     m->invalidate();
+    if (m->modelType == PCP_MODEL_NORMAL && c.stepsDone > 0) m->geometryStale = true;
     out[0] = c.converged ? c.outE : c.energy;
     out[1] = c.dt;
     out[2] = c.stepsDone;
@@ -1097,6 +1130,7 @@ int pcp_model_fire_setup(pcp_model* m, double thr, double dt0, int max_steps, do
     if (rc) return rc;
     rc = pcp_model_reset_velocities(m);
     if (rc) return rc;
+    m->geometryStale = false;
     rc = geometry(m, nullptr);
     if (rc) return rc;
     rc = force_energy(m, nullptr);
@@ -1117,6 +1151,7 @@ int pcp_model_fire_continue(pcp_model* m, int n_steps) {
     if (!m->fireExec) return fail(PCP_ERR_STATE, "pcp_model_fire_setup has not been called");
     for (int s = 0; s < n_steps; ++s) CK(cudaGraphLaunch(m->fireExec, m->stream));
     m->launches += (long long)n_steps * m->fireKernelNodes;
+    if (n_steps > 0 && m->modelType == PCP_MODEL_NORMAL) m->geometryStale = true;
     return PCP_OK;
 }
 
@@ -1189,6 +1224,7 @@ int pcp_model_get_max_unbalanced_force(pcp_model* m, double* out) {
     return sync(m);
 }
 int pcp_model_get_max_edge_length(pcp_model* m, double* out) {
+    if (m && m->geometryStale) { int grc = ensure_geometry(m); if (grc) return grc; }
     CHECK_M(m);
     CK(cudaMemcpyAsync(out, m->maxEdge, sizeof(double), cudaMemcpyDeviceToHost, m->stream));
     return sync(m);
@@ -1206,9 +1242,11 @@ int pcp_model_get_velocities(pcp_model* m, double* out, int cap, int* len) {
     CHECK_M(m); return copy_dev_out(m, reinterpret_cast<const double*>(m->vel), 2 * m->V, out, cap, len);
 }
 int pcp_model_get_areas(pcp_model* m, double* out, int cap, int* len) {
+    if (m && m->geometryStale) { int grc = ensure_geometry(m); if (grc) return grc; }
     CHECK_M(m); return copy_dev_out(m, (const double*)m->areas, m->P, out, cap, len);
 }
 int pcp_model_get_com(pcp_model* m, double* out, int cap, int* len) {
+    if (m && m->geometryStale) { int grc = ensure_geometry(m); if (grc) return grc; }
     CHECK_M(m);
     if (len) *len = 2 * m->P;
     if (!out) return PCP_OK;
@@ -1218,12 +1256,15 @@ int pcp_model_get_com(pcp_model* m, double* out, int cap, int* len) {
     return copy_dev_out(m, (const double*)m->comY, m->P, out + m->P, cap - m->P, nullptr);
 }
 int pcp_model_get_perimeters(pcp_model* m, double* out, int cap, int* len) {
+    if (m && m->geometryStale) { int grc = ensure_geometry(m); if (grc) return grc; }
     CHECK_M(m); return copy_dev_out(m, (const double*)m->perimeters, m->P, out, cap, len);
 }
 int pcp_model_get_edge_lengths(pcp_model* m, double* out, int cap, int* len) {
+    if (m && m->geometryStale) { int grc = ensure_geometry(m); if (grc) return grc; }
     CHECK_M(m); return copy_dev_out(m, (const double*)m->edgeLengths, m->V, out, cap, len);
 }
 int pcp_model_get_constraints(pcp_model* m, double* out, int cap, int* len) {
+    if (m && m->geometryStale) { int grc = ensure_geometry(m); if (grc) return grc; }
     CHECK_M(m); return copy_dev_out(m, (const double*)m->constraints, 6 * m->V, out, cap, len);
 }
 int pcp_model_get_target_areas(pcp_model* m, double* out, int cap, int* len) {
@@ -1426,26 +1467,39 @@ static double* stateless_scratch(int V) {
     return buf;
 }
 
+static int start_info(const int* d_start, int P, int& V, int& nmax) {
+    std::vector<int> h(P + 1, 0);
+    if (P > 0) CK(cudaMemcpy(h.data(), d_start, (P + 1) * sizeof(int), cudaMemcpyDeviceToHost));
+    V = h[P];
+    nmax = 0;
+    for (int p = 0; p < P; ++p) nmax = std::max(nmax, h[p + 1] - h[p]);
+    return PCP_OK;
+}
+
 int pcp_project_force(const double* d_pos, const int* d_start, int P, const double* d_constraints,
                       double* d_force, void* stream) {
-    int V = 0;
-    if (P > 0) CK(cudaMemcpy(&V, d_start + P, sizeof(int), cudaMemcpyDeviceToHost));
+    int V = 0, nmax = 0;
+    int rc = start_info(d_start, P, V, nmax);
+    if (rc) return rc;
+    if (constraints_init() != cudaSuccess) return fail(PCP_ERR_CUDA, "kernel setup failed");
     double* s = stateless_scratch(V);
     if (!s) return fail(PCP_ERR_CUDA, "scratch allocation failed");
-    CK(launch_project(reinterpret_cast<const double2*>(d_pos), d_start, P, d_constraints,
-                      reinterpret_cast<double2*>(d_force), s, V, nullptr, nullptr, nullptr,
+    CK(launch_project(reinterpret_cast<const double2*>(d_pos), d_start, P, nmax, d_constraints,
+                      reinterpret_cast<double2*>(d_force), s, V, 0, nullptr, nullptr, nullptr,
                       (cudaStream_t)stream));
     return PCP_OK;
 }
 
 int pcp_shake_project(double* d_pos, const int* d_start, int P, const double* d_tl,
                       const double* d_ta, int max_iter, double tol, int* d_max_iters, void* stream) {
-    int V = 0;
-    if (P > 0) CK(cudaMemcpy(&V, d_start + P, sizeof(int), cudaMemcpyDeviceToHost));
+    int V = 0, nmax = 0;
+    int rc = start_info(d_start, P, V, nmax);
+    if (rc) return rc;
+    if (constraints_init() != cudaSuccess) return fail(PCP_ERR_CUDA, "kernel setup failed");
     double* s = stateless_scratch(V);
     if (!s) return fail(PCP_ERR_CUDA, "scratch allocation failed");
     CK(cudaMemsetAsync(d_max_iters, 0, sizeof(int), (cudaStream_t)stream));
-    CK(launch_shake(reinterpret_cast<double2*>(d_pos), d_start, P, d_tl, d_ta, max_iter, tol,
+    CK(launch_shake(reinterpret_cast<double2*>(d_pos), d_start, P, nmax, d_tl, d_ta, max_iter, tol,
                     d_max_iters, s, V, nullptr, (cudaStream_t)stream));
     return PCP_OK;
 }

@@ -12,7 +12,7 @@ namespace pcp {
 // Largest polygon the warp-per-pair contact kernel stages in shared memory;
 // bigger polygons (and pairs with more crossings than a warp buffers) take
 // the block-per-pair path, which handles up to kSlowRing vertices per pair.
-constexpr int kFastRing = 128;
+constexpr int kFastRing = 64;
 constexpr int kFastRecords = 64;
 constexpr int kSlowRing = 2048;
 constexpr int kSlowRecords = 2048;
@@ -140,14 +140,18 @@ cudaError_t launch_overlap_force(const double2* pos, const int* start, const int
                                  const int* gate, cudaStream_t st);
 
 // constraints
-cudaError_t launch_project(const double2* pos, const int* start, int P,
+cudaError_t constraints_init();
+// nmax: largest vertex count of a polygon (decides whether the per-polygon
+// scratch fits in shared memory)
+cudaError_t launch_project(const double2* pos, const int* start, int P, int nmax,
                            const double* constraints, double2* force, double* scratch, int V,
-                           Ctrl* fireCtrl, const int* gate, double2* vel, cudaStream_t st);
-cudaError_t launch_shake(double2* pos, const int* start, int P, const double* targetEdge,
+                           int areaFromPositions, Ctrl* fireCtrl, const int* gate, double2* vel,
+                           cudaStream_t st);
+cudaError_t launch_shake(double2* pos, const int* start, int P, int nmax, const double* targetEdge,
                          const double* targetArea, int maxIter, double tol, int* maxItersOut,
                          double* scratch, int V, const int* gate, cudaStream_t st);
 // scratch doubles per vertex needed by launch_project / launch_shake
-constexpr int kScratchPerVertex = 17;
+constexpr int kScratchPerVertex = 36;
 cudaError_t launch_xpbd_iteration(double2* pos, const int* start, int P,
                                   const double* targetEdge, const double* targetArea,
                                   double* devOut, cudaStream_t st);
