@@ -322,17 +322,18 @@ __host__ __device__ constexpr size_t shake_ws_bytes(int NV, int N) {
     return (size_t)NV * (3 * 16 + 4 * 8 + 2 * 4) + (size_t)N * 12 * 4;
 }
 
-// Parallel cyclic reduction of the N rows in buffer 0 of w (three
-// right-hand sides); leaves x = r / b in p0, p1, p2.  One warp, rows strided.
-__device__ void pcr3(ShakeWS& w, int N) {
+// Parallel cyclic reduction of N rows (arrays [2][N]: buffer 0 holds the
+// system, buffer 1 is scratch) with three right-hand sides; leaves the
+// solutions x = r / b in p0, p1, p2 (buffer 0).  One warp, rows strided.
+__device__ void pcr3f(float* pa, float* pb, float* pc, float* p0, float* p1, float* p2, int N) {
     const int lane = threadIdx.x & 31;
     int cur = 0;
     for (int d = 1; d < N; d <<= 1) {
         int nxt = cur ^ 1;
-        const float *a = w.pa + cur * N, *b = w.pb + cur * N, *c = w.pc + cur * N;
-        const float *r0 = w.p0 + cur * N, *r1 = w.p1 + cur * N, *r2 = w.p2 + cur * N;
-        float *a2 = w.pa + nxt * N, *b2 = w.pb + nxt * N, *c2 = w.pc + nxt * N;
-        float *s0 = w.p0 + nxt * N, *s1 = w.p1 + nxt * N, *s2 = w.p2 + nxt * N;
+        const float *a = pa + cur * N, *b = pb + cur * N, *c = pc + cur * N;
+        const float *r0 = p0 + cur * N, *r1 = p1 + cur * N, *r2 = p2 + cur * N;
+        float *a2 = pa + nxt * N, *b2 = pb + nxt * N, *c2 = pc + nxt * N;
+        float *s0 = p0 + nxt * N, *s1 = p1 + nxt * N, *s2 = p2 + nxt * N;
         for (int i = lane; i < N; i += 32) {
             int im = i - d, ip = i + d;
             float na = 0.f, nc = 0.f;
@@ -354,15 +355,39 @@ __device__ void pcr3(ShakeWS& w, int N) {
         __syncwarp();
         cur = nxt;
     }
-    // solutions into buffer 0 (when the final buffer is 1 it is a distinct array)
-    const float *b = w.pb + cur * N, *r0 = w.p0 + cur * N, *r1 = w.p1 + cur * N;
-    const float *r2 = w.p2 + cur * N;
+    const float *b = pb + cur * N, *r0 = p0 + cur * N, *r1 = p1 + cur * N, *r2 = p2 + cur * N;
     for (int i = lane; i < N; i += 32) {
         float ib = 1.0f / b[i];
         float x0 = r0[i] * ib, x1 = r1[i] * ib, x2 = r2[i] * ib;
-        w.p0[i] = x0; w.p1[i] = x1; w.p2[i] = x2;
+        p0[i] = x0; p1[i] = x1; p2[i] = x2;
     }
     __syncwarp();
+}
+
+__device__ __forceinline__ void pcr3(ShakeWS& w, int N) { pcr3f(w.pa, w.pb, w.pc, w.p0, w.p1, w.p2, N); }
+
+// Sherman-Morrison split of a cyclic tridiagonal system held in PCR buffer 0
+// (rows 0..n-1; a = sub-, b = main, c = super-diagonal; the cyclic corners
+// sit in a[0] and c[n-1]): the corners are removed and the correction vector
+// is placed in p2.  False when gamma == 0.
+__device__ __forceinline__ bool sm_split(float* pa, float* pb, float* pc, float* p2, int n,
+                                         float& gamma, float& beta) {
+    const int lane = threadIdx.x & 31;
+    gamma = -pb[0];
+    beta = pa[0];
+    float alpha = pc[n - 1];
+    bool ok = gamma != 0.f;
+    __syncwarp();
+    if (lane == 0 && ok) {
+        pb[0] = pb[0] - gamma;
+        pb[n - 1] = pb[n - 1] - alpha * beta / gamma;
+        pa[0] = 0.f;
+        pc[n - 1] = 0.f;
+        p2[0] = gamma;
+        p2[n - 1] = alpha;
+    }
+    __syncwarp();
+    return ok;
 }
 
 __global__ void k_shake(double2* __restrict__ pos, const int* __restrict__ start, int P,
@@ -540,69 +565,39 @@ cudaError_t launch_shake(double2* pos, const int* start, int P, int nmax, const 
 }
 
 // Warp-per-polygon form of the projection for systems with few polygons
-// (small systems leave most SMs idle with one polygon per thread): per-vertex
-// work runs across the lanes and J^T J is solved by FP64 parallel cyclic
-// reduction (Sherman-Morrison split of the cyclic corners, rows padded to a
-// power of two).  Same mathematics as k_project.
+// (4096 polygons give only 128 warps of thread-per-polygon work): per-vertex
+// work runs across the lanes; (J^T J) x = J^T v is solved by mixed-precision
+// iterative refinement -- the residual J^T (v - J x) and every update are
+// FP64, each correction is solved in FP32 by parallel cyclic reduction
+// (Sherman-Morrison split of the cyclic corners, rows padded to a power of
+// two).  Each FP32 solve gains ~kappa * 6e-8 (kappa(J^T J) ~ (n/pi)^2), so
+// three rounds reach FP64 accuracy for polygons of up to a few hundred
+// vertices.  Same mathematics as k_project.
 //
 // areaFromPositions: take the unit area gradient from the positions (the
 // normalised areaComp of updatePolygonGeometryKernel, kernels.cuh:303,313)
 // instead of the constraints array; the device-resident FIRE step uses this
 // because its positions are those the reference's last geometry call saw.
+constexpr int kProjRounds = 3;
+
 struct ProjWS {
-    double2 *t, *a, *f, *f2, *q;
-    double *pa, *pb, *pc, *p0, *p1, *p2;   // [2][N] each
+    double2 *t, *f, *q;            // unit edges, F' and q (FP64)
+    float *mb, *mc;                // J^T J diagonal and super-diagonal (FP32)
+    float *pa, *pb, *pc, *p0, *p1, *p2;   // PCR rows [2][N]
 };
 __device__ __forceinline__ ProjWS proj_ws(unsigned char* base, int NV, int N) {
     ProjWS w;
     double2* d = reinterpret_cast<double2*>(base);
-    w.t = d; w.a = d + NV; w.f = d + 2 * NV; w.f2 = d + 3 * NV; w.q = d + 4 * NV;
-    double* q = reinterpret_cast<double*>(d + 5 * NV);
+    w.t = d; w.f = d + NV; w.q = d + 2 * NV;
+    float* f = reinterpret_cast<float*>(d + 3 * NV);
+    w.mb = f; w.mc = f + NV;
+    float* q = f + 2 * NV;
     w.pa = q; w.pb = q + 2 * N; w.pc = q + 4 * N; w.p0 = q + 6 * N; w.p1 = q + 8 * N; w.p2 = q + 10 * N;
     return w;
 }
+// bytes of one polygon's workspace; a multiple of 16 when NV is even
 __host__ __device__ constexpr size_t proj_ws_bytes(int NV, int N) {
-    return (size_t)NV * 80 + (size_t)N * 12 * 8;
-}
-
-__device__ void pcr3_d(ProjWS& w, int N) {
-    const int lane = threadIdx.x & 31;
-    int cur = 0;
-    for (int d = 1; d < N; d <<= 1) {
-        int nxt = cur ^ 1;
-        const double *a = w.pa + cur * N, *b = w.pb + cur * N, *c = w.pc + cur * N;
-        const double *r0 = w.p0 + cur * N, *r1 = w.p1 + cur * N, *r2 = w.p2 + cur * N;
-        double *a2 = w.pa + nxt * N, *b2 = w.pb + nxt * N, *c2 = w.pc + nxt * N;
-        double *s0 = w.p0 + nxt * N, *s1 = w.p1 + nxt * N, *s2 = w.p2 + nxt * N;
-        for (int i = lane; i < N; i += 32) {
-            int im = i - d, ip = i + d;
-            double na = 0.0, nc = 0.0;
-            double nb = b[i], n0 = r0[i], n1 = r1[i], n2 = r2[i];
-            if (im >= 0) {
-                double k1 = a[i] / b[im];
-                na = -k1 * a[im];
-                nb -= k1 * c[im];
-                n0 -= k1 * r0[im]; n1 -= k1 * r1[im]; n2 -= k1 * r2[im];
-            }
-            if (ip < N) {
-                double k2 = c[i] / b[ip];
-                nc = -k2 * c[ip];
-                nb -= k2 * a[ip];
-                n0 -= k2 * r0[ip]; n1 -= k2 * r1[ip]; n2 -= k2 * r2[ip];
-            }
-            a2[i] = na; b2[i] = nb; c2[i] = nc; s0[i] = n0; s1[i] = n1; s2[i] = n2;
-        }
-        __syncwarp();
-        cur = nxt;
-    }
-    const double *b = w.pb + cur * N, *r0 = w.p0 + cur * N, *r1 = w.p1 + cur * N;
-    const double *r2 = w.p2 + cur * N;
-    for (int i = lane; i < N; i += 32) {
-        double ib = 1.0 / b[i];
-        double x0 = r0[i] * ib, x1 = r1[i] * ib, x2 = r2[i] * ib;
-        w.p0[i] = x0; w.p1[i] = x1; w.p2[i] = x2;
-    }
-    __syncwarp();
+    return (size_t)NV * (48 + 8) + (size_t)N * 12 * 4;
 }
 
 __global__ void k_project_warp(const double2* __restrict__ pos, const int* __restrict__ start,
@@ -624,10 +619,13 @@ __global__ void k_project_warp(const double2* __restrict__ pos, const int* __res
         dt = fire->dt;
         if (blockIdx.x == 0 && threadIdx.x == 0 && fire->rollback == 0) {
             fire->proceed = proceed ? 1 : 0;
+            // the energy-increase rollback path runs when the step is not a
+            // SHAKE failure and the energy went up (model.cpp:450-453)
             fire->rbGate = (!fire->shakeFailed && rb && fire->active) ? 1 : 0;
         }
     }
     double sP = 0.0, sV = 0.0, sF = 0.0, mF = 0.0;
+    bool bad = false;
     if (p < P) {
         int st = start[p], n = start[p + 1] - st;
         if (n >= 3) {
@@ -646,97 +644,106 @@ __global__ void k_project_warp(const double2* __restrict__ pos, const int* __res
                 int kn = (k + 1 == n) ? 0 : k + 1, kp = (k == 0) ? n - 1 : k - 1;
                 double2 xk = pos[st + k], xn = pos[st + kn];
                 double dx = wrap(xn.x - xk.x), dy = wrap(xn.y - xk.y);
-                double len = sqrt(dx * dx + dy * dy);
+                double len2 = dx * dx + dy * dy;
                 double2 t = make_double2(0.0, 0.0);
-                bool ok = !(len < 1e-14);
-                if (ok) { double il = 1.0 / len; t = make_double2(dx * il, dy * il); }
+                bool ok = !(len2 < 1e-28);          // |e| >= 1e-14 (kernels.cuh:399)
+                if (ok) { double il = rsqrt(len2); t = make_double2(dx * il, dy * il); }
                 w.t[k] = t;
-                w.pb[k] = ok ? 2.0 : 1.0;
+                w.mb[k] = ok ? 2.0f : 1.0f;
                 w.f[k] = force[st + k];
+                double2 a;
                 if (areaFromPositions) {
                     double2 xp = pos[st + kp];
-                    double a0 = -wrap(xp.y - xn.y), a1 = wrap(xp.x - xn.x);
-                    w.a[k] = make_double2(a0, a1);
-                    an += a0 * a0 + a1 * a1;
+                    a = make_double2(-wrap(xp.y - xn.y), wrap(xp.x - xn.x));
+                    an += a.x * a.x + a.y * a.y;
                 } else {
                     const double* c = constraints + 6 * (size_t)(st + k);
-                    w.a[k] = make_double2(c[0], c[1]);
+                    a = make_double2(c[0], c[1]);
                 }
+                w.q[k] = a;
             }
             if (areaFromPositions) {
                 an = warp_sum(an);
                 double ir = an > 0.0 ? 1.0 / sqrt(an) : 1.0;
                 for (int k = lane; k < n; k += 32) {
-                    double2 a = w.a[k];
-                    w.a[k] = make_double2(a.x * ir, a.y * ir);
+                    double2 a = w.q[k];
+                    w.q[k] = make_double2(a.x * ir, a.y * ir);
                 }
             }
             __syncwarp();
             for (int k = lane; k < n; k += 32) {
-                int kn = (k + 1 == n) ? 0 : k + 1, kp = (k == 0) ? n - 1 : k - 1;
-                double2 t = w.t[k], tn = w.t[kn], tp = w.t[kp];
-                double2 f0 = w.f[k], f1 = w.f[kn], a0 = w.a[k], a1 = w.a[kn];
-                w.pc[k] = -(t.x * tn.x + t.y * tn.y);
-                w.pa[k] = -(tp.x * t.x + tp.y * t.y);
-                w.p0[k] = t.x * (f1.x - f0.x) + t.y * (f1.y - f0.y);
-                w.p1[k] = t.x * (a1.x - a0.x) + t.y * (a1.y - a0.y);
-                w.p2[k] = 0.0;
-            }
-            for (int k = n + lane; k < N; k += 32) {
-                w.pa[k] = 0.0; w.pb[k] = 1.0; w.pc[k] = 0.0;
-                w.p0[k] = 0.0; w.p1[k] = 0.0; w.p2[k] = 0.0;
+                int kn = (k + 1 == n) ? 0 : k + 1;
+                double2 t = w.t[k], tn = w.t[kn];
+                w.mc[k] = (float)(-(t.x * tn.x + t.y * tn.y));
             }
             __syncwarp();
-            double gamma = -w.pb[0], beta = w.pa[0], alpha = w.pc[n - 1];
-            __syncwarp();
-            if (lane == 0) {
-                w.pb[0] = w.pb[0] - gamma;
-                w.pb[n - 1] = w.pb[n - 1] - alpha * beta / gamma;
-                w.pa[0] = 0.0; w.pc[n - 1] = 0.0;
-                w.p2[0] = gamma; w.p2[n - 1] = alpha;
+            for (int round = 0; round < kProjRounds && !bad; ++round) {
+                // residual right-hand sides J^T F', J^T q (FP64) and the FP32 rows
+                for (int k = lane; k < n; k += 32) {
+                    int kn = (k + 1 == n) ? 0 : k + 1, kp = (k == 0) ? n - 1 : k - 1;
+                    double2 t = w.t[k], f0 = w.f[k], f1 = w.f[kn], a0 = w.q[k], a1 = w.q[kn];
+                    w.p0[k] = (float)(t.x * (f1.x - f0.x) + t.y * (f1.y - f0.y));
+                    w.p1[k] = (float)(t.x * (a1.x - a0.x) + t.y * (a1.y - a0.y));
+                    w.p2[k] = 0.f;
+                    w.pb[k] = w.mb[k];
+                    w.pc[k] = w.mc[k];
+                    w.pa[k] = w.mc[kp];
+                }
+                for (int k = n + lane; k < N; k += 32) {
+                    w.pa[k] = 0.f; w.pb[k] = 1.f; w.pc[k] = 0.f;
+                    w.p0[k] = 0.f; w.p1[k] = 0.f; w.p2[k] = 0.f;
+                }
+                __syncwarp();
+                float gamma, beta;
+                if (!sm_split(w.pa, w.pb, w.pc, w.p2, n, gamma, beta)) { bad = true; break; }
+                pcr3f(w.pa, w.pb, w.pc, w.p0, w.p1, w.p2, N);
+                float den = 1.f + w.p2[0] + beta * w.p2[n - 1] / gamma;
+                float fl = (w.p0[0] + beta * w.p0[n - 1] / gamma) / den;
+                float fm = (w.p1[0] + beta * w.p1[n - 1] / gamma) / den;
+                __syncwarp();
+                for (int k = lane; k < n; k += 32) {
+                    float s = w.p2[k];
+                    w.p0[k] -= fl * s;
+                    w.p1[k] -= fm * s;
+                }
+                __syncwarp();
+                // F' -= J lambda, q -= J mu with (J x)_k = -x_k t_k + x_{k-1} t_{k-1}
+                for (int k = lane; k < n; k += 32) {
+                    int kp = (k == 0) ? n - 1 : k - 1;
+                    double2 t = w.t[k], tp = w.t[kp];
+                    double l0 = (double)w.p0[k], l0p = (double)w.p0[kp];
+                    double l1 = (double)w.p1[k], l1p = (double)w.p1[kp];
+                    double2 f = w.f[k], a = w.q[k];
+                    f.x -= -l0 * t.x + l0p * tp.x; f.y -= -l0 * t.y + l0p * tp.y;
+                    a.x -= -l1 * t.x + l1p * tp.x; a.y -= -l1 * t.y + l1p * tp.y;
+                    w.f[k] = f; w.q[k] = a;
+                }
+                __syncwarp();
             }
-            __syncwarp();
-            pcr3_d(w, N);
-            double den = 1.0 + w.p2[0] + beta * w.p2[n - 1] / gamma;
-            double f0 = (w.p0[0] + beta * w.p0[n - 1] / gamma) / den;
-            double f1 = (w.p1[0] + beta * w.p1[n - 1] / gamma) / den;
-            __syncwarp();
-            for (int k = lane; k < n; k += 32) {
-                double s = w.p2[k];
-                w.p0[k] -= f0 * s;
-                w.p1[k] -= f1 * s;
-            }
-            __syncwarp();
-            double qF = 0.0, qq = 0.0;
-            for (int k = lane; k < n; k += 32) {
-                int kp = (k == 0) ? n - 1 : k - 1;
-                double2 t = w.t[k], tp = w.t[kp];
-                double l0 = w.p0[k], l0p = w.p0[kp], l1 = w.p1[k], l1p = w.p1[kp];
-                // (J x)_k = -x_k t_k + x_{k-1} t_{k-1}
-                double2 f = w.f[k], a = w.a[k];
-                double fx = f.x - (-l0 * t.x + l0p * tp.x), fy = f.y - (-l0 * t.y + l0p * tp.y);
-                double qx = a.x - (-l1 * t.x + l1p * tp.x), qy = a.y - (-l1 * t.y + l1p * tp.y);
-                w.f2[k] = make_double2(fx, fy);
-                w.q[k] = make_double2(qx, qy);
-                qF += qx * fx + qy * fy;
-                qq += qx * qx + qy * qy;
-            }
-            qF = warp_sum(qF);
-            qq = warp_sum(qq);
-            double coef = (sqrt(qq) > 1e-14) ? qF / qq : 0.0;
-            for (int k = lane; k < n; k += 32) {
-                double2 f1v = w.f2[k], q = w.q[k];
-                double fx = f1v.x - coef * q.x, fy = f1v.y - coef * q.y;
-                force[st + k] = make_double2(fx, fy);
-                mF = fmax(mF, fmax(fabs(fx), fabs(fy)));
-                if (proceed) {
-                    double2 v = vel[st + k];
-                    v.x += 0.5 * dt * fx;
-                    v.y += 0.5 * dt * fy;
-                    vel[st + k] = v;
-                    sP += fx * v.x + fy * v.y;
-                    sV += v.x * v.x + v.y * v.y;
-                    sF += fx * fx + fy * fy;
+            if (!bad) {
+                double qF = 0.0, qq = 0.0;
+                for (int k = lane; k < n; k += 32) {
+                    double2 f = w.f[k], q = w.q[k];
+                    qF += q.x * f.x + q.y * f.y;
+                    qq += q.x * q.x + q.y * q.y;
+                }
+                qF = warp_sum(qF);
+                qq = warp_sum(qq);
+                double coef = (sqrt(qq) > 1e-14) ? qF / qq : 0.0;   // kernels.cuh:464
+                for (int k = lane; k < n; k += 32) {
+                    double2 f = w.f[k], q = w.q[k];
+                    double fx = f.x - coef * q.x, fy = f.y - coef * q.y;
+                    force[st + k] = make_double2(fx, fy);
+                    mF = fmax(mF, fmax(fabs(fx), fabs(fy)));
+                    if (proceed) {
+                        double2 v = vel[st + k];
+                        v.x += 0.5 * dt * fx;
+                        v.y += 0.5 * dt * fy;
+                        vel[st + k] = v;
+                        sP += fx * v.x + fy * v.y;
+                        sV += v.x * v.x + v.y * v.y;
+                        sF += fx * fx + fy * fy;
+                    }
                 }
             }
         } else {
@@ -755,6 +762,7 @@ __global__ void k_project_warp(const double2* __restrict__ pos, const int* __res
         }
     }
     if (fire) {
+        if (bad && lane == 0) atomicOr(&fire->flags, kFlagNonFinite);
         mF = warp_maxd(mF);
         if (lane == 0) atomic_max_nonneg(&fire->maxF, mF);
         if (proceed) {
@@ -797,7 +805,7 @@ cudaError_t launch_project(const double2* pos, const int* start, int P, int nmax
             pos, start, P, constraints, force, scratch, V, sn, areaFromPositions, fireCtrl, vel, gate);
         return cudaGetLastError();
     }
-    int nv = nmax;
+    int nv = (nmax + 1) & ~1;          // even, so each workspace stays 16-byte aligned
     int N = 4;
     while (N < nv) N <<= 1;
     size_t per = proj_ws_bytes(nv, N);
@@ -952,10 +960,10 @@ __global__ void k_fire_after_shake(double2* __restrict__ pos, double2* __restric
         pos[i] = save[i];
         vel[i] = make_double2(0.0, 0.0);
     } else {
-        double dt = c->dt;
+        double idt = 1.0 / c->dt;
         double2 x = pos[i], y = verlet[i], v = vel[i];
-        v.x += wrap(x.x - y.x) / dt;
-        v.y += wrap(x.y - y.y) / dt;
+        v.x += wrap(x.x - y.x) * idt;
+        v.y += wrap(x.y - y.y) * idt;
         vel[i] = v;
     }
 }
@@ -1036,15 +1044,23 @@ __global__ void k_fire_bend(double2* __restrict__ vel, const double2* __restrict
                             int V, const Ctrl* __restrict__ c, const int* gate) {
     if (gate_closed(gate)) return;
     if (!c->proceed) return;
+    __shared__ double s_coef[2];
+    if (threadIdx.x == 0) {
+        // the mixing coefficients once per block (two square roots, a division)
+        double fn = sqrt(c->ff), vn = sqrt(c->vv), a = c->alpha;
+        s_coef[0] = 1.0 - a;
+        s_coef[1] = fn > 0.0 ? a * vn / fn : -1.0;
+    }
+    __syncthreads();
     int i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= V) return;
     double P = c->P;
     if (P > 0.0) {
-        double fn = sqrt(c->ff), vn = sqrt(c->vv), a = c->alpha;
-        if (fn > 0.0) {
-            double s = a * vn / fn;
+        double s = s_coef[1];
+        if (s >= 0.0) {
+            double a1 = s_coef[0];
             double2 v = vel[i], f = force[i];
-            vel[i] = make_double2((1.0 - a) * v.x + s * f.x, (1.0 - a) * v.y + s * f.y);
+            vel[i] = make_double2(a1 * v.x + s * f.x, a1 * v.y + s * f.y);
         }
     } else {
         vel[i] = make_double2(0.0, 0.0);
