@@ -1,12 +1,15 @@
 /*
  * pcp_gb300.h -- C ABI of the GB300-native (sm_103a) polygon overlap path.
  *
- * Library: libpcp_gb300.so (built in-tree by pycudapolygon_gb300/build.py).
+ * Library: libpcp_gb300.so (built in-tree by pycudapolygon_gb300/buildlib.py).
  * Every function returns an int status (PCP_OK == 0) and never exits the
  * process; pcp_last_error() gives the message of the last failure on the
- * calling thread.  No function allocates device memory except
- * pcp_model_create and the pcp_model_set_* / pcp_model_initialize_*
- * functions that size the model's buffers (as the reference's setters do).
+ * calling thread.  Device memory is allocated by pcp_model_create and the
+ * pcp_model_set_* / pcp_model_initialize_* functions that size the model's
+ * buffers (as the reference's setters do), by model calls whose contact
+ * buffers must grow, and by pcp_project_force / pcp_shake_project, which
+ * keep one process-wide scratch buffer that grows to the largest vertex
+ * count they have seen.
  *
  * Two layers, each replacing one seam of camdennis/pyCudaPolygon:
  *
