@@ -259,6 +259,31 @@ int pcp_shake_project(double* d_pos, const int* d_start, int num_polygons,
                       const double* d_target_edge_lengths, const double* d_target_areas,
                       int max_iter, double tol, int* d_max_iters, void* stream);
 
+/* No counterpart in the reference: pcp_shake_project for callers that may
+ * not allocate device memory -- plugins whose host owns the device's memory
+ * through its own pool and hands the plugin only the buffers it passes in,
+ * and loops where the device-wide synchronisation of cudaMalloc/cudaFree is
+ * not allowed.  The same kernel, arguments and results as
+ * pcp_shake_project, but the workspace is a static device array of this
+ * library sized for PCP_SHAKE_NOALLOC_MAX_VERTICES vertices (4.5 MiB); the
+ * call makes no cudaMalloc, cudaFree or other allocation.
+ *   - More than PCP_SHAKE_NOALLOC_MAX_VERTICES vertices in total
+ *     (startIndices[num_polygons]) returns PCP_ERR_CAPACITY and launches
+ *     nothing.  The call reads startIndices[num_polygons] back to the host
+ *     and waits for `stream` to do that check.
+ *   - The first call on a device looks up the array's device address (it
+ *     may load the library's kernels onto that device); make that first
+ *     call before any stream capture.
+ *   - Every call on a device shares the one array and it keeps the last
+ *     call's contents (each polygon writes its part before reading it;
+ *     *d_max_iters is cleared by the call).  Calls whose kernels overlap on
+ *     the GPU -- on two streams, or from two host threads -- race on it. */
+#define PCP_SHAKE_NOALLOC_MAX_VERTICES 16384
+int pcp_shake_project_noalloc(double* d_pos, const int* d_start, int num_polygons,
+                              const double* d_target_edge_lengths,
+                              const double* d_target_areas, int max_iter, double tol,
+                              int* d_max_iters, void* stream);
+
 /* updatePositionsKernel (kernels.cuh:1433-1438): x = frac(x + dt F) */
 int pcp_update_positions(double* d_pos, const double* d_force, int num_vertices,
                          double dt, void* stream);

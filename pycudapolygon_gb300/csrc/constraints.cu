@@ -13,6 +13,8 @@
 #include <cuda_runtime.h>
 #include <math.h>
 
+#include <mutex>
+
 #include "pcp_common.cuh"
 #include "pcp_internal.h"
 
@@ -1156,6 +1158,52 @@ cudaError_t launch_fire_finish(double2* vel, const double2* force, int V, Ctrl* 
                                const int* gate, cudaStream_t st) {
     k_fire_bend<<<nblk(V, 256), 256, 0, st>>>(vel, force, V, c, gate);
     k_fire_scalars<<<1, 1, 0, st>>>(c, gate);
+    return cudaGetLastError();
+}
+
+// ---------------------------------------------- SHAKE without allocation ----
+// Workspace of pcp_shake_project_noalloc: a fixed array in this module's own
+// device memory, for callers that may not allocate device memory.  Polygon p
+// works in doubles [kScratchPerVertex * start[p], kScratchPerVertex *
+// start[p+1]) and writes every element of its slice before reading it, so
+// nothing in the array has to start at zero.  There is one array per device
+// and every call on that device shares it: calls whose kernels overlap on the
+// GPU race on it.
+static __device__ __align__(256) double
+    g_shake_noalloc_scratch[(size_t)kScratchPerVertex * PCP_SHAKE_NOALLOC_MAX_VERTICES];
+
+// Device address of the array on the current device.  It is looked up once
+// per device, by the first call made with that device current; the lookup
+// can load this module onto the device, so that first call belongs before
+// any stream capture.
+cudaError_t shake_noalloc_scratch(double** out) {
+    constexpr int kMaxDevices = 64;
+    static std::mutex mu;
+    static double* addr[kMaxDevices] = {};
+    int dev = 0;
+    cudaError_t e = cudaGetDevice(&dev);
+    if (e != cudaSuccess) return e;
+    if (dev < 0 || dev >= kMaxDevices) return cudaErrorInvalidDevice;
+    std::lock_guard<std::mutex> lock(mu);
+    if (!addr[dev]) {
+        void* p = nullptr;
+        e = cudaGetSymbolAddress(&p, g_shake_noalloc_scratch);
+        if (e != cudaSuccess) return e;
+        addr[dev] = static_cast<double*>(p);
+    }
+    *out = addr[dev];
+    return cudaSuccess;
+}
+
+// k_shake with every polygon's workspace in `scratch` (none in shared
+// memory, so the launch needs no attribute set-up)
+cudaError_t launch_shake_noalloc(double2* pos, const int* start, int P, const double* targetEdge,
+                                 const double* targetArea, int maxIter, double tol,
+                                 int* maxItersOut, double* scratch, cudaStream_t st) {
+    if (P <= 0) return cudaSuccess;
+    constexpr int wpb = 8;
+    k_shake<<<nblk(P, wpb), 32 * wpb, 0, st>>>(pos, start, P, targetEdge, targetArea, maxIter, tol,
+                                               maxItersOut, scratch, 0, nullptr);
     return cudaGetLastError();
 }
 

@@ -1504,6 +1504,33 @@ int pcp_shake_project(double* d_pos, const int* d_start, int P, const double* d_
     return PCP_OK;
 }
 
+// Same computation as pcp_shake_project with the workspace in a static device
+// array: no cudaMalloc, cudaFree or other allocation.  Reads start[P] back to
+// the host (waiting for the stream) to check the size against the array.
+int pcp_shake_project_noalloc(double* d_pos, const int* d_start, int P, const double* d_tl,
+                              const double* d_ta, int max_iter, double tol, int* d_max_iters,
+                              void* stream) {
+    if (P < 0) return fail(PCP_ERR_ARG, "negative polygon count");
+    if (!d_max_iters) return fail(PCP_ERR_ARG, "null d_max_iters");
+    cudaStream_t st = (cudaStream_t)stream;
+    double* scratch = nullptr;
+    CK(shake_noalloc_scratch(&scratch));
+    int V = 0;
+    if (P > 0) {
+        CK(cudaMemcpyAsync(&V, d_start + P, sizeof(int), cudaMemcpyDeviceToHost, st));
+        CK(cudaStreamSynchronize(st));
+    }
+    if (V < 0 || V > PCP_SHAKE_NOALLOC_MAX_VERTICES)
+        return fail(PCP_ERR_CAPACITY,
+                    "pcp_shake_project_noalloc: %d vertices exceed its static workspace of %d "
+                    "vertices; use pcp_shake_project",
+                    V, PCP_SHAKE_NOALLOC_MAX_VERTICES);
+    CK(cudaMemsetAsync(d_max_iters, 0, sizeof(int), st));
+    CK(launch_shake_noalloc(reinterpret_cast<double2*>(d_pos), d_start, P, d_tl, d_ta, max_iter,
+                            tol, d_max_iters, scratch, st));
+    return PCP_OK;
+}
+
 int pcp_update_positions(double* d_pos, const double* d_force, int V, double dt, void* stream) {
     CK(launch_update_positions(d_pos, d_force, V, dt, (cudaStream_t)stream));
     return PCP_OK;

@@ -152,6 +152,12 @@ cudaError_t launch_shake(double2* pos, const int* start, int P, int nmax, const 
                          double* scratch, int V, const int* gate, cudaStream_t st);
 // scratch doubles per vertex needed by launch_project / launch_shake
 constexpr int kScratchPerVertex = 36;
+// pcp_shake_project_noalloc: device address of its static workspace on the
+// current device, and k_shake launched with every workspace in it
+cudaError_t shake_noalloc_scratch(double** out);
+cudaError_t launch_shake_noalloc(double2* pos, const int* start, int P, const double* targetEdge,
+                                 const double* targetArea, int maxIter, double tol,
+                                 int* maxItersOut, double* scratch, cudaStream_t st);
 cudaError_t launch_xpbd_iteration(double2* pos, const int* start, int P,
                                   const double* targetEdge, const double* targetArea,
                                   double* devOut, cudaStream_t st);
