@@ -65,7 +65,7 @@ class ClockSampler:
         try:
             self.proc = subprocess.Popen(
                 ["nvidia-smi", "-i", str(self.index), "--query-gpu=" + self.Q,
-                 "--format=csv,noheader,nounits", "-lms", "200"],
+                 "--format=csv,noheader,nounits", "-lms", "100"],
                 stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
             self.t = threading.Thread(target=self._read, daemon=True)
             self.t.start()
@@ -394,10 +394,29 @@ def run_reference(args, ws, rank):
     }))
 
 
+def run_stages(args):
+    """Each stage of one overlap evaluation, constraint projection and SHAKE
+    run once per round through the Model API (no graph, no gates), so that a
+    profiler captures exactly one launch of every kernel per round."""
+    import torch
+    lib, m, s = prepare_gpu(args.seed)
+    for _ in range(args.stages):
+        m.updateNeighborCells()
+        m.updateNeighbors()
+        m.updateOutersections()
+        m.updateForceEnergy()
+        m.projectForce()
+        m.updatePositions(1e-3)          # off the constraint manifold, as after a Verlet move
+        m.shakeProject(5, 1e-15)
+    torch.cuda.synchronize()
+    print(json.dumps({"stages": args.stages, "pairs": m.getPairCount(),
+                      "launches": m.getLaunchCount()}))
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
-    ap.add_argument("--steps", type=int, default=50)
+    ap.add_argument("--steps", type=int, default=1000)
     ap.add_argument("--warmup", type=int, default=5)
     ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
     ap.add_argument("--seed", type=int, default=2024)
@@ -405,12 +424,17 @@ def main():
     ap.add_argument("--no-e2e", action="store_true")
     ap.add_argument("--no-cpu", action="store_true")
     ap.add_argument("--no-roofline", action="store_true")
+    ap.add_argument("--stages", type=int, default=0,
+                    help="profiling mode: run every stage this many times, no timing")
     args = ap.parse_args()
     if args.warmup < 3 and args.impl == "gb300":
         args.warmup = 3
     ws, rank, local = dist_env()
     if args.impl == "reference":
         run_reference(args, ws, rank)
+        return
+    if args.stages > 0:
+        run_stages(args)
         return
     run_gpu(args, ws, rank, local)
 

@@ -130,7 +130,8 @@ __global__ void __launch_bounds__(kConsThreads)
 k_project(const double2* __restrict__ pos, const int* __restrict__ start, int P,
           const double* __restrict__ constraints, double2* __restrict__ force,
           double* __restrict__ scratch, int V, int smemN, int areaFromPositions, Ctrl* fire,
-          double2* __restrict__ vel, const int* gate) {
+          double2* __restrict__ vel, cudaGraphConditionalHandle rbCond, int useCond,
+          const int* gate) {
     if (gate_closed(gate)) return;
     extern __shared__ double cons_smem[];
     int p = blockIdx.x * blockDim.x + threadIdx.x;
@@ -145,7 +146,9 @@ k_project(const double2* __restrict__ pos, const int* __restrict__ start, int P,
             fire->proceed = proceed ? 1 : 0;
             // the energy-increase rollback path runs when the step is not a
             // SHAKE failure and the energy went up (model.cpp:450-453)
-            fire->rbGate = (!fire->shakeFailed && rb && fire->active) ? 1 : 0;
+            int go = (!fire->shakeFailed && rb && fire->active) ? 1 : 0;
+            fire->rbGate = go;
+            if (useCond) cudaGraphSetConditional(rbCond, (unsigned int)go);
         }
     }
     double sP = 0.0, sV = 0.0, sF = 0.0, mF = 0.0;
@@ -396,7 +399,7 @@ __global__ void k_shake(double2* __restrict__ pos, const int* __restrict__ start
                         const double* __restrict__ targetEdge,
                         const double* __restrict__ targetArea, int maxIter, double tol,
                         int* __restrict__ itersOut, double* __restrict__ scratch, int nmaxSmem,
-                        const int* gate) {
+                        Ctrl* fire, cudaGraphConditionalHandle retryCond, const int* gate) {
     if (gate_closed(gate)) return;
     extern __shared__ __align__(16) unsigned char shake_smem[];
     const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
@@ -543,11 +546,31 @@ __global__ void k_shake(double2* __restrict__ pos, const int* __restrict__ start
         }
     }
     if (lane == 0 && it > 0) atomicMax(itersOut, it);
+    if (fire) {
+        // first attempt of a FIRE step (model.cpp:431-436): the last block to
+        // finish reads the largest iteration count and decides the retry
+        __syncthreads();
+        if (threadIdx.x == 0) {
+            __threadfence();
+            unsigned int t = atomicAdd(&fire->shakeTicket, 1u);
+            if (t == gridDim.x - 1) {
+                __threadfence();
+                int it1 = atomicOr(itersOut, 0);
+                fire->shakeLast = it1;
+                int nr = (it1 >= fire->shakeIter) ? 1 : 0;
+                int go = (nr && fire->active) ? 1 : 0;
+                fire->needRetry = nr;
+                fire->retryGate = go;
+                cudaGraphSetConditional(retryCond, (unsigned int)go);
+            }
+        }
+    }
 }
 
 cudaError_t launch_shake(double2* pos, const int* start, int P, int nmax, const double* targetEdge,
                          const double* targetArea, int maxIter, double tol, int* maxItersOut,
-                         double* scratch, int V, const int* gate, cudaStream_t st) {
+                         double* scratch, int V, const int* gate, cudaStream_t st, Ctrl* fire,
+                         cudaGraphConditionalHandle retryCond) {
     (void)V;
     if (P <= 0) return cudaSuccess;
     // per-warp workspace in shared memory when it fits (polygons up to ~1000
@@ -562,7 +585,8 @@ cudaError_t launch_shake(double2* pos, const int* start, int P, int nmax, const 
     if (per * wpb > 200 * 1024) { nmaxSmem = 0; per = 0; wpb = 8; }
     size_t smem = per * wpb;
     k_shake<<<nblk(P, wpb), 32 * wpb, smem, st>>>(pos, start, P, targetEdge, targetArea, maxIter,
-                                                   tol, maxItersOut, scratch, nmaxSmem, gate);
+                                                   tol, maxItersOut, scratch, nmaxSmem, fire,
+                                                   retryCond, gate);
     return cudaGetLastError();
 }
 
@@ -606,7 +630,8 @@ __global__ void k_project_warp(const double2* __restrict__ pos, const int* __res
                                int P, const double* __restrict__ constraints,
                                double2* __restrict__ force, double* __restrict__ scratch,
                                int nmaxSmem, int areaFromPositions, Ctrl* fire,
-                               double2* __restrict__ vel, const int* gate) {
+                               double2* __restrict__ vel, cudaGraphConditionalHandle rbCond,
+                               int useCond, const int* gate) {
     if (gate_closed(gate)) return;
     extern __shared__ __align__(16) unsigned char proj_smem[];
     const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
@@ -623,7 +648,9 @@ __global__ void k_project_warp(const double2* __restrict__ pos, const int* __res
             fire->proceed = proceed ? 1 : 0;
             // the energy-increase rollback path runs when the step is not a
             // SHAKE failure and the energy went up (model.cpp:450-453)
-            fire->rbGate = (!fire->shakeFailed && rb && fire->active) ? 1 : 0;
+            int go = (!fire->shakeFailed && rb && fire->active) ? 1 : 0;
+            fire->rbGate = go;
+            if (useCond) cudaGraphSetConditional(rbCond, (unsigned int)go);
         }
     }
     double sP = 0.0, sV = 0.0, sF = 0.0, mF = 0.0;
@@ -798,13 +825,14 @@ cudaError_t constraints_init() {
 cudaError_t launch_project(const double2* pos, const int* start, int P, int nmax,
                            const double* constraints, double2* force, double* scratch, int V,
                            int areaFromPositions, Ctrl* fireCtrl, const int* gate, double2* vel,
-                           cudaStream_t st) {
+                           cudaStream_t st, cudaGraphConditionalHandle rbCond, int useCond) {
     if (P <= 0) return cudaSuccess;
     if (P >= 128 * sm_count()) {
         int sn = smem_vertices(nmax, kProjArrays);
         size_t smem = (size_t)sn * kProjArrays * kConsThreads * sizeof(double);
         k_project<<<nblk(P, kConsThreads), kConsThreads, smem, st>>>(
-            pos, start, P, constraints, force, scratch, V, sn, areaFromPositions, fireCtrl, vel, gate);
+            pos, start, P, constraints, force, scratch, V, sn, areaFromPositions, fireCtrl, vel,
+            rbCond, useCond, gate);
         return cudaGetLastError();
     }
     int nv = (nmax + 1) & ~1;          // even, so each workspace stays 16-byte aligned
@@ -817,7 +845,7 @@ cudaError_t launch_project(const double2* pos, const int* start, int P, int nmax
     if (per * wpb > 200 * 1024) { nmaxSmem = 0; per = 0; wpb = 8; }
     k_project_warp<<<nblk(P, wpb), 32 * wpb, per * wpb, st>>>(pos, start, P, constraints, force,
                                                               scratch, nmaxSmem, areaFromPositions,
-                                                              fireCtrl, vel, gate);
+                                                              fireCtrl, vel, rbCond, useCond, gate);
     return cudaGetLastError();
 }
 
@@ -903,62 +931,72 @@ cudaError_t launch_xpbd_iteration(double2* pos, const int* start, int P,
 // All FIRE scalars stay in the device control block; the step is a fixed
 // launch sequence, so it is captured once as a CUDA graph.
 
-// step start: save positions, record E_pre, Verlet half-kick + drift
+// zero the contact-search counters (everything in Ctrl before `energy`)
+__device__ __forceinline__ void zero_contact_counters(Ctrl* c) {
+    int* w = reinterpret_cast<int*>(c);
+    constexpr int n = (int)(offsetof(Ctrl, energy) / sizeof(int));
+#pragma unroll
+    for (int i = 0; i < n; ++i) w[i] = 0;
+}
+
+// Step start (model.cpp:405-430): the per-step resets of the control block,
+// snapshots of x, v and F (for the rollbacks and for buffer-overflow
+// recovery), the Verlet half-kick and drift, the pre-SHAKE copy of the new
+// positions (`verlet`, may be null) and F = 0 for the coming force pass.
 __global__ void k_fire_begin(double2* __restrict__ pos, double2* __restrict__ vel,
-                             const double2* __restrict__ force, double2* __restrict__ save,
-                             int V, Ctrl* __restrict__ c, const int* gate) {
+                             double2* __restrict__ force, double2* __restrict__ save,
+                             double2* __restrict__ velSnap, double2* __restrict__ forceSnap,
+                             double2* __restrict__ verlet, int V, int resetContacts,
+                             Ctrl* __restrict__ c, const int* gate) {
     if (gate_closed(gate)) return;
     int i = blockIdx.x * blockDim.x + threadIdx.x;
-    double dt = c->dt;
+    const double dt = c->dt;
+    if (i == 0) {
+        c->ePre = c->energy;
+        c->energy = 0.0;
+        c->snapDt = dt; c->snapAlpha = c->alpha; c->snapNPos = c->nPos;
+        c->maxF = 0.0;
+        c->P = 0.0; c->vv = 0.0; c->ff = 0.0;
+        c->shakeIters1 = 0; c->shakeIters2 = 0;
+        c->needRetry = 0; c->retryGate = 0;
+        c->shakeFailed = 0;
+        c->rollback = 0; c->rbGate = 0; c->proceed = 0;
+        c->shakeTicket = 0; c->bendTicket = 0;
+        if (resetContacts) zero_contact_counters(c);
+    }
     if (i < V) {
         double2 x = pos[i], v = vel[i], f = force[i];
         save[i] = x;
+        velSnap[i] = v;
+        forceSnap[i] = f;
         v.x += 0.5 * dt * f.x; v.y += 0.5 * dt * f.y;
         double px = x.x + dt * v.x, py = x.y + dt * v.y;
         vel[i] = v;
-        pos[i] = make_double2(px - floor(px), py - floor(py));
+        double2 xn = make_double2(px - floor(px), py - floor(py));
+        pos[i] = xn;
+        if (verlet) verlet[i] = xn;
+        force[i] = make_double2(0.0, 0.0);
     }
 }
 
-// per-step resets of the control block (runs before k_fire_begin)
-__global__ void k_fire_reset(Ctrl* __restrict__ c, const int* gate) {
-    if (gate_closed(gate)) return;
-    c->ePre = c->energy;
-    c->energy = 0.0;
-    c->snapDt = c->dt; c->snapAlpha = c->alpha; c->snapNPos = c->nPos;
-    c->maxF = 0.0;
-    c->P = 0.0; c->vv = 0.0; c->ff = 0.0;
-    c->shakeIters1 = 0; c->shakeIters2 = 0;
-    c->needRetry = 0; c->retryGate = 0;
-    c->shakeFailed = 0;
-    c->rollback = 0; c->rbGate = 0; c->proceed = 0;
-}
-
-// which == 1: after the first SHAKE attempt; which == 2: after the retry
-__global__ void k_fire_shake_check(Ctrl* __restrict__ c, int which, const int* gate) {
-    if (gate_closed(gate)) return;
-    if (which == 1) {
-        c->shakeLast = c->shakeIters1;
-        c->needRetry = (c->shakeIters1 >= c->shakeIter) ? 1 : 0;
-        c->retryGate = c->needRetry && c->active;
-    } else {
-        if (c->needRetry) {
-            c->shakeLast = c->shakeIters2;
-            c->shakeFailed = (c->shakeIters2 >= 10 * c->shakeIter) ? 1 : 0;
-        }
-    }
-}
-
-// SHAKE failure: restore the step's start positions and zero v; success:
-// rederive v from the SHAKE displacement (model.cpp:431-438)
+// After SHAKE (model.cpp:431-438): the outcome of the retry (when the first
+// attempt asked for one), then on failure restore the step's start positions
+// and zero v, on success rederive v from the SHAKE displacement.
 __global__ void k_fire_after_shake(double2* __restrict__ pos, double2* __restrict__ vel,
                                    const double2* __restrict__ save,
                                    const double2* __restrict__ verlet, int V,
-                                   const Ctrl* __restrict__ c, const int* gate) {
+                                   Ctrl* __restrict__ c, const int* gate) {
     if (gate_closed(gate)) return;
     int i = blockIdx.x * blockDim.x + threadIdx.x;
+    const bool retried = c->needRetry != 0;
+    const bool failed = retried && c->shakeIters2 >= 10 * c->shakeIter;
+    if (i == 0 && retried) {
+        c->shakeLast = c->shakeIters2;
+        c->shakeFailed = failed ? 1 : 0;
+        c->condLaunches += 1;          // the retry ran in a conditional body
+    }
     if (i >= V) return;
-    if (c->shakeFailed) {
+    if (failed) {
         pos[i] = save[i];
         vel[i] = make_double2(0.0, 0.0);
     } else {
@@ -970,14 +1008,20 @@ __global__ void k_fire_after_shake(double2* __restrict__ pos, double2* __restric
     }
 }
 
-// energy-increase rollback (model.cpp:453-465): restore positions, zero v,
-// zero the force and energy before they are recomputed
+// Energy-increase rollback (model.cpp:453-465), first kernel of the
+// rollback body: restore positions, zero v and F, zero the energy, max |F|
+// and (when the body searches contacts) the contact counters.
 __global__ void k_fire_rollback(double2* __restrict__ pos, double2* __restrict__ vel,
                                 double2* __restrict__ force, const double2* __restrict__ save,
-                                int V, Ctrl* __restrict__ c, const int* gate) {
-    if (gate_closed(gate)) return;
+                                int V, int resetContacts, Ctrl* __restrict__ c) {
     int i = blockIdx.x * blockDim.x + threadIdx.x;
-    if (i == 0) { c->energy = 0.0; c->maxF = 0.0; }
+    if (i == 0) {
+        c->rollback = 1;
+        c->energy = 0.0;
+        c->maxF = 0.0;
+        if (resetContacts) zero_contact_counters(c);
+        c->condLaunches += (unsigned long long)c->rbBodyKernels;
+    }
     if (i >= V) return;
     pos[i] = save[i];
     vel[i] = make_double2(0.0, 0.0);
@@ -994,9 +1038,11 @@ __global__ void k_zero_force(double2* __restrict__ force, int V, Ctrl* __restric
 }
 
 // velocity update for models without projection (soft-body / hybrid):
-// v += dt/2 F, accumulate F.v, |v|^2, |F|^2, max |F|
+// v += dt/2 F, accumulate F.v, |v|^2, |F|^2, max |F|; decides the rollback
+// and sets `rbCond` of the step graph when `useCond`
 __global__ void k_fire_velocity(double2* __restrict__ vel, const double2* __restrict__ force,
-                                int V, Ctrl* __restrict__ c, const int* gate) {
+                                int V, Ctrl* __restrict__ c, cudaGraphConditionalHandle rbCond,
+                                int useCond, const int* gate) {
     if (gate_closed(gate)) return;
     int i = blockIdx.x * blockDim.x + threadIdx.x;
     double E = c->energy, E0 = c->ePre;
@@ -1004,7 +1050,9 @@ __global__ void k_fire_velocity(double2* __restrict__ vel, const double2* __rest
     bool proceed = !c->shakeFailed && !rb && c->rollback == 0;
     if (i == 0 && c->rollback == 0) {
         c->proceed = proceed ? 1 : 0;
-        c->rbGate = (!c->shakeFailed && rb && c->active) ? 1 : 0;
+        int go = (!c->shakeFailed && rb && c->active) ? 1 : 0;
+        c->rbGate = go;
+        if (useCond) cudaGraphSetConditional(rbCond, (unsigned int)go);
     }
     double sP = 0.0, sV = 0.0, sF = 0.0, mF = 0.0;
     if (i < V) {
@@ -1041,38 +1089,9 @@ __global__ void k_fire_maxf(const double2* __restrict__ force, int V, Ctrl* __re
     if ((threadIdx.x & 31) == 0) atomic_max_nonneg(&c->maxF, mF);
 }
 
-// bend v toward F when the step proceeds (model.cpp:471-484)
-__global__ void k_fire_bend(double2* __restrict__ vel, const double2* __restrict__ force,
-                            int V, const Ctrl* __restrict__ c, const int* gate) {
-    if (gate_closed(gate)) return;
-    if (!c->proceed) return;
-    __shared__ double s_coef[2];
-    if (threadIdx.x == 0) {
-        // the mixing coefficients once per block (two square roots, a division)
-        double fn = sqrt(c->ff), vn = sqrt(c->vv), a = c->alpha;
-        s_coef[0] = 1.0 - a;
-        s_coef[1] = fn > 0.0 ? a * vn / fn : -1.0;
-    }
-    __syncthreads();
-    int i = blockIdx.x * blockDim.x + threadIdx.x;
-    if (i >= V) return;
-    double P = c->P;
-    if (P > 0.0) {
-        double s = s_coef[1];
-        if (s >= 0.0) {
-            double a1 = s_coef[0];
-            double2 v = vel[i], f = force[i];
-            vel[i] = make_double2(a1 * v.x + s * f.x, a1 * v.y + s * f.y);
-        }
-    } else {
-        vel[i] = make_double2(0.0, 0.0);
-    }
-}
-
 // scalar bookkeeping of the step (model.cpp:444-485) and the stop test of
-// Model::minimizeFIRE (model.cpp:500)
-__global__ void k_fire_scalars(Ctrl* __restrict__ c, const int* gate) {
-    if (gate_closed(gate)) return;
+// Model::minimizeFIRE (model.cpp:500); one thread
+__device__ void fire_scalars(Ctrl* __restrict__ c) {
     if (c->flags & (kFlagPairOverflow | kFlagRecordOverflow | kFlagSlowOverflow |
                     kFlagFixOverflow | kFlagCapacity)) {
         // a contact buffer overflowed: stop here; the host grows the buffers
@@ -1107,25 +1126,52 @@ __global__ void k_fire_scalars(Ctrl* __restrict__ c, const int* gate) {
     if (c->stepLimit > 0 && c->stepsDone >= c->stepLimit) c->active = 0;
 }
 
-// mark the rollback as taken (the flag the rollback kernels gate on is set
-// by k_project / k_fire_velocity; the scalars kernel needs `rollback`)
-__global__ void k_fire_mark_rollback(Ctrl* __restrict__ c, const int* gate) {
+// Step end: bend v toward F when the step proceeds (model.cpp:471-484); the
+// last block to finish then does the scalar bookkeeping (every block has
+// read alpha, P, |v|, |F| before it takes its ticket).
+__global__ void k_fire_bend(double2* __restrict__ vel, const double2* __restrict__ force,
+                            int V, Ctrl* __restrict__ c, const int* gate) {
     if (gate_closed(gate)) return;
-    c->rollback = 1;
+    __shared__ double s_coef[3];
+    if (threadIdx.x == 0) {
+        // the mixing coefficients once per block (two square roots, a division)
+        double fn = sqrt(c->ff), vn = sqrt(c->vv), a = c->alpha;
+        s_coef[0] = 1.0 - a;
+        s_coef[1] = fn > 0.0 ? a * vn / fn : -1.0;
+        s_coef[2] = c->proceed ? c->P : 0.0;
+    }
+    __syncthreads();
+    int i = blockIdx.x * blockDim.x + threadIdx.x;
+    const bool go = c->proceed != 0;
+    if (go && i < V) {
+        if (s_coef[2] > 0.0) {
+            double sc = s_coef[1];
+            if (sc >= 0.0) {
+                double a1 = s_coef[0];
+                double2 v = vel[i], f = force[i];
+                vel[i] = make_double2(a1 * v.x + sc * f.x, a1 * v.y + sc * f.y);
+            }
+        } else {
+            vel[i] = make_double2(0.0, 0.0);
+        }
+    }
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        __threadfence();
+        unsigned int t = atomicAdd(&c->bendTicket, 1u);
+        if (t == gridDim.x - 1) {
+            __threadfence();
+            fire_scalars(c);
+        }
+    }
 }
 
 // --------------------------------------------------------------- launchers ----
-cudaError_t launch_fire_reset(Ctrl* c, const int* gate, cudaStream_t st) {
-    k_fire_reset<<<1, 1, 0, st>>>(c, gate);
-    return cudaGetLastError();
-}
-cudaError_t launch_fire_begin(double2* pos, double2* vel, const double2* force, double2* save,
-                              int V, Ctrl* c, const int* gate, cudaStream_t st) {
-    k_fire_begin<<<nblk(V, 256), 256, 0, st>>>(pos, vel, force, save, V, c, gate);
-    return cudaGetLastError();
-}
-cudaError_t launch_fire_shake_check(Ctrl* c, int which, const int* gate, cudaStream_t st) {
-    k_fire_shake_check<<<1, 1, 0, st>>>(c, which, gate);
+cudaError_t launch_fire_begin(double2* pos, double2* vel, double2* force, double2* save,
+                              double2* velSnap, double2* forceSnap, double2* verlet, int V,
+                              int resetContacts, Ctrl* c, const int* gate, cudaStream_t st) {
+    k_fire_begin<<<nblk(V, 256), 256, 0, st>>>(pos, vel, force, save, velSnap, forceSnap, verlet,
+                                               V, resetContacts, c, gate);
     return cudaGetLastError();
 }
 cudaError_t launch_fire_after_shake(double2* pos, double2* vel, const double2* save,
@@ -1135,9 +1181,8 @@ cudaError_t launch_fire_after_shake(double2* pos, double2* vel, const double2* s
     return cudaGetLastError();
 }
 cudaError_t launch_fire_rollback(double2* pos, double2* vel, double2* force, const double2* save,
-                                 int V, Ctrl* c, const int* gate, cudaStream_t st) {
-    k_fire_mark_rollback<<<1, 1, 0, st>>>(c, gate);
-    k_fire_rollback<<<nblk(V, 256), 256, 0, st>>>(pos, vel, force, save, V, c, gate);
+                                 int V, int resetContacts, Ctrl* c, cudaStream_t st) {
+    k_fire_rollback<<<nblk(V, 256), 256, 0, st>>>(pos, vel, force, save, V, resetContacts, c);
     return cudaGetLastError();
 }
 cudaError_t launch_zero_force(double2* force, int V, Ctrl* c, const int* gate, cudaStream_t st) {
@@ -1145,8 +1190,9 @@ cudaError_t launch_zero_force(double2* force, int V, Ctrl* c, const int* gate, c
     return cudaGetLastError();
 }
 cudaError_t launch_fire_velocity(double2* vel, const double2* force, int V, Ctrl* c,
+                                 cudaGraphConditionalHandle rbCond, int useCond,
                                  const int* gate, cudaStream_t st) {
-    k_fire_velocity<<<nblk(V, 256), 256, 0, st>>>(vel, force, V, c, gate);
+    k_fire_velocity<<<nblk(V, 256), 256, 0, st>>>(vel, force, V, c, rbCond, useCond, gate);
     return cudaGetLastError();
 }
 cudaError_t launch_fire_maxf(const double2* force, int V, Ctrl* c, const int* gate,
@@ -1157,7 +1203,6 @@ cudaError_t launch_fire_maxf(const double2* force, int V, Ctrl* c, const int* ga
 cudaError_t launch_fire_finish(double2* vel, const double2* force, int V, Ctrl* c,
                                const int* gate, cudaStream_t st) {
     k_fire_bend<<<nblk(V, 256), 256, 0, st>>>(vel, force, V, c, gate);
-    k_fire_scalars<<<1, 1, 0, st>>>(c, gate);
     return cudaGetLastError();
 }
 
@@ -1203,7 +1248,7 @@ cudaError_t launch_shake_noalloc(double2* pos, const int* start, int P, const do
     if (P <= 0) return cudaSuccess;
     constexpr int wpb = 8;
     k_shake<<<nblk(P, wpb), 32 * wpb, 0, st>>>(pos, start, P, targetEdge, targetArea, maxIter, tol,
-                                               maxItersOut, scratch, 0, nullptr);
+                                               maxItersOut, scratch, 0, nullptr, 0, nullptr);
     return cudaGetLastError();
 }
 

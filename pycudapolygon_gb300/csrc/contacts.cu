@@ -52,9 +52,10 @@ __global__ void k_reset_contacts(Ctrl* __restrict__ ctrl, const int* gate) {
 
 __global__ void __launch_bounds__(256)
 k_prepass(const double2* __restrict__ pos, const int* __restrict__ start,
-          const int* __restrict__ cellLocation, int P, int B, double2* __restrict__ edgeVec,
-          float4* __restrict__ vtx, float4* __restrict__ polyInfo, int* __restrict__ polyFlags,
-          int* __restrict__ unsafeList, Ctrl* __restrict__ ctrl, const int* gate) {
+          const int* __restrict__ cellLocation, int* __restrict__ cellOut, int P, int B,
+          double2* __restrict__ edgeVec, float4* __restrict__ vtx, float4* __restrict__ polyInfo,
+          int* __restrict__ polyFlags, int* __restrict__ unsafeList, Ctrl* __restrict__ ctrl,
+          const int* gate) {
     if (gate_closed(gate)) return;
     int p = blockIdx.x * (blockDim.x / 32) + threadIdx.x / 32;
     int lane = threadIdx.x & 31;
@@ -77,8 +78,16 @@ k_prepass(const double2* __restrict__ pos, const int* __restrict__ start,
         edgeVec[k] = make_double2(wrap(pn.x - pk.x), wrap(pn.y - pk.y));
         float fx = (float)pk.x, fy = (float)pk.y;
         // cell (x, y) of the edge midpoint as updateNeighborsKernel splits it
-        // with the current box size (kernels.cuh:727-729)
-        int cell = cellLocation[k];
+        // with the current box size (kernels.cuh:727-729); with cellOut the
+        // cells are computed here from the same positions
+        // (updateNeighborCellsKernel) and stored for the getters
+        int cell;
+        if (cellOut) {
+            cell = midpoint_cell_of(pk, pn, B);
+            cellOut[k] = cell;
+        } else {
+            cell = cellLocation[k];
+        }
         vtx[k] = make_float4(fx, fy, __int_as_float(cell % B), __int_as_float(cell / B));
         float lx = wrapf(fx - f0x), ly = wrapf(fy - f0y);
         float nxl = wrapf((float)pn.x - fx), nyl = wrapf((float)pn.y - fy);
@@ -741,84 +750,128 @@ __device__ __forceinline__ void add_f(double2* F, int v, double fx, double fy) {
 // the interior chain of updateForceEnergyInteriorKernel (kernels.cuh:
 // 1354-1424): whole edges of si strictly between the entry edge i and the
 // exit edge l, each taken relative to the record's own entry point.
-__global__ void __launch_bounds__(256)
+//
+// GB300's FP64 pipe charges a warp instruction whatever its active lanes, so
+// the work is cut into lane-sized pieces: a warp takes kForceRecs records;
+// the exterior part of each record is split over a lane pair (one gDf per
+// lane), then the interior-chain edges of all of the warp's records are
+// dealt out one per lane.  Small blocks spread the few thousand warps over
+// every SM.
+constexpr int kForceRecs = 16;
+constexpr int kForceWarps = 2;
+
+__global__ void __launch_bounds__(32 * kForceWarps)
 k_overlap_force(const double2* __restrict__ pos, const int* __restrict__ start,
                 const int* __restrict__ next, int V, ContactWS ws, Ctrl* __restrict__ ctrl,
                 double2* __restrict__ force, const int* gate) {
     if (gate_closed(gate)) return;
-    int I = min(ctrl->numRecords, ws.capRecords);
+    const int lane = threadIdx.x & 31;
+    const int half = lane & 1;
+    const int I = min(ctrl->numRecords, ws.capRecords);
+    const int warpsTotal = gridDim.x * kForceWarps;
     double eLocal = 0.0;
-    for (int r = blockIdx.x * blockDim.x + threadIdx.x; r < I; r += gridDim.x * blockDim.x) {
-        unsigned long long inter = ws.recKey[r], outer = ws.recOuter[r];
-        if (inter == outer) continue;
-        int s1 = (int)((inter >> 32) & 0xFFFF), s2 = (int)(inter >> 48);
-        int iLoc = (int)((inter >> 16) & 0xFFFF), jLoc = (int)(inter & 0xFFFF);
-        int kLoc = (int)((outer >> 16) & 0xFFFF), lLoc = (int)(outer & 0xFFFF);
-        int start1 = start[s1], start2 = start[s2];
-        int i = start1 + iLoc, j = start2 + jLoc, k = start2 + kLoc, l = start1 + lLoc;
-        if (i >= V || j >= V || k >= V || l >= V) {
-            atomicOr(&ctrl->flags, kFlagNonFinite);
-            continue;
+    for (int base = (blockIdx.x * kForceWarps + (threadIdx.x >> 5)) * kForceRecs; base < I;
+         base += warpsTotal * kForceRecs) {
+        const int r = base + (lane >> 1);
+        bool valid = r < I;
+        unsigned long long inter = 0, outer = 0;
+        if (valid) { inter = ws.recKey[r]; outer = ws.recOuter[r]; }
+        valid = valid && inter != outer;
+        int start1 = 0, n1 = 0, iLoc = 0, lDist = 0;
+        double2 sp = make_double2(0.0, 0.0);
+        if (valid) {
+            int s1 = (int)((inter >> 32) & 0xFFFF), s2 = (int)(inter >> 48);
+            iLoc = (int)((inter >> 16) & 0xFFFF);
+            int jLoc = (int)(inter & 0xFFFF);
+            int kLoc = (int)((outer >> 16) & 0xFFFF), lLoc = (int)(outer & 0xFFFF);
+            start1 = start[s1];
+            int start2 = start[s2];
+            n1 = start[s1 + 1] - start1;
+            int i = start1 + iLoc, j = start2 + jLoc, k = start2 + kLoc, l = start1 + lLoc;
+            if (i >= V || j >= V || k >= V || l >= V) {
+                if (half == 0) atomicOr(&ctrl->flags, kFlagNonFinite);
+                valid = false;
+                n1 = 0;
+            } else {
+                int zi = next[i], zk = next[k];
+                double2 pi = pos[i], pk = pos[k], pzi = pos[zi], pzk = pos[zk];
+                double2 r1 = make_double2(wrap(pzi.x - pi.x), wrap(pzi.y - pi.y));
+                double2 r2 = make_double2(wrap(pzk.x - pk.x), wrap(pzk.y - pk.y));
+                double t1 = (double)ws.recTU[r].y;
+                double t2 = (double)ws.recUT[r].y;
+                double2 fij = make_double2(wrap(pi.x + t1 * r1.x), wrap(pi.y + t1 * r1.y));
+                double2 fkl = make_double2(wrap(pk.x + t2 * r2.x), wrap(pk.y + t2 * r2.y));
+                sp = fij;
+                // Both lanes of the pair run one h/g12 and one gDf on operands
+                // chosen by parity (no divergent branches):
+                //   i == l : h(fij, fkl); even: gDf(i, zi, j, zj) . g1,
+                //            odd: gDf(k, zk, i, zi) . g2; energy once
+                //   i != l : even: h(fij, zi), gDf(i, zi, j, zj) . g1, zi += g2;
+                //            odd: h(l, fkl), gDf(k, zk, l, zl) . g2, l += g1
+                const bool same = (i == l);
+                int v0, v1, v2, v3;
+                if (half == 0) { v0 = i; v1 = zi; v2 = j; v3 = next[j]; }
+                else if (same) { v0 = k; v1 = zk; v2 = i; v3 = zi; }
+                else { v0 = k; v1 = zk; v2 = l; v3 = next[l]; }
+                double2 q0 = half ? pk : pi, q1 = half ? pzk : pzi;
+                double2 q2 = pos[v2], q3 = pos[v3];
+                double2 hA = (!same && half) ? q2 : fij;
+                double2 hB = (same || half) ? fkl : pzi;
+                double2 gA, gB;
+                double eh = h_g12(hA, hB, sp, gA, gB);
+                if (!same || half == 0) eLocal += eh;
+                double2 g = half ? gB : gA;
+                double2 x1 = (!same && !half) ? gB : make_double2(0.0, 0.0);
+                double2 x2 = (!same && half) ? gA : make_double2(0.0, 0.0);
+                double2 o[4];
+                gDf(q0, q1, q2, q3, g, o);
+                add_f(force, v0, -o[0].x, -o[0].y);
+                add_f(force, v1, -(o[1].x + x1.x), -(o[1].y + x1.y));
+                add_f(force, v2, -(o[2].x + x2.x), -(o[2].y + x2.y));
+                add_f(force, v3, -o[3].x, -o[3].y);
+                if (n1 > 0) lDist = ((lLoc - iLoc) % n1 + n1) % n1;
+            }
         }
-        int zi = next[i], zj = next[j], zk = next[k], zl = next[l];
-        double2 pi = pos[i], pj = pos[j], pk = pos[k], pl = pos[l];
-        double2 pzi = pos[zi], pzj = pos[zj], pzk = pos[zk], pzl = pos[zl];
-        double2 r1 = make_double2(wrap(pzi.x - pi.x), wrap(pzi.y - pi.y));
-        double2 r2 = make_double2(wrap(pzk.x - pk.x), wrap(pzk.y - pk.y));
-        double t1 = (double)ws.recTU[r].y;
-        double t2 = (double)ws.recUT[r].y;
-        double2 fij = make_double2(wrap(pi.x + t1 * r1.x), wrap(pi.y + t1 * r1.y));
-        double2 fkl = make_double2(wrap(pk.x + t2 * r2.x), wrap(pk.y + t2 * r2.y));
-        double2 sp = fij;
-        double e = 0.0;
-        double2 o[4];
-        if (i == l) {
-            double2 g1, g2;
-            e += h_g12(fij, fkl, sp, g1, g2);
-            gDf(pi, pzi, pj, pzj, g1, o);
-            add_f(force, i, -o[0].x, -o[0].y);
-            add_f(force, zi, -o[1].x, -o[1].y);
-            add_f(force, j, -o[2].x, -o[2].y);
-            add_f(force, zj, -o[3].x, -o[3].y);
-            gDf(pk, pzk, pi, pzi, g2, o);
-            add_f(force, k, -o[0].x, -o[0].y);
-            add_f(force, zk, -o[1].x, -o[1].y);
-            add_f(force, i, -o[2].x, -o[2].y);
-            add_f(force, zi, -o[3].x, -o[3].y);
-        } else {
-            double2 g1a, g2a, g1b, g2b;
-            e += h_g12(fij, pzi, sp, g1a, g2a);
-            e += h_g12(pl, fkl, sp, g1b, g2b);
-            gDf(pi, pzi, pj, pzj, g1a, o);
-            add_f(force, i, -o[0].x, -o[0].y);
-            add_f(force, j, -o[2].x, -o[2].y);
-            add_f(force, zi, -(o[1].x + g2a.x), -(o[1].y + g2a.y));
-            add_f(force, zj, -o[3].x, -o[3].y);
-            gDf(pk, pzk, pl, pzl, g2b, o);
-            add_f(force, l, -(g1b.x + o[2].x), -(g1b.y + o[2].y));
-            add_f(force, k, -o[0].x, -o[0].y);
-            add_f(force, zl, -o[3].x, -o[3].y);
-            add_f(force, zk, -o[1].x, -o[1].y);
+        // interior chains: the even lane of each pair owns its record's chain
+        int cnt = (valid && half == 0 && lDist > 1) ? lDist - 1 : 0;
+        int incl = cnt;
+#pragma unroll
+        for (int d = 1; d < 32; d <<= 1) {
+            int t = __shfl_up_sync(PCP_FULL, incl, d);
+            if (lane >= d) incl += t;
         }
-        // interior chain
-        int n1 = start[s1 + 1] - start1;
-        if (n1 > 0) {
-            int lDist = ((lLoc - iLoc) % n1 + n1) % n1;
-            for (int step = 1; step < lDist; ++step) {
-                int mLoc = iLoc + step;
-                if (mLoc >= n1) mLoc -= n1;
-                int mv = start1 + mLoc;
+        const int total = __shfl_sync(PCP_FULL, incl, 31);
+        for (int b = 0; b < total; b += 32) {
+            const int item = b + lane;
+            // owner = first lane whose inclusive count exceeds item
+            int own = 0;
+#pragma unroll
+            for (int w = 16; w > 0; w >>= 1) {
+                int v = __shfl_sync(PCP_FULL, incl, own + w - 1);
+                if (v <= item) own += w;
+            }
+            int oIncl = __shfl_sync(PCP_FULL, incl, own);
+            int oCnt = __shfl_sync(PCP_FULL, cnt, own);
+            int oStart = __shfl_sync(PCP_FULL, start1, own);
+            int oN = __shfl_sync(PCP_FULL, n1, own);
+            int oI = __shfl_sync(PCP_FULL, iLoc, own);
+            double2 osp = make_double2(__shfl_sync(PCP_FULL, sp.x, own),
+                                       __shfl_sync(PCP_FULL, sp.y, own));
+            if (item < total) {
+                int step = item - (oIncl - oCnt) + 1;
+                int mLoc = oI + step;
+                if (mLoc >= oN) mLoc -= oN;
+                int mv = oStart + mLoc;
                 int nv = next[mv];
                 double2 g1, g2;
-                e += h_g12(pos[mv], pos[nv], sp, g1, g2);
+                eLocal += h_g12(pos[mv], pos[nv], osp, g1, g2);
                 add_f(force, mv, -g1.x, -g1.y);
                 add_f(force, nv, -g2.x, -g2.y);
             }
         }
-        eLocal += e;
     }
     eLocal = warp_sum(eLocal);
-    if ((threadIdx.x & 31) == 0 && eLocal != 0.0) atomicAdd(&ctrl->energy, eLocal / 2.0);
+    if (lane == 0 && eLocal != 0.0) atomicAdd(&ctrl->energy, eLocal / 2.0);
 }
 
 // ------------------------------------------------------------ launchers ----
@@ -841,15 +894,18 @@ cudaError_t contacts_init() {
 
 cudaError_t launch_contacts(const double2* pos, const int* start, const int* shapeId,
                             const int* cellLocation, int P, int V, int B, ContactWS& ws,
-                            Ctrl* ctrl, const int* gate, cudaStream_t st, int stages) {
-    // stages: bit 0 = reset + prepass + broad phase, bit 1 = narrow phase
+                            Ctrl* ctrl, const int* gate, cudaStream_t st, int stages,
+                            int* cellOut) {
+    // stages: bit 0 = reset + prepass + broad phase, bit 1 = narrow phase,
+    // bit 2 = the counters were reset by the caller's kernel (no reset)
     (void)shapeId; (void)V;
     if (B < 1) B = 1;
     if (stages & 1) {
-    k_reset_contacts<<<1, 64, 0, st>>>(ctrl, gate);
+    if (!(stages & 4)) k_reset_contacts<<<1, 64, 0, st>>>(ctrl, gate);
     if (P <= 0) return cudaGetLastError();
-    k_prepass<<<nblocks(P, 8), 256, 0, st>>>(pos, start, cellLocation, P, B, ws.edgeVec, ws.vtx,
-                                             ws.polyInfo, ws.polyFlags, ws.unsafeList, ctrl, gate);
+    k_prepass<<<nblocks(P, 8), 256, 0, st>>>(pos, start, cellLocation, cellOut, P, B, ws.edgeVec,
+                                             ws.vtx, ws.polyInfo, ws.polyFlags, ws.unsafeList,
+                                             ctrl, gate);
     k_grid_count<<<nblocks(P, 256), 256, 0, st>>>(ws.polyInfo, ws.polyFlags, P, ws.gridCount,
                                                   ctrl, gate);
     k_grid_scan<<<1, 1024, 0, st>>>(ws.gridCount, ws.gridStart, ws.gridFill, ctrl, gate);
@@ -877,8 +933,9 @@ cudaError_t launch_contacts_finish(const int* start, ContactWS& ws, Ctrl* ctrl,
 cudaError_t launch_overlap_force(const double2* pos, const int* start, const int* next,
                                  int V, ContactWS& ws, Ctrl* ctrl, double2* force,
                                  const int* gate, cudaStream_t st) {
-    int grid = sm_count() * 8;
-    k_overlap_force<<<grid, 256, 0, st>>>(pos, start, next, V, ws, ctrl, force, gate);
+    // one pass over up to 4 * SMs * kForceWarps * kForceRecs records
+    int grid = sm_count() * 4;
+    k_overlap_force<<<grid, 32 * kForceWarps, 0, st>>>(pos, start, next, V, ws, ctrl, force, gate);
     return cudaGetLastError();
 }
 

@@ -25,10 +25,6 @@
 
 using namespace pcp;
 
-namespace pcp {
-cudaError_t launch_fire_reset(Ctrl* c, const int* gate, cudaStream_t st);
-}
-
 namespace {
 
 thread_local std::string g_err;
@@ -117,11 +113,18 @@ struct pcp_model {
     unsigned long long fireGen = 0;
     int fireShakeIter = -1, fireModel = -1, fireB = -1;
     int fireKernelNodes = 0;   // kernel launches one FIRE step graph makes
+    int rbBodyKernels = 0;     // kernels of its rollback body (counted on the device)
+    cudaStream_t sideStream = nullptr, bodyStream = nullptr;   // capture helpers
+    cudaEvent_t evFork = nullptr, evJoin = nullptr;
 
     ~pcp_model() { release(); }
 
     void release() {
         if (fireExec) { cudaGraphExecDestroy(fireExec); fireExec = nullptr; }
+        if (sideStream) { cudaStreamDestroy(sideStream); sideStream = nullptr; }
+        if (bodyStream) { cudaStreamDestroy(bodyStream); bodyStream = nullptr; }
+        if (evFork) { cudaEventDestroy(evFork); evFork = nullptr; }
+        if (evJoin) { cudaEventDestroy(evJoin); evJoin = nullptr; }
         dfree(&pos); dfree(&force); dfree(&vel); dfree(&posTMP); dfree(&posTMP2); dfree(&posTent);
         dfree(&velSnap); dfree(&forceSnap);
         dfree(&edgeLengths); dfree(&constraints); dfree(&scratch);
@@ -416,9 +419,11 @@ int upload(pcp_model* m, void* dst, const void* src, size_t bytes) {
 }
 
 // ---- the force evaluation (Model::updateForceEnergy, model.cpp:363-395) ----
-int force_energy(pcp_model* m, const int* gate) {
-    CK(launch_zero_force(m->force, m->V, m->ctrl, gate, m->stream));
-    m->launches++;
+int force_energy(pcp_model* m, const int* gate, bool zeroed = false) {
+    if (!zeroed) {
+        CK(launch_zero_force(m->force, m->V, m->ctrl, gate, m->stream));
+        m->launches++;
+    }
     int t = m->modelType;
     bool overlap = (t == PCP_MODEL_NORMAL || t == PCP_MODEL_HYBRID);
     bool edge = (t == PCP_MODEL_SOFT_BODY || t == PCP_MODEL_EDGE_ONLY || t == PCP_MODEL_HYBRID);
@@ -459,33 +464,88 @@ int ensure_geometry(pcp_model* m) {
 }
 
 // ---- FIRE step graph ------------------------------------------------------
-int record_fire_step(pcp_model* m) {
+// Adds an IF node with condition `h` after the work captured so far on `st`
+// and starts capturing its body on `body`.
+int begin_if(cudaStream_t st, cudaGraphConditionalHandle h, cudaStream_t body) {
+    cudaStreamCaptureStatus cs;
+    cudaGraph_t g = nullptr;
+    const cudaGraphNode_t* deps = nullptr;
+    const cudaGraphEdgeData* edges = nullptr;
+    size_t nd = 0;
+    CK(cudaStreamGetCaptureInfo(st, &cs, nullptr, &g, &deps, &edges, &nd));
+    if (cs != cudaStreamCaptureStatusActive) return fail(PCP_ERR_CUDA, "stream is not capturing");
+    cudaGraphNodeParams p = {cudaGraphNodeTypeConditional};
+    p.conditional.handle = h;
+    p.conditional.type = cudaGraphCondTypeIf;
+    p.conditional.size = 1;
+    cudaGraphNode_t node;
+    CK(cudaGraphAddNode(&node, g, deps, edges, nd, &p));
+    CK(cudaStreamUpdateCaptureDependencies(st, &node, nullptr, 1,
+                                           cudaStreamSetCaptureDependencies));
+    CK(cudaStreamBeginCaptureToGraph(body, p.conditional.phGraph_out[0], nullptr, nullptr, 0,
+                                     cudaStreamCaptureModeThreadLocal));
+    return PCP_OK;
+}
+
+int count_kernel_nodes(cudaGraph_t g) {
+    size_t nn = 0;
+    if (cudaGraphGetNodes(g, nullptr, &nn) != cudaSuccess) return 0;
+    std::vector<cudaGraphNode_t> nodes(nn);
+    if (nn) cudaGraphGetNodes(g, nodes.data(), &nn);
+    int k = 0;
+    for (size_t i = 0; i < nn; ++i) {
+        cudaGraphNodeType t;
+        if (cudaGraphNodeGetType(nodes[i], &t) == cudaSuccess && t == cudaGraphNodeTypeKernel) ++k;
+    }
+    return k;
+}
+
+// One FIRE step (Model::minimizeFIREStep, model.cpp:405-486) recorded on the
+// capturing stream m->stream.  Graph layout (normal model with SHAKE):
+//
+//   begin --+-- SHAKE -- [IF retry: SHAKE x10] -- after_shake --+-- force --
+//           +-- contact search on the pre-SHAKE copy ------------+
+//   -- projection (decides the rollback) -- [IF rollback: restore, contact
+//   search, force, projection] -- bend + scalar bookkeeping
+//
+// The contact search reads the positions the reference searches (after the
+// Verlet move, before SHAKE) from their copy, so it runs beside SHAKE.  The
+// two IF bodies run only when a kernel of the step sets their condition.
+int record_fire_step(pcp_model* m, cudaGraphConditionalHandle retryCond,
+                     cudaGraphConditionalHandle rbCond) {
     const int* gA = &m->ctrl->active;
-    const int* gRetry = &m->ctrl->retryGate;
-    const int* gRb = &m->ctrl->rbGate;
     cudaStream_t st = m->stream;
     bool needsI = (m->modelType == PCP_MODEL_NORMAL || m->modelType == PCP_MODEL_HYBRID);
     bool rigid = (m->modelType == PCP_MODEL_NORMAL);
+    bool shake = rigid && m->fireShakeIter > 0;
     int V = m->V;
-    CK(launch_fire_reset(m->ctrl, gA, st));
-    CK(cudaMemcpyAsync(m->velSnap, m->vel, V * sizeof(double2), cudaMemcpyDeviceToDevice, st));
-    CK(cudaMemcpyAsync(m->forceSnap, m->force, V * sizeof(double2), cudaMemcpyDeviceToDevice, st));
-    CK(launch_fire_begin(m->pos, m->vel, m->force, m->posTMP2, V, m->ctrl, gA, st));
-    if (needsI) {
-        CK(launch_neighbor_cells(m->pos, m->start, m->shapeId, V, m->boxSize, m->cellLocation, gA, st));
+    const int noReset = 3 | kContactsNoReset;
+    CK(launch_fire_begin(m->pos, m->vel, m->force, m->posTMP2, m->velSnap, m->forceSnap,
+                         shake ? m->posTMP : nullptr, V, needsI ? 1 : 0, m->ctrl, gA, st));
+    if (shake) {
+        CK(cudaEventRecord(m->evFork, st));
+        CK(cudaStreamWaitEvent(m->sideStream, m->evFork, 0));
+        CK(launch_contacts(m->posTMP, m->start, m->shapeId, m->cellLocation, m->P, V,
+                           m->boxSize, m->ws, m->ctrl, gA, m->sideStream, noReset,
+                           m->cellLocation));
+        CK(launch_contacts_finish(m->start, m->ws, m->ctrl, gA, m->sideStream));
+        CK(cudaEventRecord(m->evJoin, m->sideStream));
+        CK(launch_shake(m->pos, m->start, m->P, m->nmax, m->targetEdge, m->targetAreas,
+                        m->fireShakeIter, 1e-15, &m->ctrl->shakeIters1, m->scratch, V, gA, st,
+                        m->ctrl, retryCond));
+        int rc = begin_if(st, retryCond, m->bodyStream);
+        if (rc) return rc;
+        CK(launch_shake(m->pos, m->start, m->P, m->nmax, m->targetEdge, m->targetAreas,
+                        m->fireShakeIter * 10, 1e-15, &m->ctrl->shakeIters2, m->scratch, V,
+                        nullptr, m->bodyStream));
+        cudaGraph_t body = nullptr;
+        CK(cudaStreamEndCapture(m->bodyStream, &body));
+        CK(launch_fire_after_shake(m->pos, m->vel, m->posTMP2, m->posTMP, V, m->ctrl, gA, st));
+        CK(cudaStreamWaitEvent(st, m->evJoin, 0));
+    } else if (needsI) {
         CK(launch_contacts(m->pos, m->start, m->shapeId, m->cellLocation, m->P, V, m->boxSize,
-                           m->ws, m->ctrl, gA, st));
-        if (rigid && m->fireShakeIter > 0) {
-            CK(cudaMemcpyAsync(m->posTMP, m->pos, V * sizeof(double2), cudaMemcpyDeviceToDevice, st));
-            CK(launch_shake(m->pos, m->start, m->P, m->nmax, m->targetEdge, m->targetAreas, m->fireShakeIter,
-                            1e-15, &m->ctrl->shakeIters1, m->scratch, V, gA, st));
-            CK(launch_fire_shake_check(m->ctrl, 1, gA, st));
-            CK(launch_shake(m->pos, m->start, m->P, m->nmax, m->targetEdge, m->targetAreas,
-                            m->fireShakeIter * 10, 1e-15, &m->ctrl->shakeIters2, m->scratch, V,
-                            gRetry, st));
-            CK(launch_fire_shake_check(m->ctrl, 2, gA, st));
-            CK(launch_fire_after_shake(m->pos, m->vel, m->posTMP2, m->posTMP, V, m->ctrl, gA, st));
-        }
+                           m->ws, m->ctrl, gA, st, noReset, m->cellLocation));
+        CK(launch_contacts_finish(m->start, m->ws, m->ctrl, gA, st));
     }
     // The normal model reads nothing of the geometry inside the step (the
     // projection takes the area gradient from the positions), so the
@@ -495,35 +555,42 @@ int record_fire_step(pcp_model* m) {
         rc = geometry(m, gA);
         if (rc) return rc;
     }
-    if (needsI) CK(launch_contacts_finish(m->start, m->ws, m->ctrl, gA, st));
-    rc = force_energy(m, gA);
+    rc = force_energy(m, gA, true);
     if (rc) return rc;
     if (rigid) {
         CK(launch_project(m->pos, m->start, m->P, m->nmax, m->constraints, m->force, m->scratch, V, 1,
-                          m->ctrl, gA, m->vel, st));
+                          m->ctrl, gA, m->vel, st, rbCond, 1));
     } else {
-        CK(launch_fire_velocity(m->vel, m->force, V, m->ctrl, gA, st));
+        CK(launch_fire_velocity(m->vel, m->force, V, m->ctrl, rbCond, 1, gA, st));
     }
-    // energy-increase rollback (model.cpp:450-470), gated on rbGate
-    CK(launch_fire_rollback(m->pos, m->vel, m->force, m->posTMP2, V, m->ctrl, gRb, st));
-    if (!rigid) {
-        rc = geometry(m, gRb);
-        if (rc) return rc;
-    }
-    if (needsI) {
-        CK(launch_neighbor_cells(m->pos, m->start, m->shapeId, V, m->boxSize, m->cellLocation, gRb, st));
-        CK(launch_contacts(m->pos, m->start, m->shapeId, m->cellLocation, m->P, V, m->boxSize,
-                           m->ws, m->ctrl, gRb, st));
-        CK(launch_contacts_finish(m->start, m->ws, m->ctrl, gRb, st));
-    }
-    rc = force_energy(m, gRb);
+    // energy-increase rollback (model.cpp:450-470) as the body of an IF node
+    rc = begin_if(st, rbCond, m->bodyStream);
     if (rc) return rc;
-    if (rigid) {
-        CK(launch_project(m->pos, m->start, m->P, m->nmax, m->constraints, m->force, m->scratch, V, 1,
-                          m->ctrl, gRb, m->vel, st));
-    } else {
-        CK(launch_fire_maxf(m->force, V, m->ctrl, gRb, st));
+    m->stream = m->bodyStream;
+    CK(launch_fire_rollback(m->pos, m->vel, m->force, m->posTMP2, V, needsI ? 1 : 0, m->ctrl,
+                            m->stream));
+    if (!rigid) rc = geometry(m, nullptr);
+    if (!rc && needsI) {
+        cudaError_t e = launch_contacts(m->pos, m->start, m->shapeId, m->cellLocation, m->P, V,
+                                        m->boxSize, m->ws, m->ctrl, nullptr, m->stream, noReset,
+                                        m->cellLocation);
+        if (e == cudaSuccess) e = launch_contacts_finish(m->start, m->ws, m->ctrl, nullptr, m->stream);
+        if (e != cudaSuccess) rc = fail(PCP_ERR_CUDA, "rollback capture: %s", cudaGetErrorString(e));
     }
+    if (!rc) rc = force_energy(m, nullptr, true);
+    if (!rc) {
+        cudaError_t e = rigid
+            ? launch_project(m->pos, m->start, m->P, m->nmax, m->constraints, m->force, m->scratch,
+                             V, 1, m->ctrl, nullptr, m->vel, m->stream)
+            : launch_fire_maxf(m->force, V, m->ctrl, nullptr, m->stream);
+        if (e != cudaSuccess) rc = fail(PCP_ERR_CUDA, "rollback capture: %s", cudaGetErrorString(e));
+    }
+    m->stream = st;
+    cudaGraph_t body = nullptr;
+    cudaError_t e = cudaStreamEndCapture(m->bodyStream, &body);
+    if (rc) return rc;
+    if (e != cudaSuccess) return fail(PCP_ERR_CUDA, "rollback capture: %s", cudaGetErrorString(e));
+    m->rbBodyKernels = count_kernel_nodes(body);
     CK(launch_fire_finish(m->vel, m->force, V, m->ctrl, gA, st));
     return PCP_OK;
 }
@@ -534,6 +601,10 @@ int build_fire_graph(pcp_model* m, int shakeIter) {
         return PCP_OK;
     if (m->fireExec) { cudaGraphExecDestroy(m->fireExec); m->fireExec = nullptr; }
     m->fireShakeIter = shakeIter;
+    if (!m->sideStream) CK(cudaStreamCreateWithFlags(&m->sideStream, cudaStreamNonBlocking));
+    if (!m->bodyStream) CK(cudaStreamCreateWithFlags(&m->bodyStream, cudaStreamNonBlocking));
+    if (!m->evFork) CK(cudaEventCreateWithFlags(&m->evFork, cudaEventDisableTiming));
+    if (!m->evJoin) CK(cudaEventCreateWithFlags(&m->evJoin, cudaEventDisableTiming));
     cudaStream_t cap = nullptr;
     CK(cudaStreamCreateWithFlags(&cap, cudaStreamNonBlocking));
     cudaStream_t saved = m->stream;
@@ -543,33 +614,40 @@ int build_fire_graph(pcp_model* m, int shakeIter) {
     cudaError_t e = cudaStreamBeginCapture(cap, cudaStreamCaptureModeThreadLocal);
     int rc = PCP_OK;
     if (e == cudaSuccess) {
-        rc = record_fire_step(m);
-        e = cudaStreamEndCapture(cap, &g);
+        // the two conditions are created on the graph being captured; they
+        // read 0 at every launch of it until a kernel of the step sets them
+        cudaStreamCaptureStatus cs;
+        cudaGraph_t cg = nullptr;
+        cudaGraphConditionalHandle retryCond = 0, rbCond = 0;
+        e = cudaStreamGetCaptureInfo(cap, &cs, nullptr, &cg);
+        if (e == cudaSuccess)
+            e = cudaGraphConditionalHandleCreate(&retryCond, cg, 0, cudaGraphCondAssignDefault);
+        if (e == cudaSuccess)
+            e = cudaGraphConditionalHandleCreate(&rbCond, cg, 0, cudaGraphCondAssignDefault);
+        if (e == cudaSuccess) rc = record_fire_step(m, retryCond, rbCond);
+        cudaError_t e2 = cudaStreamEndCapture(cap, &g);
+        if (e == cudaSuccess) e = e2;
     }
     m->stream = saved;
     m->launches = savedLaunches;
     cudaStreamDestroy(cap);
     if (rc) { if (g) cudaGraphDestroy(g); return rc; }
-    if (e != cudaSuccess) return fail(PCP_ERR_CUDA, "graph capture failed: %s", cudaGetErrorString(e));
-    {
-        size_t nn = 0;
-        cudaGraphGetNodes(g, nullptr, &nn);
-        std::vector<cudaGraphNode_t> nodes(nn);
-        if (nn) cudaGraphGetNodes(g, nodes.data(), &nn);
-        int k = 0;
-        for (size_t i = 0; i < nn; ++i) {
-            cudaGraphNodeType t;
-            if (cudaGraphNodeGetType(nodes[i], &t) == cudaSuccess && t == cudaGraphNodeTypeKernel) ++k;
-        }
-        m->fireKernelNodes = k;
+    if (e != cudaSuccess) {
+        if (g) cudaGraphDestroy(g);
+        return fail(PCP_ERR_CUDA, "graph capture failed: %s", cudaGetErrorString(e));
     }
+    m->fireKernelNodes = count_kernel_nodes(g);
     e = cudaGraphInstantiate(&m->fireExec, g, 0);
     cudaGraphDestroy(g);
     if (e != cudaSuccess) return fail(PCP_ERR_CUDA, "graph instantiate failed: %s", cudaGetErrorString(e));
     m->fireGen = m->generation;
     m->fireModel = m->modelType;
     m->fireB = m->boxSize;
-    return PCP_OK;
+    // the rollback kernel counts its body's launches from the control block
+    m->ctrlHost->rbBodyKernels = m->rbBodyKernels;
+    CK(cudaMemcpyAsync(&m->ctrl->rbBodyKernels, &m->ctrlHost->rbBodyKernels, sizeof(int),
+                       cudaMemcpyHostToDevice, m->stream));
+    return sync(m);
 }
 
 struct FireParams {
@@ -588,6 +666,7 @@ int set_fire_params(pcp_model* m, const FireParams& f, bool resetRun) {
     c.active = 1;
     if (resetRun) { c.converged = 0; c.stepsDone = 0; }
     c.stepLimit = f.stepLimit;
+    c.rbBodyKernels = m->rbBodyKernels;
     CK(cudaMemcpyAsync(m->ctrl, m->ctrlHost, sizeof(Ctrl), cudaMemcpyHostToDevice, m->stream));
     return sync(m);
 }
@@ -818,7 +897,11 @@ int pcp_model_initialize_neighbor_cells(pcp_model* m) {
     m->numIntersections = 0;
     m->view = pcp_model::VIEW_NONE;
     m->invalidate();
-    // reset the record counters
+    // reset the record counters (launches counted on the device move to the
+    // host count)
+    rc = read_ctrl(m);
+    if (rc) return rc;
+    m->launches += (long long)m->ctrlHost->condLaunches;
     memset(m->ctrlHost, 0, sizeof(Ctrl));
     CK(cudaMemcpy(m->ctrl, m->ctrlHost, sizeof(Ctrl), cudaMemcpyHostToDevice));
     return PCP_OK;
@@ -1424,7 +1507,11 @@ int pcp_model_get_pair_count(pcp_model* m, long long* out) {
     return PCP_OK;
 }
 int pcp_model_get_launch_count(pcp_model* m, long long* out) {
-    CHECK_M(m); *out = m->launches; return PCP_OK;
+    CHECK_M(m);
+    int rc = read_ctrl(m);
+    if (rc) return rc;
+    *out = m->launches + (long long)m->ctrlHost->condLaunches;
+    return PCP_OK;
 }
 
 // ---- stateless launchers ----

@@ -51,15 +51,9 @@ __device__ __forceinline__ int cell_coord(double v, int B) {
     return (int)f;
 }
 
-// Cell of the midpoint of the edge that starts at vertex idx
-// (updateNeighborCellsKernel, kernels.cuh:661-707).
-__device__ __forceinline__ int midpoint_cell(const double2* __restrict__ pos,
-                                             const int* __restrict__ start,
-                                             const int* __restrict__ shapeId,
-                                             int size, int idx, int B) {
-    int v2 = idx + 1;
-    if (idx == size - 1 || shapeId[idx] != shapeId[idx + 1]) v2 = start[shapeId[idx]];
-    double2 a = pos[idx], b = pos[v2];
+// Cell of the midpoint of the edge from a to b (updateNeighborCellsKernel,
+// kernels.cuh:661-707).
+__device__ __forceinline__ int midpoint_cell_of(double2 a, double2 b, int B) {
     double x = b.x - a.x + 0.5;
     double y = b.y - a.y + 0.5;
     x = loop_wrap_unit(x);
@@ -70,6 +64,16 @@ __device__ __forceinline__ int midpoint_cell(const double2* __restrict__ pos,
     x = loop_wrap_unit(x);
     y = loop_wrap_unit(y);
     return cell_coord(y, B) * B + cell_coord(x, B);
+}
+
+// Cell of the midpoint of the edge that starts at vertex idx.
+__device__ __forceinline__ int midpoint_cell(const double2* __restrict__ pos,
+                                             const int* __restrict__ start,
+                                             const int* __restrict__ shapeId,
+                                             int size, int idx, int B) {
+    int v2 = idx + 1;
+    if (idx == size - 1 || shapeId[idx] != shapeId[idx + 1]) v2 = start[shapeId[idx]];
+    return midpoint_cell_of(pos[idx], pos[v2], B);
 }
 
 // Cells visited by updateNeighborsKernel's 3x3 stencil (kernels.cuh:737-762):

@@ -63,6 +63,12 @@ struct Ctrl {
     int snapNPos;
     double snapDt, snapAlpha;   // FIRE scalars at the start of the step
     unsigned long long pairEvals;   // cumulative candidate pairs (a < b) examined
+    // last-block tickets of the FIRE step's SHAKE and velocity-mixing kernels
+    // (zeroed by k_fire_begin) and the kernels run inside the step graph's
+    // conditional bodies (the host counts the unconditional ones)
+    unsigned int shakeTicket, bendTicket;
+    unsigned long long condLaunches;
+    int rbBodyKernels;     // kernels in the rollback body (set by the host)
 };
 
 enum : unsigned int {
@@ -130,9 +136,14 @@ cudaError_t launch_overlap_area_mc(const double2* pos, const int* start, const i
 
 // contacts
 cudaError_t contacts_init();
+// stages: bit 0 = reset + prepass + broad phase, bit 1 = narrow phase, bit 2 =
+// skip the counter reset (done by the caller); cellOut: compute the edge
+// midpoint cells in the prepass and store them there (cellLocation unused)
+constexpr int kContactsNoReset = 4;
 cudaError_t launch_contacts(const double2* pos, const int* start, const int* shapeId,
                             const int* cellLocation, int P, int V, int B, ContactWS& ws,
-                            Ctrl* ctrl, const int* gate, cudaStream_t st, int stages = 3);
+                            Ctrl* ctrl, const int* gate, cudaStream_t st, int stages = 3,
+                            int* cellOut = nullptr);
 cudaError_t launch_contacts_finish(const int* start, ContactWS& ws, Ctrl* ctrl,
                                    const int* gate, cudaStream_t st);
 cudaError_t launch_overlap_force(const double2* pos, const int* start, const int* next,
@@ -143,13 +154,19 @@ cudaError_t launch_overlap_force(const double2* pos, const int* start, const int
 cudaError_t constraints_init();
 // nmax: largest vertex count of a polygon (decides whether the per-polygon
 // scratch fits in shared memory)
+// useCond: the projection decides the FIRE step's energy rollback and sets
+// `rbCond` of the step graph
 cudaError_t launch_project(const double2* pos, const int* start, int P, int nmax,
                            const double* constraints, double2* force, double* scratch, int V,
                            int areaFromPositions, Ctrl* fireCtrl, const int* gate, double2* vel,
-                           cudaStream_t st);
+                           cudaStream_t st, cudaGraphConditionalHandle rbCond = 0,
+                           int useCond = 0);
+// fire (device-resident FIRE step, first SHAKE attempt): the last block to
+// finish decides whether the retry runs and sets `retryCond` of the step graph
 cudaError_t launch_shake(double2* pos, const int* start, int P, int nmax, const double* targetEdge,
                          const double* targetArea, int maxIter, double tol, int* maxItersOut,
-                         double* scratch, int V, const int* gate, cudaStream_t st);
+                         double* scratch, int V, const int* gate, cudaStream_t st,
+                         Ctrl* fire = nullptr, cudaGraphConditionalHandle retryCond = 0);
 // scratch doubles per vertex needed by launch_project / launch_shake
 constexpr int kScratchPerVertex = 36;
 // pcp_shake_project_noalloc: device address of its static workspace on the
@@ -163,17 +180,17 @@ cudaError_t launch_xpbd_iteration(double2* pos, const int* start, int P,
                                   double* devOut, cudaStream_t st);
 
 // FIRE pieces (device-resident scalars in Ctrl)
-cudaError_t launch_fire_reset(Ctrl* c, const int* gate, cudaStream_t st);
-cudaError_t launch_fire_begin(double2* pos, double2* vel, const double2* force, double2* save,
-                              int V, Ctrl* c, const int* gate, cudaStream_t st);
-cudaError_t launch_fire_shake_check(Ctrl* c, int which, const int* gate, cudaStream_t st);
+cudaError_t launch_fire_begin(double2* pos, double2* vel, double2* force, double2* save,
+                              double2* velSnap, double2* forceSnap, double2* verlet, int V,
+                              int resetContacts, Ctrl* c, const int* gate, cudaStream_t st);
 cudaError_t launch_fire_after_shake(double2* pos, double2* vel, const double2* save,
                                     const double2* verlet, int V, Ctrl* c, const int* gate,
                                     cudaStream_t st);
 cudaError_t launch_fire_rollback(double2* pos, double2* vel, double2* force, const double2* save,
-                                 int V, Ctrl* c, const int* gate, cudaStream_t st);
+                                 int V, int resetContacts, Ctrl* c, cudaStream_t st);
 cudaError_t launch_zero_force(double2* force, int V, Ctrl* c, const int* gate, cudaStream_t st);
 cudaError_t launch_fire_velocity(double2* vel, const double2* force, int V, Ctrl* c,
+                                 cudaGraphConditionalHandle rbCond, int useCond,
                                  const int* gate, cudaStream_t st);
 cudaError_t launch_fire_maxf(const double2* force, int V, Ctrl* c, const int* gate,
                              cudaStream_t st);
