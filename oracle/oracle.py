@@ -4,6 +4,8 @@
 of the reference's pybind `Model` (src/pybindWrapper.cpp:25-107), so a test
 can drive the CUDA model and the oracle with the same call sequence.  Only
 tests/, __graft_entry__.smoke() and bench.py's CPU legs import this module.
+Its SHAKE and FIRE parts are parity unpinned (the reference ships no source
+for them); the rest is pinned as pcp_oracle.c's header says.
 """
 import ctypes
 import os

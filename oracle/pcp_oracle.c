@@ -10,6 +10,14 @@
  * (cells, crossing decisions, packing, ordering, matching) is bit-exact.
  *
  * Only tests/, __graft_entry__.smoke() and bench.py's CPU legs use this.
+ *
+ * Pinning: the testSaver neighbour known answer, getDf, the variable-n
+ * projection, centres of mass and shoelace areas are checked against
+ * fixtures generated from the reference's own Python (tests/golden/).
+ * Parity unpinned for SHAKE and FIRE: the reference ships neither
+ * src/shake.h nor src/FIRE.h, so those parts restate the call contract
+ * (model.cpp:405-504, model.cu:576-636) and velocity-Verlet FIRE (Bitzek
+ * et al., PRL 97, 170201, 2006), and nothing of the reference pins them.
  */
 #include "pcp_oracle.h"
 
