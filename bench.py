@@ -221,9 +221,9 @@ def run_gpu(args, ws, rank, local):
 
 
 def roofline(m, s, torch, flush, args):
-    """Dominant kernel: the narrow phase (warp per candidate pair).  Algorithmic
-    bytes per launch: 16 (n_a + n_b) + 24 per candidate pair (both FP64 rings
-    and the pair entry) over the pairs it examines, self pairs counted once."""
+    """Dominant contact kernel: the narrow phase (warp per candidate pair).
+    Algorithmic bytes per launch: 16 (n_a + n_b) + 24 per pair it is handed
+    (both rings and the pair entry) and 16 n + 24 per self pair."""
     peaks = {}
     try:
         peaks = json.load(open(os.path.join(ROOT, "MEASURED_PEAKS.json")))
@@ -250,9 +250,8 @@ def roofline(m, s, torch, flush, args):
     ms = statistics.median(times)
     n = N_VERT
     P = N_POLY
-    cross = m.getPairCount()  # cumulative; the per-search count comes from the geometry
-    pairs = candidate_pairs(np.asarray(m.getPositions()), s.start_indices)
-    bytes_launch = pairs * (16 * 2 * n + 24) + P * (16 * n + 24)
+    pairs, selfs = m.getNarrowPairCount()
+    bytes_launch = pairs * (16 * 2 * n + 24) + selfs * (16 * n + 24)
     achieved = bytes_launch / (ms / 1e3) / 1e9
     traffic = None
     prof = os.path.join(ROOT, "profiles", "narrow_phase_traffic.json")
@@ -264,7 +263,8 @@ def roofline(m, s, torch, flush, args):
     roof = {"bound": "hbm", "achieved": achieved, "peak": hbm, "unit": "GB/s",
             "frac": achieved / hbm, "traffic": traffic, "peak_source": src + " (MEASURED_PEAKS.json hbm_gbs)",
             "kernel": "k_narrow + k_narrow_slow (contact stage 1)",
-            "launch_ms": ms, "algorithmic_bytes": bytes_launch, "pairs": pairs}
+            "launch_ms": ms, "algorithmic_bytes": bytes_launch, "pairs": pairs,
+            "self_pairs": selfs}
     fp64 = None
     p64 = os.path.join(ROOT, "profiles", "fp64_peak.json")
     if os.path.exists(p64):
@@ -272,7 +272,6 @@ def roofline(m, s, torch, flush, args):
             fp64 = json.load(open(p64))
         except (OSError, ValueError):
             fp64 = None
-    del cross
     return roof, fp64
 
 

@@ -220,8 +220,13 @@ int pcp_model_get_intersections_counter(pcp_model* m, int* out, int cap, int* le
  * zero-copy use from CUDA-aware callers.  Interleaved FP64 [2*numVertices]. */
 int pcp_model_device_positions(pcp_model* m, double** out);
 int pcp_model_device_forces(pcp_model* m, double** out);
-/* Number of polygon pairs the last contact search examined (pair evals). */
+/* Pair evaluations since creation: polygon pairs a < b with overlapping
+ * bounding circles taken through the contact search. */
 int pcp_model_get_pair_count(pcp_model* m, long long* out);
+/* Pairs the last contact search handed to the narrow phase: polygon pairs
+ * a < b whose bounding boxes are within the crossing margin, and self pairs
+ * (polygons not certified simple). */
+int pcp_model_get_narrow_pair_count(pcp_model* m, int* pairs_out, int* self_out);
 /* Kernel launches issued by the model since creation (for accounting). */
 int pcp_model_get_launch_count(pcp_model* m, long long* out);
 

@@ -42,6 +42,13 @@ static inline int nblocks(long long n, int threads) {
 }
 
 // ------------------------------------------------------------ prepass ----
+// Smallest FP32 fan cross product that certifies a strictly positive one,
+// per unit of the polygon's extent L (its box's larger side): each FP32
+// coordinate relative to the box centre is within 1.8e-7 of the exact value
+// for the FP64 positions, so a cross product of two (each below L) is within
+// 4 L 1.8e-7 (+ L^2 2^-22 for rounding).
+constexpr float kStarEpsPerL = 1e-6f;
+
 // Reset of the contact counters (everything in Ctrl before `energy`).
 __global__ void k_reset_contacts(Ctrl* __restrict__ ctrl, const int* gate) {
     if (gate_closed(gate)) return;
@@ -54,62 +61,108 @@ __global__ void __launch_bounds__(256)
 k_prepass(const double2* __restrict__ pos, const int* __restrict__ start,
           const int* __restrict__ cellLocation, int* __restrict__ cellOut, int P, int B,
           double2* __restrict__ edgeVec, float4* __restrict__ vtx, float4* __restrict__ polyInfo,
-          int* __restrict__ polyFlags, int* __restrict__ unsafeList, Ctrl* __restrict__ ctrl,
-          const int* gate) {
+          float4* __restrict__ polyBox, int* __restrict__ polyFlags, int* __restrict__ unsafeList,
+          Ctrl* __restrict__ ctrl, const int* gate) {
     if (gate_closed(gate)) return;
-    int p = blockIdx.x * (blockDim.x / 32) + threadIdx.x / 32;
-    int lane = threadIdx.x & 31;
-    if (p >= P) return;
-    int st = start[p], en = start[p + 1];
-    int n = en - st;
-    if (n <= 0) {   // empty polygon: no edges, never a candidate
-        if (lane == 0) { polyInfo[p] = make_float4(0.f, 0.f, 0.f, 0.f); polyFlags[p] = 0; }
-        return;
-    }
-    double2 q0 = pos[st];
-    float f0x = (float)q0.x, f0y = (float)q0.y;
-    float mnx = 0.f, mxx = 0.f, mny = 0.f, mxy = 0.f, emax = 0.f;
-    bool bad = false;
-    for (int kl = lane; kl < n; kl += 32) {
-        int k = st + kl;
-        int nx = (kl + 1 == n) ? st : k + 1;
-        double2 pk = pos[k], pn = pos[nx];
-        // r = wrap(p_next - p) exactly as updateNeighborsKernel (kernels.cuh:724-725)
-        edgeVec[k] = make_double2(wrap(pn.x - pk.x), wrap(pn.y - pk.y));
-        float fx = (float)pk.x, fy = (float)pk.y;
-        // cell (x, y) of the edge midpoint as updateNeighborsKernel splits it
-        // with the current box size (kernels.cuh:727-729); with cellOut the
-        // cells are computed here from the same positions
-        // (updateNeighborCellsKernel) and stored for the getters
-        int cell;
-        if (cellOut) {
-            cell = midpoint_cell_of(pk, pn, B);
-            cellOut[k] = cell;
-        } else {
-            cell = cellLocation[k];
+    __shared__ float s_r[8];
+    const int p = blockIdx.x * (blockDim.x / 32) + threadIdx.x / 32;
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    float Rsafe = 0.f;
+    const int st = p < P ? start[p] : 0;
+    const int n = p < P ? start[p + 1] - st : 0;
+    if (p < P && n <= 0) {   // empty polygon: no edges, never a candidate
+        if (lane == 0) {
+            polyInfo[p] = make_float4(0.f, 0.f, 0.f, 0.f);
+            polyBox[p] = make_float4(0.f, 0.f, 0.f, 0.f);
+            polyFlags[p] = 0;
         }
-        vtx[k] = make_float4(fx, fy, __int_as_float(cell % B), __int_as_float(cell / B));
-        float lx = wrapf(fx - f0x), ly = wrapf(fy - f0y);
-        float nxl = wrapf((float)pn.x - fx), nyl = wrapf((float)pn.y - fy);
-        if (!(isfinite(lx) && isfinite(ly) && isfinite(nxl) && isfinite(nyl))) bad = true;
-        mnx = fminf(mnx, lx); mxx = fmaxf(mxx, lx);
-        mny = fminf(mny, ly); mxy = fmaxf(mxy, ly);
-        emax = fmaxf(emax, sqrtf(nxl * nxl + nyl * nyl));
+    } else if (p < P) {
+        double2 q0 = pos[st];
+        float f0x = (float)q0.x, f0y = (float)q0.y;
+        float mnx = 0.f, mxx = 0.f, mny = 0.f, mxy = 0.f, emax = 0.f;
+        bool bad = false;
+        for (int kl = lane; kl < n; kl += 32) {
+            int k = st + kl;
+            int nx = (kl + 1 == n) ? st : k + 1;
+            double2 pk = pos[k], pn = pos[nx];
+            // r = wrap(p_next - p) exactly as updateNeighborsKernel (kernels.cuh:724-725)
+            edgeVec[k] = make_double2(wrap(pn.x - pk.x), wrap(pn.y - pk.y));
+            float fx = (float)pk.x, fy = (float)pk.y;
+            float fnx = (float)pn.x, fny = (float)pn.y;
+            // cell (x, y) of the edge midpoint as updateNeighborsKernel splits it
+            // with the current box size (kernels.cuh:727-729); with cellOut the
+            // cells are computed here from the same positions
+            // (updateNeighborCellsKernel) and stored for the getters
+            int cell;
+            if (cellOut) {
+                cell = midpoint_cell_fast(pk, pn, make_float2(fx, fy), make_float2(fnx, fny), B);
+                cellOut[k] = cell;
+            } else {
+                cell = cellLocation[k];
+            }
+            vtx[k] = make_float4(fx, fy, __int_as_float(cell % B), __int_as_float(cell / B));
+            float lx = wrapf(fx - f0x), ly = wrapf(fy - f0y);
+            float nxl = wrapf(fnx - fx), nyl = wrapf(fny - fy);
+            if (!(isfinite(lx) && isfinite(ly) && isfinite(nxl) && isfinite(nyl))) bad = true;
+            mnx = fminf(mnx, lx); mxx = fmaxf(mxx, lx);
+            mny = fminf(mny, ly); mxy = fmaxf(mxy, ly);
+            emax = fmaxf(emax, sqrtf(nxl * nxl + nyl * nyl));
+        }
+        mnx = warp_minf(mnx); mxx = warp_maxf(mxx);
+        mny = warp_minf(mny); mxy = warp_maxf(mxy);
+        emax = warp_maxf(emax);
+        bad = __any_sync(PCP_FULL, bad);
+        // star test about the box centre c (vertex 0's frame): every fan
+        // triangle (c, v_k, v_k+1) positive with margin and the fan winding
+        // once (the angle steps, each in (0, pi), add up to 2 pi, not 4 pi)
+        __syncwarp();
+        const float cxl = 0.5f * (mnx + mxx), cyl = 0.5f * (mny + mxy);
+        const float L = fmaxf(fmaxf(mxx - mnx, mxy - mny), 0.f);
+        float minCross = 3.0e38f, sweep = 0.f;
+        bool crossNaN = false;
+        for (int kl = lane; kl < n; kl += 32) {
+            float4 va = vtx[st + kl], vb = vtx[(kl + 1 == n) ? st : st + kl + 1];
+            float ax = wrapf(va.x - f0x) - cxl, ay = wrapf(va.y - f0y) - cyl;
+            float bx = wrapf(vb.x - f0x) - cxl, by = wrapf(vb.y - f0y) - cyl;
+            float c = ax * by - ay * bx;
+            crossNaN |= isnan(c);
+            minCross = fminf(minCross, c);
+            sweep += atan2f(c, ax * bx + ay * by);
+        }
+        minCross = warp_minf(minCross);
+        crossNaN = __any_sync(PCP_FULL, crossNaN);
+        for (int o = 16; o > 0; o >>= 1) sweep += __shfl_xor_sync(PCP_FULL, sweep, o);
+        // (polygons under 1e-4 across are left to the search: there the
+        // absolute FP32 error of the coordinates is not small against L)
+        const bool star = !crossNaN && L >= 1e-4f && minCross > kStarEpsPerL * L &&
+                          fabsf(sweep - 6.2831853f) < 1.0f;
+        if (lane == 0) {
+            float cx = f0x + 0.5f * (mnx + mxx), cy = f0y + 0.5f * (mny + mxy);
+            cx -= floorf(cx); cy -= floorf(cy);
+            float w = mxx - mnx, h = mxy - mny;
+            float R = 0.5f * sqrtf(w * w + h * h) * 1.0001f + 4e-6f;
+            bool safe = !bad && isfinite(R) && R < 0.1f && n >= 3;
+            polyInfo[p] = make_float4(cx, cy, R, emax);
+            polyBox[p] = make_float4(mnx, mxx, mny, mxy);
+            // bit 0: well formed (extent < 0.2, finite); bit 1: also simple
+            // with room to spare -- star-shaped about the box centre with
+            // every fan triangle above kStarEpsPerL L in FP32 and winding
+            // once, so non-adjacent edges lie in angular sectors about the
+            // centre that are separated by sectors of positive width and the
+            // FP64 crossing test cannot accept any of them; its self pair is
+            // not searched
+            polyFlags[p] = safe ? ((star && n >= 4) ? 3 : 1) : 0;
+            if (safe) Rsafe = R;
+            else unsafeList[atomicAdd(&ctrl->numUnsafe, 1)] = p;
+        }
     }
-    mnx = warp_minf(mnx); mxx = warp_maxf(mxx);
-    mny = warp_minf(mny); mxy = warp_maxf(mxy);
-    emax = warp_maxf(emax);
-    bad = __any_sync(PCP_FULL, bad);
-    if (lane == 0) {
-        float cx = f0x + 0.5f * (mnx + mxx), cy = f0y + 0.5f * (mny + mxy);
-        cx -= floorf(cx); cy -= floorf(cy);
-        float w = mxx - mnx, h = mxy - mny;
-        float R = 0.5f * sqrtf(w * w + h * h) * 1.0001f + 4e-6f;
-        bool safe = !bad && isfinite(R) && R < 0.1f && n >= 3;
-        polyInfo[p] = make_float4(cx, cy, R, emax);
-        polyFlags[p] = safe ? 1 : 0;
-        if (safe) atomic_max_nonneg_f(&ctrl->Rmax, R);
-        else unsafeList[atomicAdd(&ctrl->numUnsafe, 1)] = p;
+    // one atomic per block for the largest safe radius
+    if (lane == 0) s_r[warp] = Rsafe;
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        float r = 0.f;
+        for (int w = 0; w < (int)(blockDim.x >> 5); ++w) r = fmaxf(r, s_r[w]);
+        if (r > 0.f) atomic_max_nonneg_f(&ctrl->Rmax, r);
     }
 }
 
@@ -199,95 +252,144 @@ __global__ void k_grid_scatter(const float4* __restrict__ polyInfo, const int* _
     sortedPoly[gridStart[cell] + atomicAdd(&gridFill[cell], 1)] = p;
 }
 
-__device__ __forceinline__ void emit_pair(int a, int b, int2* pairs, int cap, Ctrl* ctrl) {
-    int slot = atomicAdd(&ctrl->numPairs, 1);
-    if (slot < cap) pairs[slot] = make_int2(a, b);
-    else atomicOr(&ctrl->flags, kFlagPairOverflow);
-}
-
-// warp-aggregated emission: one atomic per warp for the lanes with `ok`
-__device__ __forceinline__ void emit_pairs_warp(bool ok, int a, int b, int2* pairs, int cap,
-                                                Ctrl* ctrl) {
-    unsigned mk = __ballot_sync(PCP_FULL, ok);
-    if (!mk) return;
-    int lane = threadIdx.x & 31;
-    int leader = __ffs(mk) - 1;
-    int base = 0;
-    if (lane == leader) base = atomicAdd(&ctrl->numPairs, __popc(mk));
-    base = __shfl_sync(PCP_FULL, base, leader);
-    if (ok) {
-        int slot = base + __popc(mk & ((1u << lane) - 1u));
-        if (slot < cap) pairs[slot] = make_int2(a, b);
-        else atomicOr(&ctrl->flags, kFlagPairOverflow);
-    }
-}
-
 // One warp per polygon i: the lanes walk the polygons of the (up to) nine
-// neighbouring grid cells and keep j > i whose bounding circle meets i's.
+// neighbouring grid cells and keep j > i whose bounding circle meets i's
+// (the pair evaluations the benchmark counts) and whose bounding box, padded
+// by the narrow phase's margin, meets i's (the pairs emitted: the narrow
+// phase finds nothing in the others).  The polygons not well formed pair
+// with everyone.  Pass 1 counts, the block reserves its slots with one
+// atomic, pass 2 writes.
+__device__ __forceinline__ bool box_pair(const float4& ci, const float4& bi, const float4& cj,
+                                         const float4& bj) {
+    float ddx = wrapf(cj.x - ci.x), ddy = wrapf(cj.y - ci.y);
+    float m = 2.f * (4e-6f + 1e-3f * ci.w * cj.w) + 2e-6f;
+    float hx = 0.5f * ((bi.y - bi.x) + (bj.y - bj.x)) + m;
+    float hy = 0.5f * ((bi.w - bi.z) + (bj.w - bj.z)) + m;
+    // NaN keeps the pair
+    return !(fabsf(ddx) > hx || fabsf(ddy) > hy);
+}
+
 __global__ void __launch_bounds__(256)
-k_candidates(const float4* __restrict__ polyInfo, const int* __restrict__ flags,
-             const int* __restrict__ start, int P, const int* __restrict__ gridStart,
-             const int* __restrict__ sortedPoly, int2* __restrict__ pairs, int capPairs,
-             Ctrl* __restrict__ ctrl, const int* gate) {
+k_candidates(const float4* __restrict__ polyInfo, const float4* __restrict__ polyBox,
+             const int* __restrict__ flags, const int* __restrict__ start, int P,
+             const int* __restrict__ gridStart, const int* __restrict__ sortedPoly,
+             int2* __restrict__ pairs, int capPairs, Ctrl* __restrict__ ctrl, const int* gate) {
     if (gate_closed(gate)) return;
-    int i = blockIdx.x * (blockDim.x >> 5) + (threadIdx.x >> 5);
-    int lane = threadIdx.x & 31;
-    if (i >= P) return;
-    int n = start[i + 1] - start[i];
-    if (n <= 0) return;
-    unsigned long long evals = 0;
-    if (lane == 0 && n >= 4) emit_pair(i, i, pairs, capPairs, ctrl);
-    if (!flags[i]) {
-        // not well formed: paired with everyone (safe partners below i, all above)
-        for (int j0 = 0; j0 < P; j0 += 32) {
-            int j = j0 + lane;
-            bool ok = j < P && j != i && (j > i || flags[j]) && start[j + 1] > start[j];
-            emit_pairs_warp(ok, j < i ? j : i, j < i ? i : j, pairs, capPairs, ctrl);
-            evals += ok ? 1 : 0;
-        }
-    } else {
-        int G = ctrl->G;
-        float4 ci = polyInfo[i];
-        int gx = grid_cell(ci.x, G), gy = grid_cell(ci.y, G);
-        // the distinct neighbouring cells and their ranges
-        int cs[9], ce[9], nc = 0;
-        for (int dx = -1; dx <= 1; ++dx) {
-            int nx = gx + dx;
+    __shared__ int s_cnt[8];
+    __shared__ unsigned long long s_evals[8];
+    __shared__ int s_base;
+    const int i = blockIdx.x * (blockDim.x >> 5) + (threadIdx.x >> 5);
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    const unsigned lt = (1u << lane) - 1u;
+    const int n = i < P ? start[i + 1] - start[i] : 0;
+    const bool active = i < P && n > 0;
+    const bool safe = active && flags[i];
+    float4 ci = make_float4(0.f, 0.f, 0.f, 0.f), bi = ci;
+    // lanes 0..8 own the nine neighbouring grid cells; their ranges of
+    // sortedPoly are laid end to end and dealt out one polygon per lane
+    int ca = 0, len = 0;
+    if (safe) {
+        ci = polyInfo[i];
+        bi = polyBox[i];
+        const int G = ctrl->G;
+        if (lane < 9) {
+            int nx = grid_cell(ci.x, G) + lane / 3 - 1;
+            int ny = grid_cell(ci.y, G) + lane % 3 - 1;
             if (nx < 0) nx += G; else if (nx >= G) nx -= G;
-            for (int dy = -1; dy <= 1; ++dy) {
-                int ny = gy + dy;
-                if (ny < 0) ny += G; else if (ny >= G) ny -= G;
-                int cell = ny * G + nx;
-                int a = gridStart[cell], b = gridStart[cell + 1];
-                // cells are disjoint ranges of sortedPoly; a repeated cell
-                // (G < 3) repeats its range exactly
-                bool dup = false;
-                for (int t = 0; t < nc; ++t) dup |= (cs[t] == a && ce[t] == b);
-                if (dup || b <= a) continue;
-                cs[nc] = a; ce[nc] = b; ++nc;
-            }
-        }
-        for (int t = 0; t < nc; ++t) {
-            for (int q0 = cs[t]; q0 < ce[t]; q0 += 32) {
-                int q = q0 + lane;
-                bool ok = false;
-                int j = 0;
-                if (q < ce[t]) {
-                    j = sortedPoly[q];
-                    if (j > i) {
-                        float4 cj = polyInfo[j];
-                        float ddx = wrapf(cj.x - ci.x), ddy = wrapf(cj.y - ci.y);
-                        float rr = ci.z + cj.z + 1e-5f;
-                        ok = ddx * ddx + ddy * ddy <= rr * rr;
-                    }
-                }
-                emit_pairs_warp(ok, i, j, pairs, capPairs, ctrl);
-                evals += ok ? 1 : 0;
-            }
+            if (ny < 0) ny += G; else if (ny >= G) ny -= G;
+            int cell = ny * G + nx;
+            ca = gridStart[cell];
+            len = gridStart[cell + 1] - ca;
         }
     }
-    for (int o = 16; o > 0; o >>= 1) evals += __shfl_xor_sync(PCP_FULL, evals, o);
-    if (lane == 0 && evals) atomicAdd(&ctrl->pairEvals, evals);
+    // a repeated cell (G < 3) repeats its range exactly: keep the first
+    for (int t = 0; t < 8; ++t) {
+        int at = __shfl_sync(PCP_FULL, ca, t), lt2 = __shfl_sync(PCP_FULL, len, t);
+        if (t < lane && lane < 9 && at == ca && lt2 == len) len = 0;
+    }
+    int incl = len;
+#pragma unroll
+    for (int d = 1; d < 16; d <<= 1) {
+        int t = __shfl_up_sync(PCP_FULL, incl, d);
+        if (lane >= d) incl += t;
+    }
+    const int total = __shfl_sync(PCP_FULL, incl, 8);
+    // pass 0 counts, pass 1 writes from the reserved base
+    int base = 0;
+    for (int pass = 0; pass < 2; ++pass) {
+        int cnt = 0;
+        unsigned long long evals = 0;
+        auto put = [&](bool ok, int a, int b) {
+            unsigned mk = __ballot_sync(PCP_FULL, ok);
+            if (pass == 1 && ok) {
+                int slot = base + cnt + __popc(mk & lt);
+                if (slot < capPairs) pairs[slot] = make_int2(a, b);
+            }
+            cnt += __popc(mk);
+        };
+        if (active) {
+            // self crossings are searched unless the prepass certified the
+            // polygon simple (kernels.cuh:766-775 records s1 == s2 crossings)
+            if (n >= 4 && !(flags[i] & 2)) {
+                put(lane == 0, i, i);
+                if (pass == 0 && lane == 0) atomicAdd(&ctrl->numSelf, 1);
+            }
+            if (!safe) {
+                // not well formed: paired with everyone (safe partners below i, all above)
+                for (int j0 = 0; j0 < P; j0 += 32) {
+                    int j = j0 + lane;
+                    bool ok = j < P && j != i && (j > i || flags[j]) && start[j + 1] > start[j];
+                    put(ok, j < i ? j : i, j < i ? i : j);
+                    evals += ok ? 1 : 0;
+                }
+            } else {
+                for (int b0 = 0; b0 < total; b0 += 32) {
+                    const int item = b0 + lane;
+                    // owning cell: the first of lanes 0..8 whose running total exceeds item
+                    int own = 0;
+#pragma unroll
+                    for (int t = 0; t < 9; ++t) own += (__shfl_sync(PCP_FULL, incl, t) <= item) ? 1 : 0;
+                    int oa = __shfl_sync(PCP_FULL, ca, own < 9 ? own : 8);
+                    int oi = __shfl_sync(PCP_FULL, incl - len, own < 9 ? own : 8);
+                    bool circle = false, box = false;
+                    int j = 0;
+                    if (item < total) {
+                        j = sortedPoly[oa + item - oi];
+                        if (j > i) {
+                            float4 cj = polyInfo[j];
+                            float ddx = wrapf(cj.x - ci.x), ddy = wrapf(cj.y - ci.y);
+                            float rr = ci.z + cj.z + 1e-5f;
+                            circle = ddx * ddx + ddy * ddy <= rr * rr;
+                            box = circle && box_pair(ci, bi, cj, polyBox[j]);
+                        }
+                    }
+                    put(box, i, j);
+                    evals += circle ? 1 : 0;
+                }
+            }
+        }
+        if (pass == 0) {
+            evals = (unsigned long long)warp_sumi((int)evals);
+            if (lane == 0) { s_cnt[warp] = cnt; s_evals[warp] = evals; }
+            __syncthreads();
+            if (threadIdx.x == 0) {
+                int tot = 0;
+                unsigned long long ev = 0;
+                for (int w = 0; w < (int)(blockDim.x >> 5); ++w) {
+                    int c = s_cnt[w];
+                    s_cnt[w] = tot;
+                    tot += c;
+                    ev += s_evals[w];
+                }
+                int b0 = tot ? atomicAdd(&ctrl->numPairs, tot) : 0;
+                if (b0 + tot > capPairs) atomicOr(&ctrl->flags, kFlagPairOverflow);
+                if (ev) atomicAdd(&ctrl->pairEvals, ev);
+                s_base = b0;
+            }
+            __syncthreads();
+            base = s_base + s_cnt[warp];
+        }
+    }
 }
 
 // -------------------------------------------------------- narrow phase ----
@@ -364,30 +466,51 @@ __device__ int narrow_pair(const PairCtx& pc, const float4* ringA, const float4*
                            EdgeCand* candA, EdgeCand* candB, int* queue,
                            unsigned long long* recKey, float2* recTU, int recCap, int B,
                            const double2* __restrict__ pos, const double2* __restrict__ edgeVec,
-                           const float4* __restrict__ polyInfo) {
+                           const float4* __restrict__ polyInfo,
+                           const float4* __restrict__ polyBox,
+                           const int* __restrict__ polyFlags) {
     const int lane = threadIdx.x & 31;
     const unsigned lt = (1u << lane) - 1u;
     const int nA = pc.nA, nB = pc.nB;
     const float f0x = ringA[0].x, f0y = ringA[0].y;
     const float LA = polyInfo[pc.a].w, LB = polyInfo[pc.b].w;
     const float m = 4e-6f + 1e-3f * LA * LB;
-    // polygon boxes in A's frame
-    float ax0 = 3.f, ax1 = -3.f, ay0 = 3.f, ay1 = -3.f;
-    for (int a = lane; a < nA; a += 32) {
-        float x = wrapf(ringA[a].x - f0x), y = wrapf(ringA[a].y - f0y);
-        ax0 = fminf(ax0, x); ax1 = fmaxf(ax1, x); ay0 = fminf(ay0, y); ay1 = fmaxf(ay1, y);
-    }
-    ax0 = warp_minf(ax0); ax1 = warp_maxf(ax1); ay0 = warp_minf(ay0); ay1 = warp_maxf(ay1);
-    float ox0 = ax0 - m, ox1 = ax1 + m, oy0 = ay0 - m, oy1 = ay1 + m;
-    if (!pc.self) {
-        float bx0 = 3.f, bx1 = -3.f, by0 = 3.f, by1 = -3.f;
-        for (int b = lane; b < nB; b += 32) {
-            float x = wrapf(ringB[b].x - f0x), y = wrapf(ringB[b].y - f0y);
-            bx0 = fminf(bx0, x); bx1 = fmaxf(bx1, x); by0 = fminf(by0, y); by1 = fmaxf(by1, y);
+    // polygon boxes in A's frame.  Two well-formed polygons (extent < 0.2,
+    // and a candidate pair lies within 0.4 of A's vertex 0, so nothing wraps):
+    // A's box was measured in this frame by the prepass (the same FP32
+    // operations as the culls below) and B's box is moved from B's frame,
+    // widened by 1e-6 for the rounding of the move.  Otherwise the boxes are
+    // measured from the rings here.
+    float ox0, ox1, oy0, oy1;
+    if (polyFlags[pc.a] && polyFlags[pc.b]) {
+        const float4 ba = polyBox[pc.a];
+        ox0 = ba.x - m; ox1 = ba.y + m; oy0 = ba.z - m; oy1 = ba.w + m;
+        if (!pc.self) {
+            const float4 bb = polyBox[pc.b];
+            const float sx = wrapf(ringB[0].x - f0x), sy = wrapf(ringB[0].y - f0y);
+            ox0 = fmaxf(ba.x, bb.x + sx - 1e-6f) - m; ox1 = fminf(ba.y, bb.y + sx + 1e-6f) + m;
+            oy0 = fmaxf(ba.z, bb.z + sy - 1e-6f) - m; oy1 = fminf(ba.w, bb.w + sy + 1e-6f) + m;
+            // disjoint boxes: no edge of A (padded by m) reaches past the gap
+            if (ox0 > ox1 || oy0 > oy1) return 0;
         }
-        bx0 = warp_minf(bx0); bx1 = warp_maxf(bx1); by0 = warp_minf(by0); by1 = warp_maxf(by1);
-        ox0 = fmaxf(ax0, bx0) - m; ox1 = fminf(ax1, bx1) + m;
-        oy0 = fmaxf(ay0, by0) - m; oy1 = fminf(ay1, by1) + m;
+    } else {
+        float ax0 = 3.f, ax1 = -3.f, ay0 = 3.f, ay1 = -3.f;
+        for (int a = lane; a < nA; a += 32) {
+            float x = wrapf(ringA[a].x - f0x), y = wrapf(ringA[a].y - f0y);
+            ax0 = fminf(ax0, x); ax1 = fmaxf(ax1, x); ay0 = fminf(ay0, y); ay1 = fmaxf(ay1, y);
+        }
+        ax0 = warp_minf(ax0); ax1 = warp_maxf(ax1); ay0 = warp_minf(ay0); ay1 = warp_maxf(ay1);
+        ox0 = ax0 - m; ox1 = ax1 + m; oy0 = ay0 - m; oy1 = ay1 + m;
+        if (!pc.self) {
+            float bx0 = 3.f, bx1 = -3.f, by0 = 3.f, by1 = -3.f;
+            for (int b = lane; b < nB; b += 32) {
+                float x = wrapf(ringB[b].x - f0x), y = wrapf(ringB[b].y - f0y);
+                bx0 = fminf(bx0, x); bx1 = fmaxf(bx1, x); by0 = fminf(by0, y); by1 = fmaxf(by1, y);
+            }
+            bx0 = warp_minf(bx0); bx1 = warp_maxf(bx1); by0 = warp_minf(by0); by1 = warp_maxf(by1);
+            ox0 = fmaxf(ax0, bx0) - m; ox1 = fminf(ax1, bx1) + m;
+            oy0 = fmaxf(ay0, by0) - m; oy1 = fminf(ay1, by1) + m;
+        }
     }
     // candidate edges of each ring (edge box padded by m meets the overlap box)
     auto collect = [&](const float4* ring, int n, EdgeCand* out, float pad) -> int {
@@ -451,15 +574,22 @@ __device__ int narrow_pair(const PairCtx& pc, const float4* ringA, const float4*
         }
         rec += cnt2;
     };
-    for (int t0 = 0; t0 < nLB && !overflow; t0 += 32) {
-        int t = t0 + lane;
-        bool bval = t < nLB;
-        EdgeCand eb;
-        if (bval) eb = cb[t];
-        else { eb.box = make_float4(0.f, 0.f, 0.f, 0.f); eb.idx = 0; eb.cx = 0; eb.cy = 0; }
-        for (int i = 0; i < nLA && !overflow; ++i) {
-            EdgeCand ea = candA[i];
-            bool ok = bval;
+    // candidate edge pairs as (aw x bw) lane tiles: lane = a * bw + b, bw the
+    // power of two >= nLB (at most 32), so few-edge lists fill the warp
+    int lb = 0;
+    while ((1 << lb) < nLB && lb < 5) ++lb;
+    const int bw = 1 << lb, aw = 32 >> lb;
+    const int la = lane >> lb, lbb = lane & (bw - 1);
+    for (int b0 = 0; b0 < nLB && !overflow; b0 += bw) {
+        for (int a0 = 0; a0 < nLA && !overflow; a0 += aw) {
+            const int ia = a0 + la, ib = b0 + lbb;
+            bool ok = ia < nLA && ib < nLB;
+            EdgeCand ea, eb;
+            if (ok) { ea = candA[ia]; eb = cb[ib]; }
+            else {
+                ea.box = eb.box = make_float4(0.f, 0.f, 0.f, 0.f);
+                ea.idx = eb.idx = 0; ea.cx = eb.cx = 0; ea.cy = eb.cy = 0;
+            }
             if (pc.self) {
                 // id1 < nid, not adjacent (kernels.cuh:766-775)
                 ok = ok && eb.idx > ea.idx + 1 && !(ea.idx == 0 && eb.idx == nA - 1);
@@ -645,7 +775,8 @@ k_narrow(const double2* __restrict__ pos, const int* __restrict__ start, int B,
         const float4* ringA = &S.ring[stage][0];
         const float4* ringB = pc.self ? ringA : &S.ring[stage][kFastRing];
         int R = narrow_pair(pc, ringA, ringB, S.candA, S.candB, S.queue, S.recKey, S.recTU,
-                            kFastRecords, B, pos, ws.edgeVec, ws.polyInfo);
+                            kFastRecords, B, pos, ws.edgeVec, ws.polyInfo, ws.polyBox,
+                            ws.polyFlags);
         if (R < 0) {
             if (lane == 0) push_slow(q, ctrl, ws);
         } else if (R > 0) {
@@ -693,7 +824,8 @@ k_narrow_slow(const double2* __restrict__ pos, const int* __restrict__ start, in
         const float4* ringB = pc.self ? ring : ring + pc.nA;
         // the two candidate lists share one buffer: A from the front, B behind it
         int R = narrow_pair(pc, ring, ringB, cand, cand + pc.nA, queue, recKey, recTU,
-                            kSlowRecords, B, pos, ws.edgeVec, ws.polyInfo);
+                            kSlowRecords, B, pos, ws.edgeVec, ws.polyInfo, ws.polyBox,
+                            ws.polyFlags);
         if (R < 0) {
             if (lane == 0) atomicOr(&ctrl->flags, kFlagCapacity);
         } else if (R > 0) {
@@ -904,14 +1036,14 @@ cudaError_t launch_contacts(const double2* pos, const int* start, const int* sha
     if (!(stages & 4)) k_reset_contacts<<<1, 64, 0, st>>>(ctrl, gate);
     if (P <= 0) return cudaGetLastError();
     k_prepass<<<nblocks(P, 8), 256, 0, st>>>(pos, start, cellLocation, cellOut, P, B, ws.edgeVec,
-                                             ws.vtx, ws.polyInfo, ws.polyFlags, ws.unsafeList,
-                                             ctrl, gate);
+                                             ws.vtx, ws.polyInfo, ws.polyBox, ws.polyFlags,
+                                             ws.unsafeList, ctrl, gate);
     k_grid_count<<<nblocks(P, 256), 256, 0, st>>>(ws.polyInfo, ws.polyFlags, P, ws.gridCount,
                                                   ctrl, gate);
     k_grid_scan<<<1, 1024, 0, st>>>(ws.gridCount, ws.gridStart, ws.gridFill, ctrl, gate);
     k_grid_scatter<<<nblocks(P, 256), 256, 0, st>>>(ws.polyInfo, ws.polyFlags, P, ws.gridStart,
                                                     ws.gridFill, ws.sortedPoly, ctrl, gate);
-    k_candidates<<<nblocks(P, 8), 256, 0, st>>>(ws.polyInfo, ws.polyFlags, start, P,
+    k_candidates<<<nblocks(P, 8), 256, 0, st>>>(ws.polyInfo, ws.polyBox, ws.polyFlags, start, P,
                                                   ws.gridStart, ws.sortedPoly, ws.pairs,
                                                   ws.capPairs, ctrl, gate);
     }

@@ -153,7 +153,11 @@ __global__ void k_neighbor_cells(const double2* __restrict__ pos, const int* __r
     if (gate_closed(gate)) return;
     int i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= V) return;
-    cell[i] = midpoint_cell(pos, start, shapeId, V, i, B);
+    int v2 = i + 1;
+    if (i == V - 1 || shapeId[i] != shapeId[i + 1]) v2 = start[shapeId[i]];
+    double2 a = pos[i], b = pos[v2];
+    cell[i] = midpoint_cell_fast(a, b, make_float2((float)a.x, (float)a.y),
+                                 make_float2((float)b.x, (float)b.y), B);
 }
 
 cudaError_t launch_neighbor_cells(const double2* pos, const int* start, const int* shapeId,

@@ -137,7 +137,7 @@ struct pcp_model {
         free_ws();
     }
     void free_ws() {
-        dfree(&ws.edgeVec); dfree(&ws.vtx); dfree(&ws.polyInfo); dfree(&ws.polyFlags);
+        dfree(&ws.edgeVec); dfree(&ws.vtx); dfree(&ws.polyInfo); dfree(&ws.polyBox); dfree(&ws.polyFlags);
         dfree(&ws.gridCount); dfree(&ws.gridStart); dfree(&ws.gridFill); dfree(&ws.sortedPoly);
         dfree(&ws.unsafeList); dfree(&ws.pairs); dfree(&ws.recKey); dfree(&ws.recOuter);
         dfree(&ws.recTU); dfree(&ws.recUT); dfree(&ws.fixList); dfree(&ws.slowList);
@@ -170,7 +170,7 @@ int alloc_ws(pcp_model* m, int capPairs, int capRecords) {
     w.capSlow = std::max(1024, capPairs / 4);
     size_t V = (size_t)m->V, P = (size_t)std::max(m->P, 1);
     CK(dalloc(&w.edgeVec, V)); CK(dalloc(&w.vtx, V));
-    CK(dalloc(&w.polyInfo, P)); CK(dalloc(&w.polyFlags, P));
+    CK(dalloc(&w.polyInfo, P)); CK(dalloc(&w.polyBox, P)); CK(dalloc(&w.polyFlags, P));
     CK(dalloc(&w.gridCount, (size_t)kGridMax * kGridMax));
     CK(dalloc(&w.gridStart, (size_t)kGridMax * kGridMax + 1));
     CK(dalloc(&w.gridFill, (size_t)kGridMax * kGridMax));
@@ -1504,6 +1504,14 @@ int pcp_model_get_pair_count(pcp_model* m, long long* out) {
     int rc = read_ctrl(m);
     if (rc) return rc;
     *out = (long long)m->ctrlHost->pairEvals;
+    return PCP_OK;
+}
+int pcp_model_get_narrow_pair_count(pcp_model* m, int* pairs_out, int* self_out) {
+    CHECK_M(m);
+    int rc = read_ctrl(m);
+    if (rc) return rc;
+    if (pairs_out) *pairs_out = m->ctrlHost->numPairs - m->ctrlHost->numSelf;
+    if (self_out) *self_out = m->ctrlHost->numSelf;
     return PCP_OK;
 }
 int pcp_model_get_launch_count(pcp_model* m, long long* out) {

@@ -18,9 +18,21 @@ namespace pcp {
 
 // ---------------------------------------------------------------- wraps ----
 
-// wrap (kernels.cuh:115-119): minimum image into [-0.5, 0.5).
+// wrap (kernels.cuh:115-119): minimum image into [-0.5, 0.5),
+//   y = x + 1.5;  y = y - floor(y);  return y - 0.5;
+// For y in [0, 3) (x in [-1.5, 1.5): every difference of two positions of
+// the unit box) floor(y) is read from y's high word with integer compares,
+// and (y - floor(y)) - 0.5 = y - (floor(y) + 0.5) holds exactly (both
+// differences are exact), so the result is bit-identical with two FP64
+// adds instead of three adds and a floor.  Other y take the literal form.
 __device__ __forceinline__ double wrap(double x) {
     double y = x + 1.5;
+    int hi = __double2hiint(y);
+    if (hi >= 0 && hi < 0x40080000) {            // 0 <= y < 3 (and not NaN)
+        // floor(y) + 0.5 as a double: 0.5, 1.5 or 2.5 (low word 0)
+        int c = hi < 0x3FF00000 ? 0x3FE00000 : (hi < 0x40000000 ? 0x3FF80000 : 0x40040000);
+        return y - __hiloint2double(c, 0);
+    }
     y = y - floor(y);
     return y - 0.5;
 }
@@ -64,6 +76,31 @@ __device__ __forceinline__ int midpoint_cell_of(double2 a, double2 b, int B) {
     x = loop_wrap_unit(x);
     y = loop_wrap_unit(y);
     return cell_coord(y, B) * B + cell_coord(x, B);
+}
+
+// The same cell, decided in FP32 when that is safe.  The FP32 midpoint is
+// within 1.3e-7 of the FP64 one (coordinates rounded to float, three
+// roundings) and its product with B adds at most 3e-8 B, so it lies within
+// 1.6e-7 B cell widths of the FP64 value; when it is more than
+// 1e-4 + 4e-7 B cell widths from every cell boundary (and the edge is short,
+// so both minimum images agree) the FP64 computation lands in the same cell.
+// Otherwise, and for non-finite input, the FP64 form decides.  fa, fb are
+// a and b rounded to float.
+__device__ __forceinline__ int midpoint_cell_fast(double2 a, double2 b, float2 fa, float2 fb,
+                                                  int B) {
+    float ddx = wrapf(fb.x - fa.x), ddy = wrapf(fb.y - fa.y);
+    float mx = fa.x + 0.5f * ddx, my = fa.y + 0.5f * ddy;
+    mx -= floorf(mx);
+    my -= floorf(my);
+    float ux = mx * (float)B, uy = my * (float)B;
+    const float margin = 1e-4f + 4e-7f * (float)B;
+    bool sure = fabsf(ddx) < 0.45f && fabsf(ddy) < 0.45f &&
+                fabsf(ux - rintf(ux)) > margin && fabsf(uy - rintf(uy)) > margin;
+    if (sure) {
+        int cx = min((int)ux, B - 1), cy = min((int)uy, B - 1);
+        return cy * B + cx;
+    }
+    return midpoint_cell_of(a, b, B);
 }
 
 // Cell of the midpoint of the edge that starts at vertex idx.

@@ -31,6 +31,7 @@ struct Ctrl {
     int numSlow;
     int slowCursor;
     int numUnsafe;
+    int numSelf;           // self pairs among the candidate pairs
     int G;                 // broad-phase grid cells per axis
     unsigned int flags;    // kFlag* bits
     float Rmax;            // largest bounding radius of a well-formed polygon
@@ -87,6 +88,7 @@ struct ContactWS {
     double2* edgeVec = nullptr;     // [V] wrap(p_next - p)
     float4* vtx = nullptr;          // [V] (x, y) as float, cell, 0
     float4* polyInfo = nullptr;     // [P] centre x, y, radius, longest edge
+    float4* polyBox = nullptr;      // [P] box (x0, x1, y0, y1) relative to vertex 0 (FP32)
     int* polyFlags = nullptr;       // [P] 1 = well formed (safe for the culls)
     int* gridCount = nullptr;       // [G*G] (G <= kGridMax)
     int* gridStart = nullptr;       // [G*G + 1]

@@ -142,6 +142,11 @@ public:
     double getOverlapArea() { double v; check(pcp_model_get_overlap_area(m_, &v)); return v; }
     long long getPairCount() { long long v; check(pcp_model_get_pair_count(m_, &v)); return v; }
     long long getLaunchCount() { long long v; check(pcp_model_get_launch_count(m_, &v)); return v; }
+    std::tuple<int, int> getNarrowPairCount() {
+        int a = 0, b = 0;
+        check(pcp_model_get_narrow_pair_count(m_, &a, &b));
+        return std::make_tuple(a, b);
+    }
     std::string getModelEnum() {
         int e; check(pcp_model_get_model_enum(m_, &e));
         static const char* names[] = {"normal", "edgeOnly", "areaOnly", "softBody", "abnormal", "hybrid"};
@@ -299,6 +304,7 @@ PYBIND11_MODULE(libpyCudaPolygon, m) {
         .def("getBoxSize", &Model::getBoxSize)
         .def("getPairCount", &Model::getPairCount)
         .def("getLaunchCount", &Model::getLaunchCount)
+        .def("getNarrowPairCount", &Model::getNarrowPairCount)
         .def("devicePositions", &Model::devicePositions)
         .def("deviceForces", &Model::deviceForces)
         .def("handle", &Model::handlePtr)

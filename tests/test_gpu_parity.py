@@ -18,7 +18,7 @@ if not torch.cuda.is_available():
     pytest.skip("needs a CUDA GPU", allow_module_level=True)
 
 import pycudapolygon_gb300 as pg  # noqa: E402
-from pycudapolygon_gb300.systems import load_into, make_system  # noqa: E402
+from pycudapolygon_gb300.systems import PolygonSystem, load_into, make_system  # noqa: E402
 from oracle import oracle as orc  # noqa: E402
 
 pg.build()
@@ -124,6 +124,50 @@ def test_contact_records_bit_exact(system, box):
     np.testing.assert_array_equal(g.getNeighborCells(), o.getNeighborCells())
     np.testing.assert_array_equal(g.getNeighborIndices(), o.getNeighborIndices())
     np.testing.assert_array_equal(g.getBoxCounts(), o.getBoxCounts())
+
+
+def _odd_system():
+    """Polygons the self-crossing search must handle: a bow tie, a pentagram,
+    a reflex (non-star from vertex 0) hexagon, a polygon with a repeated
+    vertex, a thin sliver, plus regular polygons overlapping them and one
+    straddling the periodic boundary."""
+    rings = []
+    def at(c, pts, s):
+        return [((c[0] + s * x) % 1.0, (c[1] + s * y) % 1.0) for x, y in pts]
+    rings.append(at((0.20, 0.20), [(0, 0), (1, 1), (1, 0), (0, 1)], 0.05))
+    star = [(np.cos(np.pi / 2 + 4 * np.pi * k / 5), np.sin(np.pi / 2 + 4 * np.pi * k / 5))
+            for k in range(5)]
+    rings.append(at((0.50, 0.50), star, 0.04))
+    rings.append(at((0.80, 0.25), [(0, 0), (2, 0), (2, 2), (1, 0.4), (0, 2), (-0.2, 1)], 0.02))
+    rings.append(at((0.30, 0.70), [(0, 0), (1, 0), (1, 0), (1, 1), (0, 1)], 0.04))
+    rings.append(at((0.70, 0.70), [(0, 0), (1, 0.001), (2, 0), (1, -0.001)], 0.03))
+    reg = lambda n: [(np.cos(2 * np.pi * k / n), np.sin(2 * np.pi * k / n)) for k in range(n)]
+    for c in [(0.22, 0.23), (0.52, 0.48), (0.81, 0.27), (0.31, 0.71), (0.72, 0.70), (0.995, 0.5)]:
+        rings.append(at(c, reg(12), 0.03))
+    n_array = np.array([len(r) for r in rings], dtype=np.int32)
+    start = np.concatenate([[0], np.cumsum(n_array)]).astype(np.int32)
+    pos = np.array([xy for r in rings for xy in r], dtype=np.float64).reshape(-1)
+    P = len(rings)
+    sysobj = PolygonSystem(positions=pos, n_array=n_array, start_indices=start,
+                           target_areas=np.full(P, 1e-3), target_edge_lengths=np.full(P, 0.01),
+                           max_edge_length=0.1, phi=0.0)
+    return sysobj
+
+
+@pytest.mark.parametrize("box", ["system", 1, 3])
+def test_self_crossing_records_bit_exact(box):
+    system = _odd_system()
+    g, o = pair(system)
+    if box != "system":
+        g.setMaxEdgeLength(1.0 / box)
+        o.setMaxEdgeLength(1.0 / box)
+    contacts(g)
+    contacts(o)
+    keys = o.getIntersections().astype(np.uint64)
+    si = (keys >> np.uint64(32)) & np.uint64(0xFFFF)
+    sj = keys >> np.uint64(48)
+    assert np.count_nonzero(si == sj) >= 6      # bow tie 2, pentagram 5 (at least)
+    assert_records_equal(g, o)
 
 
 def test_neighbor_slots_bit_exact(system):
