@@ -1166,7 +1166,21 @@ __global__ void k_fire_bend(double2* __restrict__ vel, const double2* __restrict
     }
 }
 
+__global__ void k_set_fire_params(Ctrl* __restrict__ c, FireScalars f) {
+    c->dt = f.dt; c->alpha = f.alpha; c->nPos = f.nPos;
+    c->dtMax = f.dtMax; c->alphaStart = f.alphaStart; c->fAlpha = f.fAlpha; c->fInc = f.fInc;
+    c->fDec = f.fDec; c->nMin = f.nMin; c->shakeIter = f.shakeIter; c->threshold = f.threshold;
+    c->active = 1;
+    if (f.resetRun) { c->converged = 0; c->stepsDone = 0; }
+    c->stepLimit = f.stepLimit;
+    c->rbBodyKernels = f.rbBodyKernels;
+}
+
 // --------------------------------------------------------------- launchers ----
+cudaError_t launch_set_fire_params(Ctrl* c, const FireScalars& f, cudaStream_t st) {
+    k_set_fire_params<<<1, 1, 0, st>>>(c, f);
+    return cudaGetLastError();
+}
 cudaError_t launch_fire_begin(double2* pos, double2* vel, double2* force, double2* save,
                               double2* velSnap, double2* forceSnap, double2* verlet, int V,
                               int resetContacts, Ctrl* c, const int* gate, cudaStream_t st) {

@@ -77,6 +77,7 @@ struct pcp_model {
     double overlapArea = 0.0;
     bool topology = false;
     bool geometryStale = false;   // geometry of the current positions not yet computed
+    bool geomFromSnapshot = false;  // ... of the positions saved in posGeom instead
     std::vector<int> startHost;
     cudaStream_t stream = nullptr;
     long long launches = 0;
@@ -85,6 +86,7 @@ struct pcp_model {
     // device state
     double2 *pos = nullptr, *force = nullptr, *vel = nullptr;
     double2 *posTMP = nullptr, *posTMP2 = nullptr, *posTent = nullptr;
+    double2* posGeom = nullptr;   // positions the pending geometry belongs to
     double2 *velSnap = nullptr, *forceSnap = nullptr;
     double *edgeLengths = nullptr, *constraints = nullptr, *scratch = nullptr;
     double *areas = nullptr, *comX = nullptr, *comY = nullptr, *perimeters = nullptr;
@@ -126,6 +128,7 @@ struct pcp_model {
         if (evFork) { cudaEventDestroy(evFork); evFork = nullptr; }
         if (evJoin) { cudaEventDestroy(evJoin); evJoin = nullptr; }
         dfree(&pos); dfree(&force); dfree(&vel); dfree(&posTMP); dfree(&posTMP2); dfree(&posTent);
+        dfree(&posGeom);
         dfree(&velSnap); dfree(&forceSnap);
         dfree(&edgeLengths); dfree(&constraints); dfree(&scratch);
         dfree(&areas); dfree(&comX); dfree(&comY); dfree(&perimeters);
@@ -154,7 +157,10 @@ int alloc_vertex(pcp_model* m) {
     size_t V = (size_t)m->V;
     CK(dalloc(&m->pos, V)); CK(dalloc(&m->force, V)); CK(dalloc(&m->vel, V));
     CK(dalloc(&m->posTMP, V)); CK(dalloc(&m->posTMP2, V)); CK(dalloc(&m->posTent, V));
+    CK(dalloc(&m->posGeom, V));
     CK(dalloc(&m->velSnap, V)); CK(dalloc(&m->forceSnap, V));
+    m->geometryStale = false;
+    m->geomFromSnapshot = false;
     CK(dalloc(&m->edgeLengths, V)); CK(dalloc(&m->constraints, 6 * V));
     CK(dalloc(&m->scratch, (size_t)kScratchPerVertex * V));
     m->generation++;
@@ -448,8 +454,9 @@ int force_energy(pcp_model* m, const int* gate, bool zeroed = false) {
     return PCP_OK;
 }
 
-int geometry(pcp_model* m, const int* gate) {
-    CK(launch_geometry(m->pos, m->start, m->P, m->V, m->edgeLengths, m->areas, m->comX, m->comY,
+int geometry(pcp_model* m, const int* gate, const double2* src = nullptr) {
+    CK(launch_geometry(src ? src : m->pos, m->start, m->P, m->V, m->edgeLengths, m->areas,
+                       m->comX, m->comY,
                        m->perimeters, m->constraints, m->maxEdge, gate, m->stream));
     m->launches += 2;
     return PCP_OK;
@@ -460,7 +467,20 @@ int geometry(pcp_model* m, const int* gate) {
 int ensure_geometry(pcp_model* m) {
     if (!m->geometryStale) return PCP_OK;
     m->geometryStale = false;
-    return geometry(m, nullptr);
+    bool snap = m->geomFromSnapshot;
+    m->geomFromSnapshot = false;
+    return geometry(m, nullptr, snap ? m->posGeom : nullptr);
+}
+
+// The positions are about to change while their geometry is still pending:
+// keep a copy of them (a device-to-device copy instead of the geometry pass)
+// so the getters later see the geometry the reference computed at that point.
+int snapshot_geometry(pcp_model* m) {
+    if (!m->geometryStale || m->geomFromSnapshot) return PCP_OK;
+    CK(cudaMemcpyAsync(m->posGeom, m->pos, (size_t)m->V * sizeof(double2),
+                       cudaMemcpyDeviceToDevice, m->stream));
+    m->geomFromSnapshot = true;
+    return PCP_OK;
 }
 
 // ---- FIRE step graph ------------------------------------------------------
@@ -655,20 +675,14 @@ struct FireParams {
     int nPos, nMin, shakeIter, stepLimit;
 };
 
-// write the step parameters into the device control block
+// write the step parameters into the device control block (a one-thread
+// kernel on the model's stream: no host round trip)
 int set_fire_params(pcp_model* m, const FireParams& f, bool resetRun) {
-    int rc = read_ctrl(m);
-    if (rc) return rc;
-    Ctrl& c = *m->ctrlHost;
-    c.dt = f.dt; c.alpha = f.alpha; c.nPos = f.nPos;
-    c.dtMax = f.dtMax; c.alphaStart = f.alphaStart; c.fAlpha = f.fAlpha; c.fInc = f.fInc;
-    c.fDec = f.fDec; c.nMin = f.nMin; c.shakeIter = f.shakeIter; c.threshold = f.threshold;
-    c.active = 1;
-    if (resetRun) { c.converged = 0; c.stepsDone = 0; }
-    c.stepLimit = f.stepLimit;
-    c.rbBodyKernels = m->rbBodyKernels;
-    CK(cudaMemcpyAsync(m->ctrl, m->ctrlHost, sizeof(Ctrl), cudaMemcpyHostToDevice, m->stream));
-    return sync(m);
+    FireScalars d{f.dt, f.alpha, f.dtMax, f.alphaStart, f.fAlpha, f.fInc, f.fDec, f.threshold,
+                  f.nPos, f.nMin, f.shakeIter, f.stepLimit, resetRun ? 1 : 0, m->rbBodyKernels};
+    CK(launch_set_fire_params(m->ctrl, d, m->stream));
+    m->launches++;
+    return PCP_OK;
 }
 
 // A contact buffer overflowed inside a FIRE step: the step stopped itself
@@ -719,7 +733,10 @@ int fire_step_once(pcp_model* m, const FireParams& fp, double out[4]) {
             m->numIntersections = c.numRecords;
             m->view = pcp_model::VIEW_FINAL;
             m->invalidate();
-            if (m->modelType == PCP_MODEL_NORMAL) m->geometryStale = true;
+            if (m->modelType == PCP_MODEL_NORMAL) {
+                m->geometryStale = true;
+                m->geomFromSnapshot = false;
+            }
             return PCP_OK;
         }
     }
@@ -792,7 +809,7 @@ int pcp_model_set_num_vertices(pcp_model* m, int n) {
 }
 
 int pcp_model_set_positions(pcp_model* m, const double* host, int len) {
-    if (m && m->geometryStale) { int grc = ensure_geometry(m); if (grc) return grc; }
+    if (m && m->geometryStale) { int grc = snapshot_geometry(m); if (grc) return grc; }
     CHECK_M(m);
     if (len != 2 * m->V) {
         printf("Update numVertices before setting the positions\n");   // model.cpp:524
@@ -908,7 +925,7 @@ int pcp_model_initialize_neighbor_cells(pcp_model* m) {
 }
 
 int pcp_model_update_polygon_geometry(pcp_model* m) {
-    if (m) m->geometryStale = false;
+    if (m) { m->geometryStale = false; m->geomFromSnapshot = false; }
     CHECK_M(m);
     int rc = need_topology(m);
     if (rc) return rc;
@@ -989,7 +1006,7 @@ int pcp_model_project_force(pcp_model* m) {
 }
 
 int pcp_model_shake_project(pcp_model* m, int n_iter, double tol, int* iters_out) {
-    if (m && m->geometryStale) { int grc = ensure_geometry(m); if (grc) return grc; }
+    if (m && m->geometryStale) { int grc = snapshot_geometry(m); if (grc) return grc; }
     CHECK_M(m);
     int rc = need_topology(m);
     if (rc) return rc;
@@ -1009,7 +1026,7 @@ int pcp_model_shake_project(pcp_model* m, int n_iter, double tol, int* iters_out
 }
 
 int pcp_model_xpbd_project(pcp_model* m, int n_iter, double tol, int* iters_out) {
-    if (m && m->geometryStale) { int grc = ensure_geometry(m); if (grc) return grc; }
+    if (m && m->geometryStale) { int grc = snapshot_geometry(m); if (grc) return grc; }
     CHECK_M(m);
     int rc = need_topology(m);
     if (rc) return rc;
@@ -1034,7 +1051,7 @@ int pcp_model_xpbd_project(pcp_model* m, int n_iter, double tol, int* iters_out)
 }
 
 int pcp_model_update_positions(pcp_model* m, double dt) {
-    if (m && m->geometryStale) { int grc = ensure_geometry(m); if (grc) return grc; }
+    if (m && m->geometryStale) { int grc = snapshot_geometry(m); if (grc) return grc; }
     CHECK_M(m);
     CK(launch_update_positions(reinterpret_cast<double*>(m->pos), reinterpret_cast<const double*>(m->force),
                                m->V, dt, m->stream));
@@ -1153,6 +1170,7 @@ int pcp_model_minimize_fire(pcp_model* m, double thr, double dt0, int max_steps,
     rc = pcp_model_reset_velocities(m);
     if (rc) return rc;
     m->geometryStale = false;
+    m->geomFromSnapshot = false;
     rc = geometry(m, nullptr);
     if (rc) return rc;
     rc = force_energy(m, nullptr);
@@ -1198,7 +1216,10 @@ int pcp_model_minimize_fire(pcp_model* m, double thr, double dt0, int max_steps,
     m->numIntersections = c.numRecords;
     m->view = pcp_model::VIEW_FINAL;
     m->invalidate();
-    if (m->modelType == PCP_MODEL_NORMAL && c.stepsDone > 0) m->geometryStale = true;
+    if (m->modelType == PCP_MODEL_NORMAL && c.stepsDone > 0) {
+        m->geometryStale = true;
+        m->geomFromSnapshot = false;
+    }
     out[0] = c.converged ? c.outE : c.energy;
     out[1] = c.dt;
     out[2] = c.stepsDone;
@@ -1214,6 +1235,7 @@ int pcp_model_fire_setup(pcp_model* m, double thr, double dt0, int max_steps, do
     rc = pcp_model_reset_velocities(m);
     if (rc) return rc;
     m->geometryStale = false;
+    m->geomFromSnapshot = false;
     rc = geometry(m, nullptr);
     if (rc) return rc;
     rc = force_energy(m, nullptr);
@@ -1234,7 +1256,10 @@ int pcp_model_fire_continue(pcp_model* m, int n_steps) {
     if (!m->fireExec) return fail(PCP_ERR_STATE, "pcp_model_fire_setup has not been called");
     for (int s = 0; s < n_steps; ++s) CK(cudaGraphLaunch(m->fireExec, m->stream));
     m->launches += (long long)n_steps * m->fireKernelNodes;
-    if (n_steps > 0 && m->modelType == PCP_MODEL_NORMAL) m->geometryStale = true;
+    if (n_steps > 0 && m->modelType == PCP_MODEL_NORMAL) {
+        m->geometryStale = true;
+        m->geomFromSnapshot = false;
+    }
     return PCP_OK;
 }
 

@@ -181,6 +181,14 @@ cudaError_t launch_xpbd_iteration(double2* pos, const int* start, int P,
                                   const double* targetEdge, const double* targetArea,
                                   double* devOut, cudaStream_t st);
 
+// FIRE parameters of a run, written into Ctrl by one thread on the stream
+// (no host round trip)
+struct FireScalars {
+    double dt, alpha, dtMax, alphaStart, fAlpha, fInc, fDec, threshold;
+    int nPos, nMin, shakeIter, stepLimit, resetRun, rbBodyKernels;
+};
+cudaError_t launch_set_fire_params(Ctrl* c, const FireScalars& f, cudaStream_t st);
+
 // FIRE pieces (device-resident scalars in Ctrl)
 cudaError_t launch_fire_begin(double2* pos, double2* vel, double2* force, double2* save,
                               double2* velSnap, double2* forceSnap, double2* verlet, int V,
