@@ -132,6 +132,7 @@ k_project(const double2* __restrict__ pos, const int* __restrict__ start, int P,
           double* __restrict__ scratch, int V, int smemN, int areaFromPositions, Ctrl* fire,
           double2* __restrict__ vel, cudaGraphConditionalHandle rbCond, int useCond,
           const int* gate) {
+    pdl_enter();
     if (gate_closed(gate)) return;
     extern __shared__ double cons_smem[];
     int p = blockIdx.x * blockDim.x + threadIdx.x;
@@ -304,7 +305,7 @@ __device__ __forceinline__ int pow2_at_least(int n) {
 
 struct ShakeWS {
     double2 *xs, *r, *ar;
-    float2 *rf, *arf, *ef, *acf;
+    float2 *rf, *arf, *ef;
     float *vr, *lam;
     float *pa, *pb, *pc, *p0, *p1, *p2;   // [2][N] each
 };
@@ -314,8 +315,8 @@ __device__ __forceinline__ ShakeWS shake_ws(unsigned char* base, int NV, int N) 
     double2* d = reinterpret_cast<double2*>(base);
     w.xs = d; w.r = d + NV; w.ar = d + 2 * NV;
     float2* f2 = reinterpret_cast<float2*>(d + 3 * NV);
-    w.rf = f2; w.arf = f2 + NV; w.ef = f2 + 2 * NV; w.acf = f2 + 3 * NV;
-    float* f = reinterpret_cast<float*>(f2 + 4 * NV);
+    w.rf = f2; w.arf = f2 + NV; w.ef = f2 + 2 * NV;
+    float* f = reinterpret_cast<float*>(f2 + 3 * NV);
     w.vr = f; w.lam = f + NV;
     float* q = f + 2 * NV;
     w.pa = q; w.pb = q + 2 * N; w.pc = q + 4 * N; w.p0 = q + 6 * N; w.p1 = q + 8 * N; w.p2 = q + 10 * N;
@@ -324,7 +325,7 @@ __device__ __forceinline__ ShakeWS shake_ws(unsigned char* base, int NV, int N) 
 // bytes of one polygon's workspace (NV vertex slots, N PCR rows); a multiple
 // of 16 whenever NV is even
 __host__ __device__ constexpr size_t shake_ws_bytes(int NV, int N) {
-    return (size_t)NV * (3 * 16 + 4 * 8 + 2 * 4) + (size_t)N * 12 * 4;
+    return (size_t)NV * (3 * 16 + 3 * 8 + 2 * 4) + (size_t)N * 12 * 4;
 }
 
 // Parallel cyclic reduction of N rows (arrays [2][N]: buffer 0 holds the
@@ -395,11 +396,12 @@ __device__ __forceinline__ bool sm_split(float* pa, float* pb, float* pc, float*
     return ok;
 }
 
-__global__ void k_shake(double2* __restrict__ pos, const int* __restrict__ start, int P,
+__global__ void __launch_bounds__(256, 4) k_shake(double2* __restrict__ pos, const int* __restrict__ start, int P,
                         const double* __restrict__ targetEdge,
                         const double* __restrict__ targetArea, int maxIter, double tol,
                         int* __restrict__ itersOut, double* __restrict__ scratch, int nmaxSmem,
                         Ctrl* fire, cudaGraphConditionalHandle retryCond, const int* gate) {
+    pdl_enter();
     if (gate_closed(gate)) return;
     extern __shared__ __align__(16) unsigned char shake_smem[];
     const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
@@ -422,6 +424,9 @@ __global__ void k_shake(double2* __restrict__ pos, const int* __restrict__ start
                              n, N);
             }
             const double L = targetEdge[p], A0 = targetArea[p];
+            // worst < tol on bit patterns (tol <= 0 or NaN: never)
+            const unsigned long long tolBits =
+                tol > 0.0 ? (unsigned long long)__double_as_longlong(tol) : 0ull;
             const double invL = L > 0.0 ? 1.0 / L : 1.0;
             for (int k = lane; k < n; k += 32) w.xs[k] = pos[st + k];
             __syncwarp();
@@ -431,13 +436,16 @@ __global__ void k_shake(double2* __restrict__ pos, const int* __restrict__ start
                 double2 r = make_double2(wrap(xn.x - xk.x), wrap(xn.y - xk.y));
                 double2 a = make_double2(0.5 * wrap(xn.y - xp.y), 0.5 * wrap(xp.x - xn.x));
                 w.r[k] = r; w.ar[k] = a;
-                w.rf[k] = make_float2((float)r.x, (float)r.y);
-                w.arf[k] = make_float2((float)a.x, (float)a.y);
+                w.rf[k] = make_float2(d2f_int(r.x), d2f_int(r.y));
+                w.arf[k] = make_float2(d2f_int(a.x), d2f_int(a.y));
             }
             __syncwarp();
             for (; it < maxIter; ++it) {
                 // residuals (FP64)
-                double worst = 0.0, area = 0.0;
+                // worst residual as the bit pattern of a non-negative double
+                // (patterns order like the values; NaN sorts highest)
+                unsigned long long worst = 0ull;
+                double area = 0.0;
                 bool nonfinite = false;
                 double x0x = w.xs[0].x;
                 for (int k = lane; k < n; k += 32) {
@@ -445,29 +453,35 @@ __global__ void k_shake(double2* __restrict__ pos, const int* __restrict__ start
                     double2 xk = w.xs[k], xn = w.xs[kn], xp = w.xs[kp];
                     double ex = wrap(xn.x - xk.x), ey = wrap(xn.y - xk.y);
                     double sk = 0.5 * (ex * ex + ey * ey - L * L);
-                    double q = fabs(sk) * invL;
-                    if (!(q <= worst)) { worst = q; nonfinite |= !isfinite(q); }
+                    unsigned long long q = abs_bits(sk * invL);
+                    if (q > worst) worst = q;
                     double X1 = wrap(xk.x - x0x), X2 = wrap(xn.x - x0x);
                     area += ey * (X2 + X1) / 2.0;
-                    w.ef[k] = make_float2((float)ex, (float)ey);
-                    w.acf[k] = make_float2((float)(0.5 * wrap(xn.y - xp.y)),
-                                           (float)(0.5 * wrap(xp.x - xn.x)));
-                    w.lam[k] = (float)(-sk);      // right-hand side until the rows are built
+                    w.ef[k] = make_float2(d2f_int(ex), d2f_int(ey));
+                    w.lam[k] = d2f_int(-sk);      // right-hand side until the rows are built
                 }
-                worst = warp_maxd(worst);
+                worst = warp_max_u64(worst);
                 area = warp_sum(area);
                 nonfinite = __any_sync(PCP_FULL, nonfinite);
                 double sA = area - A0;
-                if (!(fabs(sA) <= worst)) worst = fabs(sA);
-                if (nonfinite || !isfinite(worst)) { it = maxIter; break; }
-                if (worst < tol) break;
+                {
+                    unsigned long long qa = abs_bits(sA);
+                    if (qa > worst) worst = qa;
+                }
+                if (nonfinite || !finite_bits(worst)) { it = maxIter; break; }
+                if (worst < tolBits) break;
                 __syncwarp();
                 // rows of G(x) G_ref^T (FP32) into PCR buffer 0
                 float dc = 0.f;
                 for (int k = lane; k < n; k += 32) {
                     int kn = (k + 1 == n) ? 0 : k + 1, kp = (k == 0) ? n - 1 : k - 1;
                     float2 e = w.ef[k], rk = w.rf[k], rn = w.rf[kn], rp = w.rf[kp];
-                    float2 an = w.arf[kn], ak = w.arf[k], cn = w.acf[kn], ck = w.acf[k];
+                    float2 an = w.arf[kn], ak = w.arf[k];
+                    // current area gradient at k and k+1 from the FP32 edge
+                    // vectors: (x_k+1 - x_k-1) / 2 rotated, as in the residual
+                    float2 ep = w.ef[kp], en = w.ef[kn];
+                    float2 ck = make_float2(0.5f * (e.y + ep.y), -0.5f * (e.x + ep.x));
+                    float2 cn = make_float2(0.5f * (en.y + e.y), -0.5f * (en.x + e.x));
                     w.pb[k] = 2.0f * (e.x * rk.x + e.y * rk.y);
                     w.pc[k] = -(e.x * rn.x + e.y * rn.y);
                     w.pa[k] = -(e.x * rp.x + e.y * rp.y);
@@ -516,7 +530,7 @@ __global__ void k_shake(double2* __restrict__ pos, const int* __restrict__ start
                     vy += __shfl_xor_sync(PCP_FULL, vy, o);
                     vz += __shfl_xor_sync(PCP_FULL, vz, o);
                 }
-                float mu = (-(float)sA - vy) / (dc - vz);
+                float mu = (-d2f_int(sA) - vy) / (dc - vz);
                 bool finite = isfinite(mu);
                 __syncwarp();
                 for (int k = lane; k < n; k += 32) {
@@ -527,10 +541,10 @@ __global__ void k_shake(double2* __restrict__ pos, const int* __restrict__ start
                 if (!__all_sync(PCP_FULL, finite)) { it = maxIter; break; }
                 __syncwarp();
                 // x_k += -l_k r_k + l_{k-1} r_{k-1} + mu ar_k   (FP64)
-                double mu64 = (double)mu;
+                double mu64 = f2d_int(mu);
                 for (int k = lane; k < n; k += 32) {
                     int kp = (k == 0) ? n - 1 : k - 1;
-                    double lk = (double)w.lam[k], lp = (double)w.lam[kp];
+                    double lk = f2d_int(w.lam[k]), lp = f2d_int(w.lam[kp]);
                     double2 rk = w.r[k], rp = w.r[kp], ak = w.ar[k];
                     double2 x = w.xs[k];
                     x.x += -lk * rk.x + lp * rp.x + mu64 * ak.x;
@@ -584,7 +598,7 @@ cudaError_t launch_shake(double2* pos, const int* start, int P, int nmax, const 
     int nmaxSmem = nv;
     if (per * wpb > 200 * 1024) { nmaxSmem = 0; per = 0; wpb = 8; }
     size_t smem = per * wpb;
-    k_shake<<<nblk(P, wpb), 32 * wpb, smem, st>>>(pos, start, P, targetEdge, targetArea, maxIter,
+    launch_k(k_shake, dim3(nblk(P, wpb)), dim3(32 * wpb), smem, st, pos, start, P, targetEdge, targetArea, maxIter,
                                                    tol, maxItersOut, scratch, nmaxSmem, fire,
                                                    retryCond, gate);
     return cudaGetLastError();
@@ -626,12 +640,13 @@ __host__ __device__ constexpr size_t proj_ws_bytes(int NV, int N) {
     return (size_t)NV * (48 + 8) + (size_t)N * 12 * 4;
 }
 
-__global__ void k_project_warp(const double2* __restrict__ pos, const int* __restrict__ start,
+__global__ void __launch_bounds__(256, 4) k_project_warp(const double2* __restrict__ pos, const int* __restrict__ start,
                                int P, const double* __restrict__ constraints,
                                double2* __restrict__ force, double* __restrict__ scratch,
                                int nmaxSmem, int areaFromPositions, Ctrl* fire,
                                double2* __restrict__ vel, cudaGraphConditionalHandle rbCond,
                                int useCond, const int* gate) {
+    pdl_enter();
     if (gate_closed(gate)) return;
     extern __shared__ __align__(16) unsigned char proj_smem[];
     const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
@@ -653,7 +668,8 @@ __global__ void k_project_warp(const double2* __restrict__ pos, const int* __res
             if (useCond) cudaGraphSetConditional(rbCond, (unsigned int)go);
         }
     }
-    double sP = 0.0, sV = 0.0, sF = 0.0, mF = 0.0;
+    double sP = 0.0, sV = 0.0, sF = 0.0;
+    unsigned long long mF = 0ull;      // max |F component| as a bit pattern
     bool bad = false;
     if (p < P) {
         int st = start[p], n = start[p + 1] - st;
@@ -675,7 +691,10 @@ __global__ void k_project_warp(const double2* __restrict__ pos, const int* __res
                 double dx = wrap(xn.x - xk.x), dy = wrap(xn.y - xk.y);
                 double len2 = dx * dx + dy * dy;
                 double2 t = make_double2(0.0, 0.0);
-                bool ok = !(len2 < 1e-28);          // |e| >= 1e-14 (kernels.cuh:399)
+                // |e| >= 1e-14 (kernels.cuh:399); len2 >= 0, so its bit
+                // pattern orders like its value (NaN counts as long)
+                bool ok = (unsigned long long)__double_as_longlong(len2) >=
+                          (unsigned long long)__double_as_longlong(1e-28);
                 if (ok) { double il = rsqrt(len2); t = make_double2(dx * il, dy * il); }
                 w.t[k] = t;
                 w.mb[k] = ok ? 2.0f : 1.0f;
@@ -693,7 +712,7 @@ __global__ void k_project_warp(const double2* __restrict__ pos, const int* __res
             }
             if (areaFromPositions) {
                 an = warp_sum(an);
-                double ir = an > 0.0 ? 1.0 / sqrt(an) : 1.0;
+                double ir = an > 0.0 ? rsqrt(an) : 1.0;
                 for (int k = lane; k < n; k += 32) {
                     double2 a = w.q[k];
                     w.q[k] = make_double2(a.x * ir, a.y * ir);
@@ -703,7 +722,7 @@ __global__ void k_project_warp(const double2* __restrict__ pos, const int* __res
             for (int k = lane; k < n; k += 32) {
                 int kn = (k + 1 == n) ? 0 : k + 1;
                 double2 t = w.t[k], tn = w.t[kn];
-                w.mc[k] = (float)(-(t.x * tn.x + t.y * tn.y));
+                w.mc[k] = d2f_int(-(t.x * tn.x + t.y * tn.y));
             }
             __syncwarp();
             for (int round = 0; round < kProjRounds && !bad; ++round) {
@@ -711,8 +730,8 @@ __global__ void k_project_warp(const double2* __restrict__ pos, const int* __res
                 for (int k = lane; k < n; k += 32) {
                     int kn = (k + 1 == n) ? 0 : k + 1, kp = (k == 0) ? n - 1 : k - 1;
                     double2 t = w.t[k], f0 = w.f[k], f1 = w.f[kn], a0 = w.q[k], a1 = w.q[kn];
-                    w.p0[k] = (float)(t.x * (f1.x - f0.x) + t.y * (f1.y - f0.y));
-                    w.p1[k] = (float)(t.x * (a1.x - a0.x) + t.y * (a1.y - a0.y));
+                    w.p0[k] = d2f_int(t.x * (f1.x - f0.x) + t.y * (f1.y - f0.y));
+                    w.p1[k] = d2f_int(t.x * (a1.x - a0.x) + t.y * (a1.y - a0.y));
                     w.p2[k] = 0.f;
                     w.pb[k] = w.mb[k];
                     w.pc[k] = w.mc[k];
@@ -740,8 +759,8 @@ __global__ void k_project_warp(const double2* __restrict__ pos, const int* __res
                 for (int k = lane; k < n; k += 32) {
                     int kp = (k == 0) ? n - 1 : k - 1;
                     double2 t = w.t[k], tp = w.t[kp];
-                    double l0 = (double)w.p0[k], l0p = (double)w.p0[kp];
-                    double l1 = (double)w.p1[k], l1p = (double)w.p1[kp];
+                    double l0 = f2d_int(w.p0[k]), l0p = f2d_int(w.p0[kp]);
+                    double l1 = f2d_int(w.p1[k]), l1p = f2d_int(w.p1[kp]);
                     double2 f = w.f[k], a = w.q[k];
                     f.x -= -l0 * t.x + l0p * tp.x; f.y -= -l0 * t.y + l0p * tp.y;
                     a.x -= -l1 * t.x + l1p * tp.x; a.y -= -l1 * t.y + l1p * tp.y;
@@ -758,12 +777,13 @@ __global__ void k_project_warp(const double2* __restrict__ pos, const int* __res
                 }
                 qF = warp_sum(qF);
                 qq = warp_sum(qq);
-                double coef = (sqrt(qq) > 1e-14) ? qF / qq : 0.0;   // kernels.cuh:464
+                // sqrt(qq) > 1e-14 (kernels.cuh:464)
+                double coef = (qq > 1e-28) ? qF / qq : 0.0;
                 for (int k = lane; k < n; k += 32) {
                     double2 f = w.f[k], q = w.q[k];
                     double fx = f.x - coef * q.x, fy = f.y - coef * q.y;
                     force[st + k] = make_double2(fx, fy);
-                    mF = fmax(mF, fmax(fabs(fx), fabs(fy)));
+                    mF = max_abs_bits(mF, fx, fy);
                     if (proceed) {
                         double2 v = vel[st + k];
                         v.x += 0.5 * dt * fx;
@@ -778,7 +798,7 @@ __global__ void k_project_warp(const double2* __restrict__ pos, const int* __res
         } else {
             for (int k = lane; k < n; k += 32) {
                 double2 f = force[st + k];
-                mF = fmax(mF, fmax(fabs(f.x), fabs(f.y)));
+                mF = max_abs_bits(mF, f.x, f.y);
                 if (proceed) {
                     double2 v = vel[st + k];
                     v.x += 0.5 * dt * f.x; v.y += 0.5 * dt * f.y;
@@ -792,8 +812,8 @@ __global__ void k_project_warp(const double2* __restrict__ pos, const int* __res
     }
     if (fire) {
         if (bad && lane == 0) atomicOr(&fire->flags, kFlagNonFinite);
-        mF = warp_maxd(mF);
-        if (lane == 0) atomic_max_nonneg(&fire->maxF, mF);
+        mF = warp_max_u64(mF);
+        if (lane == 0 && mF) atomicMax(reinterpret_cast<unsigned long long*>(&fire->maxF), mF);
         if (proceed) {
             sP = warp_sum(sP); sV = warp_sum(sV); sF = warp_sum(sF);
             if (lane == 0) {
@@ -830,7 +850,7 @@ cudaError_t launch_project(const double2* pos, const int* start, int P, int nmax
     if (P >= 128 * sm_count()) {
         int sn = smem_vertices(nmax, kProjArrays);
         size_t smem = (size_t)sn * kProjArrays * kConsThreads * sizeof(double);
-        k_project<<<nblk(P, kConsThreads), kConsThreads, smem, st>>>(
+        launch_k(k_project, dim3(nblk(P, kConsThreads)), dim3(kConsThreads), smem, st, 
             pos, start, P, constraints, force, scratch, V, sn, areaFromPositions, fireCtrl, vel,
             rbCond, useCond, gate);
         return cudaGetLastError();
@@ -843,7 +863,7 @@ cudaError_t launch_project(const double2* pos, const int* start, int P, int nmax
     while (wpb > 1 && per * wpb > 200 * 1024) wpb >>= 1;
     int nmaxSmem = nv;
     if (per * wpb > 200 * 1024) { nmaxSmem = 0; per = 0; wpb = 8; }
-    k_project_warp<<<nblk(P, wpb), 32 * wpb, per * wpb, st>>>(pos, start, P, constraints, force,
+    launch_k(k_project_warp, dim3(nblk(P, wpb)), dim3(32 * wpb), per * wpb, st, pos, start, P, constraints, force,
                                                               scratch, nmaxSmem, areaFromPositions,
                                                               fireCtrl, vel, rbCond, useCond, gate);
     return cudaGetLastError();
@@ -859,6 +879,7 @@ cudaError_t launch_project(const double2* pos, const int* start, int P, int nmax
 __global__ void k_xpbd(double2* __restrict__ pos, const int* __restrict__ start, int P,
                        const double* __restrict__ tl, const double* __restrict__ ta,
                        double* __restrict__ devOut) {
+    pdl_enter();
     int p = blockIdx.x * blockDim.x + threadIdx.x;
     if (p >= P) return;
     int st = start[p], n = start[p + 1] - st;
@@ -916,7 +937,7 @@ cudaError_t launch_xpbd_iteration(double2* pos, const int* start, int P,
                                   const double* targetEdge, const double* targetArea,
                                   double* devOut, cudaStream_t st) {
     if (P <= 0) return cudaSuccess;
-    k_xpbd<<<nblk(P, 128), 128, 0, st>>>(pos, start, P, targetEdge, targetArea, devOut);
+    launch_k(k_xpbd, dim3(nblk(P, 128)), dim3(128), 0, st, pos, start, P, targetEdge, targetArea, devOut);
     return cudaGetLastError();
 }
 
@@ -948,6 +969,7 @@ __global__ void k_fire_begin(double2* __restrict__ pos, double2* __restrict__ ve
                              double2* __restrict__ velSnap, double2* __restrict__ forceSnap,
                              double2* __restrict__ verlet, int V, int resetContacts,
                              Ctrl* __restrict__ c, const int* gate) {
+    pdl_enter();
     if (gate_closed(gate)) return;
     int i = blockIdx.x * blockDim.x + threadIdx.x;
     const double dt = c->dt;
@@ -986,6 +1008,7 @@ __global__ void k_fire_after_shake(double2* __restrict__ pos, double2* __restric
                                    const double2* __restrict__ save,
                                    const double2* __restrict__ verlet, int V,
                                    Ctrl* __restrict__ c, const int* gate) {
+    pdl_enter();
     if (gate_closed(gate)) return;
     int i = blockIdx.x * blockDim.x + threadIdx.x;
     const bool retried = c->needRetry != 0;
@@ -1014,6 +1037,7 @@ __global__ void k_fire_after_shake(double2* __restrict__ pos, double2* __restric
 __global__ void k_fire_rollback(double2* __restrict__ pos, double2* __restrict__ vel,
                                 double2* __restrict__ force, const double2* __restrict__ save,
                                 int V, int resetContacts, Ctrl* __restrict__ c) {
+    pdl_enter();
     int i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i == 0) {
         c->rollback = 1;
@@ -1031,6 +1055,7 @@ __global__ void k_fire_rollback(double2* __restrict__ pos, double2* __restrict__
 // zero force + energy (+ maxF) under a gate (updateForceEnergy's memsets)
 __global__ void k_zero_force(double2* __restrict__ force, int V, Ctrl* __restrict__ c,
                              const int* gate) {
+    pdl_enter();
     if (gate_closed(gate)) return;
     int i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i == 0) { c->energy = 0.0; c->maxF = 0.0; }
@@ -1043,6 +1068,7 @@ __global__ void k_zero_force(double2* __restrict__ force, int V, Ctrl* __restric
 __global__ void k_fire_velocity(double2* __restrict__ vel, const double2* __restrict__ force,
                                 int V, Ctrl* __restrict__ c, cudaGraphConditionalHandle rbCond,
                                 int useCond, const int* gate) {
+    pdl_enter();
     if (gate_closed(gate)) return;
     int i = blockIdx.x * blockDim.x + threadIdx.x;
     double E = c->energy, E0 = c->ePre;
@@ -1081,6 +1107,7 @@ __global__ void k_fire_velocity(double2* __restrict__ vel, const double2* __rest
 // max |F| only (rollback path of models without projection)
 __global__ void k_fire_maxf(const double2* __restrict__ force, int V, Ctrl* __restrict__ c,
                             const int* gate) {
+    pdl_enter();
     if (gate_closed(gate)) return;
     int i = blockIdx.x * blockDim.x + threadIdx.x;
     double mF = 0.0;
@@ -1131,6 +1158,7 @@ __device__ void fire_scalars(Ctrl* __restrict__ c) {
 // read alpha, P, |v|, |F| before it takes its ticket).
 __global__ void k_fire_bend(double2* __restrict__ vel, const double2* __restrict__ force,
                             int V, Ctrl* __restrict__ c, const int* gate) {
+    pdl_enter();
     if (gate_closed(gate)) return;
     __shared__ double s_coef[3];
     if (threadIdx.x == 0) {
@@ -1167,6 +1195,7 @@ __global__ void k_fire_bend(double2* __restrict__ vel, const double2* __restrict
 }
 
 __global__ void k_set_fire_params(Ctrl* __restrict__ c, FireScalars f) {
+    pdl_enter();
     c->dt = f.dt; c->alpha = f.alpha; c->nPos = f.nPos;
     c->dtMax = f.dtMax; c->alphaStart = f.alphaStart; c->fAlpha = f.fAlpha; c->fInc = f.fInc;
     c->fDec = f.fDec; c->nMin = f.nMin; c->shakeIter = f.shakeIter; c->threshold = f.threshold;
@@ -1178,45 +1207,45 @@ __global__ void k_set_fire_params(Ctrl* __restrict__ c, FireScalars f) {
 
 // --------------------------------------------------------------- launchers ----
 cudaError_t launch_set_fire_params(Ctrl* c, const FireScalars& f, cudaStream_t st) {
-    k_set_fire_params<<<1, 1, 0, st>>>(c, f);
+    launch_k(k_set_fire_params, dim3(1), dim3(1), 0, st, c, f);
     return cudaGetLastError();
 }
 cudaError_t launch_fire_begin(double2* pos, double2* vel, double2* force, double2* save,
                               double2* velSnap, double2* forceSnap, double2* verlet, int V,
                               int resetContacts, Ctrl* c, const int* gate, cudaStream_t st) {
-    k_fire_begin<<<nblk(V, 256), 256, 0, st>>>(pos, vel, force, save, velSnap, forceSnap, verlet,
+    launch_k(k_fire_begin, dim3(nblk(V, 256)), dim3(256), 0, st, pos, vel, force, save, velSnap, forceSnap, verlet,
                                                V, resetContacts, c, gate);
     return cudaGetLastError();
 }
 cudaError_t launch_fire_after_shake(double2* pos, double2* vel, const double2* save,
                                     const double2* verlet, int V, Ctrl* c, const int* gate,
                                     cudaStream_t st) {
-    k_fire_after_shake<<<nblk(V, 256), 256, 0, st>>>(pos, vel, save, verlet, V, c, gate);
+    launch_k(k_fire_after_shake, dim3(nblk(V, 256)), dim3(256), 0, st, pos, vel, save, verlet, V, c, gate);
     return cudaGetLastError();
 }
 cudaError_t launch_fire_rollback(double2* pos, double2* vel, double2* force, const double2* save,
                                  int V, int resetContacts, Ctrl* c, cudaStream_t st) {
-    k_fire_rollback<<<nblk(V, 256), 256, 0, st>>>(pos, vel, force, save, V, resetContacts, c);
+    launch_k(k_fire_rollback, dim3(nblk(V, 256)), dim3(256), 0, st, pos, vel, force, save, V, resetContacts, c);
     return cudaGetLastError();
 }
 cudaError_t launch_zero_force(double2* force, int V, Ctrl* c, const int* gate, cudaStream_t st) {
-    k_zero_force<<<nblk(V, 256), 256, 0, st>>>(force, V, c, gate);
+    launch_k(k_zero_force, dim3(nblk(V, 256)), dim3(256), 0, st, force, V, c, gate);
     return cudaGetLastError();
 }
 cudaError_t launch_fire_velocity(double2* vel, const double2* force, int V, Ctrl* c,
                                  cudaGraphConditionalHandle rbCond, int useCond,
                                  const int* gate, cudaStream_t st) {
-    k_fire_velocity<<<nblk(V, 256), 256, 0, st>>>(vel, force, V, c, rbCond, useCond, gate);
+    launch_k(k_fire_velocity, dim3(nblk(V, 256)), dim3(256), 0, st, vel, force, V, c, rbCond, useCond, gate);
     return cudaGetLastError();
 }
 cudaError_t launch_fire_maxf(const double2* force, int V, Ctrl* c, const int* gate,
                              cudaStream_t st) {
-    k_fire_maxf<<<nblk(V, 256), 256, 0, st>>>(force, V, c, gate);
+    launch_k(k_fire_maxf, dim3(nblk(V, 256)), dim3(256), 0, st, force, V, c, gate);
     return cudaGetLastError();
 }
 cudaError_t launch_fire_finish(double2* vel, const double2* force, int V, Ctrl* c,
                                const int* gate, cudaStream_t st) {
-    k_fire_bend<<<nblk(V, 256), 256, 0, st>>>(vel, force, V, c, gate);
+    launch_k(k_fire_bend, dim3(nblk(V, 256)), dim3(256), 0, st, vel, force, V, c, gate);
     return cudaGetLastError();
 }
 
@@ -1261,7 +1290,7 @@ cudaError_t launch_shake_noalloc(double2* pos, const int* start, int P, const do
                                  int* maxItersOut, double* scratch, cudaStream_t st) {
     if (P <= 0) return cudaSuccess;
     constexpr int wpb = 8;
-    k_shake<<<nblk(P, wpb), 32 * wpb, 0, st>>>(pos, start, P, targetEdge, targetArea, maxIter, tol,
+    launch_k(k_shake, dim3(nblk(P, wpb)), dim3(32 * wpb), 0, st, pos, start, P, targetEdge, targetArea, maxIter, tol,
                                                maxItersOut, scratch, 0, nullptr, 0, nullptr);
     return cudaGetLastError();
 }

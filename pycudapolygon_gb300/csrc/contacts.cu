@@ -51,6 +51,7 @@ constexpr float kStarEpsPerL = 1e-6f;
 
 // Reset of the contact counters (everything in Ctrl before `energy`).
 __global__ void k_reset_contacts(Ctrl* __restrict__ ctrl, const int* gate) {
+    pdl_enter();
     if (gate_closed(gate)) return;
     int* w = reinterpret_cast<int*>(ctrl);
     int n = (int)(offsetof(Ctrl, energy) / sizeof(int));
@@ -63,6 +64,7 @@ k_prepass(const double2* __restrict__ pos, const int* __restrict__ start,
           double2* __restrict__ edgeVec, float4* __restrict__ vtx, float4* __restrict__ polyInfo,
           float4* __restrict__ polyBox, int* __restrict__ polyFlags, int* __restrict__ unsafeList,
           Ctrl* __restrict__ ctrl, const int* gate) {
+    pdl_enter();
     if (gate_closed(gate)) return;
     __shared__ float s_r[8];
     const int p = blockIdx.x * (blockDim.x / 32) + threadIdx.x / 32;
@@ -184,6 +186,7 @@ __device__ __forceinline__ int grid_cell(float c, int G) {
 __global__ void k_grid_count(const float4* __restrict__ polyInfo, const int* __restrict__ flags,
                              int P, int* __restrict__ gridCount, Ctrl* __restrict__ ctrl,
                              const int* gate) {
+    pdl_enter();
     if (gate_closed(gate)) return;
     int G = grid_dim_from(ctrl->Rmax);
     int p = blockIdx.x * blockDim.x + threadIdx.x;
@@ -197,6 +200,7 @@ __global__ void k_grid_count(const float4* __restrict__ polyInfo, const int* __r
 __global__ void __launch_bounds__(1024)
 k_grid_scan(int* __restrict__ gridCount, int* __restrict__ gridStart, int* __restrict__ gridFill,
             Ctrl* __restrict__ ctrl, const int* gate) {
+    pdl_enter();
     if (gate_closed(gate)) return;
     __shared__ int warpSums[32];
     int G = ctrl->G;
@@ -243,6 +247,7 @@ __global__ void k_grid_scatter(const float4* __restrict__ polyInfo, const int* _
                                int P, const int* __restrict__ gridStart, int* __restrict__ gridFill,
                                int* __restrict__ sortedPoly, const Ctrl* __restrict__ ctrl,
                                const int* gate) {
+    pdl_enter();
     if (gate_closed(gate)) return;
     int p = blockIdx.x * blockDim.x + threadIdx.x;
     if (p >= P || !flags[p]) return;
@@ -274,6 +279,7 @@ k_candidates(const float4* __restrict__ polyInfo, const float4* __restrict__ pol
              const int* __restrict__ flags, const int* __restrict__ start, int P,
              const int* __restrict__ gridStart, const int* __restrict__ sortedPoly,
              int2* __restrict__ pairs, int capPairs, Ctrl* __restrict__ ctrl, const int* gate) {
+    pdl_enter();
     if (gate_closed(gate)) return;
     __shared__ int s_cnt[8];
     __shared__ unsigned long long s_evals[8];
@@ -716,6 +722,7 @@ __device__ __forceinline__ void push_slow(int q, Ctrl* ctrl, ContactWS& ws) {
 __global__ void __launch_bounds__(32 * kNarrowWarps)
 k_narrow(const double2* __restrict__ pos, const int* __restrict__ start, int B,
          ContactWS ws, Ctrl* __restrict__ ctrl, const int* gate) {
+    pdl_enter();
     if (gate_closed(gate)) return;
     extern __shared__ __align__(128) unsigned char smem_raw[];
     WarpSmem& S = reinterpret_cast<WarpSmem*>(smem_raw)[threadIdx.x / 32];
@@ -795,6 +802,7 @@ k_narrow(const double2* __restrict__ pos, const int* __restrict__ start, int B,
 __global__ void __launch_bounds__(32)
 k_narrow_slow(const double2* __restrict__ pos, const int* __restrict__ start, int B,
               ContactWS ws, Ctrl* __restrict__ ctrl, const int* gate) {
+    pdl_enter();
     if (gate_closed(gate)) return;
     extern __shared__ __align__(128) unsigned char smem_raw[];
     float4* ring = reinterpret_cast<float4*>(smem_raw);                    // kSlowRing
@@ -840,6 +848,7 @@ k_narrow_slow(const double2* __restrict__ pos, const int* __restrict__ start, in
 // sij, and that record is then tried as the partner.  Reproduced here.
 __global__ void k_fixup(const int* __restrict__ start, ContactWS ws, Ctrl* __restrict__ ctrl,
                         const int* gate) {
+    pdl_enter();
     if (gate_closed(gate)) return;
     int nf = min(ctrl->numFix, ws.capFix);
     if (nf == 0) return;
@@ -896,6 +905,7 @@ __global__ void __launch_bounds__(32 * kForceWarps)
 k_overlap_force(const double2* __restrict__ pos, const int* __restrict__ start,
                 const int* __restrict__ next, int V, ContactWS ws, Ctrl* __restrict__ ctrl,
                 double2* __restrict__ force, const int* gate) {
+    pdl_enter();
     if (gate_closed(gate)) return;
     const int lane = threadIdx.x & 31;
     const int half = lane & 1;
@@ -1033,32 +1043,32 @@ cudaError_t launch_contacts(const double2* pos, const int* start, const int* sha
     (void)shapeId; (void)V;
     if (B < 1) B = 1;
     if (stages & 1) {
-    if (!(stages & 4)) k_reset_contacts<<<1, 64, 0, st>>>(ctrl, gate);
+    if (!(stages & 4)) launch_k(k_reset_contacts, dim3(1), dim3(64), 0, st, ctrl, gate);
     if (P <= 0) return cudaGetLastError();
-    k_prepass<<<nblocks(P, 8), 256, 0, st>>>(pos, start, cellLocation, cellOut, P, B, ws.edgeVec,
+    launch_k(k_prepass, dim3(nblocks(P, 8)), dim3(256), 0, st, pos, start, cellLocation, cellOut, P, B, ws.edgeVec,
                                              ws.vtx, ws.polyInfo, ws.polyBox, ws.polyFlags,
                                              ws.unsafeList, ctrl, gate);
-    k_grid_count<<<nblocks(P, 256), 256, 0, st>>>(ws.polyInfo, ws.polyFlags, P, ws.gridCount,
+    launch_k(k_grid_count, dim3(nblocks(P, 256)), dim3(256), 0, st, ws.polyInfo, ws.polyFlags, P, ws.gridCount,
                                                   ctrl, gate);
-    k_grid_scan<<<1, 1024, 0, st>>>(ws.gridCount, ws.gridStart, ws.gridFill, ctrl, gate);
-    k_grid_scatter<<<nblocks(P, 256), 256, 0, st>>>(ws.polyInfo, ws.polyFlags, P, ws.gridStart,
+    launch_k(k_grid_scan, dim3(1), dim3(1024), 0, st, ws.gridCount, ws.gridStart, ws.gridFill, ctrl, gate);
+    launch_k(k_grid_scatter, dim3(nblocks(P, 256)), dim3(256), 0, st, ws.polyInfo, ws.polyFlags, P, ws.gridStart,
                                                     ws.gridFill, ws.sortedPoly, ctrl, gate);
-    k_candidates<<<nblocks(P, 8), 256, 0, st>>>(ws.polyInfo, ws.polyBox, ws.polyFlags, start, P,
+    launch_k(k_candidates, dim3(nblocks(P, 8)), dim3(256), 0, st, ws.polyInfo, ws.polyBox, ws.polyFlags, start, P,
                                                   ws.gridStart, ws.sortedPoly, ws.pairs,
                                                   ws.capPairs, ctrl, gate);
     }
     if ((stages & 2) && P > 0) {
         size_t smem = sizeof(WarpSmem) * kNarrowWarps;
         int grid = sm_count() * 4;
-        k_narrow<<<grid, 32 * kNarrowWarps, smem, st>>>(pos, start, B, ws, ctrl, gate);
-        k_narrow_slow<<<sm_count(), 32, kSlowSmem, st>>>(pos, start, B, ws, ctrl, gate);
+        launch_k(k_narrow, dim3(grid), dim3(32 * kNarrowWarps), smem, st, pos, start, B, ws, ctrl, gate);
+        launch_k(k_narrow_slow, dim3(sm_count()), dim3(32), kSlowSmem, st, pos, start, B, ws, ctrl, gate);
     }
     return cudaGetLastError();
 }
 
 cudaError_t launch_contacts_finish(const int* start, ContactWS& ws, Ctrl* ctrl,
                                    const int* gate, cudaStream_t st) {
-    k_fixup<<<1, 1024, 0, st>>>(start, ws, ctrl, gate);
+    launch_k(k_fixup, dim3(1), dim3(1024), 0, st, start, ws, ctrl, gate);
     return cudaGetLastError();
 }
 
@@ -1067,7 +1077,7 @@ cudaError_t launch_overlap_force(const double2* pos, const int* start, const int
                                  const int* gate, cudaStream_t st) {
     // one pass over up to 4 * SMs * kForceWarps * kForceRecs records
     int grid = sm_count() * 4;
-    k_overlap_force<<<grid, 32 * kForceWarps, 0, st>>>(pos, start, next, V, ws, ctrl, force, gate);
+    launch_k(k_overlap_force, dim3(grid), dim3(32 * kForceWarps), 0, st, pos, start, next, V, ws, ctrl, force, gate);
     return cudaGetLastError();
 }
 

@@ -36,6 +36,7 @@ static inline int blocks_for(long long n, int threads) {
 // updateShapeIdKernel (kernels.cuh:652-659) + computeNextPrevKernel (:127-135)
 __global__ void k_topology(const int* __restrict__ start, int P, int V, int* __restrict__ shapeId,
                            int* __restrict__ next, int* __restrict__ prev) {
+    pdl_enter();
     int p = blockIdx.x * (blockDim.x / 32) + threadIdx.x / 32;
     int lane = threadIdx.x & 31;
     if (p >= P) return;
@@ -51,11 +52,12 @@ __global__ void k_topology(const int* __restrict__ start, int P, int V, int* __r
 cudaError_t launch_topology(const int* start, int P, int V, int* shapeId, int* next, int* prev,
                             cudaStream_t st) {
     if (P <= 0) return cudaSuccess;
-    k_topology<<<blocks_for(P, 8), 256, 0, st>>>(start, P, V, shapeId, next, prev);
+    launch_k(k_topology, dim3(blocks_for(P, 8)), dim3(256), 0, st, start, P, V, shapeId, next, prev);
     return cudaGetLastError();
 }
 
 __global__ void k_zero_scalar(double* x, const int* gate) {
+    pdl_enter();
     if (gate_closed(gate)) return;
     *x = 0.0;
 }
@@ -70,6 +72,7 @@ k_geometry(const double2* __restrict__ pos, const int* __restrict__ start, int P
            double* __restrict__ edgeLengths, double* __restrict__ areas,
            double* __restrict__ comX, double* __restrict__ comY, double* __restrict__ perimeters,
            double* __restrict__ constraints, double* __restrict__ maxEdge, const int* gate) {
+    pdl_enter();
     if (gate_closed(gate)) return;
     int p = blockIdx.x * (blockDim.x / 32) + threadIdx.x / 32;
     int lane = threadIdx.x & 31;
@@ -140,8 +143,8 @@ cudaError_t launch_geometry(const double2* pos, const int* start, int P, int V,
                             const int* gate, cudaStream_t st) {
     (void)V;
     if (P <= 0) return cudaSuccess;
-    k_zero_scalar<<<1, 1, 0, st>>>(maxEdge, gate);
-    k_geometry<<<blocks_for(P, 8), 256, 0, st>>>(pos, start, P, edgeLengths, areas, comX, comY,
+    launch_k(k_zero_scalar, dim3(1), dim3(1), 0, st, maxEdge, gate);
+    launch_k(k_geometry, dim3(blocks_for(P, 8)), dim3(256), 0, st, pos, start, P, edgeLengths, areas, comX, comY,
                                                  perimeters, constraints, maxEdge, gate);
     return cudaGetLastError();
 }
@@ -150,6 +153,7 @@ cudaError_t launch_geometry(const double2* pos, const int* start, int P, int V,
 __global__ void k_neighbor_cells(const double2* __restrict__ pos, const int* __restrict__ start,
                                  const int* __restrict__ shapeId, int V, int B,
                                  int* __restrict__ cell, const int* gate) {
+    pdl_enter();
     if (gate_closed(gate)) return;
     int i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= V) return;
@@ -165,7 +169,7 @@ cudaError_t launch_neighbor_cells(const double2* pos, const int* start, const in
                                   cudaStream_t st) {
     if (V <= 0) return cudaSuccess;
     if (B < 1) B = 1;
-    k_neighbor_cells<<<blocks_for(V, 256), 256, 0, st>>>(pos, start, shapeId, V, B, cellLocation,
+    launch_k(k_neighbor_cells, dim3(blocks_for(V, 256)), dim3(256), 0, st, pos, start, shapeId, V, B, cellLocation,
                                                          gate);
     return cudaGetLastError();
 }
@@ -174,6 +178,7 @@ cudaError_t launch_neighbor_cells(const double2* pos, const int* start, const in
 // updatePositionsKernel (kernels.cuh:1433-1438)
 __global__ void k_update_positions(double* __restrict__ pos, const double* __restrict__ force,
                                    int n2, double dt) {
+    pdl_enter();
     int i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= n2) return;
     double p = pos[i] + force[i] * dt;
@@ -183,7 +188,7 @@ __global__ void k_update_positions(double* __restrict__ pos, const double* __res
 cudaError_t launch_update_positions(double* pos, const double* force, int V, double dt,
                                     cudaStream_t st) {
     if (V <= 0) return cudaSuccess;
-    k_update_positions<<<blocks_for(2LL * V, 256), 256, 0, st>>>(pos, force, 2 * V, dt);
+    launch_k(k_update_positions, dim3(blocks_for(2LL * V, 256)), dim3(256), 0, st, pos, force, 2 * V, dt);
     return cudaGetLastError();
 }
 
@@ -192,6 +197,7 @@ __global__ void k_reset_areas(double* __restrict__ pos, const int* __restrict__ 
                               const double* __restrict__ areas, const double* __restrict__ tgt,
                               const double* __restrict__ comX, const double* __restrict__ comY,
                               int n2) {
+    pdl_enter();
     int idx = blockIdx.x * blockDim.x + threadIdx.x;
     if (idx >= n2) return;
     double x = pos[idx];
@@ -209,13 +215,14 @@ cudaError_t launch_reset_areas(double* pos, const int* shapeId, const double* ar
                                const double* targetAreas, const double* comX,
                                const double* comY, int V, cudaStream_t st) {
     if (V <= 0) return cudaSuccess;
-    k_reset_areas<<<blocks_for(2LL * V, 256), 256, 0, st>>>(pos, shapeId, areas, targetAreas,
+    launch_k(k_reset_areas, dim3(blocks_for(2LL * V, 256)), dim3(256), 0, st, pos, shapeId, areas, targetAreas,
                                                             comX, comY, 2 * V);
     return cudaGetLastError();
 }
 
 // max |x| (getMaxUnbalancedForceCUDA, model.cu:91-109); out must be zeroed.
 __global__ void k_max_abs(const double* __restrict__ x, int n, double* __restrict__ out) {
+    pdl_enter();
     double m = 0.0;
     for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x)
         m = fmax(m, fabs(x[i]));
@@ -228,7 +235,7 @@ cudaError_t launch_max_abs(const double* x, int n, double* out, cudaStream_t st)
     if (e != cudaSuccess || n <= 0) return e;
     int b = blocks_for(n, 256);
     if (b > 4 * sm_count()) b = 4 * sm_count();
-    k_max_abs<<<b, 256, 0, st>>>(x, n, out);
+    launch_k(k_max_abs, dim3(b), dim3(256), 0, st, x, n, out);
     return cudaGetLastError();
 }
 
@@ -236,6 +243,7 @@ cudaError_t launch_max_abs(const double* x, int n, double* out, cudaStream_t st)
 __global__ void k_max_eff(const double* __restrict__ pos, const double* __restrict__ tent,
                           const double* __restrict__ f, int V, double scale,
                           double* __restrict__ out) {
+    pdl_enter();
     double m = 0.0;
     for (int k = blockIdx.x * blockDim.x + threadIdx.x; k < V; k += gridDim.x * blockDim.x) {
         double fx = f[2 * k] + scale * (pos[2 * k] - tent[2 * k]);
@@ -253,7 +261,7 @@ cudaError_t launch_max_effective_force(const double* pos, const double* posTent,
     if (e != cudaSuccess || V <= 0) return e;
     int b = blocks_for(V, 256);
     if (b > 4 * sm_count()) b = 4 * sm_count();
-    k_max_eff<<<b, 256, 0, st>>>(pos, posTent, force, V, scale, out);
+    launch_k(k_max_eff, dim3(b), dim3(256), 0, st, pos, posTent, force, V, scale, out);
     return cudaGetLastError();
 }
 
@@ -270,6 +278,7 @@ __global__ void k_soft_edge(const double2* __restrict__ pos, const double* __res
                             const int* __restrict__ prev, const int* __restrict__ shapeId, int V,
                             double stiffness, double* __restrict__ force,
                             double* __restrict__ energy, const int* gate) {
+    pdl_enter();
     if (gate_closed(gate)) return;
     int m = blockIdx.x * blockDim.x + threadIdx.x;
     double le = 0.0;
@@ -301,7 +310,7 @@ cudaError_t launch_soft_edge(const double2* pos, const double* targetEdgeLengths
                              const int* shapeId, int V, double stiffness, double* force,
                              double* energy, const int* gate, cudaStream_t st) {
     if (V <= 0) return cudaSuccess;
-    k_soft_edge<<<blocks_for(V, 256), 256, 0, st>>>(pos, targetEdgeLengths, edgeLengths, next,
+    launch_k(k_soft_edge, dim3(blocks_for(V, 256)), dim3(256), 0, st, pos, targetEdgeLengths, edgeLengths, next,
                                                      prev, shapeId, V, stiffness, force, energy,
                                                      gate);
     return cudaGetLastError();
@@ -314,6 +323,7 @@ __global__ void k_soft_area(const double2* __restrict__ pos, const int* __restri
                             const int* __restrict__ start, int V, double comp,
                             double* __restrict__ force, double* __restrict__ energy,
                             const int* gate) {
+    pdl_enter();
     if (gate_closed(gate)) return;
     int m = blockIdx.x * blockDim.x + threadIdx.x;
     double le = 0.0;
@@ -339,7 +349,7 @@ cudaError_t launch_soft_area(const double2* pos, const int* shapeId, const int* 
                              const int* start, int V, double compressibility, double* force,
                              double* energy, const int* gate, cudaStream_t st) {
     if (V <= 0) return cudaSuccess;
-    k_soft_area<<<blocks_for(V, 256), 256, 0, st>>>(pos, shapeId, next, prev, areas, targetAreas,
+    launch_k(k_soft_area, dim3(blocks_for(V, 256)), dim3(256), 0, st, pos, shapeId, next, prev, areas, targetAreas,
                                                      start, V, compressibility, force, energy, gate);
     return cudaGetLastError();
 }
@@ -359,6 +369,7 @@ __global__ void k_overlap_mc(const double2* __restrict__ pos, const int* __restr
                              const int* __restrict__ shapeId, const int* __restrict__ nbIdx,
                              const int* __restrict__ boxStarts, int V, int B, int d,
                              int* __restrict__ counter, unsigned long long* __restrict__ sum) {
+    pdl_enter();
     const double eps = 1e-12;
     const double pi = 3.141592653589793238462643383279;
     int idx = blockIdx.x * blockDim.x + threadIdx.x;
@@ -422,7 +433,7 @@ cudaError_t launch_overlap_area_mc(const double2* pos, const int* start, const i
     if (e != cudaSuccess) return e;
     long long total = (long long)pointDensity * pointDensity;
     if (total <= 0) return cudaSuccess;
-    k_overlap_mc<<<blocks_for(total, 128), 128, 0, st>>>(pos, start, shapeId, neighborIndices,
+    launch_k(k_overlap_mc, dim3(blocks_for(total, 128)), dim3(128), 0, st, pos, start, shapeId, neighborIndices,
                                                           boxStarts, V, B < 1 ? 1 : B,
                                                           pointDensity, counter, sum);
     return cudaGetLastError();

@@ -16,6 +16,35 @@
 
 namespace pcp {
 
+// ---------------------------------------------- programmatic dependent launch
+// Every kernel of the path starts with pdl_enter(): it waits until the
+// kernel before it on the stream has finished and its writes are visible
+// (griddepcontrol.wait, a no-op when the launch did not ask for overlap), then
+// lets the next kernel's blocks be scheduled (griddepcontrol.launch_dependents)
+// so that launch hides behind this kernel's run.
+__device__ __forceinline__ void pdl_enter() {
+    asm volatile("griddepcontrol.wait;" ::: "memory");
+    asm volatile("griddepcontrol.launch_dependents;" ::: "memory");
+}
+
+// Launch with programmatic stream serialization (the kernel must begin with
+// pdl_enter()).  Errors are reported through cudaGetLastError like <<< >>>.
+template <typename... KArgs, typename... Args>
+inline cudaError_t launch_k(void (*kernel)(KArgs...), dim3 grid, dim3 block, size_t smem,
+                            cudaStream_t st, Args... args) {
+    cudaLaunchConfig_t cfg = {};
+    cfg.gridDim = grid;
+    cfg.blockDim = block;
+    cfg.dynamicSmemBytes = smem;
+    cfg.stream = st;
+    cudaLaunchAttribute attr[1];
+    attr[0].id = cudaLaunchAttributeProgrammaticStreamSerialization;
+    attr[0].val.programmaticStreamSerializationAllowed = 1;
+    cfg.attrs = attr;
+    cfg.numAttrs = 1;
+    return cudaLaunchKernelEx(&cfg, kernel, args...);
+}
+
 // ---------------------------------------------------------------- wraps ----
 
 // wrap (kernels.cuh:115-119): minimum image into [-0.5, 0.5),
@@ -212,6 +241,66 @@ __device__ __forceinline__ void gDf(double2 vi, double2 vzi, double2 vj, double2
     out[1] = make_double2(gd * du1x + g.x * u, gd * du1y + g.y * u);
     out[2] = make_double2(gd * du2x, gd * du2y);
     out[3] = make_double2(gd * du3x, gd * du3y);
+}
+
+// ------------------------------------------- conversions on the INT pipe ----
+// On GB300 the FP64<->FP32 conversions, FP64 compares and FP64 min/max run
+// at the FP64 rate (about 1/64 of FP32), so the mixed-precision solvers
+// convert with integer operations instead.
+//
+// FP32 -> FP64, exact for normal floats; zero and denormals give +-0.
+__device__ __forceinline__ double f2d_int(float f) {
+    const unsigned u = __float_as_uint(f);
+    const unsigned e = (u >> 23) & 0xFFu;
+    const unsigned sign = u & 0x80000000u;
+    if (e == 0u) return __hiloint2double((int)sign, 0);
+    if (e == 0xFFu) return (double)f;                         // inf / NaN (not expected)
+    const unsigned m = u & 0x7FFFFFu;
+    const unsigned hi = sign | ((e + (1023u - 127u)) << 20) | (m >> 3);
+    return __hiloint2double((int)hi, (int)(m << 29));
+}
+// FP64 -> FP32 by truncation of the significand (within one float ulp of
+// the value: inputs of the FP32 solves only); magnitudes below 2^-126 give
+// +-0, above the float range +-inf, NaN stays NaN.
+__device__ __forceinline__ float d2f_int(double d) {
+    const unsigned hi = (unsigned)__double2hiint(d), lo = (unsigned)__double2loint(d);
+    const unsigned sign = hi & 0x80000000u;
+    const int e = (int)((hi >> 20) & 0x7FFu) - 1023 + 127;
+    if (e <= 0) return __uint_as_float(sign);
+    if (e >= 255) {
+        const unsigned mag = hi & 0x7FFFFFFFu;
+        const bool nan = mag > 0x7FF00000u || (mag == 0x7FF00000u && lo != 0u);
+        return __uint_as_float(nan ? 0x7FC00000u : (sign | 0x7F800000u));
+    }
+    const unsigned m = ((hi & 0xFFFFFu) << 3) | (lo >> 29);
+    return __uint_as_float(sign | ((unsigned)e << 23) | m);
+}
+// |x| as the bit pattern of a non-negative double: for finite values the
+// unsigned order of these patterns is the order of the magnitudes (NaN
+// patterns sort above +inf).
+__device__ __forceinline__ unsigned long long abs_bits(double x) {
+    return (unsigned long long)__double_as_longlong(x) & 0x7FFFFFFFFFFFFFFFull;
+}
+__device__ __forceinline__ unsigned long long warp_max_u64(unsigned long long v) {
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) {
+        unsigned long long t = __shfl_xor_sync(PCP_FULL, v, o);
+        v = t > v ? t : v;
+    }
+    return v;
+}
+// true when the pattern is that of a finite double
+__device__ __forceinline__ bool finite_bits(unsigned long long b) {
+    return (b & 0x7FF0000000000000ull) != 0x7FF0000000000000ull;
+}
+// running max of |x|, |y| as a bit pattern, NaN left out (as fmax does)
+__device__ __forceinline__ unsigned long long max_abs_bits(unsigned long long m, double x,
+                                                              double y) {
+    const unsigned long long inf = 0x7FF0000000000000ull;
+    unsigned long long a = abs_bits(x), b = abs_bits(y);
+    if (a <= inf && a > m) m = a;
+    if (b <= inf && b > m) m = b;
+    return m;
 }
 
 // ------------------------------------------------------- warp helpers ----
