@@ -265,8 +265,10 @@ def roofline(m, s, torch, flush, args):
             "kernel": "k_narrow + k_narrow_slow (contact stage 1)",
             "launch_ms": ms, "algorithmic_bytes": bytes_launch, "pairs": pairs,
             "self_pairs": selfs}
+    # the projection, SHAKE and force kernels are bound by the FP64 pipe, not
+    # by HBM: their FP64-pipe activity from the committed ncu capture
     fp64 = None
-    p64 = os.path.join(ROOT, "profiles", "fp64_peak.json")
+    p64 = os.path.join(ROOT, "profiles", "fp64_pipe_4096x32.json")
     if os.path.exists(p64):
         try:
             fp64 = json.load(open(p64))
