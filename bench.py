@@ -49,6 +49,20 @@ def dist_env():
     return ws, rank, local
 
 
+def reduce_over_ranks(ms, pairs, dist, device):
+    """Whole-job figures of independent replicas: the slowest rank's time and
+    the pair evaluations of all ranks (no data-path collective: this is the
+    only exchange, after the timed region)."""
+    import torch
+    if dist is None:
+        return float(ms), float(pairs)
+    t = torch.tensor([ms, float(pairs)], dtype=torch.float64, device=device)
+    tmax = t.clone()
+    dist.all_reduce(tmax, op=dist.ReduceOp.MAX)
+    dist.all_reduce(t, op=dist.ReduceOp.SUM)
+    return float(tmax[0]), float(t[1])
+
+
 # ------------------------------------------------------------------ clocks
 class ClockSampler:
     """nvidia-smi clocks and throttle reasons sampled during the timed region."""
@@ -186,12 +200,7 @@ def run_gpu(args, ws, rank, local):
     ms = sum(a.elapsed_time(b) for a, b in ev)
     pairs = m.getPairCount() - pairs0
     launches = m.getLaunchCount() - launches0
-    if dist:
-        t = torch.tensor([ms, float(pairs)], dtype=torch.float64, device="cuda")
-        tmax = t.clone()
-        dist.all_reduce(tmax, op=dist.ReduceOp.MAX)
-        dist.all_reduce(t, op=dist.ReduceOp.SUM)
-        ms, pairs = float(tmax[0]), float(t[1])
+    ms, pairs = reduce_over_ranks(ms, pairs, dist, "cuda")
     value = pairs / (ms / 1e3)
     result = {
         "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": ws, "steps": args.steps,

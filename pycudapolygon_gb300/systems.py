@@ -103,6 +103,22 @@ def batched_specs(num_systems, seed, p_range=(64, 1024), n_range=(12, 48),
     return specs
 
 
+def shard_by_vertices(vertex_counts, world_size):
+    """Assign independent systems to ranks with balanced total vertex counts
+    (largest first, each to the least-loaded rank; ties to the lower rank).
+    Returns one sorted list of system indices per rank.  Systems never
+    exchange data, so the shards need no collective on the data path."""
+    counts = [int(c) for c in vertex_counts]
+    order = sorted(range(len(counts)), key=lambda i: (-counts[i], i))
+    loads = [0] * world_size
+    shards = [[] for _ in range(world_size)]
+    for i in order:
+        r = min(range(world_size), key=lambda k: (loads[k], k))
+        shards[r].append(i)
+        loads[r] += counts[i]
+    return [sorted(x) for x in shards]
+
+
 def load_into(model, system, model_type=None):
     """Configure a reference-API model object (the pybind `Model`, or any
     object with the same method names) with a generated system.  The cell
