@@ -80,7 +80,7 @@ k_prepass(const double2* __restrict__ pos, const int* __restrict__ start,
         }
     } else if (p < P) {
         double2 q0 = pos[st];
-        float f0x = (float)q0.x, f0y = (float)q0.y;
+        float f0x = d2f_int(q0.x), f0y = d2f_int(q0.y);
         float mnx = 0.f, mxx = 0.f, mny = 0.f, mxy = 0.f, emax = 0.f;
         bool bad = false;
         for (int kl = lane; kl < n; kl += 32) {
@@ -89,8 +89,10 @@ k_prepass(const double2* __restrict__ pos, const int* __restrict__ start,
             double2 pk = pos[k], pn = pos[nx];
             // r = wrap(p_next - p) exactly as updateNeighborsKernel (kernels.cuh:724-725)
             edgeVec[k] = make_double2(wrap(pn.x - pk.x), wrap(pn.y - pk.y));
-            float fx = (float)pk.x, fy = (float)pk.y;
-            float fnx = (float)pn.x, fny = (float)pn.y;
+            // FP32 copies by truncation on the integer pipe (within one float
+            // ulp; the culls' margins allow for 1.2e-7)
+            float fx = d2f_int(pk.x), fy = d2f_int(pk.y);
+            float fnx = d2f_int(pn.x), fny = d2f_int(pn.y);
             // cell (x, y) of the edge midpoint as updateNeighborsKernel splits it
             // with the current box size (kernels.cuh:727-729); with cellOut the
             // cells are computed here from the same positions
@@ -255,6 +257,85 @@ __global__ void k_grid_scatter(const float4* __restrict__ polyInfo, const int* _
     float4 c = polyInfo[p];
     int cell = grid_cell(c.y, G) * G + grid_cell(c.x, G);
     sortedPoly[gridStart[cell] + atomicAdd(&gridFill[cell], 1)] = p;
+}
+
+// The three steps above in one block, for systems of up to kFusedMaxPolys
+// polygons: counts in shared memory when the grid has at most kFusedCells
+// cells (else in gridCount, which is left zeroed), an exclusive scan into
+// gridStart, and the scatter through atomic increments of the scanned
+// starts (a counting sort; the order inside a cell is arbitrary, as with
+// k_grid_scatter).
+constexpr int kFusedCells = 8192;
+constexpr int kFusedMaxPolys = 65536;
+__global__ void __launch_bounds__(1024)
+k_grid_fused(const float4* __restrict__ polyInfo, const int* __restrict__ flags, int P,
+             int* __restrict__ gridCount, int* __restrict__ gridStart,
+             int* __restrict__ sortedPoly, Ctrl* __restrict__ ctrl, const int* gate) {
+    pdl_enter();
+    if (gate_closed(gate)) return;
+    __shared__ int s_cnt[kFusedCells];
+    __shared__ int warpSums[32];
+    const int G = grid_dim_from(ctrl->Rmax);
+    const int N = G * G;
+    if (threadIdx.x == 0) ctrl->G = G;
+    const bool inSmem = N <= kFusedCells;
+    int* cnt = inSmem ? s_cnt : gridCount;
+    if (inSmem)
+        for (int i = threadIdx.x; i < N; i += blockDim.x) s_cnt[i] = 0;
+    __syncthreads();
+    for (int p = threadIdx.x; p < P; p += blockDim.x) {
+        if (!flags[p]) continue;
+        float4 c = polyInfo[p];
+        atomicAdd(&cnt[grid_cell(c.y, G) * G + grid_cell(c.x, G)], 1);
+    }
+    __syncthreads();
+    // exclusive scan: contiguous runs per thread, then across warps
+    const int per = (N + blockDim.x - 1) / blockDim.x;
+    const int b0 = threadIdx.x * per;
+    int local = 0;
+    for (int i = 0; i < per; ++i) {
+        int idx = b0 + i;
+        if (idx < N) local += cnt[idx];
+    }
+    const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+    int incl = local;
+    for (int o = 1; o < 32; o <<= 1) {
+        int t = __shfl_up_sync(PCP_FULL, incl, o);
+        if (lane >= o) incl += t;
+    }
+    if (lane == 31) warpSums[w] = incl;
+    __syncthreads();
+    if (w == 0) {
+        int v = lane < (int)(blockDim.x >> 5) ? warpSums[lane] : 0;
+        int sc = v;
+        for (int o = 1; o < 32; o <<= 1) {
+            int t = __shfl_up_sync(PCP_FULL, sc, o);
+            if (lane >= o) sc += t;
+        }
+        warpSums[lane] = sc - v;
+    }
+    __syncthreads();
+    int run = warpSums[w] + incl - local;
+    for (int i = 0; i < per; ++i) {
+        int idx = b0 + i;
+        if (idx < N) {
+            int c = cnt[idx];
+            gridStart[idx] = run;
+            cnt[idx] = run;
+            run += c;
+        }
+    }
+    if (threadIdx.x == blockDim.x - 1) gridStart[N] = run;
+    __syncthreads();
+    for (int p = threadIdx.x; p < P; p += blockDim.x) {
+        if (!flags[p]) continue;
+        float4 c = polyInfo[p];
+        sortedPoly[atomicAdd(&cnt[grid_cell(c.y, G) * G + grid_cell(c.x, G)], 1)] = p;
+    }
+    if (!inSmem) {
+        __syncthreads();
+        for (int i = threadIdx.x; i < N; i += blockDim.x) gridCount[i] = 0;
+    }
 }
 
 // One warp per polygon i: the lanes walk the polygons of the (up to) nine
@@ -1048,11 +1129,16 @@ cudaError_t launch_contacts(const double2* pos, const int* start, const int* sha
     launch_k(k_prepass, dim3(nblocks(P, 8)), dim3(256), 0, st, pos, start, cellLocation, cellOut, P, B, ws.edgeVec,
                                              ws.vtx, ws.polyInfo, ws.polyBox, ws.polyFlags,
                                              ws.unsafeList, ctrl, gate);
-    launch_k(k_grid_count, dim3(nblocks(P, 256)), dim3(256), 0, st, ws.polyInfo, ws.polyFlags, P, ws.gridCount,
-                                                  ctrl, gate);
-    launch_k(k_grid_scan, dim3(1), dim3(1024), 0, st, ws.gridCount, ws.gridStart, ws.gridFill, ctrl, gate);
-    launch_k(k_grid_scatter, dim3(nblocks(P, 256)), dim3(256), 0, st, ws.polyInfo, ws.polyFlags, P, ws.gridStart,
-                                                    ws.gridFill, ws.sortedPoly, ctrl, gate);
+    if (P <= kFusedMaxPolys) {
+        launch_k(k_grid_fused, dim3(1), dim3(1024), 0, st, ws.polyInfo, ws.polyFlags, P,
+                 ws.gridCount, ws.gridStart, ws.sortedPoly, ctrl, gate);
+    } else {
+        launch_k(k_grid_count, dim3(nblocks(P, 256)), dim3(256), 0, st, ws.polyInfo, ws.polyFlags, P, ws.gridCount,
+                                                      ctrl, gate);
+        launch_k(k_grid_scan, dim3(1), dim3(1024), 0, st, ws.gridCount, ws.gridStart, ws.gridFill, ctrl, gate);
+        launch_k(k_grid_scatter, dim3(nblocks(P, 256)), dim3(256), 0, st, ws.polyInfo, ws.polyFlags, P, ws.gridStart,
+                                                        ws.gridFill, ws.sortedPoly, ctrl, gate);
+    }
     launch_k(k_candidates, dim3(nblocks(P, 8)), dim3(256), 0, st, ws.polyInfo, ws.polyBox, ws.polyFlags, start, P,
                                                   ws.gridStart, ws.sortedPoly, ws.pairs,
                                                   ws.capPairs, ctrl, gate);
@@ -1061,7 +1147,8 @@ cudaError_t launch_contacts(const double2* pos, const int* start, const int* sha
         size_t smem = sizeof(WarpSmem) * kNarrowWarps;
         int grid = sm_count() * 4;
         launch_k(k_narrow, dim3(grid), dim3(32 * kNarrowWarps), smem, st, pos, start, B, ws, ctrl, gate);
-        launch_k(k_narrow_slow, dim3(sm_count()), dim3(32), kSlowSmem, st, pos, start, B, ws, ctrl, gate);
+        // pairs for the block path are rare: a few blocks take them in turn
+        launch_k(k_narrow_slow, dim3(16), dim3(32), kSlowSmem, st, pos, start, B, ws, ctrl, gate);
     }
     return cudaGetLastError();
 }

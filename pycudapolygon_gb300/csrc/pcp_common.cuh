@@ -107,12 +107,13 @@ __device__ __forceinline__ int midpoint_cell_of(double2 a, double2 b, int B) {
     return cell_coord(y, B) * B + cell_coord(x, B);
 }
 
-// The same cell, decided in FP32 when that is safe.  The FP32 midpoint is
-// within 1.3e-7 of the FP64 one (coordinates rounded to float, three
-// roundings) and its product with B adds at most 3e-8 B, so it lies within
-// 1.6e-7 B cell widths of the FP64 value; when it is more than
-// 1e-4 + 4e-7 B cell widths from every cell boundary (and the edge is short,
-// so both minimum images agree) the FP64 computation lands in the same cell.
+// The same cell, decided in FP32 when that is safe.  With the coordinates
+// within one float ulp (6e-8) of the FP64 ones, the FP32 midpoint is within
+// 2.6e-7 of the FP64 one (four further roundings) and its product with B adds
+// at most 3e-8 B, so it lies within 2.9e-7 B cell widths of the FP64 value;
+// when it is more than 1e-4 + 4e-7 B cell widths from every cell boundary
+// (and the edge is short, so both minimum images agree) the FP64
+// computation lands in the same cell.
 // Otherwise, and for non-finite input, the FP64 form decides.  fa, fb are
 // a and b rounded to float.
 __device__ __forceinline__ int midpoint_cell_fast(double2 a, double2 b, float2 fa, float2 fb,
