@@ -331,6 +331,8 @@ __host__ __device__ constexpr size_t shake_ws_bytes(int NV, int N) {
 // Parallel cyclic reduction of N rows (arrays [2][N]: buffer 0 holds the
 // system, buffer 1 is scratch) with three right-hand sides; leaves the
 // solutions x = r / b in p0, p1, p2 (buffer 0).  One warp, rows strided.
+// Its results only steer iterations whose residuals are FP64, so the fast
+// FP32 division (2 ulp) is enough.
 __device__ void pcr3f(float* pa, float* pb, float* pc, float* p0, float* p1, float* p2, int N) {
     const int lane = threadIdx.x & 31;
     int cur = 0;
@@ -345,13 +347,13 @@ __device__ void pcr3f(float* pa, float* pb, float* pc, float* p0, float* p1, flo
             float na = 0.f, nc = 0.f;
             float nb = b[i], n0 = r0[i], n1 = r1[i], n2 = r2[i];
             if (im >= 0) {
-                float k1 = a[i] / b[im];
+                float k1 = __fdividef(a[i], b[im]);
                 na = -k1 * a[im];
                 nb -= k1 * c[im];
                 n0 -= k1 * r0[im]; n1 -= k1 * r1[im]; n2 -= k1 * r2[im];
             }
             if (ip < N) {
-                float k2 = c[i] / b[ip];
+                float k2 = __fdividef(c[i], b[ip]);
                 nc = -k2 * c[ip];
                 nb -= k2 * a[ip];
                 n0 -= k2 * r0[ip]; n1 -= k2 * r1[ip]; n2 -= k2 * r2[ip];
@@ -363,7 +365,7 @@ __device__ void pcr3f(float* pa, float* pb, float* pc, float* p0, float* p1, flo
     }
     const float *b = pb + cur * N, *r0 = p0 + cur * N, *r1 = p1 + cur * N, *r2 = p2 + cur * N;
     for (int i = lane; i < N; i += 32) {
-        float ib = 1.0f / b[i];
+        float ib = __fdividef(1.0f, b[i]);
         float x0 = r0[i] * ib, x1 = r1[i] * ib, x2 = r2[i] * ib;
         p0[i] = x0; p1[i] = x1; p2[i] = x2;
     }
@@ -622,6 +624,7 @@ constexpr int kProjRounds = 3;
 
 struct ProjWS {
     double2 *t, *f, *q;            // unit edges, F' and q (FP64)
+    float2* tf;                    // unit edges (FP32)
     float *mb, *mc;                // J^T J diagonal and super-diagonal (FP32)
     float *pa, *pb, *pc, *p0, *p1, *p2;   // PCR rows [2][N]
 };
@@ -629,7 +632,8 @@ __device__ __forceinline__ ProjWS proj_ws(unsigned char* base, int NV, int N) {
     ProjWS w;
     double2* d = reinterpret_cast<double2*>(base);
     w.t = d; w.f = d + NV; w.q = d + 2 * NV;
-    float* f = reinterpret_cast<float*>(d + 3 * NV);
+    w.tf = reinterpret_cast<float2*>(d + 3 * NV);
+    float* f = reinterpret_cast<float*>(w.tf + NV);
     w.mb = f; w.mc = f + NV;
     float* q = f + 2 * NV;
     w.pa = q; w.pb = q + 2 * N; w.pc = q + 4 * N; w.p0 = q + 6 * N; w.p1 = q + 8 * N; w.p2 = q + 10 * N;
@@ -637,7 +641,7 @@ __device__ __forceinline__ ProjWS proj_ws(unsigned char* base, int NV, int N) {
 }
 // bytes of one polygon's workspace; a multiple of 16 when NV is even
 __host__ __device__ constexpr size_t proj_ws_bytes(int NV, int N) {
-    return (size_t)NV * (48 + 8) + (size_t)N * 12 * 4;
+    return (size_t)NV * (48 + 8 + 8) + (size_t)N * 12 * 4;
 }
 
 __global__ void __launch_bounds__(256, 4) k_project_warp(const double2* __restrict__ pos, const int* __restrict__ start,
@@ -697,6 +701,7 @@ __global__ void __launch_bounds__(256, 4) k_project_warp(const double2* __restri
                           (unsigned long long)__double_as_longlong(1e-28);
                 if (ok) { double il = rsqrt(len2); t = make_double2(dx * il, dy * il); }
                 w.t[k] = t;
+                w.tf[k] = make_float2(d2f_int(t.x), d2f_int(t.y));
                 w.mb[k] = ok ? 2.0f : 1.0f;
                 w.f[k] = force[st + k];
                 double2 a;
@@ -755,16 +760,34 @@ __global__ void __launch_bounds__(256, 4) k_project_warp(const double2* __restri
                     w.p1[k] -= fm * s;
                 }
                 __syncwarp();
-                // F' -= J lambda, q -= J mu with (J x)_k = -x_k t_k + x_{k-1} t_{k-1}
-                for (int k = lane; k < n; k += 32) {
-                    int kp = (k == 0) ? n - 1 : k - 1;
-                    double2 t = w.t[k], tp = w.t[kp];
-                    double l0 = f2d_int(w.p0[k]), l0p = f2d_int(w.p0[kp]);
-                    double l1 = f2d_int(w.p1[k]), l1p = f2d_int(w.p1[kp]);
-                    double2 f = w.f[k], a = w.q[k];
-                    f.x -= -l0 * t.x + l0p * tp.x; f.y -= -l0 * t.y + l0p * tp.y;
-                    a.x -= -l1 * t.x + l1p * tp.x; a.y -= -l1 * t.y + l1p * tp.y;
-                    w.f[k] = f; w.q[k] = a;
+                // F' -= J lambda, q -= J mu with (J x)_k = -x_k t_k + x_{k-1} t_{k-1}.
+                // An error in the direction of an update that leaves span(J)
+                // is invisible to the next residual J^T F', so the first
+                // (full-size) update uses the FP64 tangents; the later ones
+                // are corrections of relative size ~1e-5 and take FP32
+                // products (error ~1e-7 of the correction), added in FP64.
+                if (round == 0) {
+                    for (int k = lane; k < n; k += 32) {
+                        int kp = (k == 0) ? n - 1 : k - 1;
+                        double2 t = w.t[k], tp = w.t[kp];
+                        double l0 = f2d_int(w.p0[k]), l0p = f2d_int(w.p0[kp]);
+                        double l1 = f2d_int(w.p1[k]), l1p = f2d_int(w.p1[kp]);
+                        double2 f = w.f[k], a = w.q[k];
+                        f.x -= -l0 * t.x + l0p * tp.x; f.y -= -l0 * t.y + l0p * tp.y;
+                        a.x -= -l1 * t.x + l1p * tp.x; a.y -= -l1 * t.y + l1p * tp.y;
+                        w.f[k] = f; w.q[k] = a;
+                    }
+                } else {
+                    for (int k = lane; k < n; k += 32) {
+                        int kp = (k == 0) ? n - 1 : k - 1;
+                        float2 t = w.tf[k], tp = w.tf[kp];
+                        float l0 = w.p0[k], l0p = w.p0[kp];
+                        float l1 = w.p1[k], l1p = w.p1[kp];
+                        double2 f = w.f[k], a = w.q[k];
+                        f.x += f2d_int(l0 * t.x - l0p * tp.x); f.y += f2d_int(l0 * t.y - l0p * tp.y);
+                        a.x += f2d_int(l1 * t.x - l1p * tp.x); a.y += f2d_int(l1 * t.y - l1p * tp.y);
+                        w.f[k] = f; w.q[k] = a;
+                    }
                 }
                 __syncwarp();
             }
