@@ -549,13 +549,14 @@ __device__ __forceinline__ unsigned long long pack_key(int sj, int si, int i, in
 //  3. the reference's 3x3 cell rule on the edge-midpoint cells.
 struct EdgeCand { float4 box; int idx, cx, cy, pad; };
 
-__device__ int narrow_pair(const PairCtx& pc, const float4* ringA, const float4* ringB,
-                           EdgeCand* candA, EdgeCand* candB, int* queue,
-                           unsigned long long* recKey, float2* recTU, int recCap, int B,
-                           const double2* __restrict__ pos, const double2* __restrict__ edgeVec,
-                           const float4* __restrict__ polyInfo,
-                           const float4* __restrict__ polyBox,
-                           const int* __restrict__ polyFlags) {
+// Culls 1 and 2 of a staged pair: fills candA / candB with the edges whose
+// boxes meet the overlap box (self pair: candA only) and returns their
+// counts through nLA / nLB (0 when the polygon boxes are disjoint).
+__device__ void narrow_cull(const PairCtx& pc, const float4* ringA, const float4* ringB,
+                            EdgeCand* candA, EdgeCand* candB,
+                            const float4* __restrict__ polyInfo,
+                            const float4* __restrict__ polyBox,
+                            const int* __restrict__ polyFlags, int& nLAout, int& nLBout) {
     const int lane = threadIdx.x & 31;
     const unsigned lt = (1u << lane) - 1u;
     const int nA = pc.nA, nB = pc.nB;
@@ -578,7 +579,7 @@ __device__ int narrow_pair(const PairCtx& pc, const float4* ringA, const float4*
             ox0 = fmaxf(ba.x, bb.x + sx - 1e-6f) - m; ox1 = fminf(ba.y, bb.y + sx + 1e-6f) + m;
             oy0 = fmaxf(ba.z, bb.z + sy - 1e-6f) - m; oy1 = fminf(ba.w, bb.w + sy + 1e-6f) + m;
             // disjoint boxes: no edge of A (padded by m) reaches past the gap
-            if (ox0 > ox1 || oy0 > oy1) return 0;
+            if (ox0 > ox1 || oy0 > oy1) { nLAout = 0; nLBout = 0; return; }
         }
     } else {
         float ax0 = 3.f, ax1 = -3.f, ay0 = 3.f, ay1 = -3.f;
@@ -627,6 +628,24 @@ __device__ int narrow_pair(const PairCtx& pc, const float4* ringA, const float4*
     __syncwarp();
     const EdgeCand* cb = pc.self ? candA : candB;
     if (pc.self) nLB = nLA;
+    nLAout = nLA;
+    nLBout = nLB;
+}
+
+__device__ int narrow_pair(const PairCtx& pc, const float4* ringA, const float4* ringB,
+                           EdgeCand* candA, EdgeCand* candB, int* queue,
+                           unsigned long long* recKey, float2* recTU, int recCap, int B,
+                           const double2* __restrict__ pos, const double2* __restrict__ edgeVec,
+                           const float4* __restrict__ polyInfo,
+                           const float4* __restrict__ polyBox,
+                           const int* __restrict__ polyFlags) {
+    const int lane = threadIdx.x & 31;
+    const unsigned lt = (1u << lane) - 1u;
+    const int nA = pc.nA;
+    int nLA = 0, nLB = 0;
+    narrow_cull(pc, ringA, ringB, candA, candB, polyInfo, polyBox, polyFlags, nLA, nLB);
+    if (nLA == 0 || nLB == 0) return 0;
+    const EdgeCand* cb = pc.self ? candA : candB;
     bool wrapB = B >= 3;
     int qn = 0;
     int rec = 0;
@@ -716,15 +735,17 @@ __device__ int narrow_pair(const PairCtx& pc, const float4* ringA, const float4*
 // t >= u), take the smallest cyclic edge distance d = (l - i) mod n_si, then
 // the smallest u, then the smallest key (first in the reference's sorted
 // scan).  Writes the pair's records to global memory.
-__device__ void match_and_write(const PairCtx& pc, int R, const unsigned long long* recKey,
-                                const float2* recTU, Ctrl* ctrl, ContactWS& ws) {
+__device__ unsigned long long match_and_write(const PairCtx& pc, int R,
+                                              const unsigned long long* recKey,
+                                              const float2* recTU, Ctrl* ctrl, ContactWS& ws,
+                                              bool publishMax = true) {
     const int lane = threadIdx.x & 31;
     int base = 0;
     if (lane == 0) base = atomicAdd(&ctrl->numRecords, R);
     base = __shfl_sync(PCP_FULL, base, 0);
     if (base + R > ws.capRecords) {
         if (lane == 0) atomicOr(&ctrl->flags, kFlagRecordOverflow);
-        return;
+        return 0ull;
     }
     unsigned long long kmax = 0;
     for (int r = lane; r < R; r += 32) {
@@ -771,7 +792,10 @@ __device__ void match_and_write(const PairCtx& pc, int R, const unsigned long lo
         unsigned long long t = __shfl_xor_sync(PCP_FULL, kmax, o);
         kmax = t > kmax ? t : kmax;
     }
-    if (lane == 0 && R > 0) atomicMax(&ctrl->maxKey, kmax);
+    // the largest key (k_fixup's partner of last resort): published here, or
+    // gathered by the caller and published once
+    if (publishMax && lane == 0 && R > 0) atomicMax(&ctrl->maxKey, kmax);
+    return kmax;
 }
 
 __device__ __forceinline__ PairCtx make_ctx(int2 pr, const int* __restrict__ start) {
@@ -783,16 +807,28 @@ __device__ __forceinline__ PairCtx make_ctx(int2 pr, const int* __restrict__ sta
     return pc;
 }
 
+constexpr int kNarrowWarps = 4;
+// warp path: pairs whose crossings are still being tested (see k_narrow)
+constexpr int kSlots = 4;
+constexpr int kSlotRecords = 32;
+struct PairSlot {
+    int a, b, stA, stB, nA, nB, self, q;
+    int R;             // records found so far
+    int outstanding;   // queued edge pairs not yet tested
+    int state;         // kSlot* bits
+};
+constexpr int kSlotBusy = 1, kSlotDone = 2, kSlotOverflow = 4;
+
 struct alignas(16) WarpSmem {
     float4 ring[2][2 * kFastRing];
     EdgeCand candA[kFastRing];
     EdgeCand candB[kFastRing];
-    unsigned long long recKey[kFastRecords];
-    float2 recTU[kFastRecords];
+    unsigned long long recKey[kSlots][kSlotRecords];
+    float2 recTU[kSlots][kSlotRecords];
     int queue[64];
+    PairSlot slot[kSlots];
     unsigned long long bar[2];
 };
-constexpr int kNarrowWarps = 4;
 
 __device__ __forceinline__ void push_slow(int q, Ctrl* ctrl, ContactWS& ws) {
     int s = atomicAdd(&ctrl->numSlow, 1);
@@ -800,6 +836,40 @@ __device__ __forceinline__ void push_slow(int q, Ctrl* ctrl, ContactWS& ws) {
     else atomicOr(&ctrl->flags, kFlagSlowOverflow);
 }
 
+// Conservative FP32 form of the crossing test of edges (p, p2) and (q, q2):
+// false only when the FP64 test of cross_exact certainly rejects the pair.
+// The FP32 coordinates are within 6e-8 of the FP64 ones, so every component
+// of r = p2 - p, s = q2 - q, g = q - p is within d = 1.5e-7 of the FP64
+// vector (same minimum image while all components stay below 0.45), and
+// each of denom, g x s, g x r is within E = 4 M d + 2 d^2 + 4 2^-24 M^2 of
+// its FP64 value (M bounds the components).  With |denom| > E + 1e-12 the
+// FP64 denominator has the same sign and passes the 1e-12 test; t <= 0 is
+// then certain when (g x s) sgn < -E, t >= 1 when (g x s - denom) sgn > 2.5 E
+// (monotone rounding of the FP64 division), and likewise for u.
+__device__ __forceinline__ bool maybe_cross(float4 p, float4 p2, float4 q, float4 q2) {
+    const float rx = wrapf(p2.x - p.x), ry = wrapf(p2.y - p.y);
+    const float sx = wrapf(q2.x - q.x), sy = wrapf(q2.y - q.y);
+    const float gx = wrapf(q.x - p.x), gy = wrapf(q.y - p.y);
+    const float M = fmaxf(fmaxf(fmaxf(fabsf(rx), fabsf(ry)), fmaxf(fabsf(sx), fabsf(sy))),
+                          fmaxf(fabsf(gx), fabsf(gy)));
+    if (!(M < 0.45f)) return true;                      // (NaN too)
+    const float d = 1.5e-7f, Mb = M + d;
+    const float E = 4.f * Mb * d + 2.f * d * d + 2.4e-7f * Mb * Mb;
+    const float den = rx * sy - ry * sx;
+    if (!(fabsf(den) > E + 1e-12f)) return true;
+    const float sg = den > 0.f ? 1.f : -1.f;
+    const float nt = (gx * sy - gy * sx) * sg, nu = (gx * ry - gy * rx) * sg, dd = den * sg;
+    if (nt < -E || nu < -E) return false;
+    if (nt - dd > 2.5f * E || nu - dd > 2.5f * E) return false;
+    return true;
+}
+
+// Warp per pair (pairs claimed dynamically), rings staged by bulk copies into
+// a double buffer with bounded mbarrier waits.  The FP32 culls and the FP32
+// crossing test run per pair; the edge pairs they cannot reject are queued,
+// tagged with their pair's slot, and go through the exact FP64 test 32 at a
+// time across up to kSlots pairs, so the FP64 pipe sees full warps.  A pair
+// is matched and written once its last queued edge pair has been tested.
 __global__ void __launch_bounds__(32 * kNarrowWarps)
 k_narrow(const double2* __restrict__ pos, const int* __restrict__ start, int B,
          ContactWS ws, Ctrl* __restrict__ ctrl, const int* gate) {
@@ -808,18 +878,103 @@ k_narrow(const double2* __restrict__ pos, const int* __restrict__ start, int B,
     extern __shared__ __align__(128) unsigned char smem_raw[];
     WarpSmem& S = reinterpret_cast<WarpSmem*>(smem_raw)[threadIdx.x / 32];
     const int lane = threadIdx.x & 31;
+    const unsigned lt = (1u << lane) - 1u;
     const int numPairs = min(ctrl->numPairs, ws.capPairs);
     if (lane == 0) {
         mbar_init(&S.bar[0], 1);
         mbar_init(&S.bar[1], 1);
         fence_barrier_init();
     }
+    if (lane < kSlots) S.slot[lane].state = 0;
     __syncwarp();
     uint32_t phase[2] = {0u, 0u};
-    // claim the first pair and start its copy
-    int q = 0;
-    if (lane == 0) q = atomicAdd(&ctrl->pairCursor, 1);
-    q = __shfl_sync(PCP_FULL, q, 0);
+    int qn_ = 0;   // queued edge pairs
+    unsigned long long warpMaxKey = 0ull;
+
+    // exact FP64 test of the first cnt queued edge pairs
+    auto run_batch = [&](int cnt) {
+        bool hit = false;
+        unsigned long long key = 0;
+        float2 tuf = make_float2(0.f, 0.f);
+        int t = -1;
+        if (lane < cnt) {
+            int e = S.queue[lane];
+            t = e >> 16;
+            const PairSlot& sl = S.slot[t];
+            if (!(sl.state & kSlotOverflow)) {
+                int ea = e & 0xFF, eb = (e >> 8) & 0xFF;
+                int id1 = sl.stA + ea, nid = sl.stB + eb;
+                Crossing c = cross_exact(pos[id1], ws.edgeVec[id1], pos[nid], ws.edgeVec[nid]);
+                if (c.hit) {
+                    hit = true;
+                    if (c.denom > 0) {   // kernels.cuh:796-799, 862-867
+                        key = pack_key(sl.a, sl.b, eb, ea);
+                        tuf = make_float2((float)c.tt, (float)c.uu);
+                    } else {             // kernels.cuh:800-804, 868-873
+                        key = pack_key(sl.b, sl.a, ea, eb);
+                        tuf = make_float2((float)c.uu, (float)c.tt);
+                    }
+                }
+            }
+        }
+        for (int k = 0; k < kSlots; ++k) {
+            unsigned me = __ballot_sync(PCP_FULL, t == k);
+            if (!me) continue;
+            unsigned mh = __ballot_sync(PCP_FULL, hit && t == k);
+            int R0 = S.slot[k].R;
+            if (hit && t == k) {
+                int at = R0 + __popc(mh & lt);
+                if (at < kSlotRecords) { S.recKey[k][at] = key; S.recTU[k][at] = tuf; }
+            }
+            __syncwarp();
+            if (lane == 0) {
+                S.slot[k].R = R0 + __popc(mh);
+                if (R0 + __popc(mh) > kSlotRecords) S.slot[k].state |= kSlotOverflow;
+                S.slot[k].outstanding -= __popc(me);
+            }
+            __syncwarp();
+        }
+        // drop the tested entries from the front of the queue
+        int rest = qn_ - cnt;
+        int v = lane < rest ? S.queue[cnt + lane] : 0;
+        __syncwarp();
+        if (lane < rest) S.queue[lane] = v;
+        qn_ = rest;
+        __syncwarp();
+    };
+    // match and write (or hand to the block path) every slot whose pair is
+    // enumerated and fully tested
+    auto finalize_ready = [&]() {
+        for (int k = 0; k < kSlots; ++k) {
+            const int st = S.slot[k].state;
+            if ((st & kSlotBusy) && (st & kSlotDone) && S.slot[k].outstanding == 0) {
+                const PairSlot sl = S.slot[k];
+                if (sl.state & kSlotOverflow) {
+                    if (lane == 0) push_slow(sl.q, ctrl, ws);
+                } else if (sl.R > 0) {
+                    PairCtx pc;
+                    pc.a = sl.a; pc.b = sl.b; pc.stA = sl.stA; pc.stB = sl.stB;
+                    pc.nA = sl.nA; pc.nB = sl.nB; pc.self = sl.self != 0;
+                    unsigned long long km =
+                        match_and_write(pc, sl.R, S.recKey[k], S.recTU[k], ctrl, ws, false);
+                    warpMaxKey = km > warpMaxKey ? km : warpMaxKey;
+                }
+                __syncwarp();
+                if (lane == 0) S.slot[k].state = 0;
+                __syncwarp();
+            }
+        }
+    };
+    auto free_slot = [&]() -> int {
+        for (int k = 0; k < kSlots; ++k)
+            if (!(S.slot[k].state & kSlotBusy)) return k;
+        return -1;
+    };
+
+    // pairs dealt out round robin (warp w takes w, w + W, ...): no claim
+    // atomics on the hot path
+    const int warpsTotal = gridDim.x * kNarrowWarps;
+    int q = blockIdx.x * kNarrowWarps + (threadIdx.x >> 5);
     auto issue = [&](int qq, int stage) -> bool {
         // returns true when a copy was issued for pair qq into `stage`
         if (qq >= numPairs) return false;
@@ -837,12 +992,11 @@ k_narrow(const double2* __restrict__ pos, const int* __restrict__ start, int B,
         }
         return true;
     };
+    const bool wrapB = B >= 3;
     int stage = 0;
     bool inflight = issue(q, stage);
     while (q < numPairs) {
-        int qn = 0;
-        if (lane == 0) qn = atomicAdd(&ctrl->pairCursor, 1);
-        qn = __shfl_sync(PCP_FULL, qn, 0);
+        const int qn = q + warpsTotal;
         PairCtx pc = make_ctx(ws.pairs[q], start);
         if (!inflight) {
             // too large (or degenerate) for the warp path: hand to the block path
@@ -860,21 +1014,80 @@ k_narrow(const double2* __restrict__ pos, const int* __restrict__ start, int B,
             return;
         }
         phase[stage] ^= 1u;
-        const float4* ringA = &S.ring[stage][0];
-        const float4* ringB = pc.self ? ringA : &S.ring[stage][kFastRing];
-        int R = narrow_pair(pc, ringA, ringB, S.candA, S.candB, S.queue, S.recKey, S.recTU,
-                            kFastRecords, B, pos, ws.edgeVec, ws.polyInfo, ws.polyBox,
-                            ws.polyFlags);
-        if (R < 0) {
-            if (lane == 0) push_slow(q, ctrl, ws);
-        } else if (R > 0) {
-            match_and_write(pc, R, S.recKey, S.recTU, ctrl, ws);
+        // a slot for this pair (test what is queued when all are taken)
+        int t = free_slot();
+        if (t < 0) {
+            if (qn_ > 0) run_batch(qn_);
+            finalize_ready();
+            t = free_slot();
+        }
+        if (lane == 0) {
+            PairSlot& sl = S.slot[t];
+            sl.a = pc.a; sl.b = pc.b; sl.stA = pc.stA; sl.stB = pc.stB;
+            sl.nA = pc.nA; sl.nB = pc.nB; sl.self = pc.self ? 1 : 0; sl.q = q;
+            sl.R = 0; sl.outstanding = 0; sl.state = kSlotBusy;
         }
         __syncwarp();
+        const float4* ringA = &S.ring[stage][0];
+        const float4* ringB = pc.self ? ringA : &S.ring[stage][kFastRing];
+        int nLA = 0, nLB = 0;
+        narrow_cull(pc, ringA, ringB, S.candA, S.candB, ws.polyInfo, ws.polyBox, ws.polyFlags,
+                    nLA, nLB);
+        const EdgeCand* cb = pc.self ? S.candA : S.candB;
+        const int nA = pc.nA, nB = pc.nB;
+        // candidate edge pairs as (aw x bw) lane tiles: lane = a * bw + b
+        int lb = 0;
+        while ((1 << lb) < nLB && lb < 5) ++lb;
+        const int bw = 1 << lb, aw = 32 >> lb;
+        const int la = lane >> lb, lbb = lane & (bw - 1);
+        for (int b0 = 0; b0 < nLB; b0 += bw) {
+            for (int a0 = 0; a0 < nLA; a0 += aw) {
+                const int ia = a0 + la, ib = b0 + lbb;
+                bool ok = ia < nLA && ib < nLB;
+                EdgeCand ea, eb;
+                if (ok) { ea = S.candA[ia]; eb = cb[ib]; }
+                else {
+                    ea.box = eb.box = make_float4(0.f, 0.f, 0.f, 0.f);
+                    ea.idx = eb.idx = 0; ea.cx = eb.cx = 0; ea.cy = eb.cy = 0;
+                }
+                if (pc.self) {
+                    // id1 < nid, not adjacent (kernels.cuh:766-775)
+                    ok = ok && eb.idx > ea.idx + 1 && !(ea.idx == 0 && eb.idx == nA - 1);
+                }
+                ok = ok && !(eb.box.x > ea.box.y || eb.box.y < ea.box.x ||
+                             eb.box.z > ea.box.w || eb.box.w < ea.box.z);
+                if (wrapB) {
+                    int dx = abs(ea.cx - eb.cx), dy = abs(ea.cy - eb.cy);
+                    ok = ok && (dx <= 1 || dx == B - 1) && (dy <= 1 || dy == B - 1);
+                }
+                if (ok) {
+                    const int an = (ea.idx + 1 == nA) ? 0 : ea.idx + 1;
+                    const int bn = (eb.idx + 1 == nB) ? 0 : eb.idx + 1;
+                    ok = maybe_cross(ringA[ea.idx], ringA[an], ringB[eb.idx], ringB[bn]);
+                }
+                unsigned mk = __ballot_sync(PCP_FULL, ok);
+                if (mk) {
+                    if (ok) S.queue[qn_ + __popc(mk & lt)] = ea.idx | (eb.idx << 8) | (t << 16);
+                    if (lane == 0) S.slot[t].outstanding += __popc(mk);
+                    qn_ += __popc(mk);
+                    __syncwarp();
+                    if (qn_ >= 32) {
+                        run_batch(32);
+                        finalize_ready();   // other pairs may be complete now
+                    }
+                }
+            }
+        }
+        if (lane == 0) S.slot[t].state |= kSlotDone;
+        __syncwarp();
+        finalize_ready();
         stage = other;
         inflight = nextInflight;
         q = qn;
     }
+    if (qn_ > 0) run_batch(qn_);
+    finalize_ready();
+    if (lane == 0 && warpMaxKey) atomicMax(&ctrl->maxKey, warpMaxKey);
 }
 
 // Block path: one warp per block, rings loaded with plain loads into a large
