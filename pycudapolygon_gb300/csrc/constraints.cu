@@ -17,6 +17,7 @@
 
 #include "pcp_common.cuh"
 #include "pcp_internal.h"
+#include "pcp_fire.cuh"
 
 namespace pcp {
 
@@ -402,7 +403,9 @@ __global__ void __launch_bounds__(256, 4) k_shake(double2* __restrict__ pos, con
                         const double* __restrict__ targetEdge,
                         const double* __restrict__ targetArea, int maxIter, double tol,
                         int* __restrict__ itersOut, double* __restrict__ scratch, int nmaxSmem,
-                        Ctrl* fire, cudaGraphConditionalHandle retryCond, const int* gate) {
+                        Ctrl* fire, cudaGraphConditionalHandle retryCond,
+                        double2* __restrict__ vel, const Ctrl* __restrict__ dtc,
+                        const int* gate) {
     pdl_enter();
     if (gate_closed(gate)) return;
     extern __shared__ __align__(16) unsigned char shake_smem[];
@@ -555,9 +558,24 @@ __global__ void __launch_bounds__(256, 4) k_shake(double2* __restrict__ pos, con
                 }
                 __syncwarp();
             }
-            for (int k = lane; k < n; k += 32) {
-                double2 v = w.xs[k];
-                pos[st + k] = make_double2(v.x - floor(v.x), v.y - floor(v.y));
+            if (vel) {
+                // FIRE step: v += wrap(x_shake - x_before) / dt, the reference's
+                // rederivation from the displacement (model.cpp:436-438); a retry
+                // adds its own displacement on top
+                const double idt = 1.0 / dtc->dt;
+                for (int k = lane; k < n; k += 32) {
+                    double2 x = w.xs[k], y = pos[st + k], v = vel[st + k];
+                    x = make_double2(x.x - floor(x.x), x.y - floor(x.y));
+                    v.x += wrap(x.x - y.x) * idt;
+                    v.y += wrap(x.y - y.y) * idt;
+                    vel[st + k] = v;
+                    pos[st + k] = x;
+                }
+            } else {
+                for (int k = lane; k < n; k += 32) {
+                    double2 v = w.xs[k];
+                    pos[st + k] = make_double2(v.x - floor(v.x), v.y - floor(v.y));
+                }
             }
         }
     }
@@ -586,7 +604,7 @@ __global__ void __launch_bounds__(256, 4) k_shake(double2* __restrict__ pos, con
 cudaError_t launch_shake(double2* pos, const int* start, int P, int nmax, const double* targetEdge,
                          const double* targetArea, int maxIter, double tol, int* maxItersOut,
                          double* scratch, int V, const int* gate, cudaStream_t st, Ctrl* fire,
-                         cudaGraphConditionalHandle retryCond) {
+                         cudaGraphConditionalHandle retryCond, double2* vel, const Ctrl* dtc) {
     (void)V;
     if (P <= 0) return cudaSuccess;
     // per-warp workspace in shared memory when it fits (polygons up to ~1000
@@ -602,7 +620,7 @@ cudaError_t launch_shake(double2* pos, const int* start, int P, int nmax, const 
     size_t smem = per * wpb;
     launch_k(k_shake, dim3(nblk(P, wpb)), dim3(32 * wpb), smem, st, pos, start, P, targetEdge, targetArea, maxIter,
                                                    tol, maxItersOut, scratch, nmaxSmem, fire,
-                                                   retryCond, gate);
+                                                   retryCond, vel, dtc, gate);
     return cudaGetLastError();
 }
 
@@ -975,14 +993,6 @@ cudaError_t launch_xpbd_iteration(double2* pos, const int* start, int P,
 // All FIRE scalars stay in the device control block; the step is a fixed
 // launch sequence, so it is captured once as a CUDA graph.
 
-// zero the contact-search counters (everything in Ctrl before `energy`)
-__device__ __forceinline__ void zero_contact_counters(Ctrl* c) {
-    int* w = reinterpret_cast<int*>(c);
-    constexpr int n = (int)(offsetof(Ctrl, energy) / sizeof(int));
-#pragma unroll
-    for (int i = 0; i < n; ++i) w[i] = 0;
-}
-
 // Step start (model.cpp:405-430): the per-step resets of the control block,
 // snapshots of x, v and F (for the rollbacks and for buffer-overflow
 // recovery), the Verlet half-kick and drift, the pre-SHAKE copy of the new
@@ -997,16 +1007,7 @@ __global__ void k_fire_begin(double2* __restrict__ pos, double2* __restrict__ ve
     int i = blockIdx.x * blockDim.x + threadIdx.x;
     const double dt = c->dt;
     if (i == 0) {
-        c->ePre = c->energy;
-        c->energy = 0.0;
-        c->snapDt = dt; c->snapAlpha = c->alpha; c->snapNPos = c->nPos;
-        c->maxF = 0.0;
-        c->P = 0.0; c->vv = 0.0; c->ff = 0.0;
-        c->shakeIters1 = 0; c->shakeIters2 = 0;
-        c->needRetry = 0; c->retryGate = 0;
-        c->shakeFailed = 0;
-        c->rollback = 0; c->rbGate = 0; c->proceed = 0;
-        c->shakeTicket = 0; c->bendTicket = 0;
+        fire_step_resets(c);
         if (resetContacts) zero_contact_counters(c);
     }
     if (i < V) {
@@ -1024,34 +1025,23 @@ __global__ void k_fire_begin(double2* __restrict__ pos, double2* __restrict__ ve
     }
 }
 
-// After SHAKE (model.cpp:431-438): the outcome of the retry (when the first
-// attempt asked for one), then on failure restore the step's start positions
-// and zero v, on success rederive v from the SHAKE displacement.
-__global__ void k_fire_after_shake(double2* __restrict__ pos, double2* __restrict__ vel,
-                                   const double2* __restrict__ save,
-                                   const double2* __restrict__ verlet, int V,
-                                   Ctrl* __restrict__ c, const int* gate) {
+// Last kernel of the SHAKE-retry body (model.cpp:431-438): the retry's
+// outcome; when it failed too, restore the step's start positions and zero
+// v (the SHAKE kernels have already rederived v from their displacements).
+__global__ void k_fire_retry_outcome(double2* __restrict__ pos, double2* __restrict__ vel,
+                                     const double2* __restrict__ save, int V,
+                                     Ctrl* __restrict__ c) {
     pdl_enter();
-    if (gate_closed(gate)) return;
     int i = blockIdx.x * blockDim.x + threadIdx.x;
-    const bool retried = c->needRetry != 0;
-    const bool failed = retried && c->shakeIters2 >= 10 * c->shakeIter;
-    if (i == 0 && retried) {
+    const bool failed = c->shakeIters2 >= 10 * c->shakeIter;
+    if (i == 0) {
         c->shakeLast = c->shakeIters2;
         c->shakeFailed = failed ? 1 : 0;
-        c->condLaunches += 1;          // the retry ran in a conditional body
+        c->condLaunches += 2;          // the retry SHAKE and this kernel
     }
-    if (i >= V) return;
-    if (failed) {
-        pos[i] = save[i];
-        vel[i] = make_double2(0.0, 0.0);
-    } else {
-        double idt = 1.0 / c->dt;
-        double2 x = pos[i], y = verlet[i], v = vel[i];
-        v.x += wrap(x.x - y.x) * idt;
-        v.y += wrap(x.y - y.y) * idt;
-        vel[i] = v;
-    }
+    if (i >= V || !failed) return;
+    pos[i] = save[i];
+    vel[i] = make_double2(0.0, 0.0);
 }
 
 // Energy-increase rollback (model.cpp:453-465), first kernel of the
@@ -1172,6 +1162,7 @@ __device__ void fire_scalars(Ctrl* __restrict__ c) {
     }
     c->dt = dt; c->alpha = alpha; c->nPos = nPos;
     c->stepsDone += 1;
+    c->Rmax = 0.f;     // for the next step's fused start (see zero_contact_counters_but_rmax)
     if (c->maxF <= c->threshold) { c->converged = 1; c->active = 0; }
     if (c->stepLimit > 0 && c->stepsDone >= c->stepLimit) c->active = 0;
 }
@@ -1226,6 +1217,7 @@ __global__ void k_set_fire_params(Ctrl* __restrict__ c, FireScalars f) {
     if (f.resetRun) { c->converged = 0; c->stepsDone = 0; }
     c->stepLimit = f.stepLimit;
     c->rbBodyKernels = f.rbBodyKernels;
+    c->Rmax = 0.f;
 }
 
 // --------------------------------------------------------------- launchers ----
@@ -1240,10 +1232,9 @@ cudaError_t launch_fire_begin(double2* pos, double2* vel, double2* force, double
                                                V, resetContacts, c, gate);
     return cudaGetLastError();
 }
-cudaError_t launch_fire_after_shake(double2* pos, double2* vel, const double2* save,
-                                    const double2* verlet, int V, Ctrl* c, const int* gate,
-                                    cudaStream_t st) {
-    launch_k(k_fire_after_shake, dim3(nblk(V, 256)), dim3(256), 0, st, pos, vel, save, verlet, V, c, gate);
+cudaError_t launch_fire_retry_outcome(double2* pos, double2* vel, const double2* save, int V,
+                                      Ctrl* c, cudaStream_t st) {
+    launch_k(k_fire_retry_outcome, dim3(nblk(V, 256)), dim3(256), 0, st, pos, vel, save, V, c);
     return cudaGetLastError();
 }
 cudaError_t launch_fire_rollback(double2* pos, double2* vel, double2* force, const double2* save,
@@ -1314,7 +1305,8 @@ cudaError_t launch_shake_noalloc(double2* pos, const int* start, int P, const do
     if (P <= 0) return cudaSuccess;
     constexpr int wpb = 8;
     launch_k(k_shake, dim3(nblk(P, wpb)), dim3(32 * wpb), 0, st, pos, start, P, targetEdge, targetArea, maxIter, tol,
-                                               maxItersOut, scratch, 0, nullptr, 0, nullptr);
+                                               maxItersOut, scratch, 0, nullptr, 0, nullptr, nullptr,
+                                               nullptr);
     return cudaGetLastError();
 }
 

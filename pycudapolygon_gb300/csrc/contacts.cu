@@ -32,6 +32,7 @@
 
 #include "pcp_common.cuh"
 #include "pcp_internal.h"
+#include "pcp_fire.cuh"
 
 namespace pcp {
 
@@ -59,11 +60,11 @@ __global__ void k_reset_contacts(Ctrl* __restrict__ ctrl, const int* gate) {
 }
 
 __global__ void __launch_bounds__(256)
-k_prepass(const double2* __restrict__ pos, const int* __restrict__ start,
+k_prepass(double2* __restrict__ pos, const int* __restrict__ start,
           const int* __restrict__ cellLocation, int* __restrict__ cellOut, int P, int B,
           double2* __restrict__ edgeVec, float4* __restrict__ vtx, float4* __restrict__ polyInfo,
-          float4* __restrict__ polyBox, int* __restrict__ polyFlags, int* __restrict__ unsafeList,
-          Ctrl* __restrict__ ctrl, const int* gate) {
+          float4* __restrict__ polyBox, int* __restrict__ polyFlags,
+          Ctrl* __restrict__ ctrl, FireMove mv, const int* gate) {
     pdl_enter();
     if (gate_closed(gate)) return;
     __shared__ float s_r[8];
@@ -72,6 +73,17 @@ k_prepass(const double2* __restrict__ pos, const int* __restrict__ start,
     float Rsafe = 0.f;
     const int st = p < P ? start[p] : 0;
     const int n = p < P ? start[p + 1] - st : 0;
+    if (mv.pos) {
+        // start of a FIRE step: resets (Rmax was zeroed at the end of the
+        // last step and is accumulated below), then this polygon's Verlet move
+        if (blockIdx.x == 0 && threadIdx.x == 0) {
+            fire_step_resets(mv.c);
+            zero_contact_counters_but_rmax(mv.c);
+        }
+        const double dt = mv.c->dt;
+        for (int kl = lane; kl < n; kl += 32) pos[st + kl] = fire_move_vertex(mv, st + kl, dt);
+        __syncwarp();
+    }
     if (p < P && n <= 0) {   // empty polygon: no edges, never a candidate
         if (lane == 0) {
             polyInfo[p] = make_float4(0.f, 0.f, 0.f, 0.f);
@@ -157,7 +169,6 @@ k_prepass(const double2* __restrict__ pos, const int* __restrict__ start,
             // not searched
             polyFlags[p] = safe ? ((star && n >= 4) ? 3 : 1) : 0;
             if (safe) Rsafe = R;
-            else unsafeList[atomicAdd(&ctrl->numUnsafe, 1)] = p;
         }
     }
     // one atomic per block for the largest safe radius
@@ -1339,9 +1350,12 @@ cudaError_t launch_contacts(const double2* pos, const int* start, const int* sha
     if (stages & 1) {
     if (!(stages & 4)) launch_k(k_reset_contacts, dim3(1), dim3(64), 0, st, ctrl, gate);
     if (P <= 0) return cudaGetLastError();
-    launch_k(k_prepass, dim3(nblocks(P, 8)), dim3(256), 0, st, pos, start, cellLocation, cellOut, P, B, ws.edgeVec,
-                                             ws.vtx, ws.polyInfo, ws.polyBox, ws.polyFlags,
-                                             ws.unsafeList, ctrl, gate);
+    if (!(stages & kContactsNoPrepass)) {
+        FireMove none = {};
+        launch_k(k_prepass, dim3(nblocks(P, 8)), dim3(256), 0, st, const_cast<double2*>(pos), start,
+                 cellLocation, cellOut, P, B, ws.edgeVec, ws.vtx, ws.polyInfo, ws.polyBox,
+                 ws.polyFlags, ctrl, none, gate);
+    }
     if (P <= kFusedMaxPolys) {
         launch_k(k_grid_fused, dim3(1), dim3(1024), 0, st, ws.polyInfo, ws.polyFlags, P,
                  ws.gridCount, ws.gridStart, ws.sortedPoly, ctrl, gate);
@@ -1363,6 +1377,17 @@ cudaError_t launch_contacts(const double2* pos, const int* start, const int* sha
         // pairs for the block path are rare: a few blocks take them in turn
         launch_k(k_narrow_slow, dim3(16), dim3(32), kSlowSmem, st, pos, start, B, ws, ctrl, gate);
     }
+    return cudaGetLastError();
+}
+
+cudaError_t launch_prepass_move(double2* verlet, const int* start, int* cellOut, int P, int B,
+                                ContactWS& ws, Ctrl* ctrl, const int* gate, cudaStream_t st,
+                                const FireMove& mv) {
+    if (B < 1) B = 1;
+    if (P <= 0) return cudaSuccess;
+    launch_k(k_prepass, dim3(nblocks(P, 8)), dim3(256), 0, st, verlet, start,
+             static_cast<const int*>(nullptr), cellOut, P, B, ws.edgeVec, ws.vtx, ws.polyInfo,
+             ws.polyBox, ws.polyFlags, ctrl, mv, gate);
     return cudaGetLastError();
 }
 

@@ -523,8 +523,8 @@ int count_kernel_nodes(cudaGraph_t g) {
 // One FIRE step (Model::minimizeFIREStep, model.cpp:405-486) recorded on the
 // capturing stream m->stream.  Graph layout (normal model with SHAKE):
 //
-//   begin --+-- SHAKE -- [IF retry: SHAKE x10] -- after_shake --+-- force --
-//           +-- contact search on the pre-SHAKE copy ------------+
+//   begin --+-- SHAKE (+ v) -- [IF retry: SHAKE x10 (+ v), outcome] --+-- force --
+//           +-- contact search on the pre-SHAKE copy ------------------+
 //   -- projection (decides the rollback) -- [IF rollback: restore, contact
 //   search, force, projection] -- bend + scalar bookkeeping
 //
@@ -540,31 +540,41 @@ int record_fire_step(pcp_model* m, cudaGraphConditionalHandle retryCond,
     bool shake = rigid && m->fireShakeIter > 0;
     int V = m->V;
     const int noReset = 3 | kContactsNoReset;
-    CK(launch_fire_begin(m->pos, m->vel, m->force, m->posTMP2, m->velSnap, m->forceSnap,
-                         shake ? m->posTMP : nullptr, V, needsI ? 1 : 0, m->ctrl, gA, st));
+    if (needsI) {
+        // the step start fused with the contact prepass: x, v, F moved in
+        // place, the moved positions copied to posTMP (read by the search)
+        FireMove mv = {m->pos, m->vel, m->force, m->posTMP2, m->velSnap, m->forceSnap, m->ctrl};
+        CK(launch_prepass_move(shake ? m->posTMP : m->pos, m->start, m->cellLocation, m->P,
+                               m->boxSize, m->ws, m->ctrl, gA, st, mv));
+    } else {
+        CK(launch_fire_begin(m->pos, m->vel, m->force, m->posTMP2, m->velSnap, m->forceSnap,
+                             nullptr, V, 0, m->ctrl, gA, st));
+    }
     if (shake) {
         CK(cudaEventRecord(m->evFork, st));
         CK(cudaStreamWaitEvent(m->sideStream, m->evFork, 0));
         CK(launch_contacts(m->posTMP, m->start, m->shapeId, m->cellLocation, m->P, V,
-                           m->boxSize, m->ws, m->ctrl, gA, m->sideStream, noReset,
-                           m->cellLocation));
+                           m->boxSize, m->ws, m->ctrl, gA, m->sideStream,
+                           noReset | kContactsNoPrepass, m->cellLocation));
         CK(launch_contacts_finish(m->start, m->ws, m->ctrl, gA, m->sideStream));
         CK(cudaEventRecord(m->evJoin, m->sideStream));
+        // SHAKE rederives v from its displacement itself (model.cpp:436-438)
         CK(launch_shake(m->pos, m->start, m->P, m->nmax, m->targetEdge, m->targetAreas,
                         m->fireShakeIter, 1e-15, &m->ctrl->shakeIters1, m->scratch, V, gA, st,
-                        m->ctrl, retryCond));
+                        m->ctrl, retryCond, m->vel, m->ctrl));
         int rc = begin_if(st, retryCond, m->bodyStream);
         if (rc) return rc;
         CK(launch_shake(m->pos, m->start, m->P, m->nmax, m->targetEdge, m->targetAreas,
                         m->fireShakeIter * 10, 1e-15, &m->ctrl->shakeIters2, m->scratch, V,
-                        nullptr, m->bodyStream));
+                        nullptr, m->bodyStream, nullptr, 0, m->vel, m->ctrl));
+        CK(launch_fire_retry_outcome(m->pos, m->vel, m->posTMP2, V, m->ctrl, m->bodyStream));
         cudaGraph_t body = nullptr;
         CK(cudaStreamEndCapture(m->bodyStream, &body));
-        CK(launch_fire_after_shake(m->pos, m->vel, m->posTMP2, m->posTMP, V, m->ctrl, gA, st));
         CK(cudaStreamWaitEvent(st, m->evJoin, 0));
     } else if (needsI) {
         CK(launch_contacts(m->pos, m->start, m->shapeId, m->cellLocation, m->P, V, m->boxSize,
-                           m->ws, m->ctrl, gA, st, noReset, m->cellLocation));
+                           m->ws, m->ctrl, gA, st, noReset | kContactsNoPrepass,
+                           m->cellLocation));
         CK(launch_contacts_finish(m->start, m->ws, m->ctrl, gA, st));
     }
     // The normal model reads nothing of the geometry inside the step (the
@@ -706,6 +716,7 @@ int recover_fire(pcp_model* m, bool& redo) {
     c.energy = c.ePre;
     c.dt = c.snapDt; c.alpha = c.snapAlpha; c.nPos = c.snapNPos;
     c.flags = 0; c.needsRecovery = 0; c.active = 1;
+    c.Rmax = 0.f;            // the step's fused start accumulates it afresh
     *m->ctrlHost = c;
     CK(cudaMemcpyAsync(m->ctrl, m->ctrlHost, sizeof(Ctrl), cudaMemcpyHostToDevice, m->stream));
     rc = sync(m);

@@ -1,0 +1,59 @@
+// pcp_fire.cuh -- device helpers of the FIRE step shared by the contact and
+// constraint translation units (sm_103a).
+#pragma once
+
+#include <stddef.h>
+
+#include "pcp_common.cuh"
+#include "pcp_internal.h"
+
+namespace pcp {
+
+// zero the contact-search counters (everything in Ctrl before `energy`)
+__device__ __forceinline__ void zero_contact_counters(Ctrl* c) {
+    int* w = reinterpret_cast<int*>(c);
+    constexpr int n = (int)(offsetof(Ctrl, energy) / sizeof(int));
+#pragma unroll
+    for (int i = 0; i < n; ++i) w[i] = 0;
+}
+
+// the same but for Rmax, which the prepass accumulates while this runs in
+// the fused step-start kernel (it is zeroed at the end of the step before)
+__device__ __forceinline__ void zero_contact_counters_but_rmax(Ctrl* c) {
+    const float r = c->Rmax;
+    zero_contact_counters(c);
+    c->Rmax = r;
+}
+
+// per-step resets of the control block at the start of a FIRE step
+__device__ __forceinline__ void fire_step_resets(Ctrl* c) {
+    c->ePre = c->energy;
+    c->energy = 0.0;
+    c->snapDt = c->dt; c->snapAlpha = c->alpha; c->snapNPos = c->nPos;
+    c->maxF = 0.0;
+    c->P = 0.0; c->vv = 0.0; c->ff = 0.0;
+    c->shakeIters1 = 0; c->shakeIters2 = 0;
+    c->needRetry = 0; c->retryGate = 0;
+    c->shakeFailed = 0;
+    c->rollback = 0; c->rbGate = 0; c->proceed = 0;
+    c->shakeTicket = 0; c->bendTicket = 0;
+}
+
+// Verlet half-kick and drift of vertex i (model.cpp:405-430) with the
+// snapshots the rollbacks and the overflow recovery restore from; F = 0 for
+// the coming force pass.  Returns the new position.
+__device__ __forceinline__ double2 fire_move_vertex(const FireMove& mv, int i, double dt) {
+    double2 x = mv.pos[i], v = mv.vel[i], f = mv.force[i];
+    mv.save[i] = x;
+    mv.velSnap[i] = v;
+    mv.forceSnap[i] = f;
+    v.x += 0.5 * dt * f.x; v.y += 0.5 * dt * f.y;
+    double px = x.x + dt * v.x, py = x.y + dt * v.y;
+    mv.vel[i] = v;
+    double2 xn = make_double2(px - floor(px), py - floor(py));
+    mv.pos[i] = xn;
+    mv.force[i] = make_double2(0.0, 0.0);
+    return xn;
+}
+
+}  // namespace pcp

@@ -104,6 +104,13 @@ struct ContactWS {
     int* slowList = nullptr;        // [capSlow] pair indices for the block path
 };
 
+// The Verlet move of a FIRE step, done by the step-start kernel (pos == null:
+// no move): x, v, F in place, and their snapshots.
+struct FireMove {
+    double2 *pos, *vel, *force, *save, *velSnap, *forceSnap;
+    Ctrl* c;
+};
+
 // --- launchers (all asynchronous on `st`) ---
 cudaError_t launch_topology(const int* start, int P, int V, int* shapeId, int* next, int* prev,
                             cudaStream_t st);
@@ -142,10 +149,19 @@ cudaError_t contacts_init();
 // skip the counter reset (done by the caller); cellOut: compute the edge
 // midpoint cells in the prepass and store them there (cellLocation unused)
 constexpr int kContactsNoReset = 4;
+// bit 3: skip the prepass (already run by launch_prepass_move)
+constexpr int kContactsNoPrepass = 8;
 cudaError_t launch_contacts(const double2* pos, const int* start, const int* shapeId,
                             const int* cellLocation, int P, int V, int B, ContactWS& ws,
                             Ctrl* ctrl, const int* gate, cudaStream_t st, int stages = 3,
                             int* cellOut = nullptr);
+// The start of a FIRE step fused with the contact prepass (warp per polygon):
+// the control-block resets, the Verlet move of mv (positions moved in place
+// and copied to `verlet`, which the search then reads), and the prepass on
+// the moved positions with the cells stored in cellOut.
+cudaError_t launch_prepass_move(double2* verlet, const int* start, int* cellOut, int P, int B,
+                                ContactWS& ws, Ctrl* ctrl, const int* gate, cudaStream_t st,
+                                const FireMove& mv);
 cudaError_t launch_contacts_finish(const int* start, ContactWS& ws, Ctrl* ctrl,
                                    const int* gate, cudaStream_t st);
 cudaError_t launch_overlap_force(const double2* pos, const int* start, const int* next,
@@ -164,11 +180,13 @@ cudaError_t launch_project(const double2* pos, const int* start, int P, int nmax
                            cudaStream_t st, cudaGraphConditionalHandle rbCond = 0,
                            int useCond = 0);
 // fire (device-resident FIRE step, first SHAKE attempt): the last block to
-// finish decides whether the retry runs and sets `retryCond` of the step graph
+// finish decides whether the retry runs and sets `retryCond` of the step
+// graph; vel (with dtc for dt): also rederive v from the SHAKE displacement
 cudaError_t launch_shake(double2* pos, const int* start, int P, int nmax, const double* targetEdge,
                          const double* targetArea, int maxIter, double tol, int* maxItersOut,
                          double* scratch, int V, const int* gate, cudaStream_t st,
-                         Ctrl* fire = nullptr, cudaGraphConditionalHandle retryCond = 0);
+                         Ctrl* fire = nullptr, cudaGraphConditionalHandle retryCond = 0,
+                         double2* vel = nullptr, const Ctrl* dtc = nullptr);
 // scratch doubles per vertex needed by launch_project / launch_shake
 constexpr int kScratchPerVertex = 36;
 // pcp_shake_project_noalloc: device address of its static workspace on the
@@ -193,9 +211,8 @@ cudaError_t launch_set_fire_params(Ctrl* c, const FireScalars& f, cudaStream_t s
 cudaError_t launch_fire_begin(double2* pos, double2* vel, double2* force, double2* save,
                               double2* velSnap, double2* forceSnap, double2* verlet, int V,
                               int resetContacts, Ctrl* c, const int* gate, cudaStream_t st);
-cudaError_t launch_fire_after_shake(double2* pos, double2* vel, const double2* save,
-                                    const double2* verlet, int V, Ctrl* c, const int* gate,
-                                    cudaStream_t st);
+cudaError_t launch_fire_retry_outcome(double2* pos, double2* vel, const double2* save, int V,
+                                      Ctrl* c, cudaStream_t st);
 cudaError_t launch_fire_rollback(double2* pos, double2* vel, double2* force, const double2* save,
                                  int V, int resetContacts, Ctrl* c, cudaStream_t st);
 cudaError_t launch_zero_force(double2* force, int V, Ctrl* c, const int* gate, cudaStream_t st);

@@ -290,6 +290,46 @@ def test_fire_steps_parity():
     assert np.abs(d).max() < 1e-9
 
 
+def test_fire_rollback_state_matches_reference():
+    """An energy-increase rollback (model.cpp:450-470) leaves the step's start
+    positions, the force, energy and max |F| there, and the contact records of
+    those positions: the oracle recomputes them all, as the reference does;
+    the GPU restores its step-start snapshot and refreshes the records when
+    they are read.  This system's FIRE run rolls back at step 42."""
+    s = make_system(32, 12, 0.88, seed=9)
+    g, o = pair(s)
+    for m in (g, o):
+        m.shakeProject(200, 1e-15)
+        contacts(m)
+        m.updateForceEnergy()
+        m.projectForce()
+    st_g = st_o = (1e-3, 0.1, 0)
+    rolled = None
+    for step in range(60):
+        x_o = np.asarray(o.getPositions()).copy()
+        x_g = np.asarray(g.getPositions()).copy()
+        rg = g.minimizeFIREStep(*st_g)
+        ro = o.minimizeFIREStep(*st_o)
+        assert rg[0] == pytest.approx(ro[0], rel=1e-9, abs=1e-14), step
+        assert rg[1:] == pytest.approx(ro[1:], rel=1e-12), step
+        st_g, st_o = rg[1:], ro[1:]
+        if np.array_equal(np.asarray(o.getPositions()), x_o) and o.getLastShakeIters() < 50:
+            rolled = step
+            assert np.array_equal(np.asarray(g.getPositions()), x_g)
+            break
+    assert rolled is not None
+    assert g.getEnergy() == pytest.approx(o.getEnergy(), rel=1e-9)
+    assert_forces_close(g.getForces(), o.getForces())
+    assert g.getMaxUnbalancedForce() == pytest.approx(o.getMaxUnbalancedForce(), rel=1e-9)
+    assert_records_equal(g, o)
+    # and the run continues from the restored state
+    rg = g.minimizeFIREStep(*st_g)
+    ro = o.minimizeFIREStep(*st_o)
+    assert rg[0] == pytest.approx(ro[0], rel=1e-9, abs=1e-14)
+    d = (np.asarray(g.getPositions()) - o.getPositions() + 0.5) % 1.0 - 0.5
+    assert np.abs(d).max() < 1e-9
+
+
 def test_minimize_fire_matches_step_loop():
     """Model::minimizeFIRE (graph loop with the stop test on the device) walks
     the same trajectory as repeated minimizeFIREStep calls."""
