@@ -399,6 +399,56 @@ __device__ __forceinline__ bool sm_split(float* pa, float* pb, float* pc, float*
     return ok;
 }
 
+// Position correction of one vertex, x_k += -l_k r_k + l_{k-1} r_{k-1} +
+// mu ar_k, with the FP32 multipliers.  In FP64 while the correction is
+// large.  Once the sum S of the terms' magnitudes is below 2^-26 (the later
+// iterations, whose corrections are the FP32 solve's small leftovers) the
+// FP32 form is used: its error, at most 6 * 2^-24 * S < 6e-15, is far below
+// the 1e-12 position tolerance, and it turns 8 FP64 operations per vertex
+// into the 2 adds.
+__device__ __forceinline__ void shake_update(double2& x, float lk, float lp, float mu, double mu64,
+                                             double2 rk, double2 rp, double2 ak, float2 rkf,
+                                             float2 rpf, float2 akf) {
+    const float S = fabsf(lk) * (fabsf(rkf.x) + fabsf(rkf.y)) +
+                    fabsf(lp) * (fabsf(rpf.x) + fabsf(rpf.y)) +
+                    fabsf(mu) * (fabsf(akf.x) + fabsf(akf.y));
+    if (S < 0x1p-26f) {
+        const float dx = -lk * rkf.x + lp * rpf.x + mu * akf.x;
+        const float dy = -lk * rkf.y + lp * rpf.y + mu * akf.y;
+        x.x += f2d_int(dx);
+        x.y += f2d_int(dy);
+    } else {
+        const double l64 = f2d_int(lk), p64 = f2d_int(lp);
+        x.x += -l64 * rk.x + p64 * rp.x + mu64 * ak.x;
+        x.y += -l64 * rk.y + p64 * rp.y + mu64 * ak.y;
+    }
+}
+
+// End of a SHAKE launch, reached by every thread of the block: the largest
+// iteration count, and in the first attempt of a FIRE step (model.cpp:431-436)
+// the last block to finish reads it and decides the retry.
+__device__ __forceinline__ void shake_finish(int it, int* itersOut, Ctrl* fire,
+                                             cudaGraphConditionalHandle retryCond) {
+    if ((threadIdx.x & 31) == 0 && it > 0) atomicMax(itersOut, it);
+    if (fire) {
+        __syncthreads();
+        if (threadIdx.x == 0) {
+            __threadfence();
+            unsigned int t = atomicAdd(&fire->shakeTicket, 1u);
+            if (t == gridDim.x - 1) {
+                __threadfence();
+                int it1 = atomicOr(itersOut, 0);
+                fire->shakeLast = it1;
+                int nr = (it1 >= fire->shakeIter) ? 1 : 0;
+                int go = (nr && fire->active) ? 1 : 0;
+                fire->needRetry = nr;
+                fire->retryGate = go;
+                cudaGraphSetConditional(retryCond, (unsigned int)go);
+            }
+        }
+    }
+}
+
 __global__ void __launch_bounds__(256, 4) k_shake(double2* __restrict__ pos, const int* __restrict__ start, int P,
                         const double* __restrict__ targetEdge,
                         const double* __restrict__ targetArea, int maxIter, double tol,
@@ -461,12 +511,12 @@ __global__ void __launch_bounds__(256, 4) k_shake(double2* __restrict__ pos, con
                     unsigned long long q = abs_bits(sk * invL);
                     if (q > worst) worst = q;
                     double X1 = wrap(xk.x - x0x), X2 = wrap(xn.x - x0x);
-                    area += ey * (X2 + X1) / 2.0;
+                    area += ey * (X2 + X1);       // halved after the sum (exact)
                     w.ef[k] = make_float2(d2f_int(ex), d2f_int(ey));
                     w.lam[k] = d2f_int(-sk);      // right-hand side until the rows are built
                 }
                 worst = warp_max_u64(worst);
-                area = warp_sum(area);
+                area = warp_sum(area) * 0.5;
                 nonfinite = __any_sync(PCP_FULL, nonfinite);
                 double sA = area - A0;
                 {
@@ -545,15 +595,13 @@ __global__ void __launch_bounds__(256, 4) k_shake(double2* __restrict__ pos, con
                 }
                 if (!__all_sync(PCP_FULL, finite)) { it = maxIter; break; }
                 __syncwarp();
-                // x_k += -l_k r_k + l_{k-1} r_{k-1} + mu ar_k   (FP64)
+                // x_k += -l_k r_k + l_{k-1} r_{k-1} + mu ar_k
                 double mu64 = f2d_int(mu);
                 for (int k = lane; k < n; k += 32) {
                     int kp = (k == 0) ? n - 1 : k - 1;
-                    double lk = f2d_int(w.lam[k]), lp = f2d_int(w.lam[kp]);
-                    double2 rk = w.r[k], rp = w.r[kp], ak = w.ar[k];
                     double2 x = w.xs[k];
-                    x.x += -lk * rk.x + lp * rp.x + mu64 * ak.x;
-                    x.y += -lk * rk.y + lp * rp.y + mu64 * ak.y;
+                    shake_update(x, w.lam[k], w.lam[kp], mu, mu64, w.r[k], w.r[kp], w.ar[k], w.rf[k],
+                                 w.rf[kp], w.arf[k]);
                     w.xs[k] = x;
                 }
                 __syncwarp();
@@ -579,26 +627,174 @@ __global__ void __launch_bounds__(256, 4) k_shake(double2* __restrict__ pos, con
             }
         }
     }
-    if (lane == 0 && it > 0) atomicMax(itersOut, it);
-    if (fire) {
-        // first attempt of a FIRE step (model.cpp:431-436): the last block to
-        // finish reads the largest iteration count and decides the retry
-        __syncthreads();
-        if (threadIdx.x == 0) {
-            __threadfence();
-            unsigned int t = atomicAdd(&fire->shakeTicket, 1u);
-            if (t == gridDim.x - 1) {
-                __threadfence();
-                int it1 = atomicOr(itersOut, 0);
-                fire->shakeLast = it1;
-                int nr = (it1 >= fire->shakeIter) ? 1 : 0;
-                int go = (nr && fire->active) ? 1 : 0;
-                fire->needRetry = nr;
-                fire->retryGate = go;
-                cudaGraphSetConditional(retryCond, (unsigned int)go);
+    shake_finish(it, itersOut, fire, retryCond);
+}
+
+__device__ __forceinline__ double2 shfl2(double2 v, int src) {
+    return make_double2(__shfl_sync(PCP_FULL, v.x, src), __shfl_sync(PCP_FULL, v.y, src));
+}
+__device__ __forceinline__ float2 shfl2(float2 v, int src) {
+    return make_float2(__shfl_sync(PCP_FULL, v.x, src), __shfl_sync(PCP_FULL, v.y, src));
+}
+
+// pcr3f with row i held by lane i (rows 0..N-1, N <= 32; partner rows read
+// by shuffles), expression for expression: leaves the solutions in q0..q2.
+__device__ __forceinline__ void lanes_pcr3(float a, float b, float c, float& q0, float& q1,
+                                           float& q2, int N, int lane) {
+    for (int d = 1; d < N; d <<= 1) {
+        const float am = __shfl_up_sync(PCP_FULL, a, d), bm = __shfl_up_sync(PCP_FULL, b, d);
+        const float cm = __shfl_up_sync(PCP_FULL, c, d);
+        const float m0 = __shfl_up_sync(PCP_FULL, q0, d), m1 = __shfl_up_sync(PCP_FULL, q1, d);
+        const float m2 = __shfl_up_sync(PCP_FULL, q2, d);
+        const float ap = __shfl_down_sync(PCP_FULL, a, d), bp = __shfl_down_sync(PCP_FULL, b, d);
+        const float cp = __shfl_down_sync(PCP_FULL, c, d);
+        const float p0 = __shfl_down_sync(PCP_FULL, q0, d), p1 = __shfl_down_sync(PCP_FULL, q1, d);
+        const float p2 = __shfl_down_sync(PCP_FULL, q2, d);
+        float na = 0.f, nc = 0.f;
+        float nb = b, n0 = q0, n1 = q1, n2 = q2;
+        if (lane - d >= 0) {
+            float k1 = __fdividef(a, bm);
+            na = -k1 * am;
+            nb -= k1 * cm;
+            n0 -= k1 * m0; n1 -= k1 * m1; n2 -= k1 * m2;
+        }
+        if (lane + d < N) {
+            float k2 = __fdividef(c, bp);
+            nc = -k2 * cp;
+            nb -= k2 * ap;
+            n0 -= k2 * p0; n1 -= k2 * p1; n2 -= k2 * p2;
+        }
+        a = na; b = nb; c = nc; q0 = n0; q1 = n1; q2 = n2;
+    }
+    float ib = __fdividef(1.0f, b);
+    float x0 = q0 * ib, x1 = q1 * ib, x2 = q2 * ib;
+    q0 = x0; q1 = x1; q2 = x2;
+}
+
+// k_shake for polygons of at most 32 vertices: one vertex per lane, the
+// positions, reference gradients and rows held in registers, neighbours'
+// values and the parallel cyclic reduction's partner rows read by warp
+// shuffles instead of a shared-memory workspace.  Operation for operation the
+// arithmetic of k_shake (same expressions, same reduction trees), so the two
+// give bit-identical positions and iteration counts.  Lanes n..31 hold
+// identity rows and contribute zero to every sum.
+__global__ void __launch_bounds__(128, 7) k_shake_lanes(double2* __restrict__ pos,
+                        const int* __restrict__ start, int P,
+                        const double* __restrict__ targetEdge,
+                        const double* __restrict__ targetArea, int maxIter, double tol,
+                        int* __restrict__ itersOut, Ctrl* fire,
+                        cudaGraphConditionalHandle retryCond, double2* __restrict__ vel,
+                        const Ctrl* __restrict__ dtc, const int* gate) {
+    pdl_enter();
+    if (gate_closed(gate)) return;
+    const int lane = threadIdx.x & 31;
+    const int p = blockIdx.x * (blockDim.x >> 5) + (threadIdx.x >> 5);
+    int it = 0;
+    if (p < P) {
+        const int st = start[p], n = start[p + 1] - st;
+        if (n >= 3 && n <= 32 && maxIter > 0) {
+            const bool live = lane < n;
+            const int kn = (lane + 1 >= n) ? 0 : lane + 1;
+            const int kp = (lane == 0) ? n - 1 : lane - 1;
+            const int N = pow2_at_least(n);
+            const double L = targetEdge[p], A0 = targetArea[p];
+            const unsigned long long tolBits =
+                tol > 0.0 ? (unsigned long long)__double_as_longlong(tol) : 0ull;
+            const double invL = L > 0.0 ? 1.0 / L : 1.0;
+            double2 x = live ? pos[st + lane] : make_double2(0.0, 0.0);
+            double2 r, ar;
+            {
+                const double2 xn = shfl2(x, kn), xp = shfl2(x, kp);
+                r = make_double2(wrap(xn.x - x.x), wrap(xn.y - x.y));
+                ar = make_double2(0.5 * wrap(xn.y - xp.y), 0.5 * wrap(xp.x - xn.x));
+            }
+            const float2 rf = make_float2(d2f_int(r.x), d2f_int(r.y));
+            const float2 arf = make_float2(d2f_int(ar.x), d2f_int(ar.y));
+            const double2 rp = shfl2(r, kp);
+            const float2 rnf = shfl2(rf, kn), rpf = shfl2(rf, kp), anf = shfl2(arf, kn);
+            for (; it < maxIter; ++it) {
+                // residuals (FP64)
+                const double2 xn = shfl2(x, kn);
+                const double x0x = __shfl_sync(PCP_FULL, x.x, 0);
+                const double ex = wrap(xn.x - x.x), ey = wrap(xn.y - x.y);
+                const double sk = 0.5 * (ex * ex + ey * ey - L * L);
+                unsigned long long worst = live ? abs_bits(sk * invL) : 0ull;
+                const double X1 = wrap(x.x - x0x);
+                const double X2 = __shfl_sync(PCP_FULL, X1, kn);   // wrap(x_k+1 - x_0)
+                double area = 0.0;
+                if (live) area += ey * (X2 + X1);
+                worst = warp_max_u64(worst);
+                area = warp_sum(area) * 0.5;
+                const double sA = area - A0;
+                {
+                    unsigned long long qa = abs_bits(sA);
+                    if (qa > worst) worst = qa;
+                }
+                if (!finite_bits(worst)) { it = maxIter; break; }
+                if (worst < tolBits) break;
+                // rows of G(x) G_ref^T (FP32)
+                const float2 e = make_float2(d2f_int(ex), d2f_int(ey));
+                const float2 ep = shfl2(e, kp), en = shfl2(e, kn);
+                float a = 0.f, b = 1.f, c = 0.f, q0 = 0.f, q1 = 0.f, q2 = 0.f, vr = 0.f, dc = 0.f;
+                if (live) {
+                    const float2 ck = make_float2(0.5f * (e.y + ep.y), -0.5f * (e.x + ep.x));
+                    const float2 cn = make_float2(0.5f * (en.y + e.y), -0.5f * (en.x + e.x));
+                    b = 2.0f * (e.x * rf.x + e.y * rf.y);
+                    c = -(e.x * rnf.x + e.y * rnf.y);
+                    a = -(e.x * rpf.x + e.y * rpf.y);
+                    q0 = d2f_int(-sk);
+                    q1 = e.x * (anf.x - arf.x) + e.y * (anf.y - arf.y);
+                    vr = (cn.x - ck.x) * rf.x + (cn.y - ck.y) * rf.y;
+                    dc += ck.x * arf.x + ck.y * arf.y;
+                }
+                for (int o = 16; o > 0; o >>= 1) dc += __shfl_xor_sync(PCP_FULL, dc, o);
+                // Sherman-Morrison: move the cyclic corners out of the matrix
+                const float gamma = -__shfl_sync(PCP_FULL, b, 0);
+                const float beta = __shfl_sync(PCP_FULL, a, 0);
+                const float alpha = __shfl_sync(PCP_FULL, c, n - 1);
+                if (!(gamma != 0.f)) { it = maxIter; break; }
+                if (lane == 0) { b = b - gamma; a = 0.f; q2 = gamma; }
+                if (lane == n - 1) { b = b - alpha * beta / gamma; c = 0.f; q2 = alpha; }
+                lanes_pcr3(a, b, c, q0, q1, q2, N, lane);
+                const float y0 = __shfl_sync(PCP_FULL, q0, 0), yl = __shfl_sync(PCP_FULL, q0, n - 1);
+                const float z0 = __shfl_sync(PCP_FULL, q1, 0), zl = __shfl_sync(PCP_FULL, q1, n - 1);
+                const float s0 = __shfl_sync(PCP_FULL, q2, 0), sl = __shfl_sync(PCP_FULL, q2, n - 1);
+                float den = 1.f + s0 + beta * sl / gamma;
+                float fy = (y0 + beta * yl / gamma) / den;
+                float fz = (z0 + beta * zl / gamma) / den;
+                float vy = 0.f, vz = 0.f;
+                const float yk = q0 - fy * q2, zk = q1 - fz * q2;
+                if (live) { vy += vr * yk; vz += vr * zk; }
+                for (int o = 16; o > 0; o >>= 1) {
+                    vy += __shfl_xor_sync(PCP_FULL, vy, o);
+                    vz += __shfl_xor_sync(PCP_FULL, vz, o);
+                }
+                float mu = (-d2f_int(sA) - vy) / (dc - vz);
+                bool finite = isfinite(mu);
+                const float l = yk - mu * zk;
+                if (live) finite = finite && isfinite(l);
+                if (!__all_sync(PCP_FULL, finite)) { it = maxIter; break; }
+                const float lp = __shfl_sync(PCP_FULL, l, kp);
+                double mu64 = f2d_int(mu);
+                if (live) shake_update(x, l, lp, mu, mu64, r, rp, ar, rf, rpf, arf);
+            }
+            if (live) {
+                double2 y = make_double2(x.x - floor(x.x), x.y - floor(x.y));
+                if (vel) {
+                    // FIRE step: v += wrap(x_shake - x_before) / dt, the
+                    // reference's rederivation from the displacement
+                    // (model.cpp:436-438); a retry adds its own displacement
+                    const double idt = 1.0 / dtc->dt;
+                    double2 x0 = pos[st + lane], v = vel[st + lane];
+                    v.x += wrap(y.x - x0.x) * idt;
+                    v.y += wrap(y.y - x0.y) * idt;
+                    vel[st + lane] = v;
+                }
+                pos[st + lane] = y;
             }
         }
     }
+    shake_finish(it, itersOut, fire, retryCond);
 }
 
 cudaError_t launch_shake(double2* pos, const int* start, int P, int nmax, const double* targetEdge,
@@ -607,6 +803,12 @@ cudaError_t launch_shake(double2* pos, const int* start, int P, int nmax, const 
                          cudaGraphConditionalHandle retryCond, double2* vel, const Ctrl* dtc) {
     (void)V;
     if (P <= 0) return cudaSuccess;
+    if (nmax <= 32) {
+        const int wpb = 4;
+        launch_k(k_shake_lanes, dim3(nblk(P, wpb)), dim3(32 * wpb), 0, st, pos, start, P, targetEdge,
+                 targetArea, maxIter, tol, maxItersOut, fire, retryCond, vel, dtc, gate);
+        return cudaGetLastError();
+    }
     // per-warp workspace in shared memory when it fits (polygons up to ~1000
     // vertices), else a per-polygon slice of the global scratch
     int nv = (nmax + 1) & ~1;          // even, so each workspace stays 16-byte aligned
@@ -866,6 +1068,161 @@ __global__ void __launch_bounds__(256, 4) k_project_warp(const double2* __restri
     }
 }
 
+// k_project_warp for polygons of at most 32 vertices: one vertex per lane,
+// tangents, F', q and the rows in registers, neighbours' values and the
+// reduction's partner rows read by shuffles (no shared-memory workspace, no
+// warp barriers).  The same mathematics and rounds as k_project_warp.
+__global__ void __launch_bounds__(128, 7) k_project_lanes(const double2* __restrict__ pos,
+                               const int* __restrict__ start, int P,
+                               const double* __restrict__ constraints,
+                               double2* __restrict__ force, int areaFromPositions, Ctrl* fire,
+                               double2* __restrict__ vel, cudaGraphConditionalHandle rbCond,
+                               int useCond, const int* gate) {
+    pdl_enter();
+    if (gate_closed(gate)) return;
+    const int lane = threadIdx.x & 31;
+    const int p = blockIdx.x * (blockDim.x >> 5) + (threadIdx.x >> 5);
+    bool proceed = false;
+    double dt = 0.0;
+    if (fire) {
+        double E = fire->energy, E0 = fire->ePre;
+        bool rb = E > E0 + fmax(fabs(E0) * 1e-10, 1e-14);
+        proceed = !fire->shakeFailed && !rb && fire->rollback == 0;
+        dt = fire->dt;
+        if (blockIdx.x == 0 && threadIdx.x == 0 && fire->rollback == 0) {
+            fire->proceed = proceed ? 1 : 0;
+            // the energy-increase rollback path runs when the step is not a
+            // SHAKE failure and the energy went up (model.cpp:450-453)
+            int go = (!fire->shakeFailed && rb && fire->active) ? 1 : 0;
+            fire->rbGate = go;
+            if (useCond) cudaGraphSetConditional(rbCond, (unsigned int)go);
+        }
+    }
+    double sP = 0.0, sV = 0.0, sF = 0.0;
+    unsigned long long mF = 0ull;      // max |F component| as a bit pattern
+    bool bad = false;
+    if (p < P) {
+        const int st = start[p], n = start[p + 1] - st;
+        const bool live = lane < n;
+        double2 f = live ? force[st + lane] : make_double2(0.0, 0.0);
+        if (n >= 3 && n <= 32) {
+            const int kn = (lane + 1 >= n) ? 0 : lane + 1;
+            const int kp = (lane == 0) ? n - 1 : lane - 1;
+            const int N = pow2_at_least(n);
+            const double2 x = live ? pos[st + lane] : make_double2(0.0, 0.0);
+            const double2 xn = shfl2(x, kn);
+            double2 t = make_double2(0.0, 0.0);
+            float mb = 1.0f;
+            {
+                double dx = wrap(xn.x - x.x), dy = wrap(xn.y - x.y);
+                double len2 = dx * dx + dy * dy;
+                // |e| >= 1e-14 (kernels.cuh:399); len2 >= 0, so its bit
+                // pattern orders like its value (NaN counts as long)
+                bool ok = (unsigned long long)__double_as_longlong(len2) >=
+                          (unsigned long long)__double_as_longlong(1e-28);
+                if (ok) { double il = rsqrt(len2); t = make_double2(dx * il, dy * il); mb = 2.0f; }
+            }
+            double2 q;
+            if (areaFromPositions) {
+                const double2 xp = shfl2(x, kp);
+                q = make_double2(-wrap(xp.y - xn.y), wrap(xp.x - xn.x));
+                double an = live ? q.x * q.x + q.y * q.y : 0.0;
+                an = warp_sum(an);
+                double ir = an > 0.0 ? rsqrt(an) : 1.0;
+                q = make_double2(q.x * ir, q.y * ir);
+            } else {
+                q = make_double2(0.0, 0.0);
+                if (live) {
+                    const double* c = constraints + 6 * (size_t)(st + lane);
+                    q = make_double2(c[0], c[1]);
+                }
+            }
+            const float2 tf = make_float2(d2f_int(t.x), d2f_int(t.y));
+            const double2 tn = shfl2(t, kn), tp = shfl2(t, kp);
+            const float2 tpf = shfl2(tf, kp);
+            const float mc = d2f_int(-(t.x * tn.x + t.y * tn.y));
+            const float mcp = __shfl_sync(PCP_FULL, mc, kp);
+            for (int round = 0; round < kProjRounds; ++round) {
+                // residual right-hand sides J^T F', J^T q (FP64) and the FP32 rows
+                const double2 fn = shfl2(f, kn), qn = shfl2(q, kn);
+                float a = 0.f, b = 1.f, c = 0.f, q0 = 0.f, q1 = 0.f, q2 = 0.f;
+                if (live) {
+                    q0 = d2f_int(t.x * (fn.x - f.x) + t.y * (fn.y - f.y));
+                    q1 = d2f_int(t.x * (qn.x - q.x) + t.y * (qn.y - q.y));
+                    b = mb; c = mc; a = mcp;
+                }
+                // Sherman-Morrison: move the cyclic corners out of the matrix
+                const float gamma = -__shfl_sync(PCP_FULL, b, 0);
+                const float beta = __shfl_sync(PCP_FULL, a, 0);
+                const float alpha = __shfl_sync(PCP_FULL, c, n - 1);
+                if (!(gamma != 0.f)) { bad = true; break; }
+                if (lane == 0) { b = b - gamma; a = 0.f; q2 = gamma; }
+                if (lane == n - 1) { b = b - alpha * beta / gamma; c = 0.f; q2 = alpha; }
+                lanes_pcr3(a, b, c, q0, q1, q2, N, lane);
+                const float s0 = __shfl_sync(PCP_FULL, q2, 0), sl = __shfl_sync(PCP_FULL, q2, n - 1);
+                const float y0 = __shfl_sync(PCP_FULL, q0, 0), yl = __shfl_sync(PCP_FULL, q0, n - 1);
+                const float z0 = __shfl_sync(PCP_FULL, q1, 0), zl = __shfl_sync(PCP_FULL, q1, n - 1);
+                float den = 1.f + s0 + beta * sl / gamma;
+                float fl = (y0 + beta * yl / gamma) / den;
+                float fm = (z0 + beta * zl / gamma) / den;
+                const float l0 = q0 - fl * q2, l1 = q1 - fm * q2;
+                const float l0p = __shfl_sync(PCP_FULL, l0, kp), l1p = __shfl_sync(PCP_FULL, l1, kp);
+                // F' -= J lambda, q -= J mu with (J x)_k = -x_k t_k + x_{k-1} t_{k-1}:
+                // the first (full-size) update with the FP64 tangents, the later
+                // corrections (relative size ~1e-5) with FP32 products added in
+                // FP64 -- an error outside span(J) would be invisible to the
+                // next residual J^T F'
+                if (live) {
+                    if (round == 0) {
+                        double L0 = f2d_int(l0), L0p = f2d_int(l0p);
+                        double L1 = f2d_int(l1), L1p = f2d_int(l1p);
+                        f.x -= -L0 * t.x + L0p * tp.x; f.y -= -L0 * t.y + L0p * tp.y;
+                        q.x -= -L1 * t.x + L1p * tp.x; q.y -= -L1 * t.y + L1p * tp.y;
+                    } else {
+                        f.x += f2d_int(l0 * tf.x - l0p * tpf.x); f.y += f2d_int(l0 * tf.y - l0p * tpf.y);
+                        q.x += f2d_int(l1 * tf.x - l1p * tpf.x); q.y += f2d_int(l1 * tf.y - l1p * tpf.y);
+                    }
+                }
+            }
+            if (!bad) {
+                double qF = live ? q.x * f.x + q.y * f.y : 0.0;
+                double qq = live ? q.x * q.x + q.y * q.y : 0.0;
+                qF = warp_sum(qF);
+                qq = warp_sum(qq);
+                // sqrt(qq) > 1e-14 (kernels.cuh:464)
+                double coef = (qq > 1e-28) ? qF / qq : 0.0;
+                f = make_double2(f.x - coef * q.x, f.y - coef * q.y);
+                if (live) force[st + lane] = f;
+            }
+        }
+        if (live && !bad) {
+            mF = max_abs_bits(mF, f.x, f.y);
+            if (proceed) {
+                double2 v = vel[st + lane];
+                v.x += 0.5 * dt * f.x;
+                v.y += 0.5 * dt * f.y;
+                vel[st + lane] = v;
+                sP += f.x * v.x + f.y * v.y;
+                sV += v.x * v.x + v.y * v.y;
+                sF += f.x * f.x + f.y * f.y;
+            }
+        }
+    }
+    if (fire) {
+        if (bad && lane == 0) atomicOr(&fire->flags, kFlagNonFinite);
+        mF = warp_max_u64(mF);
+        if (lane == 0 && mF) atomicMax(reinterpret_cast<unsigned long long*>(&fire->maxF), mF);
+        if (proceed) {
+            sP = warp_sum(sP); sV = warp_sum(sV); sF = warp_sum(sF);
+            if (lane == 0) {
+                atomicAdd(&fire->P, sP);
+                atomicAdd(&fire->vv, sV);
+                atomicAdd(&fire->ff, sF);
+            }
+        }
+    }
+}
+
 cudaError_t constraints_init() {
     static bool done = false;
     if (done) return cudaSuccess;
@@ -894,6 +1251,12 @@ cudaError_t launch_project(const double2* pos, const int* start, int P, int nmax
         launch_k(k_project, dim3(nblk(P, kConsThreads)), dim3(kConsThreads), smem, st, 
             pos, start, P, constraints, force, scratch, V, sn, areaFromPositions, fireCtrl, vel,
             rbCond, useCond, gate);
+        return cudaGetLastError();
+    }
+    if (nmax <= 32) {
+        const int wpb = 4;
+        launch_k(k_project_lanes, dim3(nblk(P, wpb)), dim3(32 * wpb), 0, st, pos, start, P,
+                 constraints, force, areaFromPositions, fireCtrl, vel, rbCond, useCond, gate);
         return cudaGetLastError();
     }
     int nv = (nmax + 1) & ~1;          // even, so each workspace stays 16-byte aligned
