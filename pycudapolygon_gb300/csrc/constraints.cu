@@ -429,9 +429,14 @@ __device__ __forceinline__ void shake_update(double2& x, float lk, float lp, flo
 // the last block to finish reads it and decides the retry.
 __device__ __forceinline__ void shake_finish(int it, int* itersOut, Ctrl* fire,
                                              cudaGraphConditionalHandle retryCond) {
-    if ((threadIdx.x & 31) == 0 && it > 0) atomicMax(itersOut, it);
+    // one atomic per block: same-address atomics from every warp queue up
+    __shared__ int s_it;
+    if (threadIdx.x == 0) s_it = 0;
+    __syncthreads();
+    if ((threadIdx.x & 31) == 0 && it > 0) atomicMax_block(&s_it, it);
+    __syncthreads();
+    if (threadIdx.x == 0 && s_it > 0) atomicMax(itersOut, s_it);
     if (fire) {
-        __syncthreads();
         if (threadIdx.x == 0) {
             __threadfence();
             unsigned int t = atomicAdd(&fire->shakeTicket, 1u);
@@ -671,6 +676,32 @@ __device__ __forceinline__ void lanes_pcr3(float a, float b, float c, float& q0,
     q0 = x0; q1 = x1; q2 = x2;
 }
 
+// Unit tangent t_k of edge (k, k+1) of the wrapped positions held one vertex
+// per lane (kernels.cuh:399: zero for an edge shorter than 1e-14).
+__device__ __forceinline__ void lanes_tangent(double2 x, int kn, double2& t) {
+    const double2 xn = shfl2(x, kn);
+    t = make_double2(0.0, 0.0);
+    double dx = wrap(xn.x - x.x), dy = wrap(xn.y - x.y);
+    double len2 = dx * dx + dy * dy;
+    // len2 >= 0, so its bit pattern orders like its value (NaN counts as long)
+    bool ok = (unsigned long long)__double_as_longlong(len2) >=
+              (unsigned long long)__double_as_longlong(1e-28);
+    if (ok) { double il = rsqrt(len2); t = make_double2(dx * il, dy * il); }
+}
+
+// Unit area gradient of the polygon at vertex k, (x_k+1 - x_k-1) / 2 rotated
+// and normalised over the polygon (updatePolygonGeometryKernel,
+// kernels.cuh:303,313), one vertex per lane; lanes >= n (live false) hold 0.
+__device__ __forceinline__ void lanes_area_gradient(double2 x, bool live, int kn, int kp,
+                                                    double2& q) {
+    const double2 xn = shfl2(x, kn), xp = shfl2(x, kp);
+    q = make_double2(-wrap(xp.y - xn.y), wrap(xp.x - xn.x));
+    double an = live ? q.x * q.x + q.y * q.y : 0.0;
+    an = warp_sum(an);
+    double ir = an > 0.0 ? rsqrt(an) : 1.0;
+    q = make_double2(q.x * ir, q.y * ir);
+}
+
 // k_shake for polygons of at most 32 vertices: one vertex per lane, the
 // positions, reference gradients and rows held in registers, neighbours'
 // values and the parallel cyclic reduction's partner rows read by warp
@@ -795,6 +826,43 @@ __global__ void __launch_bounds__(128, 7) k_shake_lanes(double2* __restrict__ po
         }
     }
     shake_finish(it, itersOut, fire, retryCond);
+}
+
+// The unit edge tangents and unit area gradients (normalised over the
+// polygon) of the positions, one polygon per warp, stored for
+// k_project_lanes as pre[i] = t_i, pre[V + i] = q_i.  The FIRE step runs
+// this on the SHAKE branch, beside the contact search, so that the
+// projection on the step's critical path starts from them.
+__global__ void __launch_bounds__(128) k_project_pre(const double2* __restrict__ pos,
+                                                     const int* __restrict__ start, int P,
+                                                     double2* __restrict__ pre, int V,
+                                                     const int* gate) {
+    pdl_enter();
+    if (gate_closed(gate)) return;
+    const int lane = threadIdx.x & 31;
+    const int p = blockIdx.x * (blockDim.x >> 5) + (threadIdx.x >> 5);
+    if (p >= P) return;
+    const int st = start[p], n = start[p + 1] - st;
+    if (n < 3 || n > 32) return;
+    const bool live = lane < n;
+    const int kn = (lane + 1 >= n) ? 0 : lane + 1;
+    const int kp = (lane == 0) ? n - 1 : lane - 1;
+    const double2 x = live ? pos[st + lane] : make_double2(0.0, 0.0);
+    double2 t, q;
+    lanes_tangent(x, kn, t);
+    lanes_area_gradient(x, live, kn, kp, q);
+    if (live) { pre[st + lane] = t; pre[V + st + lane] = q; }
+}
+
+// launch_project's choice: thread per polygon for at least 128 polygons per
+// SM, else warp per polygon, in registers for polygons of up to 32 vertices
+bool project_uses_lanes(int P, int nmax) { return nmax <= 32 && P < 128 * sm_count(); }
+
+cudaError_t launch_project_pre(const double2* pos, const int* start, int P, int nmax,
+                               double2* pre, int V, const int* gate, cudaStream_t st) {
+    if (P <= 0 || !project_uses_lanes(P, nmax)) return cudaSuccess;
+    launch_k(k_project_pre, dim3(nblk(P, 4)), dim3(128), 0, st, pos, start, P, pre, V, gate);
+    return cudaGetLastError();
 }
 
 cudaError_t launch_shake(double2* pos, const int* start, int P, int nmax, const double* targetEdge,
@@ -1077,7 +1145,8 @@ __global__ void __launch_bounds__(128, 7) k_project_lanes(const double2* __restr
                                const double* __restrict__ constraints,
                                double2* __restrict__ force, int areaFromPositions, Ctrl* fire,
                                double2* __restrict__ vel, cudaGraphConditionalHandle rbCond,
-                               int useCond, const int* gate) {
+                               int useCond, const double2* __restrict__ pre, int V,
+                               const int* gate) {
     pdl_enter();
     if (gate_closed(gate)) return;
     const int lane = threadIdx.x & 31;
@@ -1109,34 +1178,25 @@ __global__ void __launch_bounds__(128, 7) k_project_lanes(const double2* __restr
             const int kn = (lane + 1 >= n) ? 0 : lane + 1;
             const int kp = (lane == 0) ? n - 1 : lane - 1;
             const int N = pow2_at_least(n);
-            const double2 x = live ? pos[st + lane] : make_double2(0.0, 0.0);
-            const double2 xn = shfl2(x, kn);
-            double2 t = make_double2(0.0, 0.0);
-            float mb = 1.0f;
-            {
-                double dx = wrap(xn.x - x.x), dy = wrap(xn.y - x.y);
-                double len2 = dx * dx + dy * dy;
-                // |e| >= 1e-14 (kernels.cuh:399); len2 >= 0, so its bit
-                // pattern orders like its value (NaN counts as long)
-                bool ok = (unsigned long long)__double_as_longlong(len2) >=
-                          (unsigned long long)__double_as_longlong(1e-28);
-                if (ok) { double il = rsqrt(len2); t = make_double2(dx * il, dy * il); mb = 2.0f; }
-            }
-            double2 q;
-            if (areaFromPositions) {
-                const double2 xp = shfl2(x, kp);
-                q = make_double2(-wrap(xp.y - xn.y), wrap(xp.x - xn.x));
-                double an = live ? q.x * q.x + q.y * q.y : 0.0;
-                an = warp_sum(an);
-                double ir = an > 0.0 ? rsqrt(an) : 1.0;
-                q = make_double2(q.x * ir, q.y * ir);
+            double2 t, q;
+            if (pre) {
+                t = live ? pre[st + lane] : make_double2(0.0, 0.0);
+                q = live ? pre[V + st + lane] : make_double2(0.0, 0.0);
             } else {
-                q = make_double2(0.0, 0.0);
-                if (live) {
-                    const double* c = constraints + 6 * (size_t)(st + lane);
-                    q = make_double2(c[0], c[1]);
+                const double2 x = live ? pos[st + lane] : make_double2(0.0, 0.0);
+                lanes_tangent(x, kn, t);
+                if (areaFromPositions) {
+                    lanes_area_gradient(x, live, kn, kp, q);
+                } else {
+                    q = make_double2(0.0, 0.0);
+                    if (live) {
+                        const double* c = constraints + 6 * (size_t)(st + lane);
+                        q = make_double2(c[0], c[1]);
+                    }
                 }
             }
+            // J^T J diagonal: 2 for an edge of length >= 1e-14, else 1 (t = 0)
+            const float mb = ((__double_as_longlong(t.x) | __double_as_longlong(t.y)) != 0) ? 2.0f : 1.0f;
             const float2 tf = make_float2(d2f_int(t.x), d2f_int(t.y));
             const double2 tn = shfl2(t, kn), tp = shfl2(t, kp);
             const float2 tpf = shfl2(tf, kp);
@@ -1209,12 +1269,22 @@ __global__ void __launch_bounds__(128, 7) k_project_lanes(const double2* __restr
         }
     }
     if (fire) {
+        // block partials first, then one atomic per block and quantity
+        __shared__ double s_sum[3][4];
+        __shared__ unsigned long long s_max[4];
+        const int warp = threadIdx.x >> 5, nw = blockDim.x >> 5;
         if (bad && lane == 0) atomicOr(&fire->flags, kFlagNonFinite);
         mF = warp_max_u64(mF);
-        if (lane == 0 && mF) atomicMax(reinterpret_cast<unsigned long long*>(&fire->maxF), mF);
-        if (proceed) {
-            sP = warp_sum(sP); sV = warp_sum(sV); sF = warp_sum(sF);
-            if (lane == 0) {
+        if (proceed) { sP = warp_sum(sP); sV = warp_sum(sV); sF = warp_sum(sF); }
+        if (lane == 0) { s_max[warp] = mF; s_sum[0][warp] = sP; s_sum[1][warp] = sV; s_sum[2][warp] = sF; }
+        __syncthreads();
+        if (threadIdx.x == 0) {
+            for (int w = 1; w < nw; ++w) {
+                if (s_max[w] > mF) mF = s_max[w];
+                sP += s_sum[0][w]; sV += s_sum[1][w]; sF += s_sum[2][w];
+            }
+            if (mF) atomicMax(reinterpret_cast<unsigned long long*>(&fire->maxF), mF);
+            if (proceed) {
                 atomicAdd(&fire->P, sP);
                 atomicAdd(&fire->vv, sV);
                 atomicAdd(&fire->ff, sF);
@@ -1243,7 +1313,8 @@ cudaError_t constraints_init() {
 cudaError_t launch_project(const double2* pos, const int* start, int P, int nmax,
                            const double* constraints, double2* force, double* scratch, int V,
                            int areaFromPositions, Ctrl* fireCtrl, const int* gate, double2* vel,
-                           cudaStream_t st, cudaGraphConditionalHandle rbCond, int useCond) {
+                           cudaStream_t st, cudaGraphConditionalHandle rbCond, int useCond,
+                           const double2* pre) {
     if (P <= 0) return cudaSuccess;
     if (P >= 128 * sm_count()) {
         int sn = smem_vertices(nmax, kProjArrays);
@@ -1253,10 +1324,11 @@ cudaError_t launch_project(const double2* pos, const int* start, int P, int nmax
             rbCond, useCond, gate);
         return cudaGetLastError();
     }
-    if (nmax <= 32) {
+    if (project_uses_lanes(P, nmax)) {
         const int wpb = 4;
         launch_k(k_project_lanes, dim3(nblk(P, wpb)), dim3(32 * wpb), 0, st, pos, start, P,
-                 constraints, force, areaFromPositions, fireCtrl, vel, rbCond, useCond, gate);
+                 constraints, force, areaFromPositions, fireCtrl, vel, rbCond, useCond, pre, V,
+                 gate);
         return cudaGetLastError();
     }
     int nv = (nmax + 1) & ~1;          // even, so each workspace stays 16-byte aligned

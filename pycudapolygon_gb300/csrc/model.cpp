@@ -116,8 +116,8 @@ struct pcp_model {
     int fireShakeIter = -1, fireModel = -1, fireB = -1;
     int fireKernelNodes = 0;   // kernel launches one FIRE step graph makes
     int rbBodyKernels = 0;     // kernels of its rollback body (counted on the device)
-    cudaStream_t sideStream = nullptr, bodyStream = nullptr;   // capture helpers
-    cudaEvent_t evFork = nullptr, evJoin = nullptr;
+    cudaStream_t sideStream = nullptr, bodyStream = nullptr, preStream = nullptr;   // capture helpers
+    cudaEvent_t evFork = nullptr, evJoin = nullptr, evPreFork = nullptr, evPreJoin = nullptr;
 
     ~pcp_model() { release(); }
 
@@ -127,6 +127,9 @@ struct pcp_model {
         if (bodyStream) { cudaStreamDestroy(bodyStream); bodyStream = nullptr; }
         if (evFork) { cudaEventDestroy(evFork); evFork = nullptr; }
         if (evJoin) { cudaEventDestroy(evJoin); evJoin = nullptr; }
+        if (preStream) { cudaStreamDestroy(preStream); preStream = nullptr; }
+        if (evPreFork) { cudaEventDestroy(evPreFork); evPreFork = nullptr; }
+        if (evPreJoin) { cudaEventDestroy(evPreJoin); evPreJoin = nullptr; }
         dfree(&pos); dfree(&force); dfree(&vel); dfree(&posTMP); dfree(&posTMP2); dfree(&posTent);
         dfree(&posGeom);
         dfree(&velSnap); dfree(&forceSnap);
@@ -540,6 +543,7 @@ int record_fire_step(pcp_model* m, cudaGraphConditionalHandle retryCond,
     bool shake = rigid && m->fireShakeIter > 0;
     int V = m->V;
     const int noReset = 3 | kContactsNoReset;
+    double2* pre = reinterpret_cast<double2*>(m->scratch);
     if (needsI) {
         // the step start fused with the contact prepass: x, v, F moved in
         // place, the moved positions copied to posTMP (read by the search)
@@ -570,6 +574,13 @@ int record_fire_step(pcp_model* m, cudaGraphConditionalHandle retryCond,
         CK(launch_fire_retry_outcome(m->pos, m->vel, m->posTMP2, V, m->ctrl, m->bodyStream));
         cudaGraph_t body = nullptr;
         CK(cudaStreamEndCapture(m->bodyStream, &body));
+        // the projection's tangents and area gradients of the final
+        // positions (restored ones after a failed SHAKE), on a third branch
+        // beside the end of the contact search and the force
+        CK(cudaEventRecord(m->evPreFork, st));
+        CK(cudaStreamWaitEvent(m->preStream, m->evPreFork, 0));
+        CK(launch_project_pre(m->pos, m->start, m->P, m->nmax, pre, V, gA, m->preStream));
+        CK(cudaEventRecord(m->evPreJoin, m->preStream));
         CK(cudaStreamWaitEvent(st, m->evJoin, 0));
     } else if (needsI) {
         CK(launch_contacts(m->pos, m->start, m->shapeId, m->cellLocation, m->P, V, m->boxSize,
@@ -588,8 +599,9 @@ int record_fire_step(pcp_model* m, cudaGraphConditionalHandle retryCond,
     rc = force_energy(m, gA, true);
     if (rc) return rc;
     if (rigid) {
+        if (shake) CK(cudaStreamWaitEvent(st, m->evPreJoin, 0));
         CK(launch_project(m->pos, m->start, m->P, m->nmax, m->constraints, m->force, m->scratch, V, 1,
-                          m->ctrl, gA, m->vel, st, rbCond, 1));
+                          m->ctrl, gA, m->vel, st, rbCond, 1, shake ? pre : nullptr));
     } else {
         CK(launch_fire_velocity(m->vel, m->force, V, m->ctrl, rbCond, 1, gA, st));
     }
@@ -635,6 +647,9 @@ int build_fire_graph(pcp_model* m, int shakeIter) {
     if (!m->bodyStream) CK(cudaStreamCreateWithFlags(&m->bodyStream, cudaStreamNonBlocking));
     if (!m->evFork) CK(cudaEventCreateWithFlags(&m->evFork, cudaEventDisableTiming));
     if (!m->evJoin) CK(cudaEventCreateWithFlags(&m->evJoin, cudaEventDisableTiming));
+    if (!m->preStream) CK(cudaStreamCreateWithFlags(&m->preStream, cudaStreamNonBlocking));
+    if (!m->evPreFork) CK(cudaEventCreateWithFlags(&m->evPreFork, cudaEventDisableTiming));
+    if (!m->evPreJoin) CK(cudaEventCreateWithFlags(&m->evPreJoin, cudaEventDisableTiming));
     cudaStream_t cap = nullptr;
     CK(cudaStreamCreateWithFlags(&cap, cudaStreamNonBlocking));
     cudaStream_t saved = m->stream;

@@ -174,11 +174,20 @@ cudaError_t constraints_init();
 // scratch fits in shared memory)
 // useCond: the projection decides the FIRE step's energy rollback and sets
 // `rbCond` of the step graph
+// pre ([2V] double2: unit edge tangents, then unit area gradients): when
+// non-null, the values launch_project_pre stored for the current positions
 cudaError_t launch_project(const double2* pos, const int* start, int P, int nmax,
                            const double* constraints, double2* force, double* scratch, int V,
                            int areaFromPositions, Ctrl* fireCtrl, const int* gate, double2* vel,
                            cudaStream_t st, cudaGraphConditionalHandle rbCond = 0,
-                           int useCond = 0);
+                           int useCond = 0, const double2* pre = nullptr);
+// whether launch_project runs its register (one vertex per lane) form, the
+// only one that reads `pre`
+bool project_uses_lanes(int P, int nmax);
+// the tangents and area gradients of `pos` into pre for launch_project (a
+// no-op unless project_uses_lanes(P, nmax))
+cudaError_t launch_project_pre(const double2* pos, const int* start, int P, int nmax,
+                               double2* pre, int V, const int* gate, cudaStream_t st);
 // fire (device-resident FIRE step, first SHAKE attempt): the last block to
 // finish decides whether the retry runs and sets `retryCond` of the step
 // graph; vel (with dtc for dt): also rederive v from the SHAKE displacement

@@ -257,6 +257,24 @@ def test_shake_parity(system):
                                rtol=1e-10)
 
 
+@pytest.mark.parametrize("P,n", [(4096, 32), (4096, 16), (2048, 24)])
+def test_shake_parity_at_scale(P, n):
+    """Thousands of polygons: many warps resident on every SM at once, the
+    conditions of the FIRE workload.  The iteration count and the positions
+    follow the oracle, and a second run gives the same bits."""
+    s = make_system(P, n, 0.88, seed=5)
+    g, o = pair(s)
+    it_o = o.shakeProject(200, 1e-15)
+    it_g = g.shakeProject(200, 1e-15)
+    x_g = np.asarray(g.getPositions()).copy()
+    assert abs(it_g - it_o) <= 1
+    d = (x_g - o.getPositions() + 0.5) % 1.0 - 0.5
+    assert np.abs(d).max() < 1e-12
+    g2 = load_into(lib.Model(s.num_vertices), s)
+    assert g2.shakeProject(200, 1e-15) == it_g
+    assert np.array_equal(np.asarray(g2.getPositions()), x_g)
+
+
 def test_xpbd_parity(system):
     g, o = pair(system)
     ig = g.xpbdProject(5, 0.0)
@@ -328,6 +346,56 @@ def test_fire_rollback_state_matches_reference():
     assert rg[0] == pytest.approx(ro[0], rel=1e-9, abs=1e-14)
     d = (np.asarray(g.getPositions()) - o.getPositions() + 0.5) % 1.0 - 0.5
     assert np.abs(d).max() < 1e-9
+
+
+@pytest.mark.parametrize("seed,dt,shake_iter,fails", [(1, 0.2, 1, False), (1, 1.0, 1, True),
+                                                      (2, 0.5, 2, True)])
+def test_fire_step_shake_retry_and_failure_match_reference(seed, dt, shake_iter, fails):
+    """Large first steps: SHAKE needs its retry with ten times the iterations
+    (model.cpp:431-436), and where the retry fails too, the step restores its
+    start positions and zeroes the velocities (model.cpp:437-449); the force
+    and its projection at the end are then those of the restored positions."""
+    s = make_system(64, 16, 0.85, seed=seed)
+    g, o = pair(s)
+    for m in (g, o):
+        m.shakeProject(200, 1e-15)
+        contacts(m)
+        m.updateForceEnergy()
+        m.projectForce()
+    xg0 = np.asarray(g.getPositions()).copy()
+    xo0 = np.asarray(o.getPositions()).copy()
+    args = (dt, 0.1, 0, 0.1, 0.1, 0.99, 1.1, 0.5, 5, shake_iter)
+    rg = g.minimizeFIREStep(*args)
+    ro = o.minimizeFIREStep(*args)
+    assert o.getLastShakeIters() >= shake_iter          # the retry ran
+    assert g.getLastShakeIters() == pytest.approx(o.getLastShakeIters(), abs=1)
+    assert np.array_equal(np.asarray(o.getPositions()), xo0) == fails
+    assert np.array_equal(np.asarray(g.getPositions()), xg0) == fails
+    assert rg[0] == pytest.approx(ro[0], rel=1e-9, abs=1e-14)
+    assert rg[1:] == pytest.approx(ro[1:], rel=1e-12)
+    d = (np.asarray(g.getPositions()) - o.getPositions() + 0.5) % 1.0 - 0.5
+    if fails:
+        # back at the step-start state: the usual tolerances.  The force
+        # there comes from records of the moved positions (huge), so the
+        # next steps are short ones: the first rolls back on an energy
+        # increase, the others proceed.
+        assert np.abs(d).max() < 1e-12
+        assert_forces_close(g.getForces(), o.getForces())
+        assert g.getMaxUnbalancedForce() == pytest.approx(o.getMaxUnbalancedForce(), rel=1e-9)
+        for _ in range(3):
+            rg = g.minimizeFIREStep(1e-5, *rg[2:])
+            ro = o.minimizeFIREStep(1e-5, *ro[2:])
+            assert rg[0] == pytest.approx(ro[0], rel=1e-9, abs=1e-14)
+            assert rg[1:] == pytest.approx(ro[1:], rel=1e-12)
+        d = (np.asarray(g.getPositions()) - o.getPositions() + 0.5) % 1.0 - 0.5
+        assert np.abs(d).max() < 1e-9
+    else:
+        # a step this large ends far from the pre-step shapes, where the two
+        # SHAKE solvers' 1e-15 residuals leave the positions ~1e-10 apart
+        # (not 1e-12), and the force follows them
+        assert np.abs(d).max() < 1e-9
+        of = np.asarray(o.getForces())
+        assert np.abs(np.asarray(g.getForces()) - of).max() <= 1e-7 * np.abs(of).max()
 
 
 def test_minimize_fire_matches_step_loop():
