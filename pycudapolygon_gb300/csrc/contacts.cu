@@ -560,6 +560,11 @@ __device__ __forceinline__ unsigned long long pack_key(int sj, int si, int i, in
 //  3. the reference's 3x3 cell rule on the edge-midpoint cells.
 struct EdgeCand { float4 box; int idx, cx, cy, pad; };
 
+// Hint: bring the 128-byte line holding p into L1 (no register result).
+__device__ __forceinline__ void prefetch_l1(const void* p) {
+    asm volatile("prefetch.global.L1 [%0];" ::"l"(p));
+}
+
 // Culls 1 and 2 of a staged pair: fills candA / candB with the edges whose
 // boxes meet the overlap box (self pair: candA only) and returns their
 // counts through nLA / nLB (0 when the polygon boxes are disjoint).
@@ -751,53 +756,70 @@ __device__ unsigned long long match_and_write(const PairCtx& pc, int R,
                                               const float2* recTU, Ctrl* ctrl, ContactWS& ws,
                                               bool publishMax = true) {
     const int lane = threadIdx.x & 31;
+    // the slot of the pair's records: the atomic's round trip overlaps the
+    // matching below, whose results wait in registers (up to 32 records,
+    // one per lane, in one round; more take further rounds)
     int base = 0;
     if (lane == 0) base = atomicAdd(&ctrl->numRecords, R);
-    base = __shfl_sync(PCP_FULL, base, 0);
-    if (base + R > ws.capRecords) {
-        if (lane == 0) atomicOr(&ctrl->flags, kFlagRecordOverflow);
-        return 0ull;
-    }
     unsigned long long kmax = 0;
-    for (int r = lane; r < R; r += 32) {
-        unsigned long long key = recKey[r];
-        int sj = (int)(key >> 48), si = (int)((key >> 32) & 0xFFFF);
-        int i = (int)((key >> 16) & 0xFFFF);
-        int ni = (si == pc.a) ? pc.nA : pc.nB;
-        float tVal = recTU[r].y;
-        unsigned long long grp = ((unsigned long long)si << 16) | (unsigned long long)sj;
-        bool groupSeen = false;
-        int best = -1, bestD = 0;
-        float bestU = 0.f;
-        unsigned long long bestK = 0;
-        for (int c = 0; c < R; ++c) {
-            unsigned long long kc = recKey[c];
-            if ((kc >> 32) != grp) continue;
-            groupSeen = true;
-            int l = (int)(kc & 0xFFFF);
-            float uVal = recTU[c].x;
-            if (l == i && tVal >= uVal) continue;
-            int d = (l - i + ni) % ni;
-            bool better = best < 0 || d < bestD || (d == bestD && (uVal < bestU ||
-                          (uVal == bestU && kc < bestK)));
-            if (better) { best = c; bestD = d; bestU = uVal; bestK = kc; }
+    for (int r0 = 0; r0 < R; r0 += 32) {
+        const int r = r0 + lane;
+        unsigned long long key = 0, outer = 0;
+        float2 tu = make_float2(0.f, 0.f), ut = make_float2(0.f, 0.f);
+        bool fix = false;
+        if (r < R) {
+            key = recKey[r];
+            tu = recTU[r];
+            int sj = (int)(key >> 48), si = (int)((key >> 32) & 0xFFFF);
+            int i = (int)((key >> 16) & 0xFFFF);
+            int ni = (si == pc.a) ? pc.nA : pc.nB;
+            float tVal = tu.y;
+            unsigned long long grp = ((unsigned long long)si << 16) | (unsigned long long)sj;
+            bool groupSeen = false;
+            int best = -1, bestD = 0;
+            float bestU = 0.f;
+            unsigned long long bestK = 0;
+            for (int c = 0; c < R; ++c) {
+                unsigned long long kc = recKey[c];
+                if ((kc >> 32) != grp) continue;
+                groupSeen = true;
+                int l = (int)(kc & 0xFFFF);
+                float uVal = recTU[c].x;
+                if (l == i && tVal >= uVal) continue;
+                int d = (l - i + ni) % ni;
+                bool better = best < 0 || d < bestD || (d == bestD && (uVal < bestU ||
+                              (uVal == bestU && kc < bestK)));
+                if (better) { best = c; bestD = d; bestU = uVal; bestK = kc; }
+            }
+            if (best >= 0) {
+                outer = recKey[best];
+                ut = recTU[best];
+            } else {
+                outer = key;
+                ut = tu;
+                fix = !groupSeen;
+            }
+            kmax = key > kmax ? key : kmax;
         }
-        int g = base + r;
-        ws.recKey[g] = key;
-        ws.recTU[g] = recTU[r];
-        if (best >= 0) {
-            ws.recOuter[g] = recKey[best];
-            ws.recUT[g] = recTU[best];
-        } else {
-            ws.recOuter[g] = key;
-            ws.recUT[g] = recTU[r];
-            if (!groupSeen) {
+        if (r0 == 0) {
+            base = __shfl_sync(PCP_FULL, base, 0);
+            if (base + R > ws.capRecords) {
+                if (lane == 0) atomicOr(&ctrl->flags, kFlagRecordOverflow);
+                return 0ull;
+            }
+        }
+        if (r < R) {
+            int g = base + r;
+            ws.recKey[g] = key;
+            ws.recTU[g] = tu;
+            ws.recOuter[g] = outer;
+            ws.recUT[g] = ut;
+            if (fix) {
                 int f = atomicAdd(&ctrl->numFix, 1);
                 if (f < ws.capFix) ws.fixList[f] = g;
                 else atomicOr(&ctrl->flags, kFlagFixOverflow);
             }
         }
-        kmax = key > kmax ? key : kmax;
     }
     for (int o = 16; o > 0; o >>= 1) {
         unsigned long long t = __shfl_xor_sync(PCP_FULL, kmax, o);
@@ -1000,6 +1022,22 @@ k_narrow(const double2* __restrict__ pos, const int* __restrict__ start, int B,
             mbar_arrive_expect(&S.bar[stage], bytesA + bytesB);
             bulk_g2s(&S.ring[stage][0], ws.vtx + pc.stA, bytesA, &S.bar[stage]);
             if (!pc.self) bulk_g2s(&S.ring[stage][kFastRing], ws.vtx + pc.stB, bytesB, &S.bar[stage]);
+        }
+        // the culls' per-polygon records and the FP64 rings of the exact test
+        // into L1 while the current pair is processed (lines of 8 vertices)
+        if (lane < 6) {
+            const int pp = (lane & 1) ? pc.b : pc.a;
+            const void* src = lane < 2 ? (const void*)(ws.polyInfo + pp)
+                            : lane < 4 ? (const void*)(ws.polyBox + pp) : (const void*)(ws.polyFlags + pp);
+            prefetch_l1(src);
+        } else if (lane >= 8 && lane < 24) {
+            const int k = lane & 7;                  // line k of a ring (8 vertices of 16 B)
+            const bool ringB = lane >= 16;
+            const int st0 = ringB ? pc.stB : pc.stA, n0 = ringB ? pc.nB : pc.nA;
+            if (8 * k < n0 && !(ringB && pc.self)) {
+                prefetch_l1(pos + st0 + 8 * k);
+                prefetch_l1(ws.edgeVec + st0 + 8 * k);
+            }
         }
         return true;
     };
