@@ -127,6 +127,24 @@ __device__ bool cyclic_solve(int n, Arr lo, Arr di, Arr up, int nr, Arr d0, Arr 
 constexpr int kProjArrays = 11;
 constexpr int kConsThreads = 32;
 
+__device__ void fire_scalars(Ctrl* __restrict__ c);
+
+// End of the step's force pass (the projection, or the velocity half-kick
+// of the soft models): the last block to finish does the scalar bookkeeping
+// of the step, unless the energy-increase rollback runs next (the pass in
+// its body ends the step then).  Every thread of the block calls this.
+__device__ __forceinline__ void fire_pass_end(Ctrl* __restrict__ c, bool rollbackNext) {
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        __threadfence();
+        unsigned int t = atomicAdd(&c->bendTicket, 1u);
+        if (t == gridDim.x - 1) {
+            __threadfence();
+            if (!rollbackNext) fire_scalars(c);
+        }
+    }
+}
+
 __global__ void __launch_bounds__(kConsThreads)
 k_project(const double2* __restrict__ pos, const int* __restrict__ start, int P,
           const double* __restrict__ constraints, double2* __restrict__ force,
@@ -137,18 +155,19 @@ k_project(const double2* __restrict__ pos, const int* __restrict__ start, int P,
     if (gate_closed(gate)) return;
     extern __shared__ double cons_smem[];
     int p = blockIdx.x * blockDim.x + threadIdx.x;
-    bool proceed = false;
+    bool proceed = false, rbNext = false;
     double dt = 0.0;
     if (fire) {
         double E = fire->energy, E0 = fire->ePre;
         bool rb = E > E0 + fmax(fabs(E0) * 1e-10, 1e-14);
         proceed = !fire->shakeFailed && !rb && fire->rollback == 0;
         dt = fire->dt;
+        rbNext = fire->rollback == 0 && !fire->shakeFailed && rb && fire->active;
         if (p == 0 && fire->rollback == 0) {
             fire->proceed = proceed ? 1 : 0;
             // the energy-increase rollback path runs when the step is not a
             // SHAKE failure and the energy went up (model.cpp:450-453)
-            int go = (!fire->shakeFailed && rb && fire->active) ? 1 : 0;
+            int go = rbNext ? 1 : 0;
             fire->rbGate = go;
             if (useCond) cudaGraphSetConditional(rbCond, (unsigned int)go);
         }
@@ -271,6 +290,8 @@ k_project(const double2* __restrict__ pos, const int* __restrict__ start, int P,
                 atomicAdd(&fire->ff, sF);
             }
         }
+        if ((threadIdx.x & 31) == 0) __threadfence();
+        fire_pass_end(fire, rbNext);
     }
 }
 
@@ -944,18 +965,19 @@ __global__ void __launch_bounds__(256, 4) k_project_warp(const double2* __restri
     const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
     const int wpb = blockDim.x >> 5;
     int p = blockIdx.x * wpb + warp;
-    bool proceed = false;
+    bool proceed = false, rbNext = false;
     double dt = 0.0;
     if (fire) {
         double E = fire->energy, E0 = fire->ePre;
         bool rb = E > E0 + fmax(fabs(E0) * 1e-10, 1e-14);
         proceed = !fire->shakeFailed && !rb && fire->rollback == 0;
         dt = fire->dt;
+        rbNext = fire->rollback == 0 && !fire->shakeFailed && rb && fire->active;
         if (blockIdx.x == 0 && threadIdx.x == 0 && fire->rollback == 0) {
             fire->proceed = proceed ? 1 : 0;
             // the energy-increase rollback path runs when the step is not a
             // SHAKE failure and the energy went up (model.cpp:450-453)
-            int go = (!fire->shakeFailed && rb && fire->active) ? 1 : 0;
+            int go = rbNext ? 1 : 0;
             fire->rbGate = go;
             if (useCond) cudaGraphSetConditional(rbCond, (unsigned int)go);
         }
@@ -1133,6 +1155,8 @@ __global__ void __launch_bounds__(256, 4) k_project_warp(const double2* __restri
                 atomicAdd(&fire->ff, sF);
             }
         }
+        if (lane == 0) __threadfence();
+        fire_pass_end(fire, rbNext);
     }
 }
 
@@ -1151,18 +1175,19 @@ __global__ void __launch_bounds__(128, 7) k_project_lanes(const double2* __restr
     if (gate_closed(gate)) return;
     const int lane = threadIdx.x & 31;
     const int p = blockIdx.x * (blockDim.x >> 5) + (threadIdx.x >> 5);
-    bool proceed = false;
+    bool proceed = false, rbNext = false;
     double dt = 0.0;
     if (fire) {
         double E = fire->energy, E0 = fire->ePre;
         bool rb = E > E0 + fmax(fabs(E0) * 1e-10, 1e-14);
         proceed = !fire->shakeFailed && !rb && fire->rollback == 0;
         dt = fire->dt;
+        rbNext = fire->rollback == 0 && !fire->shakeFailed && rb && fire->active;
         if (blockIdx.x == 0 && threadIdx.x == 0 && fire->rollback == 0) {
             fire->proceed = proceed ? 1 : 0;
             // the energy-increase rollback path runs when the step is not a
             // SHAKE failure and the energy went up (model.cpp:450-453)
-            int go = (!fire->shakeFailed && rb && fire->active) ? 1 : 0;
+            int go = rbNext ? 1 : 0;
             fire->rbGate = go;
             if (useCond) cudaGraphSetConditional(rbCond, (unsigned int)go);
         }
@@ -1290,6 +1315,7 @@ __global__ void __launch_bounds__(128, 7) k_project_lanes(const double2* __restr
                 atomicAdd(&fire->ff, sF);
             }
         }
+        fire_pass_end(fire, rbNext);
     }
 }
 
@@ -1445,8 +1471,11 @@ __global__ void k_fire_begin(double2* __restrict__ pos, double2* __restrict__ ve
         fire_step_resets(c);
         if (resetContacts) zero_contact_counters(c);
     }
+    const int bm = c->bendMode;
+    const double ba = c->bendA, bs = c->bendS;
     if (i < V) {
         double2 x = pos[i], v = vel[i], f = force[i];
+        v = apply_bend(v, f, bm, ba, bs);     // the previous step's bend
         save[i] = x;
         velSnap[i] = v;
         forceSnap[i] = f;
@@ -1491,6 +1520,7 @@ __global__ void k_fire_rollback(double2* __restrict__ pos, double2* __restrict__
         c->rollback = 1;
         c->energy = 0.0;
         c->maxF = 0.0;
+        c->bendTicket = 0;   // the body's force pass ends the step
         if (resetContacts) zero_contact_counters(c);
         c->condLaunches += (unsigned long long)c->rbBodyKernels;
     }
@@ -1522,9 +1552,10 @@ __global__ void k_fire_velocity(double2* __restrict__ vel, const double2* __rest
     double E = c->energy, E0 = c->ePre;
     bool rb = E > E0 + fmax(fabs(E0) * 1e-10, 1e-14);
     bool proceed = !c->shakeFailed && !rb && c->rollback == 0;
+    const bool rbNext = c->rollback == 0 && !c->shakeFailed && rb && c->active;
     if (i == 0 && c->rollback == 0) {
         c->proceed = proceed ? 1 : 0;
-        int go = (!c->shakeFailed && rb && c->active) ? 1 : 0;
+        int go = rbNext ? 1 : 0;
         c->rbGate = go;
         if (useCond) cudaGraphSetConditional(rbCond, (unsigned int)go);
     }
@@ -1550,6 +1581,8 @@ __global__ void k_fire_velocity(double2* __restrict__ vel, const double2* __rest
             atomicAdd(&c->P, sP); atomicAdd(&c->vv, sV); atomicAdd(&c->ff, sF);
         }
     }
+    if ((threadIdx.x & 31) == 0) __threadfence();
+    fire_pass_end(c, rbNext);
 }
 
 // max |F| only (rollback path of models without projection)
@@ -1561,7 +1594,8 @@ __global__ void k_fire_maxf(const double2* __restrict__ force, int V, Ctrl* __re
     double mF = 0.0;
     if (i < V) { double2 f = force[i]; mF = fmax(fabs(f.x), fabs(f.y)); }
     mF = warp_maxd(mF);
-    if ((threadIdx.x & 31) == 0) atomic_max_nonneg(&c->maxF, mF);
+    if ((threadIdx.x & 31) == 0) { atomic_max_nonneg(&c->maxF, mF); __threadfence(); }
+    fire_pass_end(c, false);    // the rollback body's pass (model.cpp:462-466)
 }
 
 // scalar bookkeeping of the step (model.cpp:444-485) and the stop test of
@@ -1573,10 +1607,12 @@ __device__ void fire_scalars(Ctrl* __restrict__ c) {
         // and redoes this step from its snapshot
         c->needsRecovery = 1;
         c->active = 0;
+        c->bendMode = 0;   // the redo starts from the step's snapshot (bent already)
         return;
     }
     double dt = c->dt, alpha = c->alpha;
     int nPos = c->nPos;
+    c->bendMode = 0;       // failure and rollback zeroed v already
     if (c->shakeFailed) {
         c->outE = c->energy;
         dt *= c->fDec; alpha = c->alphaStart; nPos = 0;
@@ -1586,12 +1622,21 @@ __device__ void fire_scalars(Ctrl* __restrict__ c) {
     } else {
         c->outE = c->energy;
         if (c->P > 0.0) {
+            // v <- (1 - alpha) v + alpha |v| / |F| F with this step's alpha
+            // (model.cpp:471-478), applied by the next step's start
+            const double fn = sqrt(c->ff), vn = sqrt(c->vv);
+            if (fn > 0.0) {
+                c->bendA = 1.0 - alpha;
+                c->bendS = alpha * vn / fn;
+                c->bendMode = 1;
+            }
             if (++nPos >= c->nMin) {
                 double nd = fmin(dt * c->fInc, c->dtMax);
                 if (nd > dt) alpha *= c->fAlpha;
                 dt = nd;
             }
         } else {
+            c->bendMode = 2;   // v <- 0 (model.cpp:479-483)
             dt *= c->fDec; alpha = c->alphaStart; nPos = 0;
         }
     }
@@ -1602,45 +1647,17 @@ __device__ void fire_scalars(Ctrl* __restrict__ c) {
     if (c->stepLimit > 0 && c->stepsDone >= c->stepLimit) c->active = 0;
 }
 
-// Step end: bend v toward F when the step proceeds (model.cpp:471-484); the
-// last block to finish then does the scalar bookkeeping (every block has
-// read alpha, P, |v|, |F| before it takes its ticket).
-__global__ void k_fire_bend(double2* __restrict__ vel, const double2* __restrict__ force,
-                            int V, Ctrl* __restrict__ c, const int* gate) {
+
+// A pending bend (Ctrl::bendMode) applied before the velocities are read
+// outside a FIRE step; the host clears the mode after this kernel.
+__global__ void k_fire_settle(double2* __restrict__ vel, const double2* __restrict__ force,
+                              int V, const Ctrl* __restrict__ c) {
     pdl_enter();
-    if (gate_closed(gate)) return;
-    __shared__ double s_coef[3];
-    if (threadIdx.x == 0) {
-        // the mixing coefficients once per block (two square roots, a division)
-        double fn = sqrt(c->ff), vn = sqrt(c->vv), a = c->alpha;
-        s_coef[0] = 1.0 - a;
-        s_coef[1] = fn > 0.0 ? a * vn / fn : -1.0;
-        s_coef[2] = c->proceed ? c->P : 0.0;
-    }
-    __syncthreads();
+    const int bm = c->bendMode;
+    if (bm == 0) return;
+    const double ba = c->bendA, bs = c->bendS;
     int i = blockIdx.x * blockDim.x + threadIdx.x;
-    const bool go = c->proceed != 0;
-    if (go && i < V) {
-        if (s_coef[2] > 0.0) {
-            double sc = s_coef[1];
-            if (sc >= 0.0) {
-                double a1 = s_coef[0];
-                double2 v = vel[i], f = force[i];
-                vel[i] = make_double2(a1 * v.x + sc * f.x, a1 * v.y + sc * f.y);
-            }
-        } else {
-            vel[i] = make_double2(0.0, 0.0);
-        }
-    }
-    __syncthreads();
-    if (threadIdx.x == 0) {
-        __threadfence();
-        unsigned int t = atomicAdd(&c->bendTicket, 1u);
-        if (t == gridDim.x - 1) {
-            __threadfence();
-            fire_scalars(c);
-        }
-    }
+    if (i < V) vel[i] = apply_bend(vel[i], force[i], bm, ba, bs);
 }
 
 __global__ void k_set_fire_params(Ctrl* __restrict__ c, FireScalars f) {
@@ -1692,9 +1709,9 @@ cudaError_t launch_fire_maxf(const double2* force, int V, Ctrl* c, const int* ga
     launch_k(k_fire_maxf, dim3(nblk(V, 256)), dim3(256), 0, st, force, V, c, gate);
     return cudaGetLastError();
 }
-cudaError_t launch_fire_finish(double2* vel, const double2* force, int V, Ctrl* c,
-                               const int* gate, cudaStream_t st) {
-    launch_k(k_fire_bend, dim3(nblk(V, 256)), dim3(256), 0, st, vel, force, V, c, gate);
+cudaError_t launch_fire_settle(double2* vel, const double2* force, int V, Ctrl* c,
+                               cudaStream_t st) {
+    launch_k(k_fire_settle, dim3(nblk(V, 256)), dim3(256), 0, st, vel, force, V, c);
     return cudaGetLastError();
 }
 

@@ -81,7 +81,9 @@ k_prepass(double2* __restrict__ pos, const int* __restrict__ start,
             zero_contact_counters_but_rmax(mv.c);
         }
         const double dt = mv.c->dt;
-        for (int kl = lane; kl < n; kl += 32) pos[st + kl] = fire_move_vertex(mv, st + kl, dt);
+        const int bm = mv.c->bendMode;
+        const double ba = mv.c->bendA, bs = mv.c->bendS;
+        for (int kl = lane; kl < n; kl += 32) pos[st + kl] = fire_move_vertex(mv, st + kl, dt, bm, ba, bs);
         __syncwarp();
     }
     if (p < P && n <= 0) {   // empty polygon: no edges, never a candidate

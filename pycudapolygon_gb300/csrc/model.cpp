@@ -633,7 +633,9 @@ int record_fire_step(pcp_model* m, cudaGraphConditionalHandle retryCond,
     if (rc) return rc;
     if (e != cudaSuccess) return fail(PCP_ERR_CUDA, "rollback capture: %s", cudaGetErrorString(e));
     m->rbBodyKernels = count_kernel_nodes(body);
-    CK(launch_fire_finish(m->vel, m->force, V, m->ctrl, gA, st));
+    // the step's scalar bookkeeping ran in the last block of the force pass
+    // (or of the rollback body's pass); the velocity bend waits for the next
+    // step's start kernel (or for a read of the velocities)
     return PCP_OK;
 }
 
@@ -1088,6 +1090,7 @@ int pcp_model_update_positions(pcp_model* m, double dt) {
 int pcp_model_reset_velocities(pcp_model* m) {
     CHECK_M(m);
     CK(cudaMemsetAsync(m->vel, 0, (size_t)m->V * sizeof(double2), m->stream));
+    CK(cudaMemsetAsync(&m->ctrl->bendMode, 0, sizeof(int), m->stream));   // nothing left to bend
     return PCP_OK;
 }
 
@@ -1373,7 +1376,13 @@ int pcp_model_get_forces(pcp_model* m, double* out, int cap, int* len) {
     CHECK_M(m); return copy_dev_out(m, reinterpret_cast<const double*>(m->force), 2 * m->V, out, cap, len);
 }
 int pcp_model_get_velocities(pcp_model* m, double* out, int cap, int* len) {
-    CHECK_M(m); return copy_dev_out(m, reinterpret_cast<const double*>(m->vel), 2 * m->V, out, cap, len);
+    CHECK_M(m);
+    if (m->V > 0) {
+        // the last FIRE step's bend, if the next step has not applied it yet
+        CK(launch_fire_settle(m->vel, m->force, m->V, m->ctrl, m->stream));
+        CK(cudaMemsetAsync(&m->ctrl->bendMode, 0, sizeof(int), m->stream));
+    }
+    return copy_dev_out(m, reinterpret_cast<const double*>(m->vel), 2 * m->V, out, cap, len);
 }
 int pcp_model_get_areas(pcp_model* m, double* out, int cap, int* len) {
     if (m && m->geometryStale) { int grc = ensure_geometry(m); if (grc) return grc; }

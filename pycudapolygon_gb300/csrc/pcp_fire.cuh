@@ -39,11 +39,23 @@ __device__ __forceinline__ void fire_step_resets(Ctrl* c) {
     c->shakeTicket = 0; c->bendTicket = 0;
 }
 
-// Verlet half-kick and drift of vertex i (model.cpp:405-430) with the
-// snapshots the rollbacks and the overflow recovery restore from; F = 0 for
-// the coming force pass.  Returns the new position.
-__device__ __forceinline__ double2 fire_move_vertex(const FireMove& mv, int i, double dt) {
+// The previous step's velocity bend (model.cpp:471-484, Ctrl::bendMode),
+// deferred to the start of this step: the same operations as at the end of
+// the previous one.
+__device__ __forceinline__ double2 apply_bend(double2 v, double2 f, int mode, double a, double s) {
+    if (mode == 1) return make_double2(a * v.x + s * f.x, a * v.y + s * f.y);
+    if (mode == 2) return make_double2(0.0, 0.0);
+    return v;
+}
+
+// Verlet half-kick and drift of vertex i (model.cpp:405-430) after the
+// previous step's bend, with the snapshots the rollbacks and the overflow
+// recovery restore from; F = 0 for the coming force pass.  Returns the new
+// position.
+__device__ __forceinline__ double2 fire_move_vertex(const FireMove& mv, int i, double dt,
+                                                    int bendMode, double bendA, double bendS) {
     double2 x = mv.pos[i], v = mv.vel[i], f = mv.force[i];
+    v = apply_bend(v, f, bendMode, bendA, bendS);
     mv.save[i] = x;
     mv.velSnap[i] = v;
     mv.forceSnap[i] = f;

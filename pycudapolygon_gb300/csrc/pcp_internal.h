@@ -70,6 +70,11 @@ struct Ctrl {
     unsigned int shakeTicket, bendTicket;
     unsigned long long condLaunches;
     int rbBodyKernels;     // kernels in the rollback body (set by the host)
+    // the velocity bend of the last step (model.cpp:471-484), applied by the
+    // next step's start or before velocities are read: 0 none, 1 v <- bendA v
+    // + bendS F, 2 v <- 0
+    int bendMode;
+    double bendA, bendS;
 };
 
 enum : unsigned int {
@@ -230,8 +235,9 @@ cudaError_t launch_fire_velocity(double2* vel, const double2* force, int V, Ctrl
                                  const int* gate, cudaStream_t st);
 cudaError_t launch_fire_maxf(const double2* force, int V, Ctrl* c, const int* gate,
                              cudaStream_t st);
-cudaError_t launch_fire_finish(double2* vel, const double2* force, int V, Ctrl* c,
-                               const int* gate, cudaStream_t st);
+// apply a pending velocity bend (Ctrl::bendMode) and clear it
+cudaError_t launch_fire_settle(double2* vel, const double2* force, int V, Ctrl* c,
+                               cudaStream_t st);
 
 int sm_count();
 
