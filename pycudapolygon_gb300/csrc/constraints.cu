@@ -283,7 +283,7 @@ k_project(const double2* __restrict__ pos, const int* __restrict__ start, int P,
         mF = warp_maxd(mF);
         if ((threadIdx.x & 31) == 0) atomic_max_nonneg(&fire->maxF, mF);
         if (proceed) {
-            sP = warp_sum(sP); sV = warp_sum(sV); sF = warp_sum(sF);
+            { const double4 t4 = warp_sum4(sP, sV, sF, 0.0); sP = t4.x; sV = t4.y; sF = t4.z; }
             if ((threadIdx.x & 31) == 0) {
                 atomicAdd(&fire->P, sP);
                 atomicAdd(&fire->vv, sV);
@@ -1108,8 +1108,10 @@ __global__ void __launch_bounds__(256, 4) k_project_warp(const double2* __restri
                     qF += q.x * f.x + q.y * f.y;
                     qq += q.x * q.x + q.y * q.y;
                 }
-                qF = warp_sum(qF);
-                qq = warp_sum(qq);
+                {
+                    const double2 t2 = warp_sum2(qF, qq);
+                    qF = t2.x; qq = t2.y;
+                }
                 // sqrt(qq) > 1e-14 (kernels.cuh:464)
                 double coef = (qq > 1e-28) ? qF / qq : 0.0;
                 for (int k = lane; k < n; k += 32) {
@@ -1148,7 +1150,7 @@ __global__ void __launch_bounds__(256, 4) k_project_warp(const double2* __restri
         mF = warp_max_u64(mF);
         if (lane == 0 && mF) atomicMax(reinterpret_cast<unsigned long long*>(&fire->maxF), mF);
         if (proceed) {
-            sP = warp_sum(sP); sV = warp_sum(sV); sF = warp_sum(sF);
+            { const double4 t4 = warp_sum4(sP, sV, sF, 0.0); sP = t4.x; sV = t4.y; sF = t4.z; }
             if (lane == 0) {
                 atomicAdd(&fire->P, sP);
                 atomicAdd(&fire->vv, sV);
@@ -1272,8 +1274,10 @@ __global__ void __launch_bounds__(128, 7) k_project_lanes(const double2* __restr
             if (!bad) {
                 double qF = live ? q.x * f.x + q.y * f.y : 0.0;
                 double qq = live ? q.x * q.x + q.y * q.y : 0.0;
-                qF = warp_sum(qF);
-                qq = warp_sum(qq);
+                {
+                    const double2 t2 = warp_sum2(qF, qq);
+                    qF = t2.x; qq = t2.y;
+                }
                 // sqrt(qq) > 1e-14 (kernels.cuh:464)
                 double coef = (qq > 1e-28) ? qF / qq : 0.0;
                 f = make_double2(f.x - coef * q.x, f.y - coef * q.y);
@@ -1300,7 +1304,7 @@ __global__ void __launch_bounds__(128, 7) k_project_lanes(const double2* __restr
         const int warp = threadIdx.x >> 5, nw = blockDim.x >> 5;
         if (bad && lane == 0) atomicOr(&fire->flags, kFlagNonFinite);
         mF = warp_max_u64(mF);
-        if (proceed) { sP = warp_sum(sP); sV = warp_sum(sV); sF = warp_sum(sF); }
+        if (proceed) { { const double4 t4 = warp_sum4(sP, sV, sF, 0.0); sP = t4.x; sV = t4.y; sF = t4.z; } }
         if (lane == 0) { s_max[warp] = mF; s_sum[0][warp] = sP; s_sum[1][warp] = sV; s_sum[2][warp] = sF; }
         __syncthreads();
         if (threadIdx.x == 0) {
@@ -1576,7 +1580,7 @@ __global__ void k_fire_velocity(double2* __restrict__ vel, const double2* __rest
     mF = warp_maxd(mF);
     if ((threadIdx.x & 31) == 0) atomic_max_nonneg(&c->maxF, mF);
     if (proceed) {
-        sP = warp_sum(sP); sV = warp_sum(sV); sF = warp_sum(sF);
+        { const double4 t4 = warp_sum4(sP, sV, sF, 0.0); sP = t4.x; sV = t4.y; sF = t4.z; }
         if ((threadIdx.x & 31) == 0) {
             atomicAdd(&c->P, sP); atomicAdd(&c->vv, sV); atomicAdd(&c->ff, sF);
         }

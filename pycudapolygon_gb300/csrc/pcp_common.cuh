@@ -311,6 +311,37 @@ __device__ __forceinline__ double warp_sum(double v) {
     for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(PCP_FULL, v, o);
     return v;
 }
+// Two warp sums for the FP64 adds of one: at the first level the lower half
+// of the warp keeps adding a and the upper half b (each lane sends its
+// partner the value it drops), then each half reduces alone; the totals are
+// broadcast from lanes 0 and 16.  5 FP64 adds instead of 10 (every lane gets
+// the same bits; the association differs from warp_sum's).
+__device__ __forceinline__ double2 warp_sum2(double a, double b) {
+    const bool hi = (threadIdx.x & 16) != 0;
+    double keep = hi ? b : a;
+    keep += __shfl_xor_sync(PCP_FULL, hi ? a : b, 16);
+#pragma unroll
+    for (int o = 8; o > 0; o >>= 1) keep += __shfl_xor_sync(PCP_FULL, keep, o);
+    return make_double2(__shfl_sync(PCP_FULL, keep, 0), __shfl_sync(PCP_FULL, keep, 16));
+}
+
+// Four warp sums for 6 FP64 adds instead of 20: the warp splits into halves
+// (a, b | c, d) and then quarters (a | b | c | d) before reducing; the totals
+// are broadcast from lanes 0, 8, 16 and 24.
+__device__ __forceinline__ double4 warp_sum4(double a, double b, double c, double d) {
+    const int lane = threadIdx.x & 31;
+    const bool h16 = (lane & 16) != 0, h8 = (lane & 8) != 0;
+    double k0 = h16 ? c : a, k1 = h16 ? d : b;
+    k0 += __shfl_xor_sync(PCP_FULL, h16 ? a : c, 16);
+    k1 += __shfl_xor_sync(PCP_FULL, h16 ? b : d, 16);
+    double keep = h8 ? k1 : k0;
+    keep += __shfl_xor_sync(PCP_FULL, h8 ? k0 : k1, 8);
+#pragma unroll
+    for (int o = 4; o > 0; o >>= 1) keep += __shfl_xor_sync(PCP_FULL, keep, o);
+    return make_double4(__shfl_sync(PCP_FULL, keep, 0), __shfl_sync(PCP_FULL, keep, 8),
+                        __shfl_sync(PCP_FULL, keep, 16), __shfl_sync(PCP_FULL, keep, 24));
+}
+
 __device__ __forceinline__ float warp_maxf(float v) {
 #pragma unroll
     for (int o = 16; o > 0; o >>= 1) v = fmaxf(v, __shfl_xor_sync(PCP_FULL, v, o));

@@ -170,6 +170,22 @@ def test_self_crossing_records_bit_exact(box):
     assert_records_equal(g, o)
 
 
+def test_geometry_parity_odd_shapes():
+    """Geometry of the odd shapes: a repeated vertex (a zero-length edge,
+    whose unit tangent the reference computes as 0/0), a bow tie, a sliver,
+    a polygon across the periodic boundary."""
+    system = _odd_system()
+    g, o = pair(system)
+    g.updatePolygonGeometry()
+    o.updatePolygonGeometry()
+    np.testing.assert_allclose(g.getAreas(), o.getAreas(), rtol=AREA_RTOL, atol=1e-17)
+    np.testing.assert_allclose(g.getPerimeters(), o.getPerimeters(), rtol=1e-12)
+    np.testing.assert_allclose(g.getEdgeLengths(), o.getEdgeLengths(), rtol=1e-12)
+    np.testing.assert_allclose(g.getConstraints(), o.getConstraints(), rtol=1e-10, atol=1e-13,
+                               equal_nan=True)
+    assert np.isnan(np.asarray(o.getConstraints())).any()
+
+
 def test_neighbor_slots_bit_exact(system):
     g, o = pair(system)
     contacts(g)
