@@ -1024,7 +1024,8 @@ void orc_project_force(orc_model* m) {
 /* returns the largest iteration count over polygons; failure = count >=     */
 /* maxIter.  Restatement (matrix SHAKE, Newton in the multipliers, the       */
 /* correction solved in single precision):                                   */
-/*   s_k = (|e_k|^2 - L^2)/2, e_k = wrap(x_{k+1} - x_k);  s_A = A - A0;       */
+/*   s_k = (|e_k|^2 - L^2)/2, e_k = u_{k+1} - u_k;  s_A = A - A0;             */
+/*   u_k = wrap(x_k - x_0), local coordinates taken once at the start;       */
 /*   stop when max(max_k |s_k|/L, |s_A|) < tol;                               */
 /*   x <- x + G_ref^T l,  (G(x) G_ref^T) l = -s,                              */
 /* G_ref the constraint gradients where SHAKE starts (rows -+e_k, grad A).    */
@@ -1086,13 +1087,19 @@ static int shake_polygon(orc_model* m, int p, int maxIter, double tol, double* w
     float *vr = acf + 2 * n, *lam = vr + n;
     float *pa = lam + n, *pb = pa + 2 * N, *pc = pb + 2 * N;
     float *p0 = pc + 2 * N, *p1 = p0 + 2 * N, *p2 = p1 + 2 * N;
-    for (int i = 0; i < 2 * n; ++i) x[i] = m->positions[2 * st + i];
+    /* local coordinates u_k = wrap(x_k - x_0): the iterations need no
+       minimum images (a polygon spans far less than half the box) */
+    const double ox = m->positions[2 * st], oy = m->positions[2 * st + 1];
+    for (int k = 0; k < n; ++k) {
+        x[2 * k] = orc_wrap(m->positions[2 * (st + k)] - ox);
+        x[2 * k + 1] = orc_wrap(m->positions[2 * (st + k) + 1] - oy);
+    }
     for (int k = 0; k < n; ++k) {
         int kn = (k + 1) % n, kp = (k + n - 1) % n;
-        r[2 * k] = orc_wrap(x[2 * kn] - x[2 * k]);
-        r[2 * k + 1] = orc_wrap(x[2 * kn + 1] - x[2 * k + 1]);
-        ar[2 * k] = 0.5 * orc_wrap(x[2 * kn + 1] - x[2 * kp + 1]);
-        ar[2 * k + 1] = 0.5 * orc_wrap(x[2 * kp] - x[2 * kn]);
+        r[2 * k] = x[2 * kn] - x[2 * k];
+        r[2 * k + 1] = x[2 * kn + 1] - x[2 * k + 1];
+        ar[2 * k] = 0.5 * (x[2 * kn + 1] - x[2 * kp + 1]);
+        ar[2 * k + 1] = 0.5 * (x[2 * kp] - x[2 * kn]);
         rf[2 * k] = (float)r[2 * k]; rf[2 * k + 1] = (float)r[2 * k + 1];
         arf[2 * k] = (float)ar[2 * k]; arf[2 * k + 1] = (float)ar[2 * k + 1];
     }
@@ -1102,15 +1109,14 @@ static int shake_polygon(orc_model* m, int p, int maxIter, double tol, double* w
         int nonfinite = 0;
         for (int k = 0; k < n; ++k) {
             int kn = (k + 1) % n, kp = (k + n - 1) % n;
-            double ex = orc_wrap(x[2 * kn] - x[2 * k]), ey = orc_wrap(x[2 * kn + 1] - x[2 * k + 1]);
+            double ex = x[2 * kn] - x[2 * k], ey = x[2 * kn + 1] - x[2 * k + 1];
             double sk = 0.5 * (ex * ex + ey * ey - L * L);
             double q = fabs(sk) * invL;
             if (!(q <= worst)) { worst = q; if (!isfinite(q)) nonfinite = 1; }
-            double X1 = orc_wrap(x[2 * k] - x[0]), X2 = orc_wrap(x[2 * kn] - x[0]);
-            area += ey * (X2 + X1) / 2.0;
+            area += ey * (x[2 * kn] + x[2 * k]) / 2.0;
             ef[2 * k] = (float)ex; ef[2 * k + 1] = (float)ey;
-            acf[2 * k] = (float)(0.5 * orc_wrap(x[2 * kn + 1] - x[2 * kp + 1]));
-            acf[2 * k + 1] = (float)(0.5 * orc_wrap(x[2 * kp] - x[2 * kn]));
+            acf[2 * k] = (float)(0.5 * (x[2 * kn + 1] - x[2 * kp + 1]));
+            acf[2 * k + 1] = (float)(0.5 * (x[2 * kp] - x[2 * kn]));
             lam[k] = (float)(-sk);
         }
         double sA = area - A0;
@@ -1163,9 +1169,10 @@ static int shake_polygon(orc_model* m, int p, int maxIter, double tol, double* w
             x[2 * k + 1] += -lk * r[2 * k + 1] + lp * r[2 * kp + 1] + mu64 * ar[2 * k + 1];
         }
     }
-    for (int i = 0; i < 2 * n; ++i) {
-        double v = x[i];
-        m->positions[2 * st + i] = v - floor(v);
+    for (int k = 0; k < n; ++k) {
+        double vx = ox + x[2 * k], vy = oy + x[2 * k + 1];
+        m->positions[2 * (st + k)] = vx - floor(vx);
+        m->positions[2 * (st + k) + 1] = vy - floor(vy);
     }
     return it;
 }

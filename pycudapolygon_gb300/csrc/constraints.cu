@@ -509,13 +509,20 @@ __global__ void __launch_bounds__(256, 4) k_shake(double2* __restrict__ pos, con
             const unsigned long long tolBits =
                 tol > 0.0 ? (unsigned long long)__double_as_longlong(tol) : 0ull;
             const double invL = L > 0.0 ? 1.0 / L : 1.0;
-            for (int k = lane; k < n; k += 32) w.xs[k] = pos[st + k];
+            const double hInvL = 0.5 * invL, L2 = L * L;
+            // local coordinates u_k = wrap(x_k - x_0) (no minimum images in
+            // the iterations), the same arithmetic as k_shake_lanes
+            const double2 o = pos[st];
+            for (int k = lane; k < n; k += 32) {
+                double2 xk = pos[st + k];
+                w.xs[k] = make_double2(wrap(xk.x - o.x), wrap(xk.y - o.y));
+            }
             __syncwarp();
             for (int k = lane; k < n; k += 32) {
                 int kn = (k + 1 == n) ? 0 : k + 1, kp = (k == 0) ? n - 1 : k - 1;
                 double2 xk = w.xs[k], xn = w.xs[kn], xp = w.xs[kp];
-                double2 r = make_double2(wrap(xn.x - xk.x), wrap(xn.y - xk.y));
-                double2 a = make_double2(0.5 * wrap(xn.y - xp.y), 0.5 * wrap(xp.x - xn.x));
+                double2 r = make_double2(xn.x - xk.x, xn.y - xk.y);
+                double2 a = make_double2(0.5 * (xn.y - xp.y), 0.5 * (xp.x - xn.x));
                 w.r[k] = r; w.ar[k] = a;
                 w.rf[k] = make_float2(d2f_int(r.x), d2f_int(r.y));
                 w.arf[k] = make_float2(d2f_int(a.x), d2f_int(a.y));
@@ -528,18 +535,16 @@ __global__ void __launch_bounds__(256, 4) k_shake(double2* __restrict__ pos, con
                 unsigned long long worst = 0ull;
                 double area = 0.0;
                 bool nonfinite = false;
-                double x0x = w.xs[0].x;
                 for (int k = lane; k < n; k += 32) {
-                    int kn = (k + 1 == n) ? 0 : k + 1, kp = (k == 0) ? n - 1 : k - 1;
-                    double2 xk = w.xs[k], xn = w.xs[kn], xp = w.xs[kp];
-                    double ex = wrap(xn.x - xk.x), ey = wrap(xn.y - xk.y);
-                    double sk = 0.5 * (ex * ex + ey * ey - L * L);
-                    unsigned long long q = abs_bits(sk * invL);
-                    if (q > worst) worst = q;
-                    double X1 = wrap(xk.x - x0x), X2 = wrap(xn.x - x0x);
-                    area += ey * (X2 + X1);       // halved after the sum (exact)
+                    int kn = (k + 1 == n) ? 0 : k + 1;
+                    double2 xk = w.xs[k], xn = w.xs[kn];
+                    double ex = xn.x - xk.x, ey = xn.y - xk.y;
+                    double q = ex * ex + ey * ey - L2;     // 2 s_k
+                    unsigned long long qb = abs_bits(q * hInvL);
+                    if (qb > worst) worst = qb;
+                    area += ey * (xn.x + xk.x);   // halved after the sum (exact)
                     w.ef[k] = make_float2(d2f_int(ex), d2f_int(ey));
-                    w.lam[k] = d2f_int(-sk);      // right-hand side until the rows are built
+                    w.lam[k] = d2f_int(-q) * 0.5f;   // right-hand side -s_k until the rows are built
                 }
                 worst = warp_max_u64(worst);
                 area = warp_sum(area) * 0.5;
@@ -632,13 +637,15 @@ __global__ void __launch_bounds__(256, 4) k_shake(double2* __restrict__ pos, con
                 }
                 __syncwarp();
             }
+            __syncwarp();   // every lane has read pos[st] (o) before it is rewritten
             if (vel) {
                 // FIRE step: v += wrap(x_shake - x_before) / dt, the reference's
                 // rederivation from the displacement (model.cpp:436-438); a retry
                 // adds its own displacement on top
                 const double idt = 1.0 / dtc->dt;
                 for (int k = lane; k < n; k += 32) {
-                    double2 x = w.xs[k], y = pos[st + k], v = vel[st + k];
+                    double2 x = make_double2(o.x + w.xs[k].x, o.y + w.xs[k].y), y = pos[st + k],
+                            v = vel[st + k];
                     x = make_double2(x.x - floor(x.x), x.y - floor(x.y));
                     v.x += wrap(x.x - y.x) * idt;
                     v.y += wrap(x.y - y.y) * idt;
@@ -647,7 +654,7 @@ __global__ void __launch_bounds__(256, 4) k_shake(double2* __restrict__ pos, con
                 }
             } else {
                 for (int k = lane; k < n; k += 32) {
-                    double2 v = w.xs[k];
+                    double2 v = make_double2(o.x + w.xs[k].x, o.y + w.xs[k].y);
                     pos[st + k] = make_double2(v.x - floor(v.x), v.y - floor(v.y));
                 }
             }
@@ -753,28 +760,33 @@ __global__ void __launch_bounds__(128, 7) k_shake_lanes(double2* __restrict__ po
             const unsigned long long tolBits =
                 tol > 0.0 ? (unsigned long long)__double_as_longlong(tol) : 0ull;
             const double invL = L > 0.0 ? 1.0 / L : 1.0;
-            double2 x = live ? pos[st + lane] : make_double2(0.0, 0.0);
+            const double hInvL = 0.5 * invL, L2 = L * L;
+            // local coordinates u_k = wrap(x_k - x_0): the iterations need no
+            // minimum images (a polygon spans far less than half the box)
+            double2 x;
+            {
+                const double2 x0 = live ? pos[st + lane] : make_double2(0.0, 0.0);
+                const double2 o = shfl2(x0, 0);
+                x = live ? make_double2(wrap(x0.x - o.x), wrap(x0.y - o.y)) : make_double2(0.0, 0.0);
+            }
             double2 r, ar;
             {
                 const double2 xn = shfl2(x, kn), xp = shfl2(x, kp);
-                r = make_double2(wrap(xn.x - x.x), wrap(xn.y - x.y));
-                ar = make_double2(0.5 * wrap(xn.y - xp.y), 0.5 * wrap(xp.x - xn.x));
+                r = make_double2(xn.x - x.x, xn.y - x.y);
+                ar = make_double2(0.5 * (xn.y - xp.y), 0.5 * (xp.x - xn.x));
             }
             const float2 rf = make_float2(d2f_int(r.x), d2f_int(r.y));
             const float2 arf = make_float2(d2f_int(ar.x), d2f_int(ar.y));
             const double2 rp = shfl2(r, kp);
             const float2 rnf = shfl2(rf, kn), rpf = shfl2(rf, kp), anf = shfl2(arf, kn);
             for (; it < maxIter; ++it) {
-                // residuals (FP64)
+                // residuals (FP64): q = |e|^2 - L^2 = 2 s_k
                 const double2 xn = shfl2(x, kn);
-                const double x0x = __shfl_sync(PCP_FULL, x.x, 0);
-                const double ex = wrap(xn.x - x.x), ey = wrap(xn.y - x.y);
-                const double sk = 0.5 * (ex * ex + ey * ey - L * L);
-                unsigned long long worst = live ? abs_bits(sk * invL) : 0ull;
-                const double X1 = wrap(x.x - x0x);
-                const double X2 = __shfl_sync(PCP_FULL, X1, kn);   // wrap(x_k+1 - x_0)
+                const double ex = xn.x - x.x, ey = xn.y - x.y;
+                const double q = ex * ex + ey * ey - L2;
+                unsigned long long worst = live ? abs_bits(q * hInvL) : 0ull;
                 double area = 0.0;
-                if (live) area += ey * (X2 + X1);
+                if (live) area += ey * (xn.x + x.x);
                 worst = warp_max_u64(worst);
                 area = warp_sum(area) * 0.5;
                 const double sA = area - A0;
@@ -794,7 +806,7 @@ __global__ void __launch_bounds__(128, 7) k_shake_lanes(double2* __restrict__ po
                     b = 2.0f * (e.x * rf.x + e.y * rf.y);
                     c = -(e.x * rnf.x + e.y * rnf.y);
                     a = -(e.x * rpf.x + e.y * rpf.y);
-                    q0 = d2f_int(-sk);
+                    q0 = d2f_int(-q) * 0.5f;
                     q1 = e.x * (anf.x - arf.x) + e.y * (anf.y - arf.y);
                     vr = (cn.x - ck.x) * rf.x + (cn.y - ck.y) * rf.y;
                     dc += ck.x * arf.x + ck.y * arf.y;
@@ -830,14 +842,19 @@ __global__ void __launch_bounds__(128, 7) k_shake_lanes(double2* __restrict__ po
                 double mu64 = f2d_int(mu);
                 if (live) shake_update(x, l, lp, mu, mu64, r, rp, ar, rf, rpf, arf);
             }
+            // the positions SHAKE started from, read again (fewer live registers
+            // through the iterations); lane 0's is x_0
+            const double2 x0 = live ? pos[st + lane] : make_double2(0.0, 0.0);
+            const double2 o = shfl2(x0, 0);
             if (live) {
-                double2 y = make_double2(x.x - floor(x.x), x.y - floor(x.y));
+                double2 y = make_double2(o.x + x.x, o.y + x.y);
+                y = make_double2(y.x - floor(y.x), y.y - floor(y.y));
                 if (vel) {
                     // FIRE step: v += wrap(x_shake - x_before) / dt, the
                     // reference's rederivation from the displacement
                     // (model.cpp:436-438); a retry adds its own displacement
                     const double idt = 1.0 / dtc->dt;
-                    double2 x0 = pos[st + lane], v = vel[st + lane];
+                    double2 v = vel[st + lane];
                     v.x += wrap(y.x - x0.x) * idt;
                     v.y += wrap(y.y - x0.y) * idt;
                     vel[st + lane] = v;
