@@ -661,13 +661,16 @@ int build_fire_graph(pcp_model* m, int shakeIter) {
     cudaError_t e = cudaStreamBeginCapture(cap, cudaStreamCaptureModeThreadLocal);
     int rc = PCP_OK;
     if (e == cudaSuccess) {
-        // the two conditions are created on the graph being captured; they
-        // read 0 at every launch of it until a kernel of the step sets them
+        // the conditions are created on the graph being captured; they read
+        // 0 at every launch of it until a kernel of the step sets them.  The
+        // SHAKE retry exists only for the normal model with SHAKE (a handle
+        // that no conditional node uses makes the instantiation fail).
         cudaStreamCaptureStatus cs;
         cudaGraph_t cg = nullptr;
         cudaGraphConditionalHandle retryCond = 0, rbCond = 0;
+        const bool retry = m->modelType == PCP_MODEL_NORMAL && shakeIter > 0;
         e = cudaStreamGetCaptureInfo(cap, &cs, nullptr, &cg);
-        if (e == cudaSuccess)
+        if (e == cudaSuccess && retry)
             e = cudaGraphConditionalHandleCreate(&retryCond, cg, 0, cudaGraphCondAssignDefault);
         if (e == cudaSuccess)
             e = cudaGraphConditionalHandleCreate(&rbCond, cg, 0, cudaGraphCondAssignDefault);
@@ -678,15 +681,19 @@ int build_fire_graph(pcp_model* m, int shakeIter) {
     m->stream = saved;
     m->launches = savedLaunches;
     cudaStreamDestroy(cap);
-    if (rc) { if (g) cudaGraphDestroy(g); return rc; }
+    if (rc) { if (g) cudaGraphDestroy(g); (void)cudaGetLastError(); return rc; }
     if (e != cudaSuccess) {
         if (g) cudaGraphDestroy(g);
+        (void)cudaGetLastError();    // not left for the next launcher's check
         return fail(PCP_ERR_CUDA, "graph capture failed: %s", cudaGetErrorString(e));
     }
     m->fireKernelNodes = count_kernel_nodes(g);
     e = cudaGraphInstantiate(&m->fireExec, g, 0);
     cudaGraphDestroy(g);
-    if (e != cudaSuccess) return fail(PCP_ERR_CUDA, "graph instantiate failed: %s", cudaGetErrorString(e));
+    if (e != cudaSuccess) {
+        (void)cudaGetLastError();    // not left for the next launcher's check
+        return fail(PCP_ERR_CUDA, "graph instantiate failed: %s", cudaGetErrorString(e));
+    }
     m->fireGen = m->generation;
     m->fireModel = m->modelType;
     m->fireB = m->boxSize;

@@ -331,6 +331,39 @@ def test_fire_steps_parity():
     assert np.abs(vg - vo).max() <= 1e-6 * np.abs(vo).max() + 1e-14
 
 
+@pytest.mark.parametrize("mt,k,c,dt0", [(3, 1.0, 1.0, 1.0), (5, 1.0, 1.0, 0.1), (1, 2.0, 0.0, 0.3),
+                                        (2, 0.0, 3.0, 0.3)])
+def test_fire_steps_soft_models_parity(mt, k, c, dt0):
+    """FIRE steps of the models without SHAKE (softBody, hybrid, edgeOnly,
+    areaOnly): the velocity half-kick and the sums in k_fire_velocity, the
+    energy rollback ending with k_fire_maxf (softBody and hybrid roll back
+    here), the step bookkeeping and the bend deferred to the next step."""
+    s = make_system(64, 16, 0.85, seed=2)
+    g, o = pair(s)
+    g.setModelEnum(lib.modelEnum(mt))
+    o.setModelEnum(mt)
+    for m in (g, o):
+        m.setTargetAreas(s.target_areas * 1.05)
+        m.setTargetEdgeLengths(s.target_edge_lengths * 0.97)
+        m.setStiffness(k)
+        m.setCompressibility(c)
+        contacts(m)
+        m.updateForceEnergy()
+    st_g = st_o = (dt0, 0.1, 0)
+    for step in range(25):
+        rg = g.minimizeFIREStep(*st_g, 1.0)
+        ro = o.minimizeFIREStep(*st_o, 1.0)
+        assert rg[0] == pytest.approx(ro[0], rel=1e-9, abs=1e-14), step
+        assert rg[1:] == pytest.approx(ro[1:], rel=1e-12), step
+        if step % 6 == 2:
+            vg, vo = np.asarray(g.getVelocities()), np.asarray(o.getVelocities())
+            assert np.abs(vg - vo).max() <= 1e-6 * np.abs(vo).max() + 1e-14, step
+        st_g, st_o = rg[1:], ro[1:]
+    d = (np.asarray(g.getPositions()) - o.getPositions() + 0.5) % 1.0 - 0.5
+    assert np.abs(d).max() < 1e-9
+    assert g.getMaxUnbalancedForce() == pytest.approx(o.getMaxUnbalancedForce(), rel=1e-9)
+
+
 def test_fire_rollback_state_matches_reference():
     """An energy-increase rollback (model.cpp:450-470) leaves the step's start
     positions, the force, energy and max |F| there, and the contact records of
