@@ -55,6 +55,7 @@ def lib():
             "orc_update_force_energy": (None, [P]),
             "orc_project_force": (None, [P]),
             "orc_shake_project": (I, [P, I, D]),
+            "orc_update_overlap_area": (D, [P, I]),
             "orc_xpbd_project": (I, [P, I, D]),
             "orc_update_positions": (None, [P, D]),
             "orc_reset_velocities": (None, [P]),
@@ -212,6 +213,12 @@ class OracleModel:
 
     def projectForce(self):
         self._L.orc_project_force(self._m)
+
+    def updateOverlapArea(self, pointDensity):
+        self._overlap = self._L.orc_update_overlap_area(self._m, int(pointDensity))
+
+    def getOverlapArea(self):
+        return self._overlap
 
     def shakeProject(self, nIter=100, tol=1e-15):
         return self._L.orc_shake_project(self._m, int(nIter), float(tol))

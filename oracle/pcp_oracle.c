@@ -1484,6 +1484,67 @@ const double* orc_constraints(const orc_model* m) { return m->constraints; }
 const double* orc_perimeters(const orc_model* m) { return m->perimeters; }
 const int* orc_shape_id(const orc_model* m) { return m->shapeId; }
 const int* orc_cell_location(const orc_model* m) { return m->cellLocation; }
+/* ------------------------------------------------------------------------ */
+/* Grid-point overlap estimate: updateOverlapAreaKernel (kernels.cuh:879-979) */
+/* and Model::updateOverlapArea (model.cpp:824-847).  Point (ix+.5, iy+.5)/d; */
+/* the polygons owning a vertex in the 3x3 cells around it (each once, at    */
+/* most 512 of them), an angle-sum inside test with the loop form of the     */
+/* minimum image (wrapPeriodic, kernels.cuh:108-113), c(c-1)/2 per point,    */
+/* the sum divided by d^2.  Uses the current cell list.                       */
+/* ------------------------------------------------------------------------ */
+static double orc_wrap_periodic(double x) {
+    x += 1.5;
+    while (x > 1.0) x -= 1.0;
+    return x - 0.5;
+}
+
+double orc_update_overlap_area(orc_model* m, int d) {
+    const double eps = 1e-12, PI = 3.141592653589793238462643383279;
+    const double* pos = m->positions;
+    const int B = m->boxSize, boxCount = B * B;
+    long long total = 0;
+    for (int idx = 0; idx < d * d; ++idx) {
+        int ix = idx % d, iy = idx / d;
+        double px = (ix + 0.5) / d, py = (iy + 0.5) / d;
+        int cellX = (int)(px * B), cellY = (int)(py * B);
+        int tracked[512], nt = 0, hits = 0, full = 0;
+        for (int dx = -1; dx <= 1 && !full; ++dx) {
+            int nx = cellX + dx;
+            if (nx < 0) nx += B; else if (nx >= B) nx -= B;
+            for (int dy = -1; dy <= 1 && !full; ++dy) {
+                int ny = cellY + dy;
+                if (ny < 0) ny += B; else if (ny >= B) ny -= B;
+                int box = ny * B + nx;
+                int si = m->countPerBox[box];
+                int sf = (box + 1 < boxCount) ? m->countPerBox[box + 1] : m->size;
+                for (int q = si; q < sf; ++q) {
+                    int poly = m->shapeId[m->neighborIndices[q]], seen = 0;
+                    for (int t = 0; t < nt; ++t) if (tracked[t] == poly) { seen = 1; break; }
+                    if (seen) continue;
+                    int s0 = m->startIndices[poly], s1 = m->startIndices[poly + 1];
+                    if (s1 - s0 < 3) continue;
+                    double ang = 0.0;
+                    double vxp = orc_wrap_periodic(pos[2 * s0] - px);
+                    double vyp = orc_wrap_periodic(pos[2 * s0 + 1] - py);
+                    double vx0 = vxp, vy0 = vyp;
+                    for (int e = s0 + 1; e < s1; ++e) {
+                        double vx = vxp + orc_wrap_periodic(pos[2 * e] - pos[2 * e - 2]);
+                        double vy = vyp + orc_wrap_periodic(pos[2 * e + 1] - pos[2 * e - 1]);
+                        ang += atan2(vxp * vy - vyp * vx, vxp * vx + vyp * vy);
+                        vxp = vx; vyp = vy;
+                    }
+                    ang += atan2(vxp * vy0 - vyp * vx0, vxp * vx0 + vyp * vy0);
+                    if (fabs(ang - 2.0 * PI) < eps) hits++;
+                    if (nt < 512) tracked[nt++] = poly;
+                    else { full = 1; break; }
+                }
+            }
+        }
+        total += (long long)hits * (hits - 1) / 2;
+    }
+    return (double)total / ((double)d * (double)d);
+}
+
 const int* orc_neighbor_indices(const orc_model* m) { return m->neighborIndices; }
 const int* orc_box_starts(const orc_model* m) { return m->countPerBox; }
 const int* orc_neighbors(const orc_model* m) { return m->neighbors; }

@@ -126,6 +126,9 @@ const double*   orc_ut(const orc_model* m);
 const double*   orc_target_areas(const orc_model* m);
 const double*   orc_target_edge_lengths(const orc_model* m);
 
+/* grid-point overlap estimate (updateOverlapAreaKernel + Model::updateOverlapArea) */
+double orc_update_overlap_area(orc_model* m, int pointDensity);
+
 #ifdef __cplusplus
 }
 #endif

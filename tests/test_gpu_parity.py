@@ -186,6 +186,21 @@ def test_geometry_parity_odd_shapes():
     assert np.isnan(np.asarray(o.getConstraints())).any()
 
 
+@pytest.mark.parametrize("density", [64, 211])
+def test_overlap_area_estimate_parity(system, density):
+    """The grid-point overlap estimate (updateOverlapAreaKernel,
+    kernels.cuh:879-979; Model::updateOverlapArea, model.cpp:824-847): the
+    count of polygon pairs over the grid points, divided by their number.
+    The counts are integers, so the estimates agree exactly."""
+    g, o = pair(system)
+    for m in (g, o):
+        m.updatePolygonGeometry()
+        m.updateNeighborCells()
+        m.updateOverlapArea(density)
+    assert g.getOverlapArea() == o.getOverlapArea()
+    assert o.getOverlapArea() > 0.0 or system.num_polygons < 50
+
+
 def test_neighbor_slots_bit_exact(system):
     g, o = pair(system)
     contacts(g)
