@@ -46,6 +46,64 @@ def _shoelace(xy):
     return 0.5 * (np.dot(x, np.roll(y, -1)) - np.dot(np.roll(x, -1), y))
 
 
+def random_polygon(rng, n):
+    """One random star polygon around the origin (polygonUtils.py:55-61):
+    cumulative random angles scaled to a full turn, random radii, size 1/8.
+    The same draws from `rng` in the same order as the reference."""
+    angles = np.cumsum(np.concatenate(([0.0], rng.random(n - 1))))
+    angles *= 2 * np.pi / angles[-1]
+    radii = rng.random(n)
+    return np.stack([radii * np.cos(angles), radii * np.sin(angles)], axis=1) / 8
+
+
+def random_polygons(rng, num_polygons, n):
+    """Positions [2 P n] of `num_polygons` random polygons of `n` vertices
+    (polygonUtils.py:63-91): each is rotated about its vertex mean by a
+    random angle, translated by a random offset and wrapped into the unit
+    box.  The same draws from `rng` in the same order as the reference, so a
+    generator seeded alike gives the same positions."""
+    out = np.zeros((num_polygons * n, 2))
+    for i in range(num_polygons):
+        pos = random_polygon(rng, n)
+        ang = rng.random() * 2 * np.pi
+        c = pos.mean(axis=0)
+        ca, sa = np.cos(ang), np.sin(ang)
+        rot = np.empty_like(pos)
+        for k in range(n):     # vertex by vertex, as the reference's rotate()
+            dx, dy = pos[k, 0] - c[0], pos[k, 1] - c[1]
+            rot[k] = (dx * ca - dy * sa + c[0], dx * sa + dy * ca + c[1])
+        rot[:, 0] += rng.random()
+        rot[:, 1] += rng.random()
+        rot = (rot + 2) % 1
+        out[i * n:(i + 1) * n] = rot
+    out = (out + 1) % 1
+    return out.reshape(-1)
+
+
+def unwrapped_scale(positions, start, target_areas):
+    """Each polygon rescaled about its vertex mean to its target area
+    (setAreas, pyCudaPolygon.py:103-144): unwrapped relative to its first
+    vertex, shoelace area (absolute value), scaled by sqrt(target / area) and
+    wrapped into [0, 1).  Polygons of zero area are left as they are."""
+    xy = np.asarray(positions, dtype=np.float64).reshape(-1, 2).copy()
+    for i in range(len(start) - 1):
+        s, e = int(start[i]), int(start[i + 1])
+        poly = xy[s:e].copy()
+        ref = poly[0].copy()
+        for j in range(1, e - s):
+            d = poly[j] - ref
+            d = d - np.round(d)
+            poly[j] = ref + d
+        x, y = poly[:, 0], poly[:, 1]
+        area = 0.5 * abs(np.dot(x, np.roll(y, -1)) - np.dot(np.roll(x, -1), y))
+        if area <= 0:
+            continue
+        scale = np.sqrt(target_areas[i] / area)
+        centroid = poly.mean(axis=0)
+        xy[s:e] = np.mod((poly - centroid) * scale + centroid, 1.0)
+    return xy.reshape(-1)
+
+
 def make_system(num_polygons, n, phi, seed, ratio=1.4, jitter=0.1):
     """Generate one system.  `n` is an int (uniform) or an int array [P]."""
     rng = np.random.default_rng(seed)

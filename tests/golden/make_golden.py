@@ -17,6 +17,11 @@ nothing at test time reads the reference:
                     unwrapped shoelace of setAreas (pyCudaPolygon.py:114-125)
   pybind_methods.json  the method names the reference binds on `Model`
                     (src/pybindWrapper.cpp:25-107)
+  shape_setters.json   the reference's generateRandomPolygons
+                    (polygonMixins/polygonUtils.py:61-89) from seeded
+                    generators, and its setAreas, setBiPerimeters and setPhi
+                    (pyCudaPolygon.py:103-234) run on a numpy stand-in for
+                    the compiled model (signed shoelace areas)
 
 The reference's model module imports matplotlib, tqdm and its compiled
 `libpyCudaPolygon`; small stand-ins are put on sys.path for the import only.
@@ -107,6 +112,101 @@ def _star_polygons(rng, ns, radius=0.04):
     pos = np.concatenate(pos)
     start = np.concatenate([[0], np.cumsum(ns)])
     return pos.reshape(-1), start
+
+
+def _numpy_base_methods():
+    """Methods of the compiled `Model` that the reference's shape setters
+    call through `lpcp.Model.<name>(self, ...)`, on numpy state: positions,
+    CSR starts, targets, the signed shoelace areas of updatePolygonGeometry
+    (kernels.cuh:295-333) and a record of the calls that touch the device."""
+    def shoelace_areas(self):
+        xy = self._pos.reshape(-1, 2)
+        out = []
+        for p in range(len(self._start) - 1):
+            poly = xy[self._start[p]:self._start[p + 1]]
+            d = poly - poly[0]
+            d = d - np.round(d)
+            x, y = d[:, 0], d[:, 1]
+            out.append(0.5 * (np.dot(x, np.roll(y, -1)) - np.dot(np.roll(x, -1), y)))
+        return np.array(out)
+    m = {
+        "setMaxEdgeLength": lambda self, v: self._calls.append(("setMaxEdgeLength", float(v))),
+        "initializeNeighborCells": lambda self: self._calls.append(("initializeNeighborCells",)),
+        "updateNeighborCells": lambda self: None,
+        "updateNeighbors": lambda self: None,
+        "updatePolygonGeometry": lambda self: setattr(self, "_areas", shoelace_areas(self)),
+        "getAreas": lambda self: list(self._areas),
+        "getPositions": lambda self: list(self._pos),
+        "setPositions": lambda self, p: setattr(self, "_pos", np.asarray(p, dtype=np.float64)),
+        "getStartIndices": lambda self: list(self._start),
+        "setStartIndices": lambda self, s: setattr(self, "_start", np.asarray(s, dtype=np.int64)),
+        "getNumVertices": lambda self: int(self._start[-1]),
+        "getNumPolygons": lambda self: len(self._start) - 1,
+        "setTargetAreas": lambda self, a: setattr(self, "_ta", np.asarray(a, dtype=np.float64)),
+        "getTargetAreas": lambda self: list(self._ta),
+        "setTargetEdgeLengths": lambda self, a: setattr(self, "_tl", np.asarray(a, dtype=np.float64)),
+        "getTargetEdgeLengths": lambda self: list(self._tl),
+        "resetAreas": lambda self: self._calls.append(("resetAreas",)),
+    }
+    return m
+
+
+def _shape_setter_cases(ref):
+    """The reference's generator and shape setters on a numpy stand-in."""
+    base = sys.modules["libpyCudaPolygon"].Model
+    for name, fn in _numpy_base_methods().items():
+        setattr(base, name, fn)
+
+    class Stand(ref.model):
+        def __init__(self, seed, start, positions=None):
+            self.rng = np.random.default_rng(seed)
+            self._start = np.asarray(start, dtype=np.int64)
+            self._pos = np.zeros(2 * int(self._start[-1])) if positions is None else \
+                np.asarray(positions, dtype=np.float64)
+            self._ta = np.ones(len(start) - 1)
+            self._tl = np.ones(len(start) - 1)
+            self._calls = []
+
+    out = {"source": "polygonMixins/polygonUtils.py:55-89 (generateRandomPolygons), "
+                     "pyCudaPolygon.py:103-144 (setAreas), :182-203 (setBiPerimeters), "
+                     ":223-234 (setPhi, the definition in effect)",
+           "generator": [], "set_areas": [], "bi_perimeters": [], "set_phi": []}
+    for seed, P, n in [(7, 6, 11), (123, 20, 16), (2024, 3, 5)]:
+        st = Stand(seed, np.arange(P + 1) * n)
+        ref.model.generateRandomPolygons(st, P, n)
+        out["generator"].append({"seed": seed, "num_polygons": P, "n": n,
+                                 "positions": st._pos.tolist()})
+    rng = np.random.default_rng(99)
+    for case in range(4):
+        P = int(rng.integers(2, 9))
+        ns = rng.integers(5, 30, size=P)
+        positions, start = _star_polygons(rng, ns)
+        targets = rng.uniform(5e-4, 3e-3, size=P)
+        st = Stand(0, start, positions)
+        ref.model.setAreas(st, targets)
+        out["set_areas"].append({"positions": positions.tolist(), "start": start.tolist(),
+                                 "targets": targets.tolist(), "result": st._pos.tolist()})
+        st = Stand(0, start, positions)
+        kappa = float(rng.uniform(3.6, 4.5))
+        ref.model.setBiPerimeters(st, kappa, 1.4)
+        out["bi_perimeters"].append({"positions": positions.tolist(), "start": start.tolist(),
+                                     "kappa": kappa, "ratio": 1.4,
+                                     "target_areas": st._ta.tolist(),
+                                     "target_edge_lengths": st._tl.tolist(),
+                                     "calls": [list(c) for c in st._calls]})
+        st = Stand(0, start, positions)
+        st._ta = rng.uniform(1e-3, 2e-3, size=P)
+        st._tl = rng.uniform(0.01, 0.02, size=P)
+        ta0, tl0 = st._ta.copy(), st._tl.copy()
+        phi = float(rng.uniform(0.5, 0.9))
+        ref.model.setPhi(st, phi)
+        out["set_phi"].append({"positions": positions.tolist(), "start": start.tolist(),
+                               "phi": phi, "target_areas_in": ta0.tolist(),
+                               "target_edge_lengths_in": tl0.tolist(),
+                               "target_areas": st._ta.tolist(),
+                               "target_edge_lengths": st._tl.tolist(),
+                               "calls": [list(c) for c in st._calls]})
+    return out
 
 
 def main():
@@ -203,6 +303,8 @@ def main():
     json.dump({"source": "src/pybindWrapper.cpp:12-108", "methods": names,
                "enums": enums}, open(os.path.join(HERE, "pybind_methods.json"), "w"),
               indent=1)
+    # ---- generator and shape setters ----
+    json.dump(_shape_setter_cases(ref), open(os.path.join(HERE, "shape_setters.json"), "w"))
     print("wrote fixtures to", HERE)
 
 
