@@ -78,7 +78,7 @@ def lib():
             sig[name] = (dp, [P])
         for name in ["orc_shape_id", "orc_cell_location", "orc_neighbor_indices",
                      "orc_box_starts", "orc_neighbors", "orc_num_neighbors",
-                     "orc_shape_counts"]:
+                     "orc_shape_counts", "orc_start_indices"]:
             sig[name] = (ip, [P])
         sig["orc_inside"] = (ctypes.POINTER(ctypes.c_uint8), [P])
         sig["orc_intersections"] = (ctypes.POINTER(ctypes.c_uint64), [P])
@@ -382,5 +382,4 @@ class OracleModel:
         return _copy(self._L.orc_target_edge_lengths(self._m), self._P(), np.float64)
 
     def getStartIndices(self):
-        # not stored separately in the ctypes view; callers keep their own copy
-        raise NotImplementedError
+        return _copy(self._L.orc_start_indices(self._m), self._P() + 1, np.int64)

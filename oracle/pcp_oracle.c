@@ -1483,6 +1483,7 @@ const double* orc_edge_lengths(const orc_model* m) { return m->edgeLengths; }
 const double* orc_constraints(const orc_model* m) { return m->constraints; }
 const double* orc_perimeters(const orc_model* m) { return m->perimeters; }
 const int* orc_shape_id(const orc_model* m) { return m->shapeId; }
+const int* orc_start_indices(const orc_model* m) { return m->startIndices; }
 const int* orc_cell_location(const orc_model* m) { return m->cellLocation; }
 /* ------------------------------------------------------------------------ */
 /* Grid-point overlap estimate: updateOverlapAreaKernel (kernels.cuh:879-979) */

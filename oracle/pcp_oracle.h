@@ -112,6 +112,7 @@ const double*   orc_edge_lengths(const orc_model* m);
 const double*   orc_constraints(const orc_model* m);
 const double*   orc_perimeters(const orc_model* m);
 const int*      orc_shape_id(const orc_model* m);
+const int*      orc_start_indices(const orc_model* m);   /* P+1 */
 const int*      orc_cell_location(const orc_model* m);
 const int*      orc_neighbor_indices(const orc_model* m);
 const int*      orc_box_starts(const orc_model* m);

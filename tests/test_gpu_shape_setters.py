@@ -78,3 +78,54 @@ def test_set_phi(i):
     assert np.sum(m.getTargetAreas()) == pytest.approx(case["phi"], rel=1e-14)
     # resetAreas (kernels.cuh:1440-1455) scaled every polygon to its target
     np.testing.assert_allclose(np.abs(m.getAreas()), case["target_areas"], rtol=1e-10)
+
+
+# ------------------------------------------------------------ GD minimiser
+from oracle import oracle as orc  # noqa: E402
+from pycudapolygon_gb300.systems import load_into, make_system  # noqa: E402
+
+
+class _OracleGD(orc.OracleModel):
+    """The oracle with the names the Python GD driver calls; the driver
+    functions themselves are the package's, so both sides run the same
+    sequence of model calls (pyCudaPolygon.py:573-647)."""
+
+    def __init__(self, V, model_name):
+        super().__init__(V)
+        self._name = model_name
+
+    def getModelEnum(self):
+        return self._name
+
+    def getnArray(self):
+        return np.diff(self.getStartIndices())
+
+    def getMaxEffectiveForce(self, dt, minimizerType="GD"):
+        return orc.OracleModel.getMaxEffectiveForce(self, dt, minimizerType != "GD")
+
+    minimizeGDStep = model.minimizeGDStep
+    minimizeGD = model.minimizeGD
+    getConstraintViolation = model.getConstraintViolation
+
+
+@pytest.mark.parametrize("name,enum", [("normal", 0), ("softBody", 3), ("hybrid", 5)])
+def test_gd_minimiser_parity(name, enum):
+    s = make_system(64, 16, 0.85, seed=3)
+    g = load_into(model(s.num_vertices), s)
+    o = load_into(_OracleGD(s.num_vertices, name), s)
+    g.setModelEnum(name)
+    o.setModelEnum(enum)
+    for m in (g, o):
+        if name == "normal":
+            m.shakeProject(200, 1e-15)
+        else:
+            m.setTargetAreas(s.target_areas * 1.05)
+            m.setTargetEdgeLengths(s.target_edge_lengths * 0.97)
+            m.setStiffness(1.0)
+            m.setCompressibility(1.0)
+    rg = g.minimizeGD(None, dt=1e-3, maxSteps=15, maxDisplacement=0.5)
+    ro = o.minimizeGD(None, dt=1e-3, maxSteps=15, maxDisplacement=0.5)
+    assert rg[0] == pytest.approx(ro[0], rel=1e-9, abs=1e-14)
+    assert rg[1] == ro[1]
+    d = (np.asarray(g.getPositions()) - o.getPositions() + 0.5) % 1.0 - 0.5
+    assert np.abs(d).max() < 1e-10
