@@ -283,7 +283,7 @@ k_project(const double2* __restrict__ pos, const int* __restrict__ start, int P,
         mF = warp_maxd(mF);
         if ((threadIdx.x & 31) == 0) atomic_max_nonneg(&fire->maxF, mF);
         if (proceed) {
-            { const double4 t4 = warp_sum4(sP, sV, sF, 0.0); sP = t4.x; sV = t4.y; sF = t4.z; }
+            { const Sum4 t4 = warp_sum4(sP, sV, sF, 0.0); sP = t4.x; sV = t4.y; sF = t4.z; }
             if ((threadIdx.x & 31) == 0) {
                 atomicAdd(&fire->P, sP);
                 atomicAdd(&fire->vv, sV);
@@ -1167,7 +1167,7 @@ __global__ void __launch_bounds__(256, 4) k_project_warp(const double2* __restri
         mF = warp_max_u64(mF);
         if (lane == 0 && mF) atomicMax(reinterpret_cast<unsigned long long*>(&fire->maxF), mF);
         if (proceed) {
-            { const double4 t4 = warp_sum4(sP, sV, sF, 0.0); sP = t4.x; sV = t4.y; sF = t4.z; }
+            { const Sum4 t4 = warp_sum4(sP, sV, sF, 0.0); sP = t4.x; sV = t4.y; sF = t4.z; }
             if (lane == 0) {
                 atomicAdd(&fire->P, sP);
                 atomicAdd(&fire->vv, sV);
@@ -1321,7 +1321,7 @@ __global__ void __launch_bounds__(128, 7) k_project_lanes(const double2* __restr
         const int warp = threadIdx.x >> 5, nw = blockDim.x >> 5;
         if (bad && lane == 0) atomicOr(&fire->flags, kFlagNonFinite);
         mF = warp_max_u64(mF);
-        if (proceed) { { const double4 t4 = warp_sum4(sP, sV, sF, 0.0); sP = t4.x; sV = t4.y; sF = t4.z; } }
+        if (proceed) { { const Sum4 t4 = warp_sum4(sP, sV, sF, 0.0); sP = t4.x; sV = t4.y; sF = t4.z; } }
         if (lane == 0) { s_max[warp] = mF; s_sum[0][warp] = sP; s_sum[1][warp] = sV; s_sum[2][warp] = sF; }
         __syncthreads();
         if (threadIdx.x == 0) {
@@ -1597,7 +1597,7 @@ __global__ void k_fire_velocity(double2* __restrict__ vel, const double2* __rest
     mF = warp_maxd(mF);
     if ((threadIdx.x & 31) == 0) atomic_max_nonneg(&c->maxF, mF);
     if (proceed) {
-        { const double4 t4 = warp_sum4(sP, sV, sF, 0.0); sP = t4.x; sV = t4.y; sF = t4.z; }
+        { const Sum4 t4 = warp_sum4(sP, sV, sF, 0.0); sP = t4.x; sV = t4.y; sF = t4.z; }
         if ((threadIdx.x & 31) == 0) {
             atomicAdd(&c->P, sP); atomicAdd(&c->vv, sV); atomicAdd(&c->ff, sF);
         }

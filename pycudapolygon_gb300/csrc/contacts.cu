@@ -1264,13 +1264,15 @@ k_overlap_force(const double2* __restrict__ pos, const int* __restrict__ start,
         unsigned long long inter = 0, outer = 0;
         if (valid) { inter = ws.recKey[r]; outer = ws.recOuter[r]; }
         valid = valid && inter != outer;
-        int start1 = 0, n1 = 0, iLoc = 0, lDist = 0;
+        int start1 = 0, n1 = 0, iLoc = 0, lLoc = 0, lDist = 0;
+        int4 idx4 = make_int4(0, 0, 0, 0);        // vertices i, j, k, l
         double2 sp = make_double2(0.0, 0.0);
         if (valid) {
             int s1 = (int)((inter >> 32) & 0xFFFF), s2 = (int)(inter >> 48);
             iLoc = (int)((inter >> 16) & 0xFFFF);
             int jLoc = (int)(inter & 0xFFFF);
-            int kLoc = (int)((outer >> 16) & 0xFFFF), lLoc = (int)(outer & 0xFFFF);
+            int kLoc = (int)((outer >> 16) & 0xFFFF);
+            lLoc = (int)(outer & 0xFFFF);
             start1 = start[s1];
             int start2 = start[s2];
             n1 = start[s1 + 1] - start1;
@@ -1280,14 +1282,29 @@ k_overlap_force(const double2* __restrict__ pos, const int* __restrict__ start,
                 valid = false;
                 n1 = 0;
             } else {
-                int zi = next[i], zk = next[k];
-                double2 pi = pos[i], pk = pos[k], pzi = pos[zi], pzk = pos[zk];
-                double2 r1 = make_double2(wrap(pzi.x - pi.x), wrap(pzi.y - pi.y));
-                double2 r2 = make_double2(wrap(pzk.x - pk.x), wrap(pzk.y - pk.y));
-                double t1 = (double)ws.recTU[r].y;
-                double t2 = (double)ws.recUT[r].y;
-                double2 fij = make_double2(wrap(pi.x + t1 * r1.x), wrap(pi.y + t1 * r1.y));
-                double2 fkl = make_double2(wrap(pk.x + t2 * r2.x), wrap(pk.y + t2 * r2.y));
+                idx4 = make_int4(i, j, k, l);
+            }
+        }
+        // the crossing points: the even lane of the pair takes f_ij on edge
+        // (i, zi), the odd one f_kl on edge (k, zk), and they swap them
+        double2 pa = make_double2(0.0, 0.0), pza = pa, ra = pa, fa = pa;
+        int za = 0;
+        if (valid) {
+            const int a = half ? idx4.z : idx4.x;
+            za = next[a];
+            pa = pos[a];
+            pza = pos[za];
+            ra = make_double2(wrap(pza.x - pa.x), wrap(pza.y - pa.y));
+            const double ta = half ? (double)ws.recUT[r].y : (double)ws.recTU[r].y;
+            fa = make_double2(wrap(pa.x + ta * ra.x), wrap(pa.y + ta * ra.y));
+        }
+        const double2 fo = make_double2(__shfl_xor_sync(PCP_FULL, fa.x, 1),
+                                        __shfl_xor_sync(PCP_FULL, fa.y, 1));
+        if (valid) {
+            {
+                const int i = idx4.x, j = idx4.y, k = idx4.z, l = idx4.w;
+                // even lane: a = i (za = zi); odd lane: a = k (za = zk)
+                const double2 fij = half ? fo : fa, fkl = half ? fa : fo;
                 sp = fij;
                 // Both lanes of the pair run one h/g12 and one gDf on operands
                 // chosen by parity (no divergent branches):
@@ -1297,13 +1314,13 @@ k_overlap_force(const double2* __restrict__ pos, const int* __restrict__ start,
                 //            odd: h(l, fkl), gDf(k, zk, l, zl) . g2, l += g1
                 const bool same = (i == l);
                 int v0, v1, v2, v3;
-                if (half == 0) { v0 = i; v1 = zi; v2 = j; v3 = next[j]; }
-                else if (same) { v0 = k; v1 = zk; v2 = i; v3 = zi; }
-                else { v0 = k; v1 = zk; v2 = l; v3 = next[l]; }
-                double2 q0 = half ? pk : pi, q1 = half ? pzk : pzi;
+                if (half == 0) { v0 = i; v1 = za; v2 = j; v3 = next[j]; }
+                else if (same) { v0 = k; v1 = za; v2 = i; v3 = next[i]; }
+                else { v0 = k; v1 = za; v2 = l; v3 = next[l]; }
+                const double2 q0 = pa;                 // p_i (even) or p_k (odd)
                 double2 q2 = pos[v2], q3 = pos[v3];
                 double2 hA = (!same && half) ? q2 : fij;
-                double2 hB = (same || half) ? fkl : pzi;
+                double2 hB = (same || half) ? fkl : pza;
                 double2 gA, gB;
                 double eh = h_g12(hA, hB, sp, gA, gB);
                 if (!same || half == 0) eLocal += eh;
@@ -1311,7 +1328,7 @@ k_overlap_force(const double2* __restrict__ pos, const int* __restrict__ start,
                 double2 x1 = (!same && !half) ? gB : make_double2(0.0, 0.0);
                 double2 x2 = (!same && half) ? gA : make_double2(0.0, 0.0);
                 double2 o[4];
-                gDf(q0, q1, q2, q3, g, o);
+                gDf_di(q0, ra, q2, q3, g, o);     // q1 - q0 is this lane's own edge
                 add_f(force, v0, -o[0].x, -o[0].y);
                 add_f(force, v1, -(o[1].x + x1.x), -(o[1].y + x1.y));
                 add_f(force, v2, -(o[2].x + x2.x), -(o[2].y + x2.y));

@@ -111,8 +111,8 @@ __device__ __forceinline__ void geometry_lanes(const double2* __restrict__ pos, 
         n1 = e20 * e20 + e21 * e21;
         n2 = u0 * u0 + u1 * u1;
     }
-    const double4 s4 = warp_sum4(sA, sX, sY, sPer);
-    const double4 t4 = warp_sum4(n0, n1, n2, 0.0);
+    const Sum4 s4 = warp_sum4(sA, sX, sY, sPer);
+    const Sum4 t4 = warp_sum4(n0, n1, n2, 0.0);
     unsigned long long em = live ? (unsigned long long)__double_as_longlong(el) : 0ull;
     for (int o = 16; o > 0; o >>= 1) {
         unsigned long long t = __shfl_xor_sync(PCP_FULL, em, o);
@@ -197,7 +197,7 @@ k_geometry(const double2* __restrict__ pos, const int* __restrict__ start, int P
         emax = fmax(emax, el);
     }
     {
-        const double4 s4 = warp_sum4(sA, sX, sY, sPer), t4 = warp_sum4(n0, n1, n2, 0.0);
+        const Sum4 s4 = warp_sum4(sA, sX, sY, sPer), t4 = warp_sum4(n0, n1, n2, 0.0);
         sA = s4.x; sX = s4.y; sY = s4.z; sPer = s4.w; n0 = t4.x; n1 = t4.y; n2 = t4.z;
     }
     emax = warp_maxd(emax);

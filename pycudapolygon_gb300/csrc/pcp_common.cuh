@@ -213,10 +213,11 @@ __device__ __forceinline__ double h_g12(double2 p1, double2 p2, double2 sp, doub
 // vzj).  Only its contractions with a row vector g are needed; this returns
 // the four 2-vectors gT df restricted to each vertex:  out[p] = (g . df[:,2p],
 // g . df[:,2p+1]).  Zero for near-parallel or degenerate edges.
-__device__ __forceinline__ void gDf(double2 vi, double2 vzi, double2 vj, double2 vzj,
-                                    double2 g, double2 out[4]) {
+// di = wrap(vzi - vi), when the caller has it already.
+__device__ __forceinline__ void gDf_di(double2 vi, double2 di, double2 vj, double2 vzj,
+                                       double2 g, double2 out[4]) {
     double djx = wrap(vzj.x - vj.x), djy = wrap(vzj.y - vj.y);
-    double dix = wrap(vzi.x - vi.x), diy = wrap(vzi.y - vi.y);
+    double dix = di.x, diy = di.y;
     double dijx = wrap(vj.x - vi.x), dijy = wrap(vj.y - vi.y);
     double w = djx * diy - djy * dix;
     double diN = dix * dix + diy * diy;
@@ -242,6 +243,10 @@ __device__ __forceinline__ void gDf(double2 vi, double2 vzi, double2 vj, double2
     out[1] = make_double2(gd * du1x + g.x * u, gd * du1y + g.y * u);
     out[2] = make_double2(gd * du2x, gd * du2y);
     out[3] = make_double2(gd * du3x, gd * du3y);
+}
+__device__ __forceinline__ void gDf(double2 vi, double2 vzi, double2 vj, double2 vzj,
+                                    double2 g, double2 out[4]) {
+    gDf_di(vi, make_double2(wrap(vzi.x - vi.x), wrap(vzi.y - vi.y)), vj, vzj, g, out);
 }
 
 // ------------------------------------------- conversions on the INT pipe ----
@@ -328,7 +333,8 @@ __device__ __forceinline__ double2 warp_sum2(double a, double b) {
 // Four warp sums for 6 FP64 adds instead of 20: the warp splits into halves
 // (a, b | c, d) and then quarters (a | b | c | d) before reducing; the totals
 // are broadcast from lanes 0, 8, 16 and 24.
-__device__ __forceinline__ double4 warp_sum4(double a, double b, double c, double d) {
+struct Sum4 { double x, y, z, w; };
+__device__ __forceinline__ Sum4 warp_sum4(double a, double b, double c, double d) {
     const int lane = threadIdx.x & 31;
     const bool h16 = (lane & 16) != 0, h8 = (lane & 8) != 0;
     double k0 = h16 ? c : a, k1 = h16 ? d : b;
@@ -338,8 +344,8 @@ __device__ __forceinline__ double4 warp_sum4(double a, double b, double c, doubl
     keep += __shfl_xor_sync(PCP_FULL, h8 ? k0 : k1, 8);
 #pragma unroll
     for (int o = 4; o > 0; o >>= 1) keep += __shfl_xor_sync(PCP_FULL, keep, o);
-    return make_double4(__shfl_sync(PCP_FULL, keep, 0), __shfl_sync(PCP_FULL, keep, 8),
-                        __shfl_sync(PCP_FULL, keep, 16), __shfl_sync(PCP_FULL, keep, 24));
+    return Sum4{__shfl_sync(PCP_FULL, keep, 0), __shfl_sync(PCP_FULL, keep, 8),
+                __shfl_sync(PCP_FULL, keep, 16), __shfl_sync(PCP_FULL, keep, 24)};
 }
 
 __device__ __forceinline__ float warp_maxf(float v) {
