@@ -753,6 +753,40 @@ __device__ int narrow_pair(const PairCtx& pc, const float4* ringA, const float4*
 // t >= u), take the smallest cyclic edge distance d = (l - i) mod n_si, then
 // the smallest u, then the smallest key (first in the reference's sorted
 // scan).  Writes the pair's records to global memory.
+// The partner (exit) of crossing `key` among a pair's R records: in the
+// reverse group (sj' = si, si' = sj), skipping records on the same edge that
+// are not ahead (l == i and t >= u), the smallest cyclic edge distance
+// d = (l - i) mod n_si, then the smallest u, then the smallest key
+// (updateOutersectionsKernel, kernels.cuh:981-1065).  -1 when there is
+// none; groupSeen tells whether the reverse group has any record at all.
+__device__ __forceinline__ int find_partner(const PairCtx& pc, int R,
+                                            const unsigned long long* recKey,
+                                            const float2* recTU, unsigned long long key,
+                                            float2 tu, bool& groupSeen) {
+    const int sj = (int)(key >> 48), si = (int)((key >> 32) & 0xFFFF);
+    const int i = (int)((key >> 16) & 0xFFFF);
+    const int ni = (si == pc.a) ? pc.nA : pc.nB;
+    const float tVal = tu.y;
+    const unsigned long long grp = ((unsigned long long)si << 16) | (unsigned long long)sj;
+    groupSeen = false;
+    int best = -1, bestD = 0;
+    float bestU = 0.f;
+    unsigned long long bestK = 0;
+    for (int c = 0; c < R; ++c) {
+        const unsigned long long kc = recKey[c];
+        if ((kc >> 32) != grp) continue;
+        groupSeen = true;
+        const int l = (int)(kc & 0xFFFF);
+        const float uVal = recTU[c].x;
+        if (l == i && tVal >= uVal) continue;
+        const int d = (l - i + ni) % ni;
+        const bool better = best < 0 || d < bestD || (d == bestD && (uVal < bestU ||
+                            (uVal == bestU && kc < bestK)));
+        if (better) { best = c; bestD = d; bestU = uVal; bestK = kc; }
+    }
+    return best;
+}
+
 __device__ unsigned long long match_and_write(const PairCtx& pc, int R,
                                               const unsigned long long* recKey,
                                               const float2* recTU, Ctrl* ctrl, ContactWS& ws,
@@ -772,27 +806,8 @@ __device__ unsigned long long match_and_write(const PairCtx& pc, int R,
         if (r < R) {
             key = recKey[r];
             tu = recTU[r];
-            int sj = (int)(key >> 48), si = (int)((key >> 32) & 0xFFFF);
-            int i = (int)((key >> 16) & 0xFFFF);
-            int ni = (si == pc.a) ? pc.nA : pc.nB;
-            float tVal = tu.y;
-            unsigned long long grp = ((unsigned long long)si << 16) | (unsigned long long)sj;
             bool groupSeen = false;
-            int best = -1, bestD = 0;
-            float bestU = 0.f;
-            unsigned long long bestK = 0;
-            for (int c = 0; c < R; ++c) {
-                unsigned long long kc = recKey[c];
-                if ((kc >> 32) != grp) continue;
-                groupSeen = true;
-                int l = (int)(kc & 0xFFFF);
-                float uVal = recTU[c].x;
-                if (l == i && tVal >= uVal) continue;
-                int d = (l - i + ni) % ni;
-                bool better = best < 0 || d < bestD || (d == bestD && (uVal < bestU ||
-                              (uVal == bestU && kc < bestK)));
-                if (better) { best = c; bestD = d; bestU = uVal; bestK = kc; }
-            }
+            const int best = find_partner(pc, R, recKey, recTU, key, tu, groupSeen);
             if (best >= 0) {
                 outer = recKey[best];
                 ut = recTU[best];
