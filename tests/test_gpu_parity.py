@@ -63,6 +63,9 @@ SYSTEMS = {
     "mid_256x24": dict(num_polygons=256, n=24, phi=0.87, seed=7),
     "tri_quads": dict(num_polygons=40, n=4, phi=0.9, seed=3),
     "varn_200": dict(num_polygons=200, n=np.random.default_rng(5).integers(12, 49, 200), phi=0.86, seed=11),
+    # ragged polygons of at most 32 vertices: the one-vertex-per-lane kernels
+    # with idle lanes and a different n in every warp
+    "varn_small": dict(num_polygons=150, n=np.random.default_rng(8).integers(5, 33, 150), phi=0.86, seed=12),
 }
 
 
