@@ -73,6 +73,10 @@ k_prepass(double2* __restrict__ pos, const int* __restrict__ start,
     float Rsafe = 0.f;
     const int st = p < P ? start[p] : 0;
     const int n = p < P ? start[p + 1] - st : 0;
+    // polygons of up to 32 vertices: one vertex per lane, the next vertex by
+    // shuffle instead of a second read of the positions just written
+    const bool lanes = n >= 1 && n <= 32;
+    double2 xl = make_double2(0.0, 0.0);
     if (mv.pos) {
         // start of a FIRE step: resets (Rmax was zeroed at the end of the
         // last step and is accumulated below), then this polygon's Verlet move
@@ -83,10 +87,81 @@ k_prepass(double2* __restrict__ pos, const int* __restrict__ start,
         const double dt = mv.c->dt;
         const int bm = mv.c->bendMode;
         const double ba = mv.c->bendA, bs = mv.c->bendS;
-        for (int kl = lane; kl < n; kl += 32) pos[st + kl] = fire_move_vertex(mv, st + kl, dt, bm, ba, bs);
-        __syncwarp();
+        if (lanes) {
+            if (lane < n) {
+                xl = fire_move_vertex(mv, st + lane, dt, bm, ba, bs);
+                pos[st + lane] = xl;
+            }
+        } else {
+            for (int kl = lane; kl < n; kl += 32)
+                pos[st + kl] = fire_move_vertex(mv, st + kl, dt, bm, ba, bs);
+            __syncwarp();
+        }
+    } else if (lanes && lane < n) {
+        xl = pos[st + lane];
     }
-    if (p < P && n <= 0) {   // empty polygon: no edges, never a candidate
+    if (p < P && lanes) {
+        // the same values as the general form below, from registers
+        const bool live = lane < n;
+        const int kn = (lane + 1 >= n) ? 0 : lane + 1;
+        const double2 xn = make_double2(__shfl_sync(PCP_FULL, xl.x, kn),
+                                        __shfl_sync(PCP_FULL, xl.y, kn));
+        const float fx = d2f_int(xl.x), fy = d2f_int(xl.y);
+        const float fnx = __shfl_sync(PCP_FULL, fx, kn), fny = __shfl_sync(PCP_FULL, fy, kn);
+        const float f0x = __shfl_sync(PCP_FULL, fx, 0), f0y = __shfl_sync(PCP_FULL, fy, 0);
+        float mnx = 0.f, mxx = 0.f, mny = 0.f, mxy = 0.f, emax = 0.f;
+        bool bad = false;
+        if (live) {
+            const int k = st + lane;
+            edgeVec[k] = make_double2(wrap(xn.x - xl.x), wrap(xn.y - xl.y));
+            int cell;
+            if (cellOut) {
+                cell = midpoint_cell_fast(xl, xn, make_float2(fx, fy), make_float2(fnx, fny), B);
+                cellOut[k] = cell;
+            } else {
+                cell = cellLocation[k];
+            }
+            vtx[k] = make_float4(fx, fy, __int_as_float(cell % B), __int_as_float(cell / B));
+            float lx = wrapf(fx - f0x), ly = wrapf(fy - f0y);
+            float nxl = wrapf(fnx - fx), nyl = wrapf(fny - fy);
+            if (!(isfinite(lx) && isfinite(ly) && isfinite(nxl) && isfinite(nyl))) bad = true;
+            mnx = fminf(mnx, lx); mxx = fmaxf(mxx, lx);
+            mny = fminf(mny, ly); mxy = fmaxf(mxy, ly);
+            emax = fmaxf(emax, sqrtf(nxl * nxl + nyl * nyl));
+        }
+        mnx = warp_minf(mnx); mxx = warp_maxf(mxx);
+        mny = warp_minf(mny); mxy = warp_maxf(mxy);
+        emax = warp_maxf(emax);
+        bad = __any_sync(PCP_FULL, bad);
+        const float cxl = 0.5f * (mnx + mxx), cyl = 0.5f * (mny + mxy);
+        const float L = fmaxf(fmaxf(mxx - mnx, mxy - mny), 0.f);
+        float minCross = 3.0e38f, sweep = 0.f;
+        bool crossNaN = false;
+        if (live) {
+            float ax = wrapf(fx - f0x) - cxl, ay = wrapf(fy - f0y) - cyl;
+            float bx = wrapf(fnx - f0x) - cxl, by = wrapf(fny - f0y) - cyl;
+            float c = ax * by - ay * bx;
+            crossNaN |= isnan(c);
+            minCross = fminf(minCross, c);
+            sweep += atan2f(c, ax * bx + ay * by);
+        }
+        minCross = warp_minf(minCross);
+        crossNaN = __any_sync(PCP_FULL, crossNaN);
+        for (int o = 16; o > 0; o >>= 1) sweep += __shfl_xor_sync(PCP_FULL, sweep, o);
+        const bool star = !crossNaN && L >= 1e-4f && minCross > kStarEpsPerL * L &&
+                          fabsf(sweep - 6.2831853f) < 1.0f;
+        if (lane == 0) {
+            float cx = f0x + 0.5f * (mnx + mxx), cy = f0y + 0.5f * (mny + mxy);
+            cx -= floorf(cx); cy -= floorf(cy);
+            float w = mxx - mnx, h = mxy - mny;
+            float R = 0.5f * sqrtf(w * w + h * h) * 1.0001f + 4e-6f;
+            bool safe = !bad && isfinite(R) && R < 0.1f && n >= 3;
+            polyInfo[p] = make_float4(cx, cy, R, emax);
+            polyBox[p] = make_float4(mnx, mxx, mny, mxy);
+            polyFlags[p] = safe ? ((star && n >= 4) ? 3 : 1) : 0;
+            if (safe) Rsafe = R;
+        }
+    } else if (p < P && n <= 0) {   // empty polygon: no edges, never a candidate
         if (lane == 0) {
             polyInfo[p] = make_float4(0.f, 0.f, 0.f, 0.f);
             polyBox[p] = make_float4(0.f, 0.f, 0.f, 0.f);
