@@ -489,6 +489,31 @@ k_candidates(const float4* __restrict__ polyInfo, const float4* __restrict__ pol
         if (lane >= d) incl += t;
     }
     const int total = __shfl_sync(PCP_FULL, incl, 8);
+    // the tests of one candidate per lane, done once when the nine cells hold
+    // at most 32 polygons (both passes use them)
+    auto test_item = [&](int item, bool& circle, bool& box, int& j) {
+        // owning cell: the first of lanes 0..8 whose running total exceeds item
+        int own = 0;
+#pragma unroll
+        for (int t = 0; t < 9; ++t) own += (__shfl_sync(PCP_FULL, incl, t) <= item) ? 1 : 0;
+        int oa = __shfl_sync(PCP_FULL, ca, own < 9 ? own : 8);
+        int oi = __shfl_sync(PCP_FULL, incl - len, own < 9 ? own : 8);
+        circle = false; box = false; j = 0;
+        if (item < total) {
+            j = sortedPoly[oa + item - oi];
+            if (j > i) {
+                float4 cj = polyInfo[j];
+                float ddx = wrapf(cj.x - ci.x), ddy = wrapf(cj.y - ci.y);
+                float rr = ci.z + cj.z + 1e-5f;
+                circle = ddx * ddx + ddy * ddy <= rr * rr;
+                box = circle && box_pair(ci, bi, cj, polyBox[j]);
+            }
+        }
+    };
+    const bool once = safe && total <= 32;
+    bool circle1 = false, box1 = false;
+    int j1 = 0;
+    if (once) test_item(lane, circle1, box1, j1);
     // pass 0 counts, pass 1 writes from the reserved base
     int base = 0;
     for (int pass = 0; pass < 2; ++pass) {
@@ -517,27 +542,14 @@ k_candidates(const float4* __restrict__ polyInfo, const float4* __restrict__ pol
                     put(ok, j < i ? j : i, j < i ? i : j);
                     evals += ok ? 1 : 0;
                 }
+            } else if (once) {
+                put(box1, i, j1);
+                evals += circle1 ? 1 : 0;
             } else {
                 for (int b0 = 0; b0 < total; b0 += 32) {
-                    const int item = b0 + lane;
-                    // owning cell: the first of lanes 0..8 whose running total exceeds item
-                    int own = 0;
-#pragma unroll
-                    for (int t = 0; t < 9; ++t) own += (__shfl_sync(PCP_FULL, incl, t) <= item) ? 1 : 0;
-                    int oa = __shfl_sync(PCP_FULL, ca, own < 9 ? own : 8);
-                    int oi = __shfl_sync(PCP_FULL, incl - len, own < 9 ? own : 8);
-                    bool circle = false, box = false;
-                    int j = 0;
-                    if (item < total) {
-                        j = sortedPoly[oa + item - oi];
-                        if (j > i) {
-                            float4 cj = polyInfo[j];
-                            float ddx = wrapf(cj.x - ci.x), ddy = wrapf(cj.y - ci.y);
-                            float rr = ci.z + cj.z + 1e-5f;
-                            circle = ddx * ddx + ddy * ddy <= rr * rr;
-                            box = circle && box_pair(ci, bi, cj, polyBox[j]);
-                        }
-                    }
+                    bool circle, box;
+                    int j;
+                    test_item(b0 + lane, circle, box, j);
                     put(box, i, j);
                     evals += circle ? 1 : 0;
                 }
