@@ -355,7 +355,8 @@ __global__ void k_grid_scatter(const float4* __restrict__ polyInfo, const int* _
 // k_grid_scatter).
 constexpr int kFusedCells = 8192;
 constexpr int kFusedMaxPolys = 65536;
-__global__ void __launch_bounds__(1024)
+constexpr int kFusedRegItems = 8;
+__global__ void __launch_bounds__(1024, 1)
 k_grid_fused(const float4* __restrict__ polyInfo, const int* __restrict__ flags, int P,
              int* __restrict__ gridCount, int* __restrict__ gridStart,
              int* __restrict__ sortedPoly, Ctrl* __restrict__ ctrl, const int* gate) {
@@ -370,11 +371,33 @@ k_grid_fused(const float4* __restrict__ polyInfo, const int* __restrict__ flags,
     int* cnt = inSmem ? s_cnt : gridCount;
     if (inSmem)
         for (int i = threadIdx.x; i < N; i += blockDim.x) s_cnt[i] = 0;
+    // up to kFusedRegItems polygons per thread: every load issued before the
+    // first atomic, and the cells kept in registers for the scatter
+    const bool inReg = P <= kFusedRegItems * (int)blockDim.x;
+    int cell[kFusedRegItems];
+    if (inReg) {
+#pragma unroll
+        for (int k = 0; k < kFusedRegItems; ++k) {
+            const int p = threadIdx.x + k * blockDim.x;
+            cell[k] = -1;
+            if (p < P) {
+                const int f = flags[p];
+                const float2 c = *reinterpret_cast<const float2*>(&polyInfo[p]);
+                if (f) cell[k] = grid_cell(c.y, G) * G + grid_cell(c.x, G);
+            }
+        }
+    }
     __syncthreads();
-    for (int p = threadIdx.x; p < P; p += blockDim.x) {
-        if (!flags[p]) continue;
-        float4 c = polyInfo[p];
-        atomicAdd(&cnt[grid_cell(c.y, G) * G + grid_cell(c.x, G)], 1);
+    if (inReg) {
+#pragma unroll
+        for (int k = 0; k < kFusedRegItems; ++k)
+            if (cell[k] >= 0) atomicAdd(&cnt[cell[k]], 1);
+    } else {
+        for (int p = threadIdx.x; p < P; p += blockDim.x) {
+            if (!flags[p]) continue;
+            float4 c = polyInfo[p];
+            atomicAdd(&cnt[grid_cell(c.y, G) * G + grid_cell(c.x, G)], 1);
+        }
     }
     __syncthreads();
     // exclusive scan: contiguous runs per thread, then across warps
@@ -415,10 +438,16 @@ k_grid_fused(const float4* __restrict__ polyInfo, const int* __restrict__ flags,
     }
     if (threadIdx.x == blockDim.x - 1) gridStart[N] = run;
     __syncthreads();
-    for (int p = threadIdx.x; p < P; p += blockDim.x) {
-        if (!flags[p]) continue;
-        float4 c = polyInfo[p];
-        sortedPoly[atomicAdd(&cnt[grid_cell(c.y, G) * G + grid_cell(c.x, G)], 1)] = p;
+    if (inReg) {
+#pragma unroll
+        for (int k = 0; k < kFusedRegItems; ++k)
+            if (cell[k] >= 0) sortedPoly[atomicAdd(&cnt[cell[k]], 1)] = threadIdx.x + k * blockDim.x;
+    } else {
+        for (int p = threadIdx.x; p < P; p += blockDim.x) {
+            if (!flags[p]) continue;
+            float4 c = polyInfo[p];
+            sortedPoly[atomicAdd(&cnt[grid_cell(c.y, G) * G + grid_cell(c.x, G)], 1)] = p;
+        }
     }
     if (!inSmem) {
         __syncthreads();
@@ -1397,7 +1426,7 @@ k_overlap_force(const double2* __restrict__ pos, const int* __restrict__ start,
             pa = pos[a];
             pza = pos[za];
             ra = make_double2(wrap(pza.x - pa.x), wrap(pza.y - pa.y));
-            const double ta = half ? (double)ws.recUT[r].y : (double)ws.recTU[r].y;
+            const double ta = f2d_int(half ? ws.recUT[r].y : ws.recTU[r].y);
             fa = make_double2(wrap(pa.x + ta * ra.x), wrap(pa.y + ta * ra.y));
         }
         const double2 fo = make_double2(__shfl_xor_sync(PCP_FULL, fa.x, 1),
@@ -1423,18 +1452,22 @@ k_overlap_force(const double2* __restrict__ pos, const int* __restrict__ start,
                 double2 q2 = pos[v2], q3 = pos[v3];
                 double2 hA = (!same && half) ? q2 : fij;
                 double2 hB = (same || half) ? fkl : pza;
-                double2 gA, gB;
-                double eh = h_g12(hA, hB, sp, gA, gB);
+                double dyg, sx;
+                double eh = h_parts(hA, hB, sp, dyg, sx);
                 if (!same || half == 0) eLocal += eh;
-                double2 g = half ? gB : gA;
-                double2 x1 = (!same && !half) ? gB : make_double2(0.0, 0.0);
-                double2 x2 = (!same && half) ? gA : make_double2(0.0, 0.0);
+                // gDf is linear in g: with -g it gives the force terms
+                // directly (g1 = (dyg, -sx) on the even lane, g2 = (dyg, sx)
+                // on the odd one; x1 = g2 moves zi, x2 = g1 moves l)
+                const double ndy = neg_int(dyg), nsx = neg_int(sx);
+                const double2 ng = make_double2(ndy, half ? nsx : sx);
+                const double2 nx1 = (!same && !half) ? make_double2(ndy, nsx) : make_double2(0.0, 0.0);
+                const double2 nx2 = (!same && half) ? make_double2(ndy, sx) : make_double2(0.0, 0.0);
                 double2 o[4];
-                gDf_di(q0, ra, q2, q3, g, o);     // q1 - q0 is this lane's own edge
-                add_f(force, v0, -o[0].x, -o[0].y);
-                add_f(force, v1, -(o[1].x + x1.x), -(o[1].y + x1.y));
-                add_f(force, v2, -(o[2].x + x2.x), -(o[2].y + x2.y));
-                add_f(force, v3, -o[3].x, -o[3].y);
+                gDf_di(q0, ra, q2, q3, ng, o);    // q1 - q0 is this lane's own edge
+                add_f(force, v0, o[0].x, o[0].y);
+                add_f(force, v1, o[1].x + nx1.x, o[1].y + nx1.y);
+                add_f(force, v2, o[2].x + nx2.x, o[2].y + nx2.y);
+                add_f(force, v3, o[3].x, o[3].y);
                 if (n1 > 0) lDist = ((lLoc - iLoc) % n1 + n1) % n1;
             }
         }
@@ -1469,10 +1502,11 @@ k_overlap_force(const double2* __restrict__ pos, const int* __restrict__ start,
                 if (mLoc >= oN) mLoc -= oN;
                 int mv = oStart + mLoc;
                 int nv = next[mv];
-                double2 g1, g2;
-                eLocal += h_g12(pos[mv], pos[nv], osp, g1, g2);
-                add_f(force, mv, -g1.x, -g1.y);
-                add_f(force, nv, -g2.x, -g2.y);
+                double dyg, sx;
+                eLocal += h_parts(pos[mv], pos[nv], osp, dyg, sx);
+                const double ndy = neg_int(dyg);
+                add_f(force, mv, ndy, sx);             // -g1
+                add_f(force, nv, ndy, neg_int(sx));    // -g2
             }
         }
     }

@@ -415,10 +415,9 @@ int copy_dev_out(pcp_model* m, const T* dsrc, int n, T* out, int cap, int* len_o
     if (len_out) *len_out = n;
     if (!out) return PCP_OK;
     if (cap < n) return fail(PCP_ERR_ARG, "output buffer holds %d elements, %d needed", cap, n);
-    int rc = sync(m);
-    if (rc) return rc;
-    if (n > 0) CK(cudaMemcpy(out, dsrc, (size_t)n * sizeof(T), cudaMemcpyDeviceToHost));
-    return PCP_OK;
+    // ordered after the model's stream work; one wait for both
+    if (n > 0) CK(cudaMemcpyAsync(out, dsrc, (size_t)n * sizeof(T), cudaMemcpyDeviceToHost, m->stream));
+    return sync(m);
 }
 
 int upload(pcp_model* m, void* dst, const void* src, size_t bytes) {

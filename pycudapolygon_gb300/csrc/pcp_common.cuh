@@ -196,16 +196,21 @@ __device__ __forceinline__ void g12(double2 p1, double2 p2, double2 sp, double2&
     g2 = make_double2(dy, r1x + r2x);
 }
 
-// h and g12 together (they share r1x, r2x).
-__device__ __forceinline__ double h_g12(double2 p1, double2 p2, double2 sp, double2& g1, double2& g2) {
+// h and g12 together (they share r1x, r2x), the gradients in the parts
+// they are made of: g1 = (dyg, -sx), g2 = (dyg, sx).
+__device__ __forceinline__ double h_parts(double2 p1, double2 p2, double2 sp, double& dyg,
+                                          double& sx) {
     double r1x = wrap(p1.x - sp.x), r1y = wrap(p1.y - sp.y);
     double r2x = wrap(p2.x - sp.x), r2y = wrap(p2.y - sp.y);
     double dyh = wrap(r2y - r1y);
-    double dyg = wrap(p2.y - p1.y);
-    double sx = r1x + r2x;
-    g1 = make_double2(dyg, -sx);
-    g2 = make_double2(dyg, sx);
+    dyg = wrap(p2.y - p1.y);
+    sx = r1x + r2x;
     return sx * dyh;
+}
+
+// -x by a flip of the sign bit on the integer pipe
+__device__ __forceinline__ double neg_int(double x) {
+    return __hiloint2double(__double2hiint(x) ^ (int)0x80000000, __double2loint(x));
 }
 
 // getDf (kernels.cuh:161-222): Jacobian of f = vi + u (vzi - vi), the point
@@ -222,27 +227,35 @@ __device__ __forceinline__ void gDf_di(double2 vi, double2 di, double2 vj, doubl
     double w = djx * diy - djy * dix;
     double diN = dix * dix + diy * diy;
     double djN = djx * djx + djy * djy;
-    if (w * w < 1e-12 * diN * djN || diN < 1e-28 || djN < 1e-28) {
+    // The degeneracy tests on the integer pipe: w^2, the limit and the
+    // squared lengths are non-negative doubles (or NaN, for which every test
+    // is false), and for those the unsigned order of the bit patterns is the
+    // order of the values.  0x3A1FB0F6BE506019 is the pattern of 1e-28.
+    const unsigned long long wwB = (unsigned long long)__double_as_longlong(w * w);
+    const unsigned long long limB = (unsigned long long)__double_as_longlong(1e-12 * diN * djN);
+    const unsigned long long tinyB = 0x3A1FB0F6BE506019ull;
+    if ((wwB < limB && limB <= 0x7FF0000000000000ull) ||
+        (unsigned long long)__double_as_longlong(diN) < tinyB ||
+        (unsigned long long)__double_as_longlong(djN) < tinyB) {
         out[0] = out[1] = out[2] = out[3] = make_double2(0.0, 0.0);
         return;
     }
     double k = djx * dijy - djy * dijx;
     double iw = 1.0 / w;
     double u = k * iw;
-    // du/d(vertex p, component b) = (dk[p][b] - u dw[p][b]) / w
-    double gd = g.x * dix + g.y * diy;       // g . di
-    // vi: dk=(djy,-djx), dw=(djy,-djx)
-    double du0x = (djy - u * djy) * iw, du0y = (-djx + u * djx) * iw;
-    // vzi: dk=0, dw=(-djy, djx)
-    double du1x = (u * djy) * iw, du1y = (-u * djx) * iw;
-    // vj: dk=(-dijy-djy, djx+dijx), dw=(-diy, dix)
-    double du2x = ((-dijy - djy) + u * diy) * iw, du2y = ((djx + dijx) - u * dix) * iw;
-    // vzj: dk=(dijy,-dijx), dw=(diy,-dix)
-    double du3x = (dijy - u * diy) * iw, du3y = (-dijx + u * dix) * iw;
-    out[0] = make_double2(gd * du0x + g.x * (1.0 - u), gd * du0y + g.y * (1.0 - u));
-    out[1] = make_double2(gd * du1x + g.x * u, gd * du1y + g.y * u);
-    out[2] = make_double2(gd * du2x, gd * du2y);
-    out[3] = make_double2(gd * du3x, gd * du3y);
+    // g . du/d(vertex, component) = s (dk - u dw) with s = (g . di) / w, and
+    // f = vi + u di passes g (1 - u) to vi and g u to vzi:
+    //   vi : (1 - u) (s djy + gx, gy - s djx)
+    //   vzi: u (s djy + gx, gy - s djx)
+    //   vj : s ((-dijy - djy) + u diy, (djx + dijx) - u dix)
+    //   vzj: s (dijy - u diy, u dix - dijx)
+    const double s = (g.x * dix + g.y * diy) * iw;
+    const double ax = fma(s, djy, g.x), ay = fma(-s, djx, g.y);
+    const double omu = 1.0 - u;
+    out[0] = make_double2(omu * ax, omu * ay);
+    out[1] = make_double2(u * ax, u * ay);
+    out[2] = make_double2(s * fma(u, diy, -dijy - djy), s * fma(-u, dix, djx + dijx));
+    out[3] = make_double2(s * fma(-u, diy, dijy), s * fma(u, dix, -dijx));
 }
 __device__ __forceinline__ void gDf(double2 vi, double2 vzi, double2 vj, double2 vzj,
                                     double2 g, double2 out[4]) {
