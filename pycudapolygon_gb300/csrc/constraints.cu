@@ -145,6 +145,38 @@ __device__ __forceinline__ void fire_pass_end(Ctrl* __restrict__ c, bool rollbac
     }
 }
 
+// The rollback test at the end of the step's force pass (model.cpp:450-453):
+// the velocities advance unless SHAKE failed or the energy went up, and the
+// energy-increase rollback runs next when the energy went up and SHAKE did
+// not fail.  Thread 0 of each block evaluates it (an FP64 compare costs a
+// warp instruction, so once per block rather than once per warp) and block
+// 0 publishes it.  Every thread of the block calls this.
+struct FireView {
+    bool proceed, rbNext;
+    double dt;
+};
+__device__ __forceinline__ FireView fire_view(Ctrl* __restrict__ c,
+                                              cudaGraphConditionalHandle rbCond, int useCond) {
+    __shared__ int s_bits;
+    __shared__ double s_dt;
+    if (threadIdx.x == 0) {
+        const double E = c->energy, E0 = c->ePre;
+        const bool rb = E > E0 + fmax(fabs(E0) * 1e-10, 1e-14);
+        const bool proceed = !c->shakeFailed && !rb && c->rollback == 0;
+        const bool rbNext = c->rollback == 0 && !c->shakeFailed && rb && c->active;
+        if (blockIdx.x == 0 && c->rollback == 0) {
+            c->proceed = proceed ? 1 : 0;
+            const int go = rbNext ? 1 : 0;
+            c->rbGate = go;
+            if (useCond) cudaGraphSetConditional(rbCond, (unsigned int)go);
+        }
+        s_bits = (proceed ? 1 : 0) | (rbNext ? 2 : 0);
+        s_dt = c->dt;
+    }
+    __syncthreads();
+    return FireView{(s_bits & 1) != 0, (s_bits & 2) != 0, s_dt};
+}
+
 __global__ void __launch_bounds__(kConsThreads)
 k_project(const double2* __restrict__ pos, const int* __restrict__ start, int P,
           const double* __restrict__ constraints, double2* __restrict__ force,
@@ -158,19 +190,8 @@ k_project(const double2* __restrict__ pos, const int* __restrict__ start, int P,
     bool proceed = false, rbNext = false;
     double dt = 0.0;
     if (fire) {
-        double E = fire->energy, E0 = fire->ePre;
-        bool rb = E > E0 + fmax(fabs(E0) * 1e-10, 1e-14);
-        proceed = !fire->shakeFailed && !rb && fire->rollback == 0;
-        dt = fire->dt;
-        rbNext = fire->rollback == 0 && !fire->shakeFailed && rb && fire->active;
-        if (p == 0 && fire->rollback == 0) {
-            fire->proceed = proceed ? 1 : 0;
-            // the energy-increase rollback path runs when the step is not a
-            // SHAKE failure and the energy went up (model.cpp:450-453)
-            int go = rbNext ? 1 : 0;
-            fire->rbGate = go;
-            if (useCond) cudaGraphSetConditional(rbCond, (unsigned int)go);
-        }
+        const FireView fv = fire_view(fire, rbCond, useCond);
+        proceed = fv.proceed; rbNext = fv.rbNext; dt = fv.dt;
     }
     double sP = 0.0, sV = 0.0, sF = 0.0, mF = 0.0;
     if (p < P) {
@@ -663,6 +684,20 @@ __global__ void __launch_bounds__(256, 4) k_shake(double2* __restrict__ pos, con
     shake_finish(it, itersOut, fire, retryCond);
 }
 
+// y - floor(y), with the FP64 floor replaced by bit tests where
+// -1 <= y < 2 (a coordinate of [0, 1] moved by far less than 1): the same
+// single rounding as y - floor(y) in each case (y, y - 1, y + 1; -0 gives +0).
+__device__ __forceinline__ double frac_unit(double y) {
+    const unsigned hi = (unsigned)__double2hiint(y);
+    const unsigned lo = (unsigned)__double2loint(y);
+    if (hi < 0x3FF00000u) return y;                          // 0 <= y < 1
+    if (hi < 0x40000000u) return y - 1.0;                    // 1 <= y < 2
+    if (hi == 0x80000000u && lo == 0u) return 0.0;           // -0
+    if (hi >= 0x80000000u && (hi < 0xBFF00000u || (hi == 0xBFF00000u && lo == 0u)))
+        return y + 1.0;                                      // -1 <= y < 0
+    return y - floor(y);
+}
+
 __device__ __forceinline__ double2 shfl2(double2 v, int src) {
     return make_double2(__shfl_sync(PCP_FULL, v.x, src), __shfl_sync(PCP_FULL, v.y, src));
 }
@@ -746,6 +781,10 @@ __global__ void __launch_bounds__(128, 7) k_shake_lanes(double2* __restrict__ po
                         const Ctrl* __restrict__ dtc, const int* gate) {
     pdl_enter();
     if (gate_closed(gate)) return;
+    // 1/dt once per block (a DDIV is a dozen FP64 warp instructions)
+    __shared__ double s_idt;
+    if (vel && threadIdx.x == 0) s_idt = 1.0 / dtc->dt;
+    __syncthreads();
     const int lane = threadIdx.x & 31;
     const int p = blockIdx.x * (blockDim.x >> 5) + (threadIdx.x >> 5);
     int it = 0;
@@ -757,9 +796,11 @@ __global__ void __launch_bounds__(128, 7) k_shake_lanes(double2* __restrict__ po
             const int kp = (lane == 0) ? n - 1 : lane - 1;
             const int N = pow2_at_least(n);
             const double L = targetEdge[p], A0 = targetArea[p];
+            // tol > 0 and L > 0 on the bit patterns (positive, up to +inf)
+            const long long tolB = __double_as_longlong(tol), LB = __double_as_longlong(L);
             const unsigned long long tolBits =
-                tol > 0.0 ? (unsigned long long)__double_as_longlong(tol) : 0ull;
-            const double invL = L > 0.0 ? 1.0 / L : 1.0;
+                (tolB > 0 && tolB <= 0x7FF0000000000000ll) ? (unsigned long long)tolB : 0ull;
+            const double invL = (LB > 0 && LB <= 0x7FF0000000000000ll) ? 1.0 / L : 1.0;
             const double hInvL = 0.5 * invL, L2 = L * L;
             // local coordinates u_k = wrap(x_k - x_0): the iterations need no
             // minimum images (a polygon spans far less than half the box)
@@ -785,11 +826,10 @@ __global__ void __launch_bounds__(128, 7) k_shake_lanes(double2* __restrict__ po
                 const double ex = xn.x - x.x, ey = xn.y - x.y;
                 const double q = ex * ex + ey * ey - L2;
                 unsigned long long worst = live ? abs_bits(q * hInvL) : 0ull;
-                double area = 0.0;
-                if (live) area += ey * (xn.x + x.x);
+                double area = live ? ey * (xn.x + x.x) : 0.0;
                 worst = warp_max_u64(worst);
-                area = warp_sum(area) * 0.5;
-                const double sA = area - A0;
+                // (sum * 0.5 is exact: one rounding either way)
+                const double sA = fma(warp_sum(area), 0.5, -A0);
                 {
                     unsigned long long qa = abs_bits(sA);
                     if (qa > worst) worst = qa;
@@ -847,13 +887,12 @@ __global__ void __launch_bounds__(128, 7) k_shake_lanes(double2* __restrict__ po
             const double2 x0 = live ? pos[st + lane] : make_double2(0.0, 0.0);
             const double2 o = shfl2(x0, 0);
             if (live) {
-                double2 y = make_double2(o.x + x.x, o.y + x.y);
-                y = make_double2(y.x - floor(y.x), y.y - floor(y.y));
+                const double2 y = make_double2(frac_unit(o.x + x.x), frac_unit(o.y + x.y));
                 if (vel) {
                     // FIRE step: v += wrap(x_shake - x_before) / dt, the
                     // reference's rederivation from the displacement
                     // (model.cpp:436-438); a retry adds its own displacement
-                    const double idt = 1.0 / dtc->dt;
+                    const double idt = s_idt;
                     double2 v = vel[st + lane];
                     v.x += wrap(y.x - x0.x) * idt;
                     v.y += wrap(y.y - x0.y) * idt;
@@ -985,19 +1024,8 @@ __global__ void __launch_bounds__(256, 4) k_project_warp(const double2* __restri
     bool proceed = false, rbNext = false;
     double dt = 0.0;
     if (fire) {
-        double E = fire->energy, E0 = fire->ePre;
-        bool rb = E > E0 + fmax(fabs(E0) * 1e-10, 1e-14);
-        proceed = !fire->shakeFailed && !rb && fire->rollback == 0;
-        dt = fire->dt;
-        rbNext = fire->rollback == 0 && !fire->shakeFailed && rb && fire->active;
-        if (blockIdx.x == 0 && threadIdx.x == 0 && fire->rollback == 0) {
-            fire->proceed = proceed ? 1 : 0;
-            // the energy-increase rollback path runs when the step is not a
-            // SHAKE failure and the energy went up (model.cpp:450-453)
-            int go = rbNext ? 1 : 0;
-            fire->rbGate = go;
-            if (useCond) cudaGraphSetConditional(rbCond, (unsigned int)go);
-        }
+        const FireView fv = fire_view(fire, rbCond, useCond);
+        proceed = fv.proceed; rbNext = fv.rbNext; dt = fv.dt;
     }
     double sP = 0.0, sV = 0.0, sF = 0.0;
     unsigned long long mF = 0ull;      // max |F component| as a bit pattern
@@ -1197,19 +1225,8 @@ __global__ void __launch_bounds__(128, 7) k_project_lanes(const double2* __restr
     bool proceed = false, rbNext = false;
     double dt = 0.0;
     if (fire) {
-        double E = fire->energy, E0 = fire->ePre;
-        bool rb = E > E0 + fmax(fabs(E0) * 1e-10, 1e-14);
-        proceed = !fire->shakeFailed && !rb && fire->rollback == 0;
-        dt = fire->dt;
-        rbNext = fire->rollback == 0 && !fire->shakeFailed && rb && fire->active;
-        if (blockIdx.x == 0 && threadIdx.x == 0 && fire->rollback == 0) {
-            fire->proceed = proceed ? 1 : 0;
-            // the energy-increase rollback path runs when the step is not a
-            // SHAKE failure and the energy went up (model.cpp:450-453)
-            int go = rbNext ? 1 : 0;
-            fire->rbGate = go;
-            if (useCond) cudaGraphSetConditional(rbCond, (unsigned int)go);
-        }
+        const FireView fv = fire_view(fire, rbCond, useCond);
+        proceed = fv.proceed; rbNext = fv.rbNext; dt = fv.dt;
     }
     double sP = 0.0, sV = 0.0, sF = 0.0;
     unsigned long long mF = 0ull;      // max |F component| as a bit pattern
@@ -1280,8 +1297,10 @@ __global__ void __launch_bounds__(128, 7) k_project_lanes(const double2* __restr
                     if (round == 0) {
                         double L0 = f2d_int(l0), L0p = f2d_int(l0p);
                         double L1 = f2d_int(l1), L1p = f2d_int(l1p);
-                        f.x -= -L0 * t.x + L0p * tp.x; f.y -= -L0 * t.y + L0p * tp.y;
-                        q.x -= -L1 * t.x + L1p * tp.x; q.y -= -L1 * t.y + L1p * tp.y;
+                        f.x = fma(-L0p, tp.x, fma(L0, t.x, f.x));
+                        f.y = fma(-L0p, tp.y, fma(L0, t.y, f.y));
+                        q.x = fma(-L1p, tp.x, fma(L1, t.x, q.x));
+                        q.y = fma(-L1p, tp.y, fma(L1, t.y, q.y));
                     } else {
                         f.x += f2d_int(l0 * tf.x - l0p * tpf.x); f.y += f2d_int(l0 * tf.y - l0p * tpf.y);
                         q.x += f2d_int(l1 * tf.x - l1p * tpf.x); q.y += f2d_int(l1 * tf.y - l1p * tpf.y);
@@ -1295,8 +1314,11 @@ __global__ void __launch_bounds__(128, 7) k_project_lanes(const double2* __restr
                     const double2 t2 = warp_sum2(qF, qq);
                     qF = t2.x; qq = t2.y;
                 }
-                // sqrt(qq) > 1e-14 (kernels.cuh:464)
-                double coef = (qq > 1e-28) ? qF / qq : 0.0;
+                // sqrt(qq) > 1e-14 (kernels.cuh:464), tested on the bit
+                // pattern (qq >= 0 or NaN; 0x3A1FB0F6BE506019 is 1e-28)
+                const unsigned long long qqB = (unsigned long long)__double_as_longlong(qq);
+                double coef = (qqB > 0x3A1FB0F6BE506019ull && qqB <= 0x7FF0000000000000ull)
+                                  ? qF / qq : 0.0;
                 f = make_double2(f.x - coef * q.x, f.y - coef * q.y);
                 if (live) force[st + lane] = f;
             }
@@ -1570,16 +1592,8 @@ __global__ void k_fire_velocity(double2* __restrict__ vel, const double2* __rest
     pdl_enter();
     if (gate_closed(gate)) return;
     int i = blockIdx.x * blockDim.x + threadIdx.x;
-    double E = c->energy, E0 = c->ePre;
-    bool rb = E > E0 + fmax(fabs(E0) * 1e-10, 1e-14);
-    bool proceed = !c->shakeFailed && !rb && c->rollback == 0;
-    const bool rbNext = c->rollback == 0 && !c->shakeFailed && rb && c->active;
-    if (i == 0 && c->rollback == 0) {
-        c->proceed = proceed ? 1 : 0;
-        int go = rbNext ? 1 : 0;
-        c->rbGate = go;
-        if (useCond) cudaGraphSetConditional(rbCond, (unsigned int)go);
-    }
+    const FireView fv = fire_view(c, rbCond, useCond);
+    const bool proceed = fv.proceed, rbNext = fv.rbNext;
     double sP = 0.0, sV = 0.0, sF = 0.0, mF = 0.0;
     if (i < V) {
         double2 f = force[i];
