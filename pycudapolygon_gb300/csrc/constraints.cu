@@ -667,7 +667,7 @@ __global__ void __launch_bounds__(256, 4) k_shake(double2* __restrict__ pos, con
                 for (int k = lane; k < n; k += 32) {
                     double2 x = make_double2(o.x + w.xs[k].x, o.y + w.xs[k].y), y = pos[st + k],
                             v = vel[st + k];
-                    x = make_double2(x.x - floor(x.x), x.y - floor(x.y));
+                    x = make_double2(frac_unit(x.x), frac_unit(x.y));
                     v.x += wrap(x.x - y.x) * idt;
                     v.y += wrap(x.y - y.y) * idt;
                     vel[st + k] = v;
@@ -676,26 +676,12 @@ __global__ void __launch_bounds__(256, 4) k_shake(double2* __restrict__ pos, con
             } else {
                 for (int k = lane; k < n; k += 32) {
                     double2 v = make_double2(o.x + w.xs[k].x, o.y + w.xs[k].y);
-                    pos[st + k] = make_double2(v.x - floor(v.x), v.y - floor(v.y));
+                    pos[st + k] = make_double2(frac_unit(v.x), frac_unit(v.y));
                 }
             }
         }
     }
     shake_finish(it, itersOut, fire, retryCond);
-}
-
-// y - floor(y), with the FP64 floor replaced by bit tests where
-// -1 <= y < 2 (a coordinate of [0, 1] moved by far less than 1): the same
-// single rounding as y - floor(y) in each case (y, y - 1, y + 1; -0 gives +0).
-__device__ __forceinline__ double frac_unit(double y) {
-    const unsigned hi = (unsigned)__double2hiint(y);
-    const unsigned lo = (unsigned)__double2loint(y);
-    if (hi < 0x3FF00000u) return y;                          // 0 <= y < 1
-    if (hi < 0x40000000u) return y - 1.0;                    // 1 <= y < 2
-    if (hi == 0x80000000u && lo == 0u) return 0.0;           // -0
-    if (hi >= 0x80000000u && (hi < 0xBFF00000u || (hi == 0xBFF00000u && lo == 0u)))
-        return y + 1.0;                                      // -1 <= y < 0
-    return y - floor(y);
 }
 
 __device__ __forceinline__ double2 shfl2(double2 v, int src) {
@@ -741,10 +727,11 @@ __device__ __forceinline__ void lanes_pcr3(float a, float b, float c, float& q0,
 
 // Unit tangent t_k of edge (k, k+1) of the wrapped positions held one vertex
 // per lane (kernels.cuh:399: zero for an edge shorter than 1e-14).
-__device__ __forceinline__ void lanes_tangent(double2 x, int kn, double2& t) {
+__device__ __forceinline__ void lanes_tangent(double2 x, int kn, double2& t, double2& d) {
     const double2 xn = shfl2(x, kn);
     t = make_double2(0.0, 0.0);
     double dx = wrap(xn.x - x.x), dy = wrap(xn.y - x.y);
+    d = make_double2(dx, dy);
     double len2 = dx * dx + dy * dy;
     // len2 >= 0, so its bit pattern orders like its value (NaN counts as long)
     bool ok = (unsigned long long)__double_as_longlong(len2) >=
@@ -907,9 +894,10 @@ __global__ void __launch_bounds__(128, 7) k_shake_lanes(double2* __restrict__ po
 
 // The unit edge tangents and unit area gradients (normalised over the
 // polygon) of the positions, one polygon per warp, stored for
-// k_project_lanes as pre[i] = t_i, pre[V + i] = q_i.  The FIRE step runs
-// this on the SHAKE branch, beside the contact search, so that the
-// projection on the step's critical path starts from them.
+// k_project_lanes as pre[i] = t_i, pre[V + i] = q_i, and the edge vectors
+// wrap(x_next - x_i) for the overlap force as pre[2V + i].  The FIRE step
+// runs this beside the end of the contact search, so that the force and the
+// projection on the step's critical path start from them.
 __global__ void __launch_bounds__(128) k_project_pre(const double2* __restrict__ pos,
                                                      const int* __restrict__ start, int P,
                                                      double2* __restrict__ pre, int V,
@@ -920,15 +908,16 @@ __global__ void __launch_bounds__(128) k_project_pre(const double2* __restrict__
     const int p = blockIdx.x * (blockDim.x >> 5) + (threadIdx.x >> 5);
     if (p >= P) return;
     const int st = start[p], n = start[p + 1] - st;
-    if (n < 3 || n > 32) return;
+    // (polygons of 1 or 2 vertices too: the force may take their edges)
+    if (n < 1 || n > 32) return;
     const bool live = lane < n;
     const int kn = (lane + 1 >= n) ? 0 : lane + 1;
     const int kp = (lane == 0) ? n - 1 : lane - 1;
     const double2 x = live ? pos[st + lane] : make_double2(0.0, 0.0);
-    double2 t, q;
-    lanes_tangent(x, kn, t);
+    double2 t, q, d;
+    lanes_tangent(x, kn, t, d);
     lanes_area_gradient(x, live, kn, kp, q);
-    if (live) { pre[st + lane] = t; pre[V + st + lane] = q; }
+    if (live) { pre[st + lane] = t; pre[V + st + lane] = q; pre[2 * (size_t)V + st + lane] = d; }
 }
 
 // launch_project's choice: thread per polygon for at least 128 polygons per
@@ -1245,7 +1234,8 @@ __global__ void __launch_bounds__(128, 7) k_project_lanes(const double2* __restr
                 q = live ? pre[V + st + lane] : make_double2(0.0, 0.0);
             } else {
                 const double2 x = live ? pos[st + lane] : make_double2(0.0, 0.0);
-                lanes_tangent(x, kn, t);
+                double2 d;
+                lanes_tangent(x, kn, t, d);
                 if (areaFromPositions) {
                     lanes_area_gradient(x, live, kn, kp, q);
                 } else {
@@ -1525,7 +1515,7 @@ __global__ void k_fire_begin(double2* __restrict__ pos, double2* __restrict__ ve
         v.x += 0.5 * dt * f.x; v.y += 0.5 * dt * f.y;
         double px = x.x + dt * v.x, py = x.y + dt * v.y;
         vel[i] = v;
-        double2 xn = make_double2(px - floor(px), py - floor(py));
+        double2 xn = make_double2(frac_unit(px), frac_unit(py));
         pos[i] = xn;
         if (verlet) verlet[i] = xn;
         force[i] = make_double2(0.0, 0.0);

@@ -1377,10 +1377,14 @@ __device__ __forceinline__ void add_f(double2* F, int v, double fx, double fy) {
 constexpr int kForceRecs = 16;
 constexpr int kForceWarps = 2;
 
+// kEdge: the edge vectors wrap(x_next - x) of the current positions are
+// given in `edge` (the FIRE step computes them beside the contact search), so
+// the kernel loads them instead of forming them (bit-identical values).
+template <bool kEdge>
 __global__ void __launch_bounds__(32 * kForceWarps)
 k_overlap_force(const double2* __restrict__ pos, const int* __restrict__ start,
                 const int* __restrict__ next, int V, ContactWS ws, Ctrl* __restrict__ ctrl,
-                double2* __restrict__ force, const int* gate) {
+                double2* __restrict__ force, const double2* __restrict__ edge, const int* gate) {
     pdl_enter();
     if (gate_closed(gate)) return;
     const int lane = threadIdx.x & 31;
@@ -1425,7 +1429,7 @@ k_overlap_force(const double2* __restrict__ pos, const int* __restrict__ start,
             za = next[a];
             pa = pos[a];
             pza = pos[za];
-            ra = make_double2(wrap(pza.x - pa.x), wrap(pza.y - pa.y));
+            ra = kEdge ? edge[a] : make_double2(wrap(pza.x - pa.x), wrap(pza.y - pa.y));
             const double ta = f2d_int(half ? ws.recUT[r].y : ws.recTU[r].y);
             fa = make_double2(wrap(pa.x + ta * ra.x), wrap(pa.y + ta * ra.y));
         }
@@ -1449,7 +1453,7 @@ k_overlap_force(const double2* __restrict__ pos, const int* __restrict__ start,
                 else if (same) { v0 = k; v1 = za; v2 = i; v3 = next[i]; }
                 else { v0 = k; v1 = za; v2 = l; v3 = next[l]; }
                 const double2 q0 = pa;                 // p_i (even) or p_k (odd)
-                double2 q2 = pos[v2], q3 = pos[v3];
+                double2 q2 = pos[v2];
                 double2 hA = (!same && half) ? q2 : fij;
                 double2 hB = (same || half) ? fkl : pza;
                 double dyg, sx;
@@ -1463,7 +1467,13 @@ k_overlap_force(const double2* __restrict__ pos, const int* __restrict__ start,
                 const double2 nx1 = (!same && !half) ? make_double2(ndy, nsx) : make_double2(0.0, 0.0);
                 const double2 nx2 = (!same && half) ? make_double2(ndy, sx) : make_double2(0.0, 0.0);
                 double2 o[4];
-                gDf_di(q0, ra, q2, q3, ng, o);    // q1 - q0 is this lane's own edge
+                // q1 - q0 is this lane's own edge; q3 - q2 the other polygon's
+                if (kEdge) {
+                    gDf_dd(q0, ra, q2, edge[v2], ng, o);
+                } else {
+                    const double2 q3 = pos[v3];
+                    gDf_di(q0, ra, q2, q3, ng, o);
+                }
                 add_f(force, v0, o[0].x, o[0].y);
                 add_f(force, v1, o[1].x + nx1.x, o[1].y + nx1.y);
                 add_f(force, v2, o[2].x + nx2.x, o[2].y + nx2.y);
@@ -1503,7 +1513,12 @@ k_overlap_force(const double2* __restrict__ pos, const int* __restrict__ start,
                 int mv = oStart + mLoc;
                 int nv = next[mv];
                 double dyg, sx;
-                eLocal += h_parts(pos[mv], pos[nv], osp, dyg, sx);
+                if (kEdge) {
+                    dyg = edge[mv].y;
+                    eLocal += h_parts_dy(pos[mv], pos[nv], osp, dyg, sx);
+                } else {
+                    eLocal += h_parts(pos[mv], pos[nv], osp, dyg, sx);
+                }
                 const double ndy = neg_int(dyg);
                 add_f(force, mv, ndy, sx);             // -g1
                 add_f(force, nv, ndy, neg_int(sx));    // -g2
@@ -1592,10 +1607,15 @@ cudaError_t launch_contacts_finish(const int* start, ContactWS& ws, Ctrl* ctrl,
 
 cudaError_t launch_overlap_force(const double2* pos, const int* start, const int* next,
                                  int V, ContactWS& ws, Ctrl* ctrl, double2* force,
-                                 const int* gate, cudaStream_t st) {
+                                 const int* gate, cudaStream_t st, const double2* edge) {
     // one pass over up to 4 * SMs * kForceWarps * kForceRecs records
     int grid = sm_count() * 4;
-    launch_k(k_overlap_force, dim3(grid), dim3(32 * kForceWarps), 0, st, pos, start, next, V, ws, ctrl, force, gate);
+    if (edge)
+        launch_k(k_overlap_force<true>, dim3(grid), dim3(32 * kForceWarps), 0, st, pos, start, next, V, ws,
+                 ctrl, force, edge, gate);
+    else
+        launch_k(k_overlap_force<false>, dim3(grid), dim3(32 * kForceWarps), 0, st, pos, start, next, V, ws,
+                 ctrl, force, edge, gate);
     return cudaGetLastError();
 }
 

@@ -427,7 +427,9 @@ int upload(pcp_model* m, void* dst, const void* src, size_t bytes) {
 }
 
 // ---- the force evaluation (Model::updateForceEnergy, model.cpp:363-395) ----
-int force_energy(pcp_model* m, const int* gate, bool zeroed = false) {
+// edgeVec: the edge vectors of the current positions when they are at hand
+int force_energy(pcp_model* m, const int* gate, bool zeroed = false,
+                 const double2* edgeVec = nullptr) {
     if (!zeroed) {
         CK(launch_zero_force(m->force, m->V, m->ctrl, gate, m->stream));
         m->launches++;
@@ -438,7 +440,7 @@ int force_energy(pcp_model* m, const int* gate, bool zeroed = false) {
     bool area = (t == PCP_MODEL_SOFT_BODY || t == PCP_MODEL_AREA_ONLY || t == PCP_MODEL_HYBRID);
     if (overlap) {
         CK(launch_overlap_force(m->pos, m->start, m->next, m->V, m->ws, m->ctrl, m->force, gate,
-                                m->stream));
+                                m->stream, edgeVec));
         m->launches++;
     }
     if (edge) {
@@ -595,10 +597,13 @@ int record_fire_step(pcp_model* m, cudaGraphConditionalHandle retryCond,
         rc = geometry(m, gA);
         if (rc) return rc;
     }
-    rc = force_energy(m, gA, true);
+    // the third branch's edge vectors (computed with the tangents) feed the
+    // force when the projection takes the one-vertex-per-lane path
+    const bool preEdges = shake && project_uses_lanes(m->P, m->nmax);
+    if (shake) CK(cudaStreamWaitEvent(st, m->evPreJoin, 0));
+    rc = force_energy(m, gA, true, preEdges ? pre + 2 * (size_t)V : nullptr);
     if (rc) return rc;
     if (rigid) {
-        if (shake) CK(cudaStreamWaitEvent(st, m->evPreJoin, 0));
         CK(launch_project(m->pos, m->start, m->P, m->nmax, m->constraints, m->force, m->scratch, V, 1,
                           m->ctrl, gA, m->vel, st, rbCond, 1, shake ? pre : nullptr));
     } else {

@@ -66,6 +66,20 @@ __device__ __forceinline__ double wrap(double x) {
     return y - 0.5;
 }
 
+// y - floor(y), with the FP64 floor replaced by bit tests where
+// -1 <= y < 2 (a coordinate of [0, 1] moved by far less than 1): the same
+// single rounding as y - floor(y) in each case (y, y - 1, y + 1; -0 gives +0).
+__device__ __forceinline__ double frac_unit(double y) {
+    const unsigned hi = (unsigned)__double2hiint(y);
+    const unsigned lo = (unsigned)__double2loint(y);
+    if (hi < 0x3FF00000u) return y;                          // 0 <= y < 1
+    if (hi < 0x40000000u) return y - 1.0;                    // 1 <= y < 2
+    if (hi == 0x80000000u && lo == 0u) return 0.0;           // -0
+    if (hi >= 0x80000000u && (hi < 0xBFF00000u || (hi == 0xBFF00000u && lo == 0u)))
+        return y + 1.0;                                      // -1 <= y < 0
+    return y - floor(y);
+}
+
 __device__ __forceinline__ double2 wrap2(double2 v) {
     return make_double2(wrap(v.x), wrap(v.y));
 }
@@ -208,6 +222,17 @@ __device__ __forceinline__ double h_parts(double2 p1, double2 p2, double2 sp, do
     return sx * dyh;
 }
 
+// the same with dyg = wrap(p2.y - p1.y) given (p1 -> p2 an edge whose
+// vector the caller holds)
+__device__ __forceinline__ double h_parts_dy(double2 p1, double2 p2, double2 sp, double dyg,
+                                             double& sx) {
+    double r1x = wrap(p1.x - sp.x), r1y = wrap(p1.y - sp.y);
+    double r2x = wrap(p2.x - sp.x), r2y = wrap(p2.y - sp.y);
+    double dyh = wrap(r2y - r1y);
+    sx = r1x + r2x;
+    return sx * dyh;
+}
+
 // -x by a flip of the sign bit on the integer pipe
 __device__ __forceinline__ double neg_int(double x) {
     return __hiloint2double(__double2hiint(x) ^ (int)0x80000000, __double2loint(x));
@@ -219,9 +244,11 @@ __device__ __forceinline__ double neg_int(double x) {
 // the four 2-vectors gT df restricted to each vertex:  out[p] = (g . df[:,2p],
 // g . df[:,2p+1]).  Zero for near-parallel or degenerate edges.
 // di = wrap(vzi - vi), when the caller has it already.
-__device__ __forceinline__ void gDf_di(double2 vi, double2 di, double2 vj, double2 vzj,
+// dj = wrap(vzj - vj) as well, when the caller has it (vzj itself is then
+// not needed).
+__device__ __forceinline__ void gDf_dd(double2 vi, double2 di, double2 vj, double2 dj,
                                        double2 g, double2 out[4]) {
-    double djx = wrap(vzj.x - vj.x), djy = wrap(vzj.y - vj.y);
+    double djx = dj.x, djy = dj.y;
     double dix = di.x, diy = di.y;
     double dijx = wrap(vj.x - vi.x), dijy = wrap(vj.y - vi.y);
     double w = djx * diy - djy * dix;
@@ -256,6 +283,10 @@ __device__ __forceinline__ void gDf_di(double2 vi, double2 di, double2 vj, doubl
     out[1] = make_double2(u * ax, u * ay);
     out[2] = make_double2(s * fma(u, diy, -dijy - djy), s * fma(-u, dix, djx + dijx));
     out[3] = make_double2(s * fma(-u, diy, dijy), s * fma(u, dix, -dijx));
+}
+__device__ __forceinline__ void gDf_di(double2 vi, double2 di, double2 vj, double2 vzj,
+                                       double2 g, double2 out[4]) {
+    gDf_dd(vi, di, vj, make_double2(wrap(vzj.x - vj.x), wrap(vzj.y - vj.y)), g, out);
 }
 __device__ __forceinline__ void gDf(double2 vi, double2 vzi, double2 vj, double2 vzj,
                                     double2 g, double2 out[4]) {

@@ -62,7 +62,7 @@ __device__ __forceinline__ double2 fire_move_vertex(const FireMove& mv, int i, d
     v.x += 0.5 * dt * f.x; v.y += 0.5 * dt * f.y;
     double px = x.x + dt * v.x, py = x.y + dt * v.y;
     mv.vel[i] = v;
-    double2 xn = make_double2(px - floor(px), py - floor(py));
+    double2 xn = make_double2(frac_unit(px), frac_unit(py));
     mv.pos[i] = xn;
     mv.force[i] = make_double2(0.0, 0.0);
     return xn;

@@ -169,9 +169,10 @@ cudaError_t launch_prepass_move(double2* verlet, const int* start, int* cellOut,
                                 const FireMove& mv);
 cudaError_t launch_contacts_finish(const int* start, ContactWS& ws, Ctrl* ctrl,
                                    const int* gate, cudaStream_t st);
+// edge: the edge vectors wrap(x_next - x) of pos, or nullptr
 cudaError_t launch_overlap_force(const double2* pos, const int* start, const int* next,
                                  int V, ContactWS& ws, Ctrl* ctrl, double2* force,
-                                 const int* gate, cudaStream_t st);
+                                 const int* gate, cudaStream_t st, const double2* edge = nullptr);
 
 // constraints
 cudaError_t constraints_init();
