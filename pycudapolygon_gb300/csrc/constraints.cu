@@ -741,14 +741,18 @@ __device__ __forceinline__ void lanes_tangent(double2 x, int kn, double2& t, dou
 
 // Unit area gradient of the polygon at vertex k, (x_k+1 - x_k-1) / 2 rotated
 // and normalised over the polygon (updatePolygonGeometryKernel,
-// kernels.cuh:303,313), one vertex per lane; lanes >= n (live false) hold 0.
-__device__ __forceinline__ void lanes_area_gradient(double2 x, bool live, int kn, int kp,
-                                                    double2& q) {
-    const double2 xn = shfl2(x, kn), xp = shfl2(x, kp);
-    q = make_double2(-wrap(xp.y - xn.y), wrap(xp.x - xn.x));
+// kernels.cuh:303,313), one vertex per lane, from the edge vectors
+// d_k = wrap(x_k+1 - x_k) that lanes_tangent forms: x_k+1 - x_k-1 =
+// d_k-1 + d_k (one add instead of a wrapped difference).  Lanes >= n (live
+// false) add nothing to the normalisation.
+__device__ __forceinline__ void lanes_area_gradient(double2 d, bool live, int kp, double2& q) {
+    const double2 dp = shfl2(d, kp);
+    q = make_double2(dp.y + d.y, -dp.x - d.x);
     double an = live ? q.x * q.x + q.y * q.y : 0.0;
     an = warp_sum(an);
-    double ir = an > 0.0 ? rsqrt(an) : 1.0;
+    // an > 0 on the bit pattern (an >= 0, or NaN)
+    const unsigned long long anB = (unsigned long long)__double_as_longlong(an);
+    double ir = (anB > 0ull && anB <= 0x7FF0000000000000ull) ? rsqrt(an) : 1.0;
     q = make_double2(q.x * ir, q.y * ir);
 }
 
@@ -916,7 +920,7 @@ __global__ void __launch_bounds__(128) k_project_pre(const double2* __restrict__
     const double2 x = live ? pos[st + lane] : make_double2(0.0, 0.0);
     double2 t, q, d;
     lanes_tangent(x, kn, t, d);
-    lanes_area_gradient(x, live, kn, kp, q);
+    lanes_area_gradient(d, live, kp, q);
     if (live) { pre[st + lane] = t; pre[V + st + lane] = q; pre[2 * (size_t)V + st + lane] = d; }
 }
 
@@ -1237,7 +1241,7 @@ __global__ void __launch_bounds__(128, 7) k_project_lanes(const double2* __restr
                 double2 d;
                 lanes_tangent(x, kn, t, d);
                 if (areaFromPositions) {
-                    lanes_area_gradient(x, live, kn, kp, q);
+                    lanes_area_gradient(d, live, kp, q);
                 } else {
                     q = make_double2(0.0, 0.0);
                     if (live) {
