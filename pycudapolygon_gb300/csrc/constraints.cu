@@ -145,12 +145,9 @@ __device__ __forceinline__ void fire_pass_end(Ctrl* __restrict__ c, bool rollbac
     }
 }
 
-// The rollback test at the end of the step's force pass (model.cpp:450-453):
-// the velocities advance unless SHAKE failed or the energy went up, and the
-// energy-increase rollback runs next when the energy went up and SHAKE did
-// not fail.  Thread 0 of each block evaluates it (an FP64 compare costs a
-// warp instruction, so once per block rather than once per warp) and block
-// 0 publishes it.  Every thread of the block calls this.
+// fire_decide once per block (an FP64 compare costs a warp instruction, so
+// once per block rather than once per warp), published by block 0; every
+// thread of the block calls this.
 struct FireView {
     bool proceed, rbNext;
     double dt;
@@ -160,17 +157,24 @@ __device__ __forceinline__ FireView fire_view(Ctrl* __restrict__ c,
     __shared__ int s_bits;
     __shared__ double s_dt;
     if (threadIdx.x == 0) {
-        const double E = c->energy, E0 = c->ePre;
-        const bool rb = E > E0 + fmax(fabs(E0) * 1e-10, 1e-14);
-        const bool proceed = !c->shakeFailed && !rb && c->rollback == 0;
-        const bool rbNext = c->rollback == 0 && !c->shakeFailed && rb && c->active;
-        if (blockIdx.x == 0 && c->rollback == 0) {
-            c->proceed = proceed ? 1 : 0;
-            const int go = rbNext ? 1 : 0;
-            c->rbGate = go;
-            if (useCond) cudaGraphSetConditional(rbCond, (unsigned int)go);
-        }
-        s_bits = (proceed ? 1 : 0) | (rbNext ? 2 : 0);
+        s_bits = fire_decide(c, blockIdx.x == 0, rbCond, useCond);
+        s_dt = c->dt;
+    }
+    __syncthreads();
+    return FireView{(s_bits & 1) != 0, (s_bits & 2) != 0, s_dt};
+}
+
+// The projection's view of the step.  In the step's own pass (mainPass) the
+// force pass has decided and published the rollback already, and a rollback
+// body may be running beside this kernel (it resets the energy), so the
+// published outcome is read; otherwise (the rollback body's pass) the test
+// itself, unpublished.  Every thread of the block calls this.
+__device__ __forceinline__ FireView fire_view_proj(Ctrl* __restrict__ c, int mainPass) {
+    __shared__ int s_bits;
+    __shared__ double s_dt;
+    if (threadIdx.x == 0) {
+        s_bits = mainPass ? ((__ldcg(&c->proceed) ? 1 : 0) | (__ldcg(&c->rbGate) ? 2 : 0))
+                          : fire_decide(c, false, 0, 0);
         s_dt = c->dt;
     }
     __syncthreads();
@@ -181,8 +185,7 @@ __global__ void __launch_bounds__(kConsThreads)
 k_project(const double2* __restrict__ pos, const int* __restrict__ start, int P,
           const double* __restrict__ constraints, double2* __restrict__ force,
           double* __restrict__ scratch, int V, int smemN, int areaFromPositions, Ctrl* fire,
-          double2* __restrict__ vel, cudaGraphConditionalHandle rbCond, int useCond,
-          const int* gate) {
+          double2* __restrict__ vel, int mainPass, const int* gate) {
     pdl_enter();
     if (gate_closed(gate)) return;
     extern __shared__ double cons_smem[];
@@ -190,7 +193,8 @@ k_project(const double2* __restrict__ pos, const int* __restrict__ start, int P,
     bool proceed = false, rbNext = false;
     double dt = 0.0;
     if (fire) {
-        const FireView fv = fire_view(fire, rbCond, useCond);
+        const FireView fv = fire_view_proj(fire, mainPass);
+        if (mainPass && fv.rbNext) return;     // the rollback body redoes the pass
         proceed = fv.proceed; rbNext = fv.rbNext; dt = fv.dt;
     }
     double sP = 0.0, sV = 0.0, sF = 0.0, mF = 0.0;
@@ -1006,8 +1010,7 @@ __global__ void __launch_bounds__(256, 4) k_project_warp(const double2* __restri
                                int P, const double* __restrict__ constraints,
                                double2* __restrict__ force, double* __restrict__ scratch,
                                int nmaxSmem, int areaFromPositions, Ctrl* fire,
-                               double2* __restrict__ vel, cudaGraphConditionalHandle rbCond,
-                               int useCond, const int* gate) {
+                               double2* __restrict__ vel, int mainPass, const int* gate) {
     pdl_enter();
     if (gate_closed(gate)) return;
     extern __shared__ __align__(16) unsigned char proj_smem[];
@@ -1017,7 +1020,8 @@ __global__ void __launch_bounds__(256, 4) k_project_warp(const double2* __restri
     bool proceed = false, rbNext = false;
     double dt = 0.0;
     if (fire) {
-        const FireView fv = fire_view(fire, rbCond, useCond);
+        const FireView fv = fire_view_proj(fire, mainPass);
+        if (mainPass && fv.rbNext) return;     // the rollback body redoes the pass
         proceed = fv.proceed; rbNext = fv.rbNext; dt = fv.dt;
     }
     double sP = 0.0, sV = 0.0, sF = 0.0;
@@ -1208,8 +1212,8 @@ __global__ void __launch_bounds__(128, 7) k_project_lanes(const double2* __restr
                                const int* __restrict__ start, int P,
                                const double* __restrict__ constraints,
                                double2* __restrict__ force, int areaFromPositions, Ctrl* fire,
-                               double2* __restrict__ vel, cudaGraphConditionalHandle rbCond,
-                               int useCond, const double2* __restrict__ pre, int V,
+                               double2* __restrict__ vel, int mainPass,
+                               const double2* __restrict__ pre, int V,
                                const int* gate) {
     pdl_enter();
     if (gate_closed(gate)) return;
@@ -1218,7 +1222,8 @@ __global__ void __launch_bounds__(128, 7) k_project_lanes(const double2* __restr
     bool proceed = false, rbNext = false;
     double dt = 0.0;
     if (fire) {
-        const FireView fv = fire_view(fire, rbCond, useCond);
+        const FireView fv = fire_view_proj(fire, mainPass);
+        if (mainPass && fv.rbNext) return;     // the rollback body redoes the pass
         proceed = fv.proceed; rbNext = fv.rbNext; dt = fv.dt;
     }
     double sP = 0.0, sV = 0.0, sF = 0.0;
@@ -1376,7 +1381,7 @@ cudaError_t constraints_init() {
 cudaError_t launch_project(const double2* pos, const int* start, int P, int nmax,
                            const double* constraints, double2* force, double* scratch, int V,
                            int areaFromPositions, Ctrl* fireCtrl, const int* gate, double2* vel,
-                           cudaStream_t st, cudaGraphConditionalHandle rbCond, int useCond,
+                           cudaStream_t st, int mainPass,
                            const double2* pre) {
     if (P <= 0) return cudaSuccess;
     if (P >= 128 * sm_count()) {
@@ -1384,13 +1389,13 @@ cudaError_t launch_project(const double2* pos, const int* start, int P, int nmax
         size_t smem = (size_t)sn * kProjArrays * kConsThreads * sizeof(double);
         launch_k(k_project, dim3(nblk(P, kConsThreads)), dim3(kConsThreads), smem, st, 
             pos, start, P, constraints, force, scratch, V, sn, areaFromPositions, fireCtrl, vel,
-            rbCond, useCond, gate);
+            mainPass, gate);
         return cudaGetLastError();
     }
     if (project_uses_lanes(P, nmax)) {
         const int wpb = 4;
         launch_k(k_project_lanes, dim3(nblk(P, wpb)), dim3(32 * wpb), 0, st, pos, start, P,
-                 constraints, force, areaFromPositions, fireCtrl, vel, rbCond, useCond, pre, V,
+                 constraints, force, areaFromPositions, fireCtrl, vel, mainPass, pre, V,
                  gate);
         return cudaGetLastError();
     }
@@ -1404,7 +1409,7 @@ cudaError_t launch_project(const double2* pos, const int* start, int P, int nmax
     if (per * wpb > 200 * 1024) { nmaxSmem = 0; per = 0; wpb = 8; }
     launch_k(k_project_warp, dim3(nblk(P, wpb)), dim3(32 * wpb), per * wpb, st, pos, start, P, constraints, force,
                                                               scratch, nmaxSmem, areaFromPositions,
-                                                              fireCtrl, vel, rbCond, useCond, gate);
+                                                              fireCtrl, vel, mainPass, gate);
     return cudaGetLastError();
 }
 

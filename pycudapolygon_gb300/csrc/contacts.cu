@@ -1384,7 +1384,8 @@ template <bool kEdge>
 __global__ void __launch_bounds__(32 * kForceWarps)
 k_overlap_force(const double2* __restrict__ pos, const int* __restrict__ start,
                 const int* __restrict__ next, int V, ContactWS ws, Ctrl* __restrict__ ctrl,
-                double2* __restrict__ force, const double2* __restrict__ edge, const int* gate) {
+                double2* __restrict__ force, const double2* __restrict__ edge, int decide,
+                cudaGraphConditionalHandle rbCond, const int* gate) {
     pdl_enter();
     if (gate_closed(gate)) return;
     const int lane = threadIdx.x & 31;
@@ -1527,6 +1528,20 @@ k_overlap_force(const double2* __restrict__ pos, const int* __restrict__ start,
     }
     eLocal = warp_sum(eLocal);
     if (lane == 0 && eLocal != 0.0) atomicAdd(&ctrl->energy, eLocal / 2.0);
+    if (decide) {
+        // the FIRE step's force pass: the last block to finish decides the
+        // energy rollback, so that the rollback body can start beside the
+        // projection
+        if (lane == 0) __threadfence();
+        __syncthreads();
+        if (threadIdx.x == 0) {
+            const unsigned int t = atomicAdd(&ctrl->forceTicket, 1u);
+            if (t == gridDim.x - 1) {
+                __threadfence();
+                (void)fire_decide(ctrl, true, rbCond, 1);
+            }
+        }
+    }
 }
 
 // ------------------------------------------------------------ launchers ----
@@ -1607,15 +1622,16 @@ cudaError_t launch_contacts_finish(const int* start, ContactWS& ws, Ctrl* ctrl,
 
 cudaError_t launch_overlap_force(const double2* pos, const int* start, const int* next,
                                  int V, ContactWS& ws, Ctrl* ctrl, double2* force,
-                                 const int* gate, cudaStream_t st, const double2* edge) {
+                                 const int* gate, cudaStream_t st, const double2* edge,
+                                 int decide, cudaGraphConditionalHandle rbCond) {
     // one pass over up to 4 * SMs * kForceWarps * kForceRecs records
     int grid = sm_count() * 4;
     if (edge)
         launch_k(k_overlap_force<true>, dim3(grid), dim3(32 * kForceWarps), 0, st, pos, start, next, V, ws,
-                 ctrl, force, edge, gate);
+                 ctrl, force, edge, decide, rbCond, gate);
     else
         launch_k(k_overlap_force<false>, dim3(grid), dim3(32 * kForceWarps), 0, st, pos, start, next, V, ws,
-                 ctrl, force, edge, gate);
+                 ctrl, force, edge, decide, rbCond, gate);
     return cudaGetLastError();
 }
 

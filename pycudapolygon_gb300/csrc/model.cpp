@@ -117,7 +117,9 @@ struct pcp_model {
     int fireKernelNodes = 0;   // kernel launches one FIRE step graph makes
     int rbBodyKernels = 0;     // kernels of its rollback body (counted on the device)
     cudaStream_t sideStream = nullptr, bodyStream = nullptr, preStream = nullptr;   // capture helpers
+    cudaStream_t ifStream = nullptr;
     cudaEvent_t evFork = nullptr, evJoin = nullptr, evPreFork = nullptr, evPreJoin = nullptr;
+    cudaEvent_t evRbFork = nullptr, evRbJoin = nullptr;
 
     ~pcp_model() { release(); }
 
@@ -128,8 +130,11 @@ struct pcp_model {
         if (evFork) { cudaEventDestroy(evFork); evFork = nullptr; }
         if (evJoin) { cudaEventDestroy(evJoin); evJoin = nullptr; }
         if (preStream) { cudaStreamDestroy(preStream); preStream = nullptr; }
+        if (ifStream) { cudaStreamDestroy(ifStream); ifStream = nullptr; }
         if (evPreFork) { cudaEventDestroy(evPreFork); evPreFork = nullptr; }
         if (evPreJoin) { cudaEventDestroy(evPreJoin); evPreJoin = nullptr; }
+        if (evRbFork) { cudaEventDestroy(evRbFork); evRbFork = nullptr; }
+        if (evRbJoin) { cudaEventDestroy(evRbJoin); evRbJoin = nullptr; }
         dfree(&pos); dfree(&force); dfree(&vel); dfree(&posTMP); dfree(&posTMP2); dfree(&posTent);
         dfree(&posGeom);
         dfree(&velSnap); dfree(&forceSnap);
@@ -428,8 +433,11 @@ int upload(pcp_model* m, void* dst, const void* src, size_t bytes) {
 
 // ---- the force evaluation (Model::updateForceEnergy, model.cpp:363-395) ----
 // edgeVec: the edge vectors of the current positions when they are at hand
+// decide: the FIRE step's force pass, whose last block decides the energy
+// rollback and sets rbCond
 int force_energy(pcp_model* m, const int* gate, bool zeroed = false,
-                 const double2* edgeVec = nullptr) {
+                 const double2* edgeVec = nullptr, int decide = 0,
+                 cudaGraphConditionalHandle rbCond = 0) {
     if (!zeroed) {
         CK(launch_zero_force(m->force, m->V, m->ctrl, gate, m->stream));
         m->launches++;
@@ -440,7 +448,7 @@ int force_energy(pcp_model* m, const int* gate, bool zeroed = false,
     bool area = (t == PCP_MODEL_SOFT_BODY || t == PCP_MODEL_AREA_ONLY || t == PCP_MODEL_HYBRID);
     if (overlap) {
         CK(launch_overlap_force(m->pos, m->start, m->next, m->V, m->ws, m->ctrl, m->force, gate,
-                                m->stream, edgeVec));
+                                m->stream, edgeVec, decide, rbCond));
         m->launches++;
     }
     if (edge) {
@@ -601,16 +609,22 @@ int record_fire_step(pcp_model* m, cudaGraphConditionalHandle retryCond,
     // force when the projection takes the one-vertex-per-lane path
     const bool preEdges = shake && project_uses_lanes(m->P, m->nmax);
     if (shake) CK(cudaStreamWaitEvent(st, m->evPreJoin, 0));
-    rc = force_energy(m, gA, true, preEdges ? pre + 2 * (size_t)V : nullptr);
+    // (the rigid model's force pass decides the energy rollback itself)
+    rc = force_energy(m, gA, true, preEdges ? pre + 2 * (size_t)V : nullptr, rigid ? 1 : 0,
+                      rbCond);
     if (rc) return rc;
+    cudaStream_t ifSt = st;
     if (rigid) {
-        CK(launch_project(m->pos, m->start, m->P, m->nmax, m->constraints, m->force, m->scratch, V, 1,
-                          m->ctrl, gA, m->vel, st, rbCond, 1, shake ? pre : nullptr));
+        // the rollback's IF node beside the projection, which does nothing
+        // when the body runs
+        CK(cudaEventRecord(m->evRbFork, st));
+        CK(cudaStreamWaitEvent(m->ifStream, m->evRbFork, 0));
+        ifSt = m->ifStream;
     } else {
         CK(launch_fire_velocity(m->vel, m->force, V, m->ctrl, rbCond, 1, gA, st));
     }
     // energy-increase rollback (model.cpp:450-470) as the body of an IF node
-    rc = begin_if(st, rbCond, m->bodyStream);
+    rc = begin_if(ifSt, rbCond, m->bodyStream);
     if (rc) return rc;
     m->stream = m->bodyStream;
     CK(launch_fire_rollback(m->pos, m->vel, m->force, m->posTMP2, V, needsI ? 1 : 0, m->ctrl,
@@ -637,6 +651,12 @@ int record_fire_step(pcp_model* m, cudaGraphConditionalHandle retryCond,
     if (rc) return rc;
     if (e != cudaSuccess) return fail(PCP_ERR_CUDA, "rollback capture: %s", cudaGetErrorString(e));
     m->rbBodyKernels = count_kernel_nodes(body);
+    if (rigid) {
+        CK(cudaEventRecord(m->evRbJoin, m->ifStream));
+        CK(launch_project(m->pos, m->start, m->P, m->nmax, m->constraints, m->force, m->scratch, V, 1,
+                          m->ctrl, gA, m->vel, st, 1, shake ? pre : nullptr));
+        CK(cudaStreamWaitEvent(st, m->evRbJoin, 0));
+    }
     // the step's scalar bookkeeping ran in the last block of the force pass
     // (or of the rollback body's pass); the velocity bend waits for the next
     // step's start kernel (or for a read of the velocities)
@@ -656,6 +676,9 @@ int build_fire_graph(pcp_model* m, int shakeIter) {
     if (!m->preStream) CK(cudaStreamCreateWithFlags(&m->preStream, cudaStreamNonBlocking));
     if (!m->evPreFork) CK(cudaEventCreateWithFlags(&m->evPreFork, cudaEventDisableTiming));
     if (!m->evPreJoin) CK(cudaEventCreateWithFlags(&m->evPreJoin, cudaEventDisableTiming));
+    if (!m->ifStream) CK(cudaStreamCreateWithFlags(&m->ifStream, cudaStreamNonBlocking));
+    if (!m->evRbFork) CK(cudaEventCreateWithFlags(&m->evRbFork, cudaEventDisableTiming));
+    if (!m->evRbJoin) CK(cudaEventCreateWithFlags(&m->evRbJoin, cudaEventDisableTiming));
     cudaStream_t cap = nullptr;
     CK(cudaStreamCreateWithFlags(&cap, cudaStreamNonBlocking));
     cudaStream_t saved = m->stream;

@@ -36,7 +36,30 @@ __device__ __forceinline__ void fire_step_resets(Ctrl* c) {
     c->needRetry = 0; c->retryGate = 0;
     c->shakeFailed = 0;
     c->rollback = 0; c->rbGate = 0; c->proceed = 0;
-    c->shakeTicket = 0; c->bendTicket = 0;
+    c->shakeTicket = 0; c->bendTicket = 0; c->forceTicket = 0;
+}
+
+// The rollback test at the end of the step's force evaluation
+// (model.cpp:450-453): the velocities advance unless SHAKE failed or the
+// energy went up, and the energy-increase rollback runs next when the energy
+// went up and SHAKE did not fail.  One thread; `publish` stores the outcome
+// (proceed, rbGate) and sets `rbCond` when `useCond`.  The energy is read
+// past L1 (other blocks of the calling kernel may have just added to it).
+// Returns proceed | rbNext << 1.
+__device__ __forceinline__ int fire_decide(Ctrl* __restrict__ c, bool publish,
+                                           cudaGraphConditionalHandle rbCond, int useCond) {
+    const double E = __ldcg(&c->energy), E0 = __ldcg(&c->ePre);
+    const int failed = __ldcg(&c->shakeFailed), rollback = __ldcg(&c->rollback);
+    const int active = __ldcg(&c->active);
+    const bool rb = E > E0 + fmax(fabs(E0) * 1e-10, 1e-14);
+    const bool proceed = !failed && !rb && rollback == 0;
+    const bool rbNext = rollback == 0 && !failed && rb && active;
+    if (publish && rollback == 0) {
+        c->proceed = proceed ? 1 : 0;
+        c->rbGate = rbNext ? 1 : 0;
+        if (useCond) cudaGraphSetConditional(rbCond, rbNext ? 1u : 0u);
+    }
+    return (proceed ? 1 : 0) | (rbNext ? 2 : 0);
 }
 
 // The previous step's velocity bend (model.cpp:471-484, Ctrl::bendMode),

@@ -75,6 +75,9 @@ struct Ctrl {
     // + bendS F, 2 v <- 0
     int bendMode;
     double bendA, bendS;
+    // blocks of the step's force pass finished (its last one decides the
+    // energy rollback)
+    unsigned int forceTicket;
 };
 
 enum : unsigned int {
@@ -170,23 +173,26 @@ cudaError_t launch_prepass_move(double2* verlet, const int* start, int* cellOut,
 cudaError_t launch_contacts_finish(const int* start, ContactWS& ws, Ctrl* ctrl,
                                    const int* gate, cudaStream_t st);
 // edge: the edge vectors wrap(x_next - x) of pos, or nullptr
+// decide: the FIRE step's force pass; its last block decides the energy
+// rollback (model.cpp:450-453) and sets `rbCond` of the step graph
 cudaError_t launch_overlap_force(const double2* pos, const int* start, const int* next,
                                  int V, ContactWS& ws, Ctrl* ctrl, double2* force,
-                                 const int* gate, cudaStream_t st, const double2* edge = nullptr);
+                                 const int* gate, cudaStream_t st, const double2* edge = nullptr,
+                                 int decide = 0, cudaGraphConditionalHandle rbCond = 0);
 
 // constraints
 cudaError_t constraints_init();
 // nmax: largest vertex count of a polygon (decides whether the per-polygon
 // scratch fits in shared memory)
-// useCond: the projection decides the FIRE step's energy rollback and sets
-// `rbCond` of the step graph
+// mainPass: the FIRE step's own pass after a force pass that decided the
+// energy rollback (launch_overlap_force with decide): the pass reads that
+// decision and does nothing when the rollback runs
 // pre ([2V] double2: unit edge tangents, then unit area gradients): when
 // non-null, the values launch_project_pre stored for the current positions
 cudaError_t launch_project(const double2* pos, const int* start, int P, int nmax,
                            const double* constraints, double2* force, double* scratch, int V,
                            int areaFromPositions, Ctrl* fireCtrl, const int* gate, double2* vel,
-                           cudaStream_t st, cudaGraphConditionalHandle rbCond = 0,
-                           int useCond = 0, const double2* pre = nullptr);
+                           cudaStream_t st, int mainPass = 0, const double2* pre = nullptr);
 // whether launch_project runs its register (one vertex per lane) form, the
 // only one that reads `pre`
 bool project_uses_lanes(int P, int nmax);
