@@ -1137,10 +1137,15 @@ k_narrow(const double2* __restrict__ pos, const int* __restrict__ start, int B,
         return -1;
     };
 
-    // pairs dealt out round robin (warp w takes w, w + W, ...): no claim
-    // atomics on the hot path
-    const int warpsTotal = gridDim.x * kNarrowWarps;
-    int q = blockIdx.x * kNarrowWarps + (threadIdx.x >> 5);
+    // pairs claimed one at a time from a shared cursor, the next one while
+    // the current one is processed: warps whose blocks became resident
+    // late (beside another kernel of the step) take fewer pairs
+    auto claim = [&]() -> int {
+        int v = 0;
+        if (lane == 0) v = atomicAdd(&ctrl->pairCursor, 1);
+        return __shfl_sync(PCP_FULL, v, 0);
+    };
+    int q = claim();
     auto issue = [&](int qq, int stage) -> bool {
         // returns true when a copy was issued for pair qq into `stage`
         if (qq >= numPairs) return false;
@@ -1178,7 +1183,7 @@ k_narrow(const double2* __restrict__ pos, const int* __restrict__ start, int B,
     int stage = 0;
     bool inflight = issue(q, stage);
     while (q < numPairs) {
-        const int qn = q + warpsTotal;
+        const int qn = claim();
         PairCtx pc = make_ctx(ws.pairs[q], start);
         if (!inflight) {
             // too large (or degenerate) for the warp path: hand to the block path
@@ -1280,6 +1285,9 @@ k_narrow_slow(const double2* __restrict__ pos, const int* __restrict__ start, in
               ContactWS ws, Ctrl* __restrict__ ctrl, const int* gate) {
     pdl_enter();
     if (gate_closed(gate)) return;
+    // k_narrow has finished claiming: its cursor back to 0 for a rerun of
+    // the narrow phase alone
+    if (blockIdx.x == 0 && threadIdx.x == 0) ctrl->pairCursor = 0;
     extern __shared__ __align__(128) unsigned char smem_raw[];
     float4* ring = reinterpret_cast<float4*>(smem_raw);                    // kSlowRing
     EdgeCand* cand = reinterpret_cast<EdgeCand*>(ring + kSlowRing);          // kSlowRing
