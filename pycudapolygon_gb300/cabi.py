@@ -49,7 +49,8 @@ _ip = ctypes.POINTER(ctypes.c_int)
 
 
 def _dptr(a):
-    return a.ctypes.data_as(_dp)
+    # a void* of the data (cheaper than data_as; the functions are unprototyped)
+    return ctypes.c_void_p(a.ctypes.data)
 
 
 def _iptr(a):
@@ -62,6 +63,7 @@ class CModel:
     def __init__(self, size):
         self.L = lib()
         self.h = ctypes.c_void_p()
+        self._out4 = (ctypes.c_double * 4)()
         _ck(self.L.pcp_model_create(_I(int(size)), ctypes.byref(self.h)))
 
     def close(self):
@@ -137,9 +139,9 @@ class CModel:
 
     def fire_step(self, dt, alpha, n_pos, dt_max=0.1, alpha_start=0.1, f_alpha=0.99,
                   f_inc=1.1, f_dec=0.5, n_min=5, shake_iter=5):
-        out = np.zeros(4)
+        out = self._out4
         self.call("fire_step", _D(dt), _D(alpha), _I(n_pos), _D(dt_max), _D(alpha_start),
-                  _D(f_alpha), _D(f_inc), _D(f_dec), _I(n_min), _I(shake_iter), _dptr(out))
+                  _D(f_alpha), _D(f_inc), _D(f_dec), _I(n_min), _I(shake_iter), out)
         return float(out[0]), float(out[1]), float(out[2]), int(out[3])
 
     def minimize_fire(self, thr, dt0, max_steps, dt_max=0.1, alpha_start=0.1, f_alpha=0.99,
