@@ -1405,90 +1405,98 @@ k_overlap_force(const double2* __restrict__ pos, const int* __restrict__ start,
          base += warpsTotal * kForceRecs) {
         const int r = base + (lane >> 1);
         bool valid = r < I;
+        // round 1: the record (keys and both crossing parameters)
         unsigned long long inter = 0, outer = 0;
-        if (valid) { inter = ws.recKey[r]; outer = ws.recOuter[r]; }
-        valid = valid && inter != outer;
-        int start1 = 0, n1 = 0, iLoc = 0, lLoc = 0, lDist = 0;
-        int4 idx4 = make_int4(0, 0, 0, 0);        // vertices i, j, k, l
-        double2 sp = make_double2(0.0, 0.0);
+        float tRec = 0.f, uRec = 0.f;
         if (valid) {
-            int s1 = (int)((inter >> 32) & 0xFFFF), s2 = (int)(inter >> 48);
+            inter = ws.recKey[r]; outer = ws.recOuter[r];
+            tRec = ws.recTU[r].y; uRec = ws.recUT[r].y;
+        }
+        valid = valid && inter != outer;
+        // round 2: both polygons' vertex ranges.  The topology is the CSR
+        // one (next = the following vertex of the polygon, cyclic), so every
+        // vertex index below is formed without reading `next`.
+        int start1 = 0, n1 = 0, iLoc = 0, lLoc = 0, lDist = 0;
+        int a = 0, za = 0, v0 = 0, v1 = 0, v2 = 0, v3 = 0;
+        bool same = false;
+        if (valid) {
+            const int s1 = (int)((inter >> 32) & 0xFFFF), s2 = (int)(inter >> 48);
             iLoc = (int)((inter >> 16) & 0xFFFF);
-            int jLoc = (int)(inter & 0xFFFF);
-            int kLoc = (int)((outer >> 16) & 0xFFFF);
+            const int jLoc = (int)(inter & 0xFFFF);
+            const int kLoc = (int)((outer >> 16) & 0xFFFF);
             lLoc = (int)(outer & 0xFFFF);
             start1 = start[s1];
-            int start2 = start[s2];
-            n1 = start[s1 + 1] - start1;
-            int i = start1 + iLoc, j = start2 + jLoc, k = start2 + kLoc, l = start1 + lLoc;
-            if (i >= V || j >= V || k >= V || l >= V) {
+            const int end1 = start[s1 + 1];
+            const int start2 = start[s2], end2 = start[s2 + 1];
+            n1 = end1 - start1;
+            const int n2 = end2 - start2;
+            const int i = start1 + iLoc, j = start2 + jLoc, k = start2 + kLoc, l = start1 + lLoc;
+            if (i >= V || j >= V || k >= V || l >= V || iLoc >= n1 || lLoc >= n1 || jLoc >= n2 ||
+                kLoc >= n2) {
                 if (half == 0) atomicOr(&ctrl->flags, kFlagNonFinite);
                 valid = false;
                 n1 = 0;
             } else {
-                idx4 = make_int4(i, j, k, l);
-            }
-        }
-        // the crossing points: the even lane of the pair takes f_ij on edge
-        // (i, zi), the odd one f_kl on edge (k, zk), and they swap them
-        double2 pa = make_double2(0.0, 0.0), pza = pa, ra = pa, fa = pa;
-        int za = 0;
-        if (valid) {
-            const int a = half ? idx4.z : idx4.x;
-            za = next[a];
-            pa = pos[a];
-            pza = pos[za];
-            ra = kEdge ? edge[a] : make_double2(wrap(pza.x - pa.x), wrap(pza.y - pa.y));
-            const double ta = f2d_int(half ? ws.recUT[r].y : ws.recTU[r].y);
-            fa = make_double2(wrap(pa.x + ta * ra.x), wrap(pa.y + ta * ra.y));
-        }
-        const double2 fo = make_double2(__shfl_xor_sync(PCP_FULL, fa.x, 1),
-                                        __shfl_xor_sync(PCP_FULL, fa.y, 1));
-        if (valid) {
-            {
-                const int i = idx4.x, j = idx4.y, k = idx4.z, l = idx4.w;
-                // even lane: a = i (za = zi); odd lane: a = k (za = zk)
-                const double2 fij = half ? fo : fa, fkl = half ? fa : fo;
-                sp = fij;
+                auto nx1 = [&](int loc) { return start1 + (loc + 1 == n1 ? 0 : loc + 1); };
+                auto nx2 = [&](int loc) { return start2 + (loc + 1 == n2 ? 0 : loc + 1); };
                 // Both lanes of the pair run one h/g12 and one gDf on operands
                 // chosen by parity (no divergent branches):
                 //   i == l : h(fij, fkl); even: gDf(i, zi, j, zj) . g1,
                 //            odd: gDf(k, zk, i, zi) . g2; energy once
                 //   i != l : even: h(fij, zi), gDf(i, zi, j, zj) . g1, zi += g2;
                 //            odd: h(l, fkl), gDf(k, zk, l, zl) . g2, l += g1
-                const bool same = (i == l);
-                int v0, v1, v2, v3;
-                if (half == 0) { v0 = i; v1 = za; v2 = j; v3 = next[j]; }
-                else if (same) { v0 = k; v1 = za; v2 = i; v3 = next[i]; }
-                else { v0 = k; v1 = za; v2 = l; v3 = next[l]; }
-                const double2 q0 = pa;                 // p_i (even) or p_k (odd)
-                double2 q2 = pos[v2];
-                double2 hA = (!same && half) ? q2 : fij;
-                double2 hB = (same || half) ? fkl : pza;
-                double dyg, sx;
-                double eh = h_parts(hA, hB, sp, dyg, sx);
-                if (!same || half == 0) eLocal += eh;
-                // gDf is linear in g: with -g it gives the force terms
-                // directly (g1 = (dyg, -sx) on the even lane, g2 = (dyg, sx)
-                // on the odd one; x1 = g2 moves zi, x2 = g1 moves l)
-                const double ndy = neg_int(dyg), nsx = neg_int(sx);
-                const double2 ng = make_double2(ndy, half ? nsx : sx);
-                const double2 nx1 = (!same && !half) ? make_double2(ndy, nsx) : make_double2(0.0, 0.0);
-                const double2 nx2 = (!same && half) ? make_double2(ndy, sx) : make_double2(0.0, 0.0);
-                double2 o[4];
-                // q1 - q0 is this lane's own edge; q3 - q2 the other polygon's
-                if (kEdge) {
-                    gDf_dd(q0, ra, q2, edge[v2], ng, o);
-                } else {
-                    const double2 q3 = pos[v3];
-                    gDf_di(q0, ra, q2, q3, ng, o);
-                }
-                add_f(force, v0, o[0].x, o[0].y);
-                add_f(force, v1, o[1].x + nx1.x, o[1].y + nx1.y);
-                add_f(force, v2, o[2].x + nx2.x, o[2].y + nx2.y);
-                add_f(force, v3, o[3].x, o[3].y);
-                if (n1 > 0) lDist = ((lLoc - iLoc) % n1 + n1) % n1;
+                same = (i == l);
+                a = half ? k : i;                        // this lane's edge (a, za)
+                za = half ? nx2(kLoc) : nx1(iLoc);
+                v0 = a; v1 = za;
+                if (half == 0) { v2 = j; v3 = nx2(jLoc); }
+                else if (same) { v2 = i; v3 = nx1(iLoc); }
+                else { v2 = l; v3 = nx1(lLoc); }
             }
+        }
+        // round 3: the vertices.  The crossing points: the even lane of the
+        // pair takes f_ij on edge (i, zi), the odd one f_kl on edge (k, zk),
+        // and they swap them.
+        double2 pa = make_double2(0.0, 0.0), pza = pa, ra = pa, fa = pa, q2 = pa, d3 = pa;
+        double2 sp = make_double2(0.0, 0.0);
+        if (valid) {
+            pa = pos[a];
+            pza = pos[za];
+            q2 = pos[v2];
+            if (kEdge) { ra = edge[a]; d3 = edge[v2]; }
+            else {
+                const double2 q3 = pos[v3];
+                ra = make_double2(wrap(pza.x - pa.x), wrap(pza.y - pa.y));
+                d3 = make_double2(wrap(q3.x - q2.x), wrap(q3.y - q2.y));
+            }
+            const double ta = f2d_int(half ? uRec : tRec);
+            fa = make_double2(wrap(pa.x + ta * ra.x), wrap(pa.y + ta * ra.y));
+        }
+        const double2 fo = make_double2(__shfl_xor_sync(PCP_FULL, fa.x, 1),
+                                        __shfl_xor_sync(PCP_FULL, fa.y, 1));
+        if (valid) {
+            const double2 fij = half ? fo : fa, fkl = half ? fa : fo;
+            sp = fij;
+            double2 hA = (!same && half) ? q2 : fij;
+            double2 hB = (same || half) ? fkl : pza;
+            double dyg, sx;
+            double eh = h_parts(hA, hB, sp, dyg, sx);
+            if (!same || half == 0) eLocal += eh;
+            // gDf is linear in g: with -g it gives the force terms directly
+            // (g1 = (dyg, -sx) on the even lane, g2 = (dyg, sx) on the odd
+            // one; x1 = g2 moves zi, x2 = g1 moves l)
+            const double ndy = neg_int(dyg), nsx = neg_int(sx);
+            const double2 ng = make_double2(ndy, half ? nsx : sx);
+            const double2 nx1v = (!same && !half) ? make_double2(ndy, nsx) : make_double2(0.0, 0.0);
+            const double2 nx2v = (!same && half) ? make_double2(ndy, sx) : make_double2(0.0, 0.0);
+            double2 o[4];
+            // (a, za) is this lane's own edge; (v2, v3) the other one
+            gDf_dd(pa, ra, q2, d3, ng, o);
+            add_f(force, v0, o[0].x, o[0].y);
+            add_f(force, v1, o[1].x + nx1v.x, o[1].y + nx1v.y);
+            add_f(force, v2, o[2].x + nx2v.x, o[2].y + nx2v.y);
+            add_f(force, v3, o[3].x, o[3].y);
+            if (n1 > 0) lDist = ((lLoc - iLoc) % n1 + n1) % n1;
         }
         // interior chains: the even lane of each pair owns its record's chain
         int cnt = (valid && half == 0 && lDist > 1) ? lDist - 1 : 0;
@@ -1499,7 +1507,15 @@ k_overlap_force(const double2* __restrict__ pos, const int* __restrict__ start,
             if (lane >= d) incl += t;
         }
         const int total = __shfl_sync(PCP_FULL, incl, 31);
-        for (int b = 0; b < total; b += 32) {
+        // rounds of 32 chain edges, one per lane; the vertices of the next
+        // round are fetched before this round's arithmetic
+        struct ChainItem {
+            double2 pm, pn, sp;      // pn: the edge vector when kEdge
+            int mv, nv;
+            bool live;
+        };
+        auto fetch = [&](int b) -> ChainItem {
+            ChainItem c;
             const int item = b + lane;
             // owner = first lane whose inclusive count exceeds item
             int own = 0;
@@ -1508,29 +1524,43 @@ k_overlap_force(const double2* __restrict__ pos, const int* __restrict__ start,
                 int v = __shfl_sync(PCP_FULL, incl, own + w - 1);
                 if (v <= item) own += w;
             }
-            int oIncl = __shfl_sync(PCP_FULL, incl, own);
-            int oCnt = __shfl_sync(PCP_FULL, cnt, own);
-            int oStart = __shfl_sync(PCP_FULL, start1, own);
-            int oN = __shfl_sync(PCP_FULL, n1, own);
-            int oI = __shfl_sync(PCP_FULL, iLoc, own);
-            double2 osp = make_double2(__shfl_sync(PCP_FULL, sp.x, own),
-                                       __shfl_sync(PCP_FULL, sp.y, own));
-            if (item < total) {
-                int step = item - (oIncl - oCnt) + 1;
-                int mLoc = oI + step;
+            const int oIncl = __shfl_sync(PCP_FULL, incl, own);
+            const int oCnt = __shfl_sync(PCP_FULL, cnt, own);
+            const int oStart = __shfl_sync(PCP_FULL, start1, own);
+            const int oN = __shfl_sync(PCP_FULL, n1, own);
+            const int oI = __shfl_sync(PCP_FULL, iLoc, own);
+            c.sp = make_double2(__shfl_sync(PCP_FULL, sp.x, own), __shfl_sync(PCP_FULL, sp.y, own));
+            c.live = item < total;
+            c.mv = 0; c.nv = 0;
+            c.pm = c.pn = make_double2(0.0, 0.0);
+            if (c.live) {
+                int mLoc = oI + item - (oIncl - oCnt) + 1;
                 if (mLoc >= oN) mLoc -= oN;
-                int mv = oStart + mLoc;
-                int nv = next[mv];
-                double dyg, sx;
-                if (kEdge) {
-                    dyg = edge[mv].y;
-                    eLocal += h_parts_dy(pos[mv], pos[nv], osp, dyg, sx);
-                } else {
-                    eLocal += h_parts(pos[mv], pos[nv], osp, dyg, sx);
+                c.mv = oStart + mLoc;
+                c.nv = oStart + (mLoc + 1 == oN ? 0 : mLoc + 1);   // next[mv]
+                c.pm = pos[c.mv];
+                c.pn = kEdge ? edge[c.mv] : pos[c.nv];
+            }
+            return c;
+        };
+        if (total > 0) {
+            ChainItem cur = fetch(0);
+            for (int b = 0; b < total; b += 32) {
+                ChainItem nxt = cur;
+                if (b + 32 < total) nxt = fetch(b + 32);
+                if (cur.live) {
+                    double dyg, sx;
+                    if (kEdge) {
+                        dyg = cur.pn.y;
+                        eLocal += h_parts_edge(cur.pm, cur.pn, cur.sp, sx);
+                    } else {
+                        eLocal += h_parts(cur.pm, cur.pn, cur.sp, dyg, sx);
+                    }
+                    const double ndy = neg_int(dyg);
+                    add_f(force, cur.mv, ndy, sx);             // -g1
+                    add_f(force, cur.nv, ndy, neg_int(sx));    // -g2
                 }
-                const double ndy = neg_int(dyg);
-                add_f(force, mv, ndy, sx);             // -g1
-                add_f(force, nv, ndy, neg_int(sx));    // -g2
+                cur = nxt;
             }
         }
     }
