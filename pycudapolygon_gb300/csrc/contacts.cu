@@ -686,16 +686,32 @@ __device__ __forceinline__ void prefetch_l1(const void* p) {
 // Culls 1 and 2 of a staged pair: fills candA / candB with the edges whose
 // boxes meet the overlap box (self pair: candA only) and returns their
 // counts through nLA / nLB (0 when the polygon boxes are disjoint).
+// The per-polygon records the culls read: longest edges, flags and boxes of
+// the pair's two polygons.
+struct PairRecs {
+    float LA, LB;
+    int flagA, flagB;
+    float4 boxA, boxB;
+};
+__device__ __forceinline__ PairRecs load_pair_recs(const PairCtx& pc,
+                                                   const float4* __restrict__ polyInfo,
+                                                   const float4* __restrict__ polyBox,
+                                                   const int* __restrict__ polyFlags) {
+    PairRecs r;
+    r.LA = polyInfo[pc.a].w; r.LB = polyInfo[pc.b].w;
+    r.flagA = polyFlags[pc.a]; r.flagB = polyFlags[pc.b];
+    r.boxA = polyBox[pc.a]; r.boxB = polyBox[pc.b];
+    return r;
+}
+
 __device__ void narrow_cull(const PairCtx& pc, const float4* ringA, const float4* ringB,
-                            EdgeCand* candA, EdgeCand* candB,
-                            const float4* __restrict__ polyInfo,
-                            const float4* __restrict__ polyBox,
-                            const int* __restrict__ polyFlags, int& nLAout, int& nLBout) {
+                            EdgeCand* candA, EdgeCand* candB, const PairRecs& pr,
+                            int& nLAout, int& nLBout) {
     const int lane = threadIdx.x & 31;
     const unsigned lt = (1u << lane) - 1u;
     const int nA = pc.nA, nB = pc.nB;
     const float f0x = ringA[0].x, f0y = ringA[0].y;
-    const float LA = polyInfo[pc.a].w, LB = polyInfo[pc.b].w;
+    const float LA = pr.LA, LB = pr.LB;
     const float m = 4e-6f + 1e-3f * LA * LB;
     // polygon boxes in A's frame.  Two well-formed polygons (extent < 0.2,
     // and a candidate pair lies within 0.4 of A's vertex 0, so nothing wraps):
@@ -704,11 +720,11 @@ __device__ void narrow_cull(const PairCtx& pc, const float4* ringA, const float4
     // widened by 1e-6 for the rounding of the move.  Otherwise the boxes are
     // measured from the rings here.
     float ox0, ox1, oy0, oy1;
-    if (polyFlags[pc.a] && polyFlags[pc.b]) {
-        const float4 ba = polyBox[pc.a];
+    if (pr.flagA && pr.flagB) {
+        const float4 ba = pr.boxA;
         ox0 = ba.x - m; ox1 = ba.y + m; oy0 = ba.z - m; oy1 = ba.w + m;
         if (!pc.self) {
-            const float4 bb = polyBox[pc.b];
+            const float4 bb = pr.boxB;
             const float sx = wrapf(ringB[0].x - f0x), sy = wrapf(ringB[0].y - f0y);
             ox0 = fmaxf(ba.x, bb.x + sx - 1e-6f) - m; ox1 = fminf(ba.y, bb.y + sx + 1e-6f) + m;
             oy0 = fmaxf(ba.z, bb.z + sy - 1e-6f) - m; oy1 = fminf(ba.w, bb.w + sy + 1e-6f) + m;
@@ -777,7 +793,8 @@ __device__ int narrow_pair(const PairCtx& pc, const float4* ringA, const float4*
     const unsigned lt = (1u << lane) - 1u;
     const int nA = pc.nA;
     int nLA = 0, nLB = 0;
-    narrow_cull(pc, ringA, ringB, candA, candB, polyInfo, polyBox, polyFlags, nLA, nLB);
+    narrow_cull(pc, ringA, ringB, candA, candB, load_pair_recs(pc, polyInfo, polyBox, polyFlags),
+                nLA, nLB);
     if (nLA == 0 || nLB == 0) return 0;
     const EdgeCand* cb = pc.self ? candA : candB;
     bool wrapB = B >= 3;
@@ -1146,11 +1163,19 @@ k_narrow(const double2* __restrict__ pos, const int* __restrict__ start, int B,
         return __shfl_sync(PCP_FULL, v, 0);
     };
     int q = claim();
-    auto issue = [&](int qq, int stage) -> bool {
+    // the culls' per-polygon records, loaded into registers one pair ahead:
+    // lanes 0/1 polyInfo of a/b, 2/3 polyBox of a/b, 4/5 polyFlags of a/b
+    auto issue = [&](int qq, int stage, float4& rec) -> bool {
         // returns true when a copy was issued for pair qq into `stage`
         if (qq >= numPairs) return false;
         PairCtx pc = make_ctx(ws.pairs[qq], start);
         if (pc.nA > kFastRing || pc.nB > kFastRing || pc.nA < 3 || pc.nB < 3) return false;
+        if (lane < 6) {
+            const int pp = (lane & 1) ? pc.b : pc.a;
+            rec = lane < 2 ? ws.polyInfo[pp]
+                : lane < 4 ? ws.polyBox[pp]
+                           : make_float4(__int_as_float(ws.polyFlags[pp]), 0.f, 0.f, 0.f);
+        }
         if (lane == 0) {
             // order this warp's earlier generic reads of the buffer before the
             // async-proxy writes that refill it
@@ -1161,14 +1186,9 @@ k_narrow(const double2* __restrict__ pos, const int* __restrict__ start, int B,
             bulk_g2s(&S.ring[stage][0], ws.vtx + pc.stA, bytesA, &S.bar[stage]);
             if (!pc.self) bulk_g2s(&S.ring[stage][kFastRing], ws.vtx + pc.stB, bytesB, &S.bar[stage]);
         }
-        // the culls' per-polygon records and the FP64 rings of the exact test
-        // into L1 while the current pair is processed (lines of 8 vertices)
-        if (lane < 6) {
-            const int pp = (lane & 1) ? pc.b : pc.a;
-            const void* src = lane < 2 ? (const void*)(ws.polyInfo + pp)
-                            : lane < 4 ? (const void*)(ws.polyBox + pp) : (const void*)(ws.polyFlags + pp);
-            prefetch_l1(src);
-        } else if (lane >= 8 && lane < 24) {
+        // the FP64 rings of the exact test into L1 while the current pair is
+        // processed (lines of 8 vertices)
+        if (lane >= 8 && lane < 24) {
             const int k = lane & 7;                  // line k of a ring (8 vertices of 16 B)
             const bool ringB = lane >= 16;
             const int st0 = ringB ? pc.stB : pc.stA, n0 = ringB ? pc.nB : pc.nA;
@@ -1181,20 +1201,22 @@ k_narrow(const double2* __restrict__ pos, const int* __restrict__ start, int B,
     };
     const bool wrapB = B >= 3;
     int stage = 0;
-    bool inflight = issue(q, stage);
+    float4 recCur = make_float4(0.f, 0.f, 0.f, 0.f);
+    bool inflight = issue(q, stage, recCur);
     while (q < numPairs) {
         const int qn = claim();
         PairCtx pc = make_ctx(ws.pairs[q], start);
         if (!inflight) {
             // too large (or degenerate) for the warp path: hand to the block path
             if (lane == 0 && pc.nA >= 1 && pc.nB >= 1) push_slow(q, ctrl, ws);
-            inflight = issue(qn, stage);
+            inflight = issue(qn, stage, recCur);
             q = qn;
             continue;
         }
         // prefetch the next pair into the other buffer while this one is processed
         int other = stage ^ 1;
-        bool nextInflight = issue(qn, other);
+        float4 recNext = recCur;
+        bool nextInflight = issue(qn, other, recNext);
         if (!mbar_wait_bounded(&S.bar[stage], phase[stage], ctrl)) {
             // the copy never landed: wait (bounded) for the prefetch too, then stop
             if (nextInflight) mbar_wait_bounded(&S.bar[other], phase[other], ctrl);
@@ -1218,8 +1240,16 @@ k_narrow(const double2* __restrict__ pos, const int* __restrict__ start, int B,
         const float4* ringA = &S.ring[stage][0];
         const float4* ringB = pc.self ? ringA : &S.ring[stage][kFastRing];
         int nLA = 0, nLB = 0;
-        narrow_cull(pc, ringA, ringB, S.candA, S.candB, ws.polyInfo, ws.polyBox, ws.polyFlags,
-                    nLA, nLB);
+        PairRecs pr;
+        pr.LA = __shfl_sync(PCP_FULL, recCur.w, 0);
+        pr.LB = __shfl_sync(PCP_FULL, recCur.w, 1);
+        pr.boxA = make_float4(__shfl_sync(PCP_FULL, recCur.x, 2), __shfl_sync(PCP_FULL, recCur.y, 2),
+                              __shfl_sync(PCP_FULL, recCur.z, 2), __shfl_sync(PCP_FULL, recCur.w, 2));
+        pr.boxB = make_float4(__shfl_sync(PCP_FULL, recCur.x, 3), __shfl_sync(PCP_FULL, recCur.y, 3),
+                              __shfl_sync(PCP_FULL, recCur.z, 3), __shfl_sync(PCP_FULL, recCur.w, 3));
+        pr.flagA = __float_as_int(__shfl_sync(PCP_FULL, recCur.x, 4));
+        pr.flagB = __float_as_int(__shfl_sync(PCP_FULL, recCur.x, 5));
+        narrow_cull(pc, ringA, ringB, S.candA, S.candB, pr, nLA, nLB);
         const EdgeCand* cb = pc.self ? S.candA : S.candB;
         const int nA = pc.nA, nB = pc.nB;
         // candidate edge pairs as (aw x bw) lane tiles: lane = a * bw + b
@@ -1270,6 +1300,7 @@ k_narrow(const double2* __restrict__ pos, const int* __restrict__ start, int B,
         finalize_ready();
         stage = other;
         inflight = nextInflight;
+        recCur = recNext;
         q = qn;
     }
     if (qn_ > 0) run_batch(qn_);
