@@ -975,7 +975,7 @@ __device__ unsigned long long match_and_write(const PairCtx& pc, int R,
         unsigned long long t = __shfl_xor_sync(PCP_FULL, kmax, o);
         kmax = t > kmax ? t : kmax;
     }
-    // the largest key (k_fixup's partner of last resort): published here, or
+    // the largest key (fixup_records' partner of last resort): published here, or
     // gathered by the caller and published once
     if (publishMax && lane == 0 && R > 0) atomicMax(&ctrl->maxKey, kmax);
     return kmax;
@@ -1311,6 +1311,8 @@ k_narrow(const double2* __restrict__ pos, const int* __restrict__ start, int B,
 // Block path: one warp per block, rings loaded with plain loads into a large
 // dynamic shared-memory area; for polygons above kFastRing vertices and for
 // pairs with more than kFastRecords crossings.
+__device__ void fixup_records(ContactWS& ws, Ctrl* __restrict__ ctrl);
+
 __global__ void __launch_bounds__(32)
 k_narrow_slow(const double2* __restrict__ pos, const int* __restrict__ start, int B,
               ContactWS ws, Ctrl* __restrict__ ctrl, const int* gate) {
@@ -1356,40 +1358,49 @@ k_narrow_slow(const double2* __restrict__ pos, const int* __restrict__ start, in
         }
         __syncwarp();
     }
+    // every record is written once the last block gets here (the fast
+    // path's before this kernel started): it fixes the empty-group records
+    if (lane == 0) __threadfence();
+    __syncwarp();
+    unsigned int t = 0;
+    if (lane == 0) t = atomicAdd(&ctrl->slowDone, 1u);
+    t = __shfl_sync(PCP_FULL, t, 0);
+    if (t == gridDim.x - 1) {
+        __threadfence();
+        fixup_records(ws, ctrl);
+    }
 }
 
 // A crossing whose reverse group is empty: the reference's binary search
 // (kernels.cuh:993-1000) stops at the last record when every key is below
 // sij, and that record is then tried as the partner.  Reproduced here.
-__global__ void k_fixup(const int* __restrict__ start, ContactWS ws, Ctrl* __restrict__ ctrl,
-                        const int* gate) {
-    pdl_enter();
-    if (gate_closed(gate)) return;
-    int nf = min(ctrl->numFix, ws.capFix);
+// Run by one warp once every record is written (the last block of the block
+// path); the records of other blocks are read past L1.
+__device__ void fixup_records(ContactWS& ws, Ctrl* __restrict__ ctrl) {
+    const int lane = threadIdx.x & 31;
+    const int nf = min((int)__ldcg(&ctrl->numFix), ws.capFix);
     if (nf == 0) return;
-    int I = min(ctrl->numRecords, ws.capRecords);
-    unsigned long long kmax = ctrl->maxKey;
+    const int I = min((int)__ldcg(&ctrl->numRecords), ws.capRecords);
+    const unsigned long long kmax = __ldcg(&ctrl->maxKey);
     // locate the record holding the largest key (keys are unique)
-    __shared__ int s_idx;
-    if (threadIdx.x == 0) s_idx = -1;
-    __syncthreads();
-    for (int g = threadIdx.x; g < I; g += blockDim.x)
-        if (ws.recKey[g] == kmax) s_idx = g;
-    __syncthreads();
-    int mi = s_idx;
+    int mi = -1;
+    for (int g0 = 0; g0 < I; g0 += 32) {
+        const int g = g0 + lane;
+        const unsigned hit = __ballot_sync(PCP_FULL, g < I && __ldcg(&ws.recKey[g]) == kmax);
+        if (hit) { mi = g0 + __ffs(hit) - 1; break; }
+    }
     if (mi < 0) return;
-    float2 tuMax = ws.recTU[mi];
-    for (int f = threadIdx.x; f < nf; f += blockDim.x) {
-        int g = ws.fixList[f];
-        unsigned long long key = ws.recKey[g];
-        int sj = (int)(key >> 48), si = (int)((key >> 32) & 0xFFFF);
-        int i = (int)((key >> 16) & 0xFFFF);
-        unsigned long long sij = ((unsigned long long)si << 48) | ((unsigned long long)sj << 32);
+    const float2 tuMax = __ldcg(&ws.recTU[mi]);
+    for (int f = lane; f < nf; f += 32) {
+        const int g = __ldcg(&ws.fixList[f]);
+        const unsigned long long key = __ldcg(&ws.recKey[g]);
+        const int sj = (int)(key >> 48), si = (int)((key >> 32) & 0xFFFF);
+        const int i = (int)((key >> 16) & 0xFFFF);
+        const unsigned long long sij = ((unsigned long long)si << 48) | ((unsigned long long)sj << 32);
         if (!(sij > kmax)) continue;
-        int l = (int)(kmax & 0xFFFF);
-        float tVal = ws.recTU[g].y;
+        const int l = (int)(kmax & 0xFFFF);
+        const float tVal = __ldcg(&ws.recTU[g]).y;
         if (l == i && tVal >= tuMax.x) continue;
-        (void)start;
         ws.recOuter[g] = kmax;
         ws.recUT[g] = tuMax;
     }
@@ -1683,11 +1694,6 @@ cudaError_t launch_prepass_move(double2* verlet, const int* start, int* cellOut,
     return cudaGetLastError();
 }
 
-cudaError_t launch_contacts_finish(const int* start, ContactWS& ws, Ctrl* ctrl,
-                                   const int* gate, cudaStream_t st) {
-    launch_k(k_fixup, dim3(1), dim3(1024), 0, st, start, ws, ctrl, gate);
-    return cudaGetLastError();
-}
 
 cudaError_t launch_overlap_force(const double2* pos, const int* start, const int* next,
                                  int V, ContactWS& ws, Ctrl* ctrl, double2* force,

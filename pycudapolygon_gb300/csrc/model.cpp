@@ -569,7 +569,6 @@ int record_fire_step(pcp_model* m, cudaGraphConditionalHandle retryCond,
         CK(launch_contacts(m->posTMP, m->start, m->shapeId, m->cellLocation, m->P, V,
                            m->boxSize, m->ws, m->ctrl, gA, m->sideStream,
                            noReset | kContactsNoPrepass, m->cellLocation));
-        CK(launch_contacts_finish(m->start, m->ws, m->ctrl, gA, m->sideStream));
         CK(cudaEventRecord(m->evJoin, m->sideStream));
         // SHAKE rederives v from its displacement itself (model.cpp:436-438)
         CK(launch_shake(m->pos, m->start, m->P, m->nmax, m->targetEdge, m->targetAreas,
@@ -595,7 +594,6 @@ int record_fire_step(pcp_model* m, cudaGraphConditionalHandle retryCond,
         CK(launch_contacts(m->pos, m->start, m->shapeId, m->cellLocation, m->P, V, m->boxSize,
                            m->ws, m->ctrl, gA, st, noReset | kContactsNoPrepass,
                            m->cellLocation));
-        CK(launch_contacts_finish(m->start, m->ws, m->ctrl, gA, st));
     }
     // The normal model reads nothing of the geometry inside the step (the
     // projection takes the area gradient from the positions), so the
@@ -634,7 +632,6 @@ int record_fire_step(pcp_model* m, cudaGraphConditionalHandle retryCond,
         cudaError_t e = launch_contacts(m->pos, m->start, m->shapeId, m->cellLocation, m->P, V,
                                         m->boxSize, m->ws, m->ctrl, nullptr, m->stream, noReset,
                                         m->cellLocation);
-        if (e == cudaSuccess) e = launch_contacts_finish(m->start, m->ws, m->ctrl, nullptr, m->stream);
         if (e != cudaSuccess) rc = fail(PCP_ERR_CUDA, "rollback capture: %s", cudaGetErrorString(e));
     }
     if (!rc) rc = force_energy(m, nullptr, true);
@@ -1037,8 +1034,8 @@ int pcp_model_update_outersections(pcp_model* m) {
     CHECK_M(m);
     int rc = need_topology(m);
     if (rc) return rc;
-    CK(launch_contacts_finish(m->start, m->ws, m->ctrl, nullptr, m->stream));
-    m->launches++;
+    // (the narrow phase matched the partners, and the last block of its
+    // block path did the empty-group fixup)
     rc = read_ctrl(m);
     if (rc) return rc;
     m->numIntersections = m->ctrlHost->numRecords;
@@ -1354,8 +1351,7 @@ int pcp_model_contacts_stage(pcp_model* m, int stage) {
                            m->ws, m->ctrl, nullptr, m->stream, stage == 0 ? 1 : 2));
         m->launches += stage == 0 ? 6 : 2;
     } else if (stage == 2) {
-        CK(launch_contacts_finish(m->start, m->ws, m->ctrl, nullptr, m->stream));
-        m->launches += 1;
+        // nothing left to launch: the fixup runs at the end of stage 1
     } else {
         return fail(PCP_ERR_ARG, "unknown contact stage %d", stage);
     }

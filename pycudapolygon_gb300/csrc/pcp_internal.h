@@ -35,6 +35,7 @@ struct Ctrl {
     int G;                 // broad-phase grid cells per axis
     unsigned int flags;    // kFlag* bits
     float Rmax;            // largest bounding radius of a well-formed polygon
+    unsigned int slowDone; // blocks of the narrow phase's block path finished
     unsigned long long maxKey;
     // ---- energy / force ----
     double energy;
@@ -170,8 +171,6 @@ cudaError_t launch_contacts(const double2* pos, const int* start, const int* sha
 cudaError_t launch_prepass_move(double2* verlet, const int* start, int* cellOut, int P, int B,
                                 ContactWS& ws, Ctrl* ctrl, const int* gate, cudaStream_t st,
                                 const FireMove& mv);
-cudaError_t launch_contacts_finish(const int* start, ContactWS& ws, Ctrl* ctrl,
-                                   const int* gate, cudaStream_t st);
 // edge: the edge vectors wrap(x_next - x) of pos, or nullptr
 // decide: the FIRE step's force pass; its last block decides the energy
 // rollback (model.cpp:450-453) and sets `rbCond` of the step graph
