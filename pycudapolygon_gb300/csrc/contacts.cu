@@ -1433,7 +1433,7 @@ constexpr int kForceWarps = 2;
 template <bool kEdge>
 __global__ void __launch_bounds__(32 * kForceWarps)
 k_overlap_force(const double2* __restrict__ pos, const int* __restrict__ start,
-                const int* __restrict__ next, int V, ContactWS ws, Ctrl* __restrict__ ctrl,
+                int V, ContactWS ws, Ctrl* __restrict__ ctrl,
                 double2* __restrict__ force, const double2* __restrict__ edge, int decide,
                 cudaGraphConditionalHandle rbCond, const int* gate) {
     pdl_enter();
@@ -1695,17 +1695,17 @@ cudaError_t launch_prepass_move(double2* verlet, const int* start, int* cellOut,
 }
 
 
-cudaError_t launch_overlap_force(const double2* pos, const int* start, const int* next,
+cudaError_t launch_overlap_force(const double2* pos, const int* start,
                                  int V, ContactWS& ws, Ctrl* ctrl, double2* force,
                                  const int* gate, cudaStream_t st, const double2* edge,
                                  int decide, cudaGraphConditionalHandle rbCond) {
     // one pass over up to 4 * SMs * kForceWarps * kForceRecs records
     int grid = sm_count() * 4;
     if (edge)
-        launch_k(k_overlap_force<true>, dim3(grid), dim3(32 * kForceWarps), 0, st, pos, start, next, V, ws,
+        launch_k(k_overlap_force<true>, dim3(grid), dim3(32 * kForceWarps), 0, st, pos, start, V, ws,
                  ctrl, force, edge, decide, rbCond, gate);
     else
-        launch_k(k_overlap_force<false>, dim3(grid), dim3(32 * kForceWarps), 0, st, pos, start, next, V, ws,
+        launch_k(k_overlap_force<false>, dim3(grid), dim3(32 * kForceWarps), 0, st, pos, start, V, ws,
                  ctrl, force, edge, decide, rbCond, gate);
     return cudaGetLastError();
 }

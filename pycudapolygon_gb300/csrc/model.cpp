@@ -447,7 +447,7 @@ int force_energy(pcp_model* m, const int* gate, bool zeroed = false,
     bool edge = (t == PCP_MODEL_SOFT_BODY || t == PCP_MODEL_EDGE_ONLY || t == PCP_MODEL_HYBRID);
     bool area = (t == PCP_MODEL_SOFT_BODY || t == PCP_MODEL_AREA_ONLY || t == PCP_MODEL_HYBRID);
     if (overlap) {
-        CK(launch_overlap_force(m->pos, m->start, m->next, m->V, m->ws, m->ctrl, m->force, gate,
+        CK(launch_overlap_force(m->pos, m->start, m->V, m->ws, m->ctrl, m->force, gate,
                                 m->stream, edgeVec, decide, rbCond));
         m->launches++;
     }

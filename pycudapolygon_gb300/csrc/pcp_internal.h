@@ -174,7 +174,7 @@ cudaError_t launch_prepass_move(double2* verlet, const int* start, int* cellOut,
 // edge: the edge vectors wrap(x_next - x) of pos, or nullptr
 // decide: the FIRE step's force pass; its last block decides the energy
 // rollback (model.cpp:450-453) and sets `rbCond` of the step graph
-cudaError_t launch_overlap_force(const double2* pos, const int* start, const int* next,
+cudaError_t launch_overlap_force(const double2* pos, const int* start,
                                  int V, ContactWS& ws, Ctrl* ctrl, double2* force,
                                  const int* gate, cudaStream_t st, const double2* edge = nullptr,
                                  int decide = 0, cudaGraphConditionalHandle rbCond = 0);
@@ -186,8 +186,9 @@ cudaError_t constraints_init();
 // mainPass: the FIRE step's own pass after a force pass that decided the
 // energy rollback (launch_overlap_force with decide): the pass reads that
 // decision and does nothing when the rollback runs
-// pre ([2V] double2: unit edge tangents, then unit area gradients): when
-// non-null, the values launch_project_pre stored for the current positions
+// pre ([3V] double2: unit edge tangents, unit area gradients, then the edge
+// vectors the overlap force loads): when non-null, the values
+// launch_project_pre stored for the current positions
 cudaError_t launch_project(const double2* pos, const int* start, int P, int nmax,
                            const double* constraints, double2* force, double* scratch, int V,
                            int areaFromPositions, Ctrl* fireCtrl, const int* gate, double2* vel,
