@@ -320,7 +320,21 @@ def test_xpbd_parity(system):
 
 # ------------------------------------------------------------------ FIRE
 def test_fire_steps_parity():
-    s = make_system(64, 16, 0.85, seed=2)
+    _fire_steps_parity(make_system(64, 16, 0.85, seed=2), 30)
+
+
+def test_fire_steps_parity_general_kernels():
+    """Polygons of 12 to 48 vertices: inside the step graph the projection is
+    the warp-per-polygon form with a shared-memory workspace, SHAKE the
+    shared-memory form, and the force forms its own edge vectors (the
+    one-vertex-per-lane kernels and the precomputed tangents and edge vectors
+    serve polygons of at most 32 vertices only)."""
+    n = np.random.default_rng(21).integers(12, 49, 120)
+    assert n.max() > 32
+    _fire_steps_parity(make_system(120, n, 0.86, seed=13), 15)
+
+
+def _fire_steps_parity(s, steps):
     g, o = pair(s)
     for m in (g, o):
         m.shakeProject(200, 1e-15)
@@ -329,7 +343,7 @@ def test_fire_steps_parity():
         m.projectForce()
     st_g = (1e-3, 0.1, 0)
     st_o = (1e-3, 0.1, 0)
-    for step in range(30):
+    for step in range(steps):
         rg = g.minimizeFIREStep(*st_g)
         ro = o.minimizeFIREStep(*st_o)
         assert rg[0] == pytest.approx(ro[0], rel=1e-9, abs=1e-14), step
