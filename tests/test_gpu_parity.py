@@ -334,6 +334,12 @@ def test_fire_steps_parity_general_kernels():
     _fire_steps_parity(make_system(120, n, 0.86, seed=13), 15)
 
 
+def test_fire_steps_parity_thread_per_polygon():
+    """20000 polygons, more than 128 per SM: inside the step graph the
+    projection takes its thread-per-polygon form."""
+    _fire_steps_parity(make_system(20000, 8, 0.85, seed=17), 4)
+
+
 def _fire_steps_parity(s, steps):
     g, o = pair(s)
     for m in (g, o):
