@@ -295,6 +295,12 @@ int pcp_shake_project_noalloc(double* d_pos, const int* d_start, int num_polygon
 int pcp_update_positions(double* d_pos, const double* d_force, int num_vertices,
                          double dt, void* stream);
 
+/* No reference counterpart: d_y[i] = the reciprocal the projection's
+ * area-gradient removal uses in place of a division (two Newton-Raphson
+ * steps from the FP32 reciprocal), for 2^-126 <= |d_x[i]| < 2^126; exposed
+ * so its error bound can be tested against 1/x. */
+int pcp_rcp_newton(const double* d_x, double* d_y, int n, void* stream);
+
 #ifdef __cplusplus
 }
 #endif

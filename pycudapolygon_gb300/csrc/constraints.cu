@@ -1314,10 +1314,14 @@ __global__ void __launch_bounds__(128, 7) k_project_lanes(const double2* __restr
                     qF = t2.x; qq = t2.y;
                 }
                 // sqrt(qq) > 1e-14 (kernels.cuh:464), tested on the bit
-                // pattern (qq >= 0 or NaN; 0x3A1FB0F6BE506019 is 1e-28)
+                // pattern (qq >= 0 or NaN; 0x3A1FB0F6BE506019 is 1e-28); the
+                // quotient by the Newton reciprocal.  qq <= 1 for the unit
+                // area gradients; a qq of 2^126 or more (corrupt input) takes
+                // coef = 0, within |qF| 2^-126 of qF / qq.
                 const unsigned long long qqB = (unsigned long long)__double_as_longlong(qq);
-                double coef = (qqB > 0x3A1FB0F6BE506019ull && qqB <= 0x7FF0000000000000ull)
-                                  ? qF / qq : 0.0;
+                double coef = 0.0;
+                if (qqB > 0x3A1FB0F6BE506019ull && qqB < 0x47D0000000000000ull)
+                    coef = qF * rcp_newton(qq);
                 f = make_double2(f.x - coef * q.x, f.y - coef * q.y);
                 if (live) force[st + lane] = f;
             }
@@ -1359,6 +1363,18 @@ __global__ void __launch_bounds__(128, 7) k_project_lanes(const double2* __restr
         }
         fire_pass_end(fire, rbNext);
     }
+}
+
+__global__ void k_rcp_newton(const double* __restrict__ x, double* __restrict__ y, int n) {
+    pdl_enter();
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i < n) y[i] = rcp_newton(x[i]);
+}
+
+cudaError_t launch_rcp_newton(const double* x, double* y, int n, cudaStream_t st) {
+    if (n <= 0) return cudaSuccess;
+    launch_k(k_rcp_newton, dim3(nblk(n, 256)), dim3(256), 0, st, x, y, n);
+    return cudaGetLastError();
 }
 
 cudaError_t constraints_init() {

@@ -1692,6 +1692,13 @@ int pcp_shake_project(double* d_pos, const int* d_start, int P, const double* d_
 // Same computation as pcp_shake_project with the workspace in a static device
 // array: no cudaMalloc, cudaFree or other allocation.  Reads start[P] back to
 // the host (waiting for the stream) to check the size against the array.
+int pcp_rcp_newton(const double* d_x, double* d_y, int n, void* stream) {
+    if (n < 0) return fail(PCP_ERR_ARG, "negative count");
+    if (n > 0 && (!d_x || !d_y)) return fail(PCP_ERR_ARG, "null buffer");
+    CK(launch_rcp_newton(d_x, d_y, n, (cudaStream_t)stream));
+    return PCP_OK;
+}
+
 int pcp_shake_project_noalloc(double* d_pos, const int* d_start, int P, const double* d_tl,
                               const double* d_ta, int max_iter, double tol, int* d_max_iters,
                               void* stream) {

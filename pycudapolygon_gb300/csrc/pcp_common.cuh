@@ -324,6 +324,20 @@ __device__ __forceinline__ float d2f_int(double d) {
     const unsigned m = ((hi & 0xFFFFFu) << 3) | (lo >> 29);
     return __uint_as_float(sign | ((unsigned)e << 23) | m);
 }
+// 1/x for a double with 2^-126 <= |x| < 2^126 (x and 1/x in the normal
+// float range): the FP32 reciprocal of the truncated value (relative error
+// below 2^-22) refined by
+// two Newton-Raphson steps y <- y + y (1 - x y), each of which squares the
+// relative error, so the result is within a few ulps of 1/x.  Four FP64 FMAs
+// instead of a division's longer sequence.
+__device__ __forceinline__ double rcp_newton(double x) {
+    double y = f2d_int(__frcp_rn(d2f_int(x)));
+    double e = fma(-x, y, 1.0);
+    y = fma(y, e, y);
+    e = fma(-x, y, 1.0);
+    return fma(y, e, y);
+}
+
 // |x| as the bit pattern of a non-negative double: for finite values the
 // unsigned order of these patterns is the order of the magnitudes (NaN
 // patterns sort above +inf).

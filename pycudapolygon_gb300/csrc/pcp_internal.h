@@ -198,6 +198,7 @@ cudaError_t launch_project(const double2* pos, const int* start, int P, int nmax
 bool project_uses_lanes(int P, int nmax);
 // the tangents and area gradients of `pos` into pre for launch_project (a
 // no-op unless project_uses_lanes(P, nmax))
+cudaError_t launch_rcp_newton(const double* x, double* y, int n, cudaStream_t st);
 cudaError_t launch_project_pre(const double2* pos, const int* start, int P, int nmax,
                                double2* pre, int V, const int* gate, cudaStream_t st);
 // fire (device-resident FIRE step, first SHAKE attempt): the last block to
