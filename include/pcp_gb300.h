@@ -270,14 +270,19 @@ int pcp_shake_project(double* d_pos, const int* d_start, int num_polygons,
  * not allocate device memory -- plugins whose host owns the device's memory
  * through its own pool and hands the plugin only the buffers it passes in,
  * and loops where the device-wide synchronisation of cudaMalloc/cudaFree is
- * not allowed.  The same kernel, arguments and results as
- * pcp_shake_project, but the workspace is a static device array of this
- * library sized for PCP_SHAKE_NOALLOC_MAX_VERTICES vertices (4.5 MiB); the
- * call makes no cudaMalloc, cudaFree or other allocation.
- *   - More than PCP_SHAKE_NOALLOC_MAX_VERTICES vertices in total
- *     (startIndices[num_polygons]) returns PCP_ERR_CAPACITY and launches
- *     nothing.  The call reads startIndices[num_polygons] back to the host
- *     and waits for `stream` to do that check.
+ * not allowed.  It always runs the warp-per-polygon SHAKE kernel with its
+ * workspace in global memory (pcp_shake_project runs the register-resident
+ * one-vertex-per-lane form when no polygon exceeds 32 vertices); positions
+ * agree with pcp_shake_project within the 1e-12 SHAKE tolerance and the
+ * iteration counts are the same.  The workspace is a static device array of
+ * this library sized for PCP_SHAKE_NOALLOC_MAX_VERTICES vertices (4.5 MiB);
+ * the call makes no cudaMalloc, cudaFree or other allocation.
+ *   - start must be CSR offsets: start[0] == 0 and start never decreasing.
+ *     A one-block kernel checks that and start[num_polygons] against the
+ *     array before anything else runs, and the call waits for `stream` to
+ *     read its verdict: offsets that are not CSR return PCP_ERR_ARG, more
+ *     than PCP_SHAKE_NOALLOC_MAX_VERTICES vertices PCP_ERR_CAPACITY, and
+ *     neither launches the SHAKE kernel or touches d_max_iters.
  *   - The first call on a device looks up the array's device address (it
  *     may load the library's kernels onto that device); make that first
  *     call before any stream capture.

@@ -1776,6 +1776,39 @@ cudaError_t launch_fire_settle(double2* vel, const double2* force, int V, Ctrl* 
 static __device__ __align__(256) double
     g_shake_noalloc_scratch[(size_t)kScratchPerVertex * PCP_SHAKE_NOALLOC_MAX_VERTICES];
 
+// Outcome of the last input check of pcp_shake_project_noalloc on this
+// device (0 valid, 1 start[0] != 0 or start decreasing, 2 more vertices than
+// the array holds); read back with cudaMemcpyFromSymbolAsync.
+static __device__ int g_shake_noalloc_status;
+
+// One block checks that the CSR offsets describe polygons inside the array:
+// start[0] == 0, start non-decreasing, start[P] <= capacity.  k_shake writes
+// doubles [kScratchPerVertex * start[p], kScratchPerVertex * start[p+1]) for
+// polygon p, so this bounds every write into the array.
+__global__ void k_shake_noalloc_check(const int* __restrict__ start, int P, int capacity) {
+    int bad = 0;
+    for (int p = threadIdx.x; p < P; p += blockDim.x)
+        if (start[p + 1] < start[p]) bad = 1;
+    bad = __syncthreads_or(bad);
+    if (threadIdx.x == 0) {
+        int status = 0;
+        if (bad || start[0] != 0) status = 1;
+        else if (start[P] > capacity) status = 2;
+        g_shake_noalloc_status = status;
+    }
+}
+
+cudaError_t shake_noalloc_check(const int* start, int P, int* status, cudaStream_t st) {
+    launch_k(k_shake_noalloc_check, dim3(1), dim3(256), 0, st, start, P,
+             (int)PCP_SHAKE_NOALLOC_MAX_VERTICES);
+    cudaError_t e = cudaGetLastError();
+    if (e != cudaSuccess) return e;
+    e = cudaMemcpyFromSymbolAsync(status, g_shake_noalloc_status, sizeof(int), 0,
+                                  cudaMemcpyDeviceToHost, st);
+    if (e != cudaSuccess) return e;
+    return cudaStreamSynchronize(st);
+}
+
 // Device address of the array on the current device.  It is looked up once
 // per device, by the first call made with that device current; the lookup
 // can load this module onto the device, so that first call belongs before

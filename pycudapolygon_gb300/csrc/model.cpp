@@ -1689,9 +1689,6 @@ int pcp_shake_project(double* d_pos, const int* d_start, int P, const double* d_
     return PCP_OK;
 }
 
-// Same computation as pcp_shake_project with the workspace in a static device
-// array: no cudaMalloc, cudaFree or other allocation.  Reads start[P] back to
-// the host (waiting for the stream) to check the size against the array.
 int pcp_rcp_newton(const double* d_x, double* d_y, int n, void* stream) {
     if (n < 0) return fail(PCP_ERR_ARG, "negative count");
     if (n > 0 && (!d_x || !d_y)) return fail(PCP_ERR_ARG, "null buffer");
@@ -1699,24 +1696,32 @@ int pcp_rcp_newton(const double* d_x, double* d_y, int n, void* stream) {
     return PCP_OK;
 }
 
+// SHAKE with its workspace in a static device array of this library: no
+// cudaMalloc, cudaFree or other allocation.  A one-block kernel checks the
+// CSR offsets against the array first and the call waits for its verdict, so
+// a start array that would reach past the array launches nothing.
 int pcp_shake_project_noalloc(double* d_pos, const int* d_start, int P, const double* d_tl,
                               const double* d_ta, int max_iter, double tol, int* d_max_iters,
                               void* stream) {
     if (P < 0) return fail(PCP_ERR_ARG, "negative polygon count");
     if (!d_max_iters) return fail(PCP_ERR_ARG, "null d_max_iters");
+    if (P > 0 && (!d_pos || !d_start || !d_tl || !d_ta))
+        return fail(PCP_ERR_ARG, "null device buffer");
     cudaStream_t st = (cudaStream_t)stream;
     double* scratch = nullptr;
     CK(shake_noalloc_scratch(&scratch));
-    int V = 0;
     if (P > 0) {
-        CK(cudaMemcpyAsync(&V, d_start + P, sizeof(int), cudaMemcpyDeviceToHost, st));
-        CK(cudaStreamSynchronize(st));
+        int status = 0;
+        CK(shake_noalloc_check(d_start, P, &status, st));
+        if (status == 1)
+            return fail(PCP_ERR_ARG,
+                        "pcp_shake_project_noalloc: start must begin at 0 and never decrease");
+        if (status == 2)
+            return fail(PCP_ERR_CAPACITY,
+                        "pcp_shake_project_noalloc: more vertices than its static workspace of %d "
+                        "vertices; use pcp_shake_project",
+                        PCP_SHAKE_NOALLOC_MAX_VERTICES);
     }
-    if (V < 0 || V > PCP_SHAKE_NOALLOC_MAX_VERTICES)
-        return fail(PCP_ERR_CAPACITY,
-                    "pcp_shake_project_noalloc: %d vertices exceed its static workspace of %d "
-                    "vertices; use pcp_shake_project",
-                    V, PCP_SHAKE_NOALLOC_MAX_VERTICES);
     CK(cudaMemsetAsync(d_max_iters, 0, sizeof(int), st));
     CK(launch_shake_noalloc(reinterpret_cast<double2*>(d_pos), d_start, P, d_tl, d_ta, max_iter,
                             tol, d_max_iters, scratch, st));

@@ -214,6 +214,9 @@ constexpr int kScratchPerVertex = 36;
 // pcp_shake_project_noalloc: device address of its static workspace on the
 // current device, and k_shake launched with every workspace in it
 cudaError_t shake_noalloc_scratch(double** out);
+// pcp_shake_project_noalloc: checks start[0..P] on the device (0 valid,
+// 1 not a CSR offset array, 2 beyond the static workspace) and waits for it.
+cudaError_t shake_noalloc_check(const int* start, int P, int* status, cudaStream_t st);
 cudaError_t launch_shake_noalloc(double2* pos, const int* start, int P, const double* targetEdge,
                                  const double* targetArea, int maxIter, double tol,
                                  int* maxItersOut, double* scratch, cudaStream_t st);

@@ -5,7 +5,10 @@ Collected last on purpose: it must hold in a fresh process (the first call
 on the device looks up the static array) and after every other test of the
 suite has run in the same process.  Positions agree within the SHAKE
 tolerance of the oracle parity tests (1e-12, minimum image); the iteration
-counts agree exactly.
+counts agree exactly.  The entry point exists for callers that cannot
+allocate device memory, so one test checks that a call leaves the device's
+free memory unchanged, and others that inputs it cannot hold are refused
+before anything runs.
 """
 import ctypes
 
@@ -87,4 +90,42 @@ def test_noalloc_shake_rejects_more_vertices_than_its_workspace():
     torch.cuda.synchronize()
     assert rc == 3                      # PCP_ERR_CAPACITY
     assert str(MAX_VERTICES) in L.pcp_last_error().decode()
+    assert int(iters.item()) == -7      # nothing launched
+
+
+def test_noalloc_shake_allocates_no_device_memory():
+    """After a first call (which looks up the array and loads the kernels),
+    a call on a larger system leaves the device's free memory unchanged."""
+    warm = make_system(num_polygons=32, n=16, phi=0.85, seed=2)
+    big = make_system(num_polygons=200, n=np.random.default_rng(3).integers(24, 97, 200),
+                      phi=0.86, seed=17)
+    assert int(warm.start_indices[-1]) < int(big.start_indices[-1]) <= MAX_VERTICES
+    bw, bb = _dev(warm), _dev(big)
+    P_w, P_b = warm.num_polygons, big.num_polygons
+    _call("pcp_shake_project_noalloc", bw, P_w)
+    torch.cuda.synchronize()
+    free_before = torch.cuda.mem_get_info()[0]
+    rc = L.pcp_shake_project_noalloc(bb["pos"].data_ptr(), bb["start"].data_ptr(), P_b,
+                                     bb["tl"].data_ptr(), bb["ta"].data_ptr(), 100, 1e-15,
+                                     bb["iters"].data_ptr(), None)
+    torch.cuda.synchronize()
+    free_after = torch.cuda.mem_get_info()[0]
+    assert rc == 0, L.pcp_last_error().decode()
+    assert 0 < int(bb["iters"].item()) < 100
+    assert free_after == free_before
+
+
+def test_noalloc_shake_rejects_offsets_that_are_not_csr():
+    """A decreasing start array would place a polygon's workspace outside the
+    array; the call refuses it before the SHAKE kernel runs."""
+    d = torch.device("cuda:0")
+    start = torch.tensor([0, 10, 5, 20], dtype=torch.int32, device=d)
+    pos = torch.zeros(40, dtype=torch.float64, device=d)
+    tl = torch.ones(3, dtype=torch.float64, device=d)
+    iters = torch.full((1,), -7, dtype=torch.int32, device=d)
+    rc = L.pcp_shake_project_noalloc(pos.data_ptr(), start.data_ptr(), 3, tl.data_ptr(),
+                                     tl.data_ptr(), 10, 1e-15, iters.data_ptr(), None)
+    torch.cuda.synchronize()
+    assert rc == 1                      # PCP_ERR_ARG
+    assert "never decrease" in L.pcp_last_error().decode()
     assert int(iters.item()) == -7      # nothing launched
