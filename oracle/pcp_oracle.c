@@ -1528,13 +1528,19 @@ double orc_update_overlap_area(orc_model* m, int d) {
                     double vxp = orc_wrap_periodic(pos[2 * s0] - px);
                     double vyp = orc_wrap_periodic(pos[2 * s0 + 1] - py);
                     double vx0 = vxp, vy0 = vyp;
+                    /* The reference's build (nvcc, default contraction)
+                     * evaluates a*b - c*d as fma(a, b, -(c*d)) and a*b + c*d
+                     * as fma(a, b, c*d).  At grid points on an edge the cross
+                     * product is zero only without the fused rounding, and
+                     * its sign picks atan2's +pi or -pi, i.e. the count:
+                     * tests/golden/ref_gpu_odd_shapes.npz pins this form. */
                     for (int e = s0 + 1; e < s1; ++e) {
                         double vx = vxp + orc_wrap_periodic(pos[2 * e] - pos[2 * e - 2]);
                         double vy = vyp + orc_wrap_periodic(pos[2 * e + 1] - pos[2 * e - 1]);
-                        ang += atan2(vxp * vy - vyp * vx, vxp * vx + vyp * vy);
+                        ang += atan2(fma(vxp, vy, -(vyp * vx)), fma(vxp, vx, vyp * vy));
                         vxp = vx; vyp = vy;
                     }
-                    ang += atan2(vxp * vy0 - vyp * vx0, vxp * vx0 + vyp * vy0);
+                    ang += atan2(fma(vxp, vy0, -(vyp * vx0)), fma(vxp, vx0, vyp * vy0));
                     if (fabs(ang - 2.0 * PI) < eps) hits++;
                     if (nt < 512) tracked[nt++] = poly;
                     else { full = 1; break; }

@@ -30,7 +30,7 @@ NVCC = os.path.join(CUDA_HOME, "bin", "nvcc")
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 CU_SOURCES = ["geometry.cu", "contacts.cu", "constraints.cu"]
 CPP_SOURCES = ["model.cpp"]
-HEADERS = ["pcp_common.cuh", "pcp_internal.h"]
+HEADERS = ["pcp_common.cuh", "pcp_internal.h", "pcp_fire.cuh"]
 
 
 def _pybind_include():

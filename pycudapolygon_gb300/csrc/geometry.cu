@@ -490,10 +490,15 @@ __global__ void k_overlap_mc(const double2* __restrict__ pos, const int* __restr
                         for (int e = s0 + 1; e < s1; e++) {
                             double vx = vxp + wrap_periodic(pos[e].x - pos[e - 1].x);
                             double vy = vyp + wrap_periodic(pos[e].y - pos[e - 1].y);
-                            ang += atan2(vxp * vy - vyp * vx, vxp * vx + vyp * vy);
+                            // the reference's contracted products, rounded
+                            // as its build rounds them (a grid point on an
+                            // edge takes its count from the cross's sign)
+                            ang += atan2(__fma_rn(vxp, vy, -__dmul_rn(vyp, vx)),
+                                         __fma_rn(vxp, vx, __dmul_rn(vyp, vy)));
                             vxp = vx; vyp = vy;
                         }
-                        ang += atan2(vxp * vy0 - vyp * vx0, vxp * vx0 + vyp * vy0);
+                        ang += atan2(__fma_rn(vxp, vy0, -__dmul_rn(vyp, vx0)),
+                                     __fma_rn(vxp, vx0, __dmul_rn(vyp, vy0)));
                         if (fabs(ang - 2.0 * pi) < eps) hits++;
                     }
                     if (nt < 512) tracked[nt++] = poly;

@@ -1,8 +1,8 @@
 """Regenerate the golden fixtures in tests/golden/ from the reference.
 
-Run in a container where the reference tree is mounted (default
-/root/reference, or $PCP_REFERENCE).  The fixtures it writes are committed, so
-nothing at test time reads the reference:
+Run where the reference tree is available, with PCP_REFERENCE set to its
+root.  The fixtures it writes are committed, so nothing at test time reads the
+reference:
 
   testsaver.json    the reference's own saved two-pentagon state
                     (tests/testSaver/state.npy, scalars.dat) and the neighbour
@@ -37,7 +37,9 @@ import types
 import numpy as np
 
 HERE = os.path.dirname(os.path.abspath(__file__))
-REF = os.environ.get("PCP_REFERENCE", "/root/reference")
+REF = os.environ.get("PCP_REFERENCE")
+if not REF:
+    raise SystemExit("set PCP_REFERENCE to the root of the reference checkout")
 
 
 def _import_reference_model():
