@@ -40,6 +40,13 @@ WORKLOAD = ("plain FIRE step at scale: 4096 polygons x 32 vertices (131072 verti
             "phi 0.88, cell list + narrow phase + outersections + overlap force + "
             "constraint projection + SHAKE (5, retry 50)")
 FIRE_ARGS = dict(dtMax=0.1, alphaStart=0.1, fAlpha=0.99, fInc=1.1, fDec=0.5, nMin=5, shakeIter=5)
+# the workload as both arms report it
+CONFIG = {"workload": WORKLOAD, "polygons": N_POLY, "vertices_per_polygon": N_VERT, "phi": PHI,
+          "l2": "flushed before every timed step (256 MiB write)",
+          "fire": "dt0 1e-3, dtMax 0.1, alpha0 0.1, fAlpha 0.99, fInc 1.1, fDec 0.5, "
+                  "nMin 5, shakeIter 5"}
+PAIR_RULE = ("pair evals are polygon pairs a < b with overlapping bounding circles; the "
+             "narrow phase receives the subset whose padded boxes also meet")
 
 
 def dist_env():
@@ -64,6 +71,70 @@ def reduce_over_ranks(ms, pairs, dist, device):
 
 
 # ------------------------------------------------------------------ clocks
+class NvmlClocks:
+    """SM clock and clock-event reasons read through NVML (libnvidia-ml, the
+    driver's library, by ctypes) every millisecond on a thread: the timed
+    region of a short run is a few milliseconds, below nvidia-smi's period.
+    Reading clocks changes no setting of the GPU."""
+    HW_SLOWDOWN, SW_THERMAL, HW_THERMAL, SW_POWER_CAP = 0x8, 0x20, 0x40, 0x4
+
+    def __init__(self, index, period_s=0.001):
+        import ctypes
+        self.ok = False
+        self.samples, self.reasons, self.max_mhz = [], 0, None
+        self.period = period_s
+        try:
+            self.nv = ctypes.CDLL("libnvidia-ml.so.1")
+        except OSError:
+            return
+        self.c = ctypes
+        if self.nv.nvmlInit_v2() != 0:
+            return
+        self.h = ctypes.c_void_p()
+        if self.nv.nvmlDeviceGetHandleByIndex_v2(ctypes.c_uint(index), ctypes.byref(self.h)) != 0:
+            return
+        mx = ctypes.c_uint()
+        if self.nv.nvmlDeviceGetMaxClockInfo(self.h, ctypes.c_int(1), ctypes.byref(mx)) == 0:
+            self.max_mhz = float(mx.value)
+        try:
+            self.reasons_fn = self.nv.nvmlDeviceGetCurrentClocksEventReasons
+        except AttributeError:
+            self.reasons_fn = self.nv.nvmlDeviceGetCurrentClocksThrottleReasons
+        self.ok = True
+
+    def _poll(self):
+        c = self.c
+        clk, rs = c.c_uint(), c.c_ulonglong()
+        while not self.stop:
+            if self.nv.nvmlDeviceGetClockInfo(self.h, c.c_int(1), c.byref(clk)) == 0:
+                self.samples.append(float(clk.value))
+            if self.reasons_fn(self.h, c.byref(rs)) == 0:
+                self.reasons |= int(rs.value)
+            time.sleep(self.period)
+
+    def __enter__(self):
+        self.stop = False
+        if self.ok:
+            self.t = threading.Thread(target=self._poll, daemon=True)
+            self.t.start()
+        return self
+
+    def __exit__(self, *a):
+        self.stop = True
+        if self.ok:
+            self.t.join(timeout=2)
+
+    def summary(self):
+        names = []
+        for bit, nm in ((self.HW_SLOWDOWN, "hw_slowdown"), (self.HW_THERMAL, "hw_thermal_slowdown"),
+                        (self.SW_THERMAL, "sw_thermal_slowdown"), (self.SW_POWER_CAP, "sw_power_cap")):
+            if self.reasons & bit:
+                names.append(nm)
+        return {"sm_mhz": statistics.median(self.samples) if self.samples else None,
+                "sm_max_mhz": self.max_mhz, "reasons": sorted(names),
+                "samples": len(self.samples), "source": "NVML every 1 ms"}
+
+
 class ClockSampler:
     """nvidia-smi clocks and throttle reasons sampled during the timed region."""
     Q = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
@@ -79,7 +150,7 @@ class ClockSampler:
         try:
             self.proc = subprocess.Popen(
                 ["nvidia-smi", "-i", str(self.index), "--query-gpu=" + self.Q,
-                 "--format=csv,noheader,nounits", "-lms", "100"],
+                 "--format=csv,noheader,nounits", "-lms", "10"],
                 stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
             self.t = threading.Thread(target=self._read, daemon=True)
             self.t.start()
@@ -185,7 +256,10 @@ def run_gpu(args, ws, rank, local):
     torch.cuda.synchronize()
     if dist:
         dist.barrier()
-    with ClockSampler(local) as clk:
+    clk = NvmlClocks(local)
+    if not clk.ok:
+        clk = ClockSampler(local)
+    with clk:
         for i in range(args.steps):
             flush.fill_(i & 255)
             ev[i][0].record()
@@ -199,6 +273,7 @@ def run_gpu(args, ws, rank, local):
         raise RuntimeError("contact buffers grew inside the timed region; rerun")
     ms = sum(a.elapsed_time(b) for a, b in ev)
     pairs = m.getPairCount() - pairs0
+    narrow_last = m.getNarrowPairCount()
     launches = m.getLaunchCount() - launches0
     ms, pairs = reduce_over_ranks(ms, pairs, dist, "cuda")
     value = pairs / (ms / 1e3)
@@ -207,12 +282,9 @@ def run_gpu(args, ws, rank, local):
         "warmup": args.warmup, "ms_per_step": ms / args.steps, "higher_is_better": True,
         "scaling": "weak", "vs_baseline": None, "dtype": "f64",
         "data": "synthetic (seeded bidisperse star polygons; the reference publishes no inputs)",
-        "config": {"workload": WORKLOAD, "polygons": N_POLY, "vertices_per_polygon": N_VERT,
-                   "phi": PHI, "parallelism": "replicas" if ws > 1 else "single",
-                   "l2": "flushed before every timed step (256 MiB write)",
-                   "pair_evals_per_step": pairs / max(1, args.steps) / ws,
-                   "fire": "dt0 1e-3, dtMax 0.1, alpha0 0.1, fAlpha 0.99, fInc 1.1, fDec 0.5, "
-                           "nMin 5, shakeIter 5"},
+        "config": dict(CONFIG, parallelism="replicas" if ws > 1 else "single"),
+        "pairs": {"rule": PAIR_RULE, "pair_evals_per_step": pairs / max(1, args.steps) / ws,
+                  "narrow_pairs_last_step": narrow_last[0] + narrow_last[1]},
         "clocks": clk.summary(),
         "gpu_launches": int(launches),
         "fire_state": {"energy": st[0], "dt": st[1], "max_force": st[4], "steps": st[5]},
@@ -223,6 +295,10 @@ def run_gpu(args, ws, rank, local):
         result["e2e"] = e2e(args, s)
     if rank == 0 and not args.no_cpu:
         result["cpu_baseline"] = cpu_baseline(args, s, pairs / max(1, args.steps) / ws)
+    if rank == 0 and not args.no_stop:
+        result["time_to_stop"] = time_to_stop(args, torch)
+    if rank == 0 and args.batch_systems > 0:
+        result["batched"] = batched(args, torch)
     if dist:
         dist.destroy_process_group()
     if rank == 0:
@@ -337,6 +413,203 @@ def e2e(args, s):
                     "pcp_model_get_positions), pinned host buffers, wall clock"}
 
 
+# ------------------------------------------------------------- time to stop
+STOP_SYSTEM = dict(num_polygons=64, n=16, phi=0.85)   # 1024 vertices
+STOP_SEEDS = list(range(1, 9))
+STOP_THR, STOP_MAX_STEPS = 1e-10, 100000
+FIRE_POS = (0.1, 0.1, 0.99, 1.1, 0.5, 5, 5)          # dtMax .. shakeIter
+
+
+def reference_driver(m, thr=STOP_THR, dt=1e-3, max_steps=STOP_MAX_STEPS):
+    """The reference's Python minimizeFIRE for the normal model
+    (pyCudaPolygon.py:674-731 with its loop, :653-672) on any object with the
+    Model method names: initForceEnergy (which sets the cell size to 0.5),
+    the small gradient step, then one minimizeFIREStep and one
+    getMaxUnbalancedForce per step until |F|max <= thr or six steps returned
+    an energy within 1e-15 of the step before.  Returns (E, dt, steps,
+    |F|max, stop reason)."""
+    m.resetVelocities()
+    m.initializeNeighborCells()
+    m.setMaxEdgeLength(0.5)
+    m.updateNeighborCells()
+    m.updateNeighbors()
+    m.updateOutersections()
+    m.updatePolygonGeometry()
+    m.updateForceEnergy()
+    m.projectForce()
+    m.updatePositions(dt)
+    m.updatePolygonGeometry()
+    m.updateNeighborCells()
+    m.updateNeighbors()
+    m.updateOutersections()
+    m.updateForceEnergy()
+    m.projectForce()
+    m.resetVelocities()
+    m.resetVelocities()
+    m.updatePolygonGeometry()
+    m.updateForceEnergy()
+    m.projectForce()
+    alpha, npos, prev, flat = 0.1, 0, 1e9, 0
+    e, f = None, None
+    for step in range(max_steps):
+        e, dt, alpha, npos = m.minimizeFIREStep(dt, alpha, npos, *FIRE_POS)
+        f = m.getMaxUnbalancedForce()
+        if abs(e - prev) < 1e-15:
+            flat += 1
+        if flat > 5:
+            return e, dt, step + 1, f, "stagnation"
+        prev = e
+        if f <= thr:
+            return e, dt, step + 1, f, "tolerance"
+    return e, dt, max_steps, f, "step limit"
+
+
+def _stop_system(seed, model):
+    from pycudapolygon_gb300.systems import load_into, make_system
+    s = make_system(seed=seed, **STOP_SYSTEM)
+    m = load_into(model(s.num_vertices), s)
+    m.shakeProject(100, 1e-15)
+    return m
+
+
+def time_to_stop(args, torch):
+    """Minimisation of the 64 x 16 (phi 0.85) systems to the reference
+    driver's stop, per system: on the GPU through the device-resident driver
+    (one call, the loop and its stop tests on the device) and through the
+    reference's per-step Python loop on the pybind module, and on the CPU
+    oracle through the same loop.  Wall time per system includes the calls
+    before the loop."""
+    import pycudapolygon_gb300 as pg
+    from oracle import oracle as orc
+    lib = pg.load_module()
+    _stop_system(STOP_SEEDS[0], lib.Model).minimizeFIREDevice(STOP_THR, 1e-3, 50)   # warm-up
+    dev, loop, cpu = [], [], []
+    for seed in STOP_SEEDS:
+        m = _stop_system(seed, lib.Model)
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        r = m.minimizeFIREDevice(STOP_THR, 1e-3, STOP_MAX_STEPS)
+        t1 = time.perf_counter()
+        st = m.fireRunStats()
+        dev.append(dict(seconds=t1 - t0, steps=r[2], energy=r[0], max_force=m.getMaxUnbalancedForce(),
+                        reason="stagnation" if st[0] else ("tolerance" if r[2] < STOP_MAX_STEPS
+                                                           else "step limit")))
+        m = _stop_system(seed, lib.Model)
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        r = reference_driver(m)
+        t1 = time.perf_counter()
+        loop.append(dict(seconds=t1 - t0, steps=r[2], energy=r[0], reason=r[4]))
+    threads = cpu_threads()
+    orc.set_threads(threads)
+    for seed in STOP_SEEDS:
+        o = _stop_system(seed, orc.OracleModel)
+        t0 = time.perf_counter()
+        r = reference_driver(o)
+        t1 = time.perf_counter()
+        cpu.append(dict(seconds=t1 - t0, steps=r[2], energy=r[0], reason=r[4]))
+
+    def mean(xs, k):
+        return sum(x[k] for x in xs) / len(xs)
+    same_steps = sum(a["steps"] == b["steps"] for a, b in zip(dev, cpu))
+    de = max(abs(a["energy"] - b["energy"]) / max(abs(b["energy"]), 1e-300)
+             for a, b in zip(dev, cpu) if a["steps"] == b["steps"]) if same_steps else None
+    return {
+        "workload": "64 polygons x 16 vertices, phi 0.85, seeds %d-%d; minimised by the "
+                    "reference's Python FIRE driver rule (stop at |F|max <= 1e-10 or after six "
+                    "steps with |dE| < 1e-15), dt0 1e-3" % (STOP_SEEDS[0], STOP_SEEDS[-1]),
+        "converged_to_1e-10": sum(d["reason"] == "tolerance" for d in dev),
+        "systems": len(STOP_SEEDS),
+        "stop_reasons": sorted(set(d["reason"] for d in dev)),
+        "steps": [d["steps"] for d in dev],
+        "gpu_device_driver_s_per_system": mean(dev, "seconds"),
+        "gpu_python_loop_s_per_system": mean(loop, "seconds"),
+        "cpu_oracle_s_per_system": mean(cpu, "seconds"),
+        "cpu_cores": threads,
+        "gpu_vs_cpu_same_stop_step": "%d/%d" % (same_steps, len(STOP_SEEDS)),
+        "gpu_vs_cpu_max_rel_energy_diff": de,
+        "final_max_force": [d["max_force"] for d in dev],
+    }
+
+
+# ------------------------------------------------------------- many systems
+BATCH_SYSTEMS, BATCH_SEED = 256, 2025
+
+
+def batched(args, torch):
+    """256 independent systems (polygons U{64..1024}, vertices per polygon
+    U{12..48}, packing fraction U[0.80, 0.92], seeded) minimised by the
+    reference Python driver's rule, per system: all at once through the
+    batch (a pool of streams, several FIRE steps per graph launch, launch
+    shapes from the autotuner), and one after the other through the
+    device-resident single-system driver with the default launch shapes."""
+    import pycudapolygon_gb300 as pg
+    from pycudapolygon_gb300.systems import batched_specs, load_into, make_system
+    lib = pg.load_module()
+    specs = batched_specs(args.batch_systems, BATCH_SEED)
+    systems = [make_system(P, nv, phi, seed=sd) for P, nv, phi, sd in specs]
+    models = []
+    for s in systems:
+        m = load_into(lib.Model(s.num_vertices), s)
+        m.shakeProject(100, 1e-15)
+        models.append(m)
+    start = [np.asarray(m.getPositions()) for m in models]
+
+    def reset():
+        for m, x in zip(models, start):
+            m.setPositions(x)
+        torch.cuda.synchronize()
+    # one after the other, default launch shapes (a 1-step run first builds
+    # each system's step graph outside the timed region)
+    seq_steps, seq_conv = [], 0
+    t_seq = 0.0
+    for m, x in zip(models, start):
+        m.minimizeFIREDevice(STOP_THR, 1e-3, 1, *FIRE_POS)
+        m.setPositions(x)
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        r = m.minimizeFIREDevice(STOP_THR, 1e-3, STOP_MAX_STEPS, *FIRE_POS)
+        t_seq += time.perf_counter() - t0
+        seq_steps.append(int(r[2]))
+        seq_conv += int(m.fireRunStats()[0] == 0 and r[2] < STOP_MAX_STEPS)
+    # all together: autotuned shapes, then a 1-step run that builds the
+    # multi-step graphs, then the timed run
+    reset()
+    b = lib.Batch()
+    for m in models:
+        b.add(m)
+    t0 = time.perf_counter()
+    b.autotune(8)
+    t_tune = time.perf_counter() - t0
+    report = json.loads(b.report())
+    reset()
+    b.minimizeFIRE(1, STOP_THR, 1e-3, 1, *FIRE_POS)
+    reset()
+    t0 = time.perf_counter()
+    out = b.minimizeFIRE(1, STOP_THR, 1e-3, STOP_MAX_STEPS, *FIRE_POS)
+    torch.cuda.synchronize()
+    t_batch = time.perf_counter() - t0
+    n = len(models)
+    return {
+        "workload": "%d systems: polygons U{64..1024}, vertices per polygon U{12..48}, "
+                    "phi U[0.80,0.92] (seed %d), %d vertices in all; each minimised by the "
+                    "reference Python driver's rule (|F|max <= 1e-10 or six steps with "
+                    "|dE| < 1e-15), dt0 1e-3" % (n, BATCH_SEED, sum(s.num_vertices for s in systems)),
+        "batched_s_per_system": t_batch / n,
+        "sequential_s_per_system": t_seq / n,
+        "speedup": t_seq / t_batch,
+        "batched_steps_total": int(out[:, 2].sum()),
+        "sequential_steps_total": int(sum(seq_steps)),
+        "batched_converged_to_1e-10": int(np.count_nonzero(out[:, 3] == 1)),
+        "sequential_converged_to_1e-10": seq_conv,
+        "batched_stopped_by_stagnation": int(np.count_nonzero(out[:, 3] == 2)),
+        "batch": "16 streams, 8 FIRE steps per graph launch; both timings include the calls "
+                 "before each system's loop",
+        "autotune_s": t_tune,
+        "autotune": report,
+    }
+
+
 # ------------------------------------------------------------------ CPU legs
 def cpu_threads():
     try:
@@ -386,21 +659,23 @@ def run_reference(args, ws, rank):
         return
     s = make_workload(args.seed)
     threads = cpu_threads()
-    secs, pairs, steps = run_cpu_steps(s, max(1, args.steps), max(0, min(args.warmup, 3)), threads)
+    secs, pairs, steps = run_cpu_steps(s, max(1, args.steps), max(0, args.warmup), threads)
     value = pairs / secs
     print(json.dumps({
         "impl": "reference", "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": ws,
-        "steps": steps, "warmup": min(args.warmup, 3), "ms_per_step": secs / steps * 1e3,
+        "steps": steps, "warmup": args.warmup, "ms_per_step": secs / steps * 1e3,
         "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64",
-        "data": "synthetic (seeded bidisperse star polygons)",
-        "config": {"workload": WORKLOAD, "polygons": N_POLY, "vertices_per_polygon": N_VERT,
-                   "phi": PHI},
+        "data": "synthetic (seeded bidisperse star polygons; the reference publishes no inputs)",
+        "config": dict(CONFIG, parallelism="single"),
+        "pairs": {"rule": PAIR_RULE, "pair_evals_per_step": pairs / steps},
         "cpu_baseline": {"value": value, "unit": UNIT, "cores": threads, "kind": "port",
                          "sample": "%d FIRE steps of the workload by the C restatement of the "
                                    "reference (oracle/), OpenMP on %d threads" % (steps, threads)},
         "e2e": {"value": value, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
-        "note": "the reference is CUDA-only and does not build as shipped (FIRE.h and shake.h "
-                "are missing); its algorithm is timed through the CPU restatement",
+        "note": "the reference has no CPU implementation of the path (its kernels are CUDA; "
+                "FIRE.h and shake.h are missing from it), so its algorithm is timed through "
+                "the CPU restatement, which is checked against the reference's own kernels' "
+                "outputs (tests/golden/ref_gpu_*.npz)",
     }))
 
 
@@ -434,10 +709,13 @@ def main():
     ap.add_argument("--no-e2e", action="store_true")
     ap.add_argument("--no-cpu", action="store_true")
     ap.add_argument("--no-roofline", action="store_true")
+    ap.add_argument("--no-stop", action="store_true")
+    ap.add_argument("--batch-systems", type=int, default=BATCH_SYSTEMS,
+                    help="systems of the many-systems leg (0: skip it)")
     ap.add_argument("--stages", type=int, default=0,
                     help="profiling mode: run every stage this many times, no timing")
     args = ap.parse_args()
-    if args.warmup < 3 and args.impl == "gb300":
+    if args.warmup < 3:
         args.warmup = 3
     ws, rank, local = dist_env()
     if args.impl == "reference":

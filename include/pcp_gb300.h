@@ -168,6 +168,29 @@ int pcp_model_fire_setup(pcp_model* m, double max_force_threshold, double dt_ini
                          double f_inc, double f_dec, int n_min, int shake_iter);
 int pcp_model_fire_continue(pcp_model* m, int n_steps);
 int pcp_model_fire_status(pcp_model* m, double out[8], int* redo_out);
+/* The stop rule of the reference's Python FIRE driver (pyCudaPolygon.py:
+ * 719-727) for the next pcp_model_fire_setup run: a step whose returned
+ * energy differs from the previous step's by less than energy_tol counts as
+ * stagnant (the count is never reset), and the run stops on the device once
+ * the count exceeds stagnant_limit.  stagnant_limit < 0 turns the rule off
+ * (the default: only |F|max and the step limit stop a run). */
+int pcp_model_fire_set_stop_rule(pcp_model* m, double energy_tol, int stagnant_limit);
+/* The last device-resident run: out = {stopped by the stagnation rule (0/1),
+ * min, sum and max over its steps of the last SHAKE iteration count}. */
+int pcp_model_fire_run_stats(pcp_model* m, double out[4]);
+/* model.minimizeFIRE of the reference's Python layer (pyCudaPolygon.py:
+ * 674-731; its loop minimizeFIRELoop, :653-672) as one call: the same model
+ * calls before the loop (initForceEnergy, which resets the cell size to 0.5,
+ * and the small gradient step), then the FIRE steps run as step-graph
+ * launches stopped on the device by |F|max <= max_force_threshold, the
+ * step limit or the stagnation rule (|dE| < 1e-15 counted, stop past 5).
+ * out = {E, dt, steps, min, sum / max_steps, max of the per-step SHAKE
+ * iterations}, the values that driver returns.  max_steps <= 0 only runs
+ * the steps before the loop (out[2] = 0). */
+int pcp_model_minimize_fire_driver(pcp_model* m, double max_force_threshold, double dt_init,
+                                   int max_steps, double dt_max, double alpha_start,
+                                   double f_alpha, double f_inc, double f_dec, int n_min,
+                                   int shake_iter, double out[6]);
 
 /* The contact search (update of the crossing records) split into its stages,
  * enqueued without waiting: 0 = per-polygon prepass and broad phase
@@ -178,6 +201,25 @@ int pcp_model_fire_status(pcp_model* m, double out[8], int* redo_out);
  * Overflow is only detected by pcp_model_update_neighbors. */
 int pcp_model_contacts_stage(pcp_model* m, int stage);
 
+/* No reference counterpart: positions from a device buffer of 2*numVertices
+ * doubles (device-to-device copy on the model's stream), for CUDA-aware
+ * callers such as the PyTorch edge.  Same effect as pcp_model_set_positions. */
+int pcp_model_set_positions_device(pcp_model* m, const double* d_pos, int len);
+/* The overlap energy with a per-vertex output written to the device buffer
+ * d_out (2*numVertices doubles, overwritten), the energy to *energy_out.
+ * search = 1 runs the contact search on the current positions first (else
+ * the records of the last search are used, as updateForceEnergy does).
+ *   mode 0: the reference's energy and force (model.cpp:363-395;
+ *           kernels.cuh:1067-1424), computed record by record -- the same
+ *           values as pcp_model_update_force_energy within rounding.
+ *   mode 1: the energy with the crossing points taken exactly (not from the
+ *           float-rounded parameters, kernels.cuh:857-858) and its exact
+ *           gradient dE/dx, including the dependence of each chain's start
+ *           point that the reference's force leaves out; no reference
+ *           counterpart (the backward of the PyTorch autograd function). */
+int pcp_model_overlap_energy_gradient(pcp_model* m, int mode, int search, double* energy_out,
+                                      double* d_out);
+
 /* ---- getters (model.cpp:654-893); arrays are copied into caller memory ---- */
 int pcp_model_get_num_vertices(pcp_model* m, int* out);
 int pcp_model_get_num_polygons(pcp_model* m, int* out);
@@ -187,6 +229,11 @@ int pcp_model_get_box_size(pcp_model* m, int* out);
 int pcp_model_get_model_enum(pcp_model* m, int* out);
 int pcp_model_get_last_shake_iters(pcp_model* m, int* out);
 int pcp_model_get_energy(pcp_model* m, double* out);
+/* Model::getMaxUnbalancedForce (model.cpp:881-883): max |force component|.
+ * Called right after pcp_model_fire_step (no other call on the model in
+ * between) it returns the maximum the step already read back with its
+ * control block, without a launch: the reference's per-step Python loop
+ * (pyCudaPolygon.py:666-668) asks for it after every step. */
 int pcp_model_get_max_unbalanced_force(pcp_model* m, double* out);
 int pcp_model_get_max_edge_length(pcp_model* m, double* out);
 int pcp_model_get_overlap_area(pcp_model* m, double* out);
@@ -231,6 +278,46 @@ int pcp_model_get_pair_count(pcp_model* m, long long* out);
 int pcp_model_get_narrow_pair_count(pcp_model* m, int* pairs_out, int* self_out);
 /* Kernel launches issued by the model since creation (for accounting). */
 int pcp_model_get_launch_count(pcp_model* m, long long* out);
+
+/* ======================================================================
+ * 1b. Many independent systems (no reference counterpart: the reference
+ *     runs one system per Model)
+ * ====================================================================== */
+typedef struct pcp_batch pcp_batch;
+int pcp_batch_create(pcp_batch** out);
+/* Destroys the batch only; the models stay with their owner. */
+int pcp_batch_destroy(pcp_batch* b);
+/* Adds a configured model (start indices, positions, targets, topology);
+ * the batch does not take ownership. */
+int pcp_batch_add(pcp_batch* b, pcp_model* m);
+int pcp_batch_size(pcp_batch* b, int* out);
+/* Streams the systems are spread over (default 16) and FIRE steps per
+ * graph launch (default 8). */
+int pcp_batch_set_streams(pcp_batch* b, int n_streams, int chunk_steps);
+/* Minimises every system of the batch: each system gets a stream of the
+ * batch's pool and is prepared as rule says (1: the reference's Python
+ * driver, pyCudaPolygon.py:674-731, with its stagnation stop; 0:
+ * Model::minimizeFIRE, model.cpp:488-504), then each launch runs
+ * chunk_steps FIRE steps of one system; the control blocks are read back
+ * once per chunk and stopped systems drop out.  out[4k..4k+3] = {E, dt,
+ * steps, stop: 1 |F|max <= thr, 2 stagnation, 0 step limit} of system k.
+ * The models get their own streams back. */
+int pcp_batch_minimize_fire(pcp_batch* b, int rule, double max_force_threshold, double dt_init,
+                            int max_steps, double dt_max, double alpha_start, double f_alpha,
+                            double f_inc, double f_dec, int n_min, int shake_iter, double* out);
+/* Launch shapes of a model's narrow phase and overlap-force pass (blocks;
+ * 0 = the default of 4 per SM).  Any grid covers the work; the best one
+ * depends on the system's size and on what runs beside it. */
+int pcp_model_set_launch_shape(pcp_model* m, int narrow_blocks, int force_blocks);
+int pcp_model_get_launch_shape(pcp_model* m, int out[2]);
+/* Autotuner: systems grouped by polygon count (classes [2^k, 2^(k+1)));
+ * per class, each candidate grid (SMs x {1/4, 1/2, 1, 2, 4} blocks) runs
+ * `steps` FIRE steps of the class's systems together from the same start
+ * positions (restored afterwards) and the fastest is set on the class's
+ * models.  shapes_out (2 per system, may be NULL) receives the choices;
+ * pcp_batch_autotune_report gives the timing table as JSON. */
+int pcp_batch_autotune(pcp_batch* b, int steps, int* shapes_out);
+int pcp_batch_autotune_report(pcp_batch* b, char* buf, int cap, int* len_out);
 
 /* ======================================================================
  * 2. Stateless kernels on caller-owned device buffers (stream = cudaStream_t)

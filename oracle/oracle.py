@@ -40,6 +40,8 @@ def lib():
             "orc_set_num_vertices": (None, [P, I]),
             "orc_set_positions": (I, [P, dp, I]),
             "orc_set_forces": (None, [P, dp, I]),
+            "orc_set_velocities": (None, [P, dp, I]),
+            "orc_set_energy": (None, [P, D]),
             "orc_set_start_indices": (None, [P, ip, I]),
             "orc_set_target_areas": (None, [P, dp, I]),
             "orc_set_target_edge_lengths": (None, [P, dp, I]),
@@ -165,6 +167,15 @@ class OracleModel:
     def setForces(self, f):
         a = np.ascontiguousarray(f, dtype=np.float64)
         self._L.orc_set_forces(self._m, _dptr(a), int(a.size))
+
+    def setVelocities(self, v):
+        """FIRE state from another implementation (test use only)."""
+        a = np.ascontiguousarray(v, dtype=np.float64)
+        self._L.orc_set_velocities(self._m, _dptr(a), int(a.size))
+
+    def setEnergy(self, e):
+        """Energy the next FIRE step takes as its start energy (test use only)."""
+        self._L.orc_set_energy(self._m, float(e))
 
     def setStartIndices(self, si):
         a = np.ascontiguousarray(si, dtype=np.int32)

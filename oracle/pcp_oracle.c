@@ -261,6 +261,15 @@ void orc_set_forces(orc_model* m, const double* f, int len) {
     memcpy(m->force, f, (size_t)len * 8);
 }
 
+/* State setters for tests that start the oracle from another
+ * implementation's FIRE state (no counterpart in the reference). */
+void orc_set_velocities(orc_model* m, const double* v, int len) {
+    if (len > 2 * m->size) len = 2 * m->size;
+    memcpy(m->velocities, v, (size_t)len * 8);
+}
+
+void orc_set_energy(orc_model* m, double e) { m->energy = e; }
+
 void orc_set_start_indices(orc_model* m, const int* si, int len) {
     int P = len - 1;
     if (P < 0) P = 0;

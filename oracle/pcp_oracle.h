@@ -61,6 +61,8 @@ void orc_set_threads(int nthreads);
 void orc_set_num_vertices(orc_model* m, int n);
 int  orc_set_positions(orc_model* m, const double* pos, int len);
 void orc_set_forces(orc_model* m, const double* f, int len);
+void orc_set_velocities(orc_model* m, const double* v, int len);
+void orc_set_energy(orc_model* m, double e);
 void orc_set_start_indices(orc_model* m, const int* si, int len);
 void orc_set_target_areas(orc_model* m, const double* a, int len);
 void orc_set_target_edge_lengths(orc_model* m, const double* l, int len);

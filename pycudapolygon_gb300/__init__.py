@@ -5,9 +5,10 @@ Layers:
   _build/libpyCudaPolygon*.so                    pybind11 module with the reference's
                                                  `Model` method table (drop-in)
   cabi.py                                        ctypes view of the C ABI
-  model.py                                       Python `model` class with the hot-path
-                                                 drivers of the reference's Python API
   systems.py                                     seeded synthetic polygon systems
+
+The reference's own Python layer (pyCudaPolygon.py, its mixins and enums)
+runs unchanged on `libpyCudaPolygon`.
 
 Nothing here falls back to a CPU path: if the compiled library is missing the
 import of `libpyCudaPolygon` fails, and every call needs a CUDA device.

@@ -1693,6 +1693,16 @@ __device__ void fire_scalars(Ctrl* __restrict__ c) {
     c->dt = dt; c->alpha = alpha; c->nPos = nPos;
     c->stepsDone += 1;
     c->Rmax = 0.f;     // for the next step's fused start (see zero_contact_counters_but_rmax)
+    const int it = c->shakeLast;
+    c->shakeMinRun = min(c->shakeMinRun, it);
+    c->shakeMaxRun = max(c->shakeMaxRun, it);
+    c->shakeSumRun += it;
+    if (c->stagnantLimit >= 0) {
+        // pyCudaPolygon.py:723-727: |E - E_prev| < 1e-15 counted, stop past 5
+        if (fabs(c->outE - c->prevE) < c->stagnantTol) c->stagnant += 1;
+        if (c->stagnant > c->stagnantLimit) { c->stagnated = 1; c->active = 0; }
+        c->prevE = c->outE;
+    }
     if (c->maxF <= c->threshold) { c->converged = 1; c->active = 0; }
     if (c->stepLimit > 0 && c->stepsDone >= c->stepLimit) c->active = 0;
 }
@@ -1716,7 +1726,13 @@ __global__ void k_set_fire_params(Ctrl* __restrict__ c, FireScalars f) {
     c->dtMax = f.dtMax; c->alphaStart = f.alphaStart; c->fAlpha = f.fAlpha; c->fInc = f.fInc;
     c->fDec = f.fDec; c->nMin = f.nMin; c->shakeIter = f.shakeIter; c->threshold = f.threshold;
     c->active = 1;
-    if (f.resetRun) { c->converged = 0; c->stepsDone = 0; }
+    if (f.resetRun) {
+        c->converged = 0; c->stepsDone = 0;
+        c->prevE = 1e9; c->stagnant = 0; c->stagnated = 0;    // pyCudaPolygon.py:707-710
+        c->shakeMinRun = 1000000000; c->shakeMaxRun = 0; c->shakeSumRun = 0;
+    }
+    c->stagnantTol = f.stagnantTol;
+    c->stagnantLimit = f.stagnantLimit;
     c->stepLimit = f.stepLimit;
     c->rbBodyKernels = f.rbBodyKernels;
     c->Rmax = 0.f;

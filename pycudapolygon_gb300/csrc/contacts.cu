@@ -1675,7 +1675,7 @@ cudaError_t launch_contacts(const double2* pos, const int* start, const int* sha
     }
     if ((stages & 2) && P > 0) {
         size_t smem = sizeof(WarpSmem) * kNarrowWarps;
-        int grid = sm_count() * 4;
+        int grid = ws.narrowBlocks > 0 ? ws.narrowBlocks : sm_count() * 4;
         launch_k(k_narrow, dim3(grid), dim3(32 * kNarrowWarps), smem, st, pos, start, B, ws, ctrl, gate);
         // pairs for the block path are rare: a few blocks take them in turn
         launch_k(k_narrow_slow, dim3(16), dim3(32), kSlowSmem, st, pos, start, B, ws, ctrl, gate);
@@ -1699,8 +1699,9 @@ cudaError_t launch_overlap_force(const double2* pos, const int* start,
                                  int V, ContactWS& ws, Ctrl* ctrl, double2* force,
                                  const int* gate, cudaStream_t st, const double2* edge,
                                  int decide, cudaGraphConditionalHandle rbCond) {
-    // one pass over up to 4 * SMs * kForceWarps * kForceRecs records
-    int grid = sm_count() * 4;
+    // one pass over up to 4 * SMs * kForceWarps * kForceRecs records (a
+    // smaller grid loops over the records)
+    int grid = ws.forceBlocks > 0 ? ws.forceBlocks : sm_count() * 4;
     if (edge)
         launch_k(k_overlap_force<true>, dim3(grid), dim3(32 * kForceWarps), 0, st, pos, start, V, ws,
                  ctrl, force, edge, decide, rbCond, gate);

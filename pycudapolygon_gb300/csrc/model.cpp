@@ -12,10 +12,12 @@
 #include <cuda_runtime.h>
 
 #include <algorithm>
+#include <chrono>
 #include <cmath>
 #include <cstdarg>
 #include <cstdio>
 #include <cstring>
+#include <map>
 #include <numeric>
 #include <string>
 #include <vector>
@@ -82,6 +84,15 @@ struct pcp_model {
     cudaStream_t stream = nullptr;
     long long launches = 0;
     unsigned long long generation = 1;
+    // every C ABI call on the model counts one; the max |F| a FIRE step
+    // read back is returned by the next call if that call is
+    // pcp_model_get_max_unbalanced_force (nothing ran in between)
+    unsigned long long callSerial = 0;
+    unsigned long long maxFSerial = 0;
+    double maxFCached = 0.0;
+    // stop rule of the device-resident loop (pcp_model_fire_set_stop_rule)
+    double stopTol = 1e-15;
+    int stopStagnant = -1;
 
     // device state
     double2 *pos = nullptr, *force = nullptr, *vel = nullptr;
@@ -96,6 +107,8 @@ struct pcp_model {
     int *cellLocation = nullptr, *shakeIters = nullptr;
     int *mcCounter = nullptr, *mcNbIdx = nullptr, *mcBoxStarts = nullptr;
     unsigned long long* mcSum = nullptr;
+    double* gradEnergy = nullptr;   // energy of pcp_model_overlap_energy_gradient
+    int* gradBad = nullptr;
     Ctrl* ctrl = nullptr;
     Ctrl* ctrlHost = nullptr;   // pinned mirror
     ContactWS ws;
@@ -110,8 +123,10 @@ struct pcp_model {
     std::vector<int> hNeighbors, hNumNeighbors, hShapeCounts;
     std::vector<uint8_t> hInside;
 
-    // FIRE graph
+    // FIRE graph (one step) and a graph of fireMultiSteps steps in a row
     cudaGraphExec_t fireExec = nullptr;
+    cudaGraphExec_t fireExecMulti = nullptr;
+    int fireMultiSteps = 0;
     unsigned long long fireGen = 0;
     int fireShakeIter = -1, fireModel = -1, fireB = -1;
     int fireKernelNodes = 0;   // kernel launches one FIRE step graph makes
@@ -125,6 +140,7 @@ struct pcp_model {
 
     void release() {
         if (fireExec) { cudaGraphExecDestroy(fireExec); fireExec = nullptr; }
+        if (fireExecMulti) { cudaGraphExecDestroy(fireExecMulti); fireExecMulti = nullptr; }
         if (sideStream) { cudaStreamDestroy(sideStream); sideStream = nullptr; }
         if (bodyStream) { cudaStreamDestroy(bodyStream); bodyStream = nullptr; }
         if (evFork) { cudaEventDestroy(evFork); evFork = nullptr; }
@@ -143,6 +159,7 @@ struct pcp_model {
         dfree(&targetAreas); dfree(&targetEdge); dfree(&maxEdge); dfree(&dtmp); dfree(&xpbdDev);
         dfree(&start); dfree(&shapeId); dfree(&next); dfree(&prev); dfree(&cellLocation);
         dfree(&shakeIters); dfree(&mcCounter); dfree(&mcNbIdx); dfree(&mcBoxStarts); dfree(&mcSum);
+        dfree(&gradEnergy); dfree(&gradBad);
         dfree(&ctrl);
         if (ctrlHost) { cudaFreeHost(ctrlHost); ctrlHost = nullptr; }
         free_ws();
@@ -660,12 +677,11 @@ int record_fire_step(pcp_model* m, cudaGraphConditionalHandle retryCond,
     return PCP_OK;
 }
 
-int build_fire_graph(pcp_model* m, int shakeIter) {
-    if (m->fireExec && m->fireGen == m->generation && m->fireShakeIter == shakeIter &&
-        m->fireModel == m->modelType && m->fireB == m->boxSize)
-        return PCP_OK;
-    if (m->fireExec) { cudaGraphExecDestroy(m->fireExec); m->fireExec = nullptr; }
-    m->fireShakeIter = shakeIter;
+// Capture nSteps consecutive FIRE steps into one executable graph (each
+// step with its own conditional handles); kernelNodes receives the kernel
+// launches of one step.
+int capture_fire_graph(pcp_model* m, int nSteps, cudaGraphExec_t* exec, int* kernelNodes) {
+    const int shakeIter = m->fireShakeIter;
     if (!m->sideStream) CK(cudaStreamCreateWithFlags(&m->sideStream, cudaStreamNonBlocking));
     if (!m->bodyStream) CK(cudaStreamCreateWithFlags(&m->bodyStream, cudaStreamNonBlocking));
     if (!m->evFork) CK(cudaEventCreateWithFlags(&m->evFork, cudaEventDisableTiming));
@@ -691,14 +707,16 @@ int build_fire_graph(pcp_model* m, int shakeIter) {
         // that no conditional node uses makes the instantiation fail).
         cudaStreamCaptureStatus cs;
         cudaGraph_t cg = nullptr;
-        cudaGraphConditionalHandle retryCond = 0, rbCond = 0;
         const bool retry = m->modelType == PCP_MODEL_NORMAL && shakeIter > 0;
         e = cudaStreamGetCaptureInfo(cap, &cs, nullptr, &cg);
-        if (e == cudaSuccess && retry)
-            e = cudaGraphConditionalHandleCreate(&retryCond, cg, 0, cudaGraphCondAssignDefault);
-        if (e == cudaSuccess)
-            e = cudaGraphConditionalHandleCreate(&rbCond, cg, 0, cudaGraphCondAssignDefault);
-        if (e == cudaSuccess) rc = record_fire_step(m, retryCond, rbCond);
+        for (int step = 0; step < nSteps && e == cudaSuccess && rc == PCP_OK; ++step) {
+            cudaGraphConditionalHandle retryCond = 0, rbCond = 0;
+            if (e == cudaSuccess && retry)
+                e = cudaGraphConditionalHandleCreate(&retryCond, cg, 0, cudaGraphCondAssignDefault);
+            if (e == cudaSuccess)
+                e = cudaGraphConditionalHandleCreate(&rbCond, cg, 0, cudaGraphCondAssignDefault);
+            if (e == cudaSuccess) rc = record_fire_step(m, retryCond, rbCond);
+        }
         cudaError_t e2 = cudaStreamEndCapture(cap, &g);
         if (e == cudaSuccess) e = e2;
     }
@@ -711,16 +729,13 @@ int build_fire_graph(pcp_model* m, int shakeIter) {
         (void)cudaGetLastError();    // not left for the next launcher's check
         return fail(PCP_ERR_CUDA, "graph capture failed: %s", cudaGetErrorString(e));
     }
-    m->fireKernelNodes = count_kernel_nodes(g);
-    e = cudaGraphInstantiate(&m->fireExec, g, 0);
+    *kernelNodes = count_kernel_nodes(g) / std::max(nSteps, 1);
+    e = cudaGraphInstantiate(exec, g, 0);
     cudaGraphDestroy(g);
     if (e != cudaSuccess) {
         (void)cudaGetLastError();    // not left for the next launcher's check
         return fail(PCP_ERR_CUDA, "graph instantiate failed: %s", cudaGetErrorString(e));
     }
-    m->fireGen = m->generation;
-    m->fireModel = m->modelType;
-    m->fireB = m->boxSize;
     // the rollback kernel counts its body's launches from the control block
     m->ctrlHost->rbBodyKernels = m->rbBodyKernels;
     CK(cudaMemcpyAsync(&m->ctrl->rbBodyKernels, &m->ctrlHost->rbBodyKernels, sizeof(int),
@@ -728,16 +743,48 @@ int build_fire_graph(pcp_model* m, int shakeIter) {
     return sync(m);
 }
 
+int build_fire_graph(pcp_model* m, int shakeIter) {
+    if (m->fireExec && m->fireGen == m->generation && m->fireShakeIter == shakeIter &&
+        m->fireModel == m->modelType && m->fireB == m->boxSize)
+        return PCP_OK;
+    if (m->fireExec) { cudaGraphExecDestroy(m->fireExec); m->fireExec = nullptr; }
+    if (m->fireExecMulti) { cudaGraphExecDestroy(m->fireExecMulti); m->fireExecMulti = nullptr; }
+    m->fireShakeIter = shakeIter;
+    int rc = capture_fire_graph(m, 1, &m->fireExec, &m->fireKernelNodes);
+    if (rc) return rc;
+    m->fireGen = m->generation;
+    m->fireModel = m->modelType;
+    m->fireB = m->boxSize;
+    return PCP_OK;
+}
+
+// The step graph and a graph of nSteps steps in a row (one launch for a
+// chunk of steps), both for the current parameters.
+int build_fire_graph_multi(pcp_model* m, int shakeIter, int nSteps) {
+    int rc = build_fire_graph(m, shakeIter);
+    if (rc) return rc;
+    if (m->fireExecMulti && m->fireMultiSteps == nSteps) return PCP_OK;
+    if (m->fireExecMulti) { cudaGraphExecDestroy(m->fireExecMulti); m->fireExecMulti = nullptr; }
+    int nodes = 0;
+    rc = capture_fire_graph(m, nSteps, &m->fireExecMulti, &nodes);
+    if (rc) return rc;
+    m->fireMultiSteps = nSteps;
+    return PCP_OK;
+}
+
 struct FireParams {
     double dt, alpha, dtMax, alphaStart, fAlpha, fInc, fDec, threshold;
     int nPos, nMin, shakeIter, stepLimit;
+    double stagnantTol = 0.0;
+    int stagnantLimit = -1;     // the Python driver's stop rule (< 0: off)
 };
 
 // write the step parameters into the device control block (a one-thread
 // kernel on the model's stream: no host round trip)
 int set_fire_params(pcp_model* m, const FireParams& f, bool resetRun) {
     FireScalars d{f.dt, f.alpha, f.dtMax, f.alphaStart, f.fAlpha, f.fInc, f.fDec, f.threshold,
-                  f.nPos, f.nMin, f.shakeIter, f.stepLimit, resetRun ? 1 : 0, m->rbBodyKernels};
+                  f.nPos, f.nMin, f.shakeIter, f.stepLimit, resetRun ? 1 : 0, m->rbBodyKernels,
+                  f.stagnantTol, f.stagnantLimit};
     CK(launch_set_fire_params(m->ctrl, d, m->stream));
     m->launches++;
     return PCP_OK;
@@ -788,6 +835,8 @@ int fire_step_once(pcp_model* m, const FireParams& fp, double out[4]) {
         if (!redo) {
             const Ctrl& c = *m->ctrlHost;
             out[0] = c.outE; out[1] = c.dt; out[2] = c.alpha; out[3] = c.nPos;
+            m->maxFCached = c.maxF;
+            m->maxFSerial = m->callSerial;
             m->lastShakeIters = c.shakeLast;
             m->numIntersections = c.numRecords;
             m->view = pcp_model::VIEW_FINAL;
@@ -812,7 +861,7 @@ extern "C" {
 const char* pcp_last_error(void) { return g_err.c_str(); }
 const char* pcp_version(void) { return "pcp_gb300 0.1 (sm_103a)"; }
 
-#define CHECK_M(m) do { if (!(m)) return fail(PCP_ERR_ARG, "null model"); } while (0)
+#define CHECK_M(m) do { if (!(m)) return fail(PCP_ERR_ARG, "null model"); ++(m)->callSerial; } while (0)
 
 int pcp_model_create(int size, pcp_model** out) {
     if (!out) return fail(PCP_ERR_ARG, "null output");
@@ -1306,9 +1355,146 @@ int pcp_model_fire_setup(pcp_model* m, double thr, double dt0, int max_steps, do
     }
     FireParams fp{dt0, alpha_start, dt_max, alpha_start, f_alpha, f_inc, f_dec, thr,
                   0, n_min, shake_iter, max_steps > 0 ? max_steps : 0};
+    fp.stagnantTol = m->stopTol;
+    fp.stagnantLimit = m->stopStagnant;
     rc = build_fire_graph(m, shake_iter);
     if (rc) return rc;
     return set_fire_params(m, fp, true);
+}
+
+int pcp_model_fire_set_stop_rule(pcp_model* m, double energy_tol, int stagnant_limit) {
+    CHECK_M(m);
+    if (!(energy_tol >= 0.0)) return fail(PCP_ERR_ARG, "energy tolerance must be >= 0");
+    m->stopTol = energy_tol;
+    m->stopStagnant = stagnant_limit < 0 ? -1 : stagnant_limit;
+    return PCP_OK;
+}
+
+int pcp_model_fire_run_stats(pcp_model* m, double out[4]) {
+    CHECK_M(m);
+    int rc = read_ctrl(m);
+    if (rc) return rc;
+    const Ctrl& c = *m->ctrlHost;
+    out[0] = c.stagnated;
+    out[1] = c.stepsDone > 0 ? (double)c.shakeMinRun : 1e9;
+    out[2] = (double)c.shakeSumRun;
+    out[3] = (double)c.shakeMaxRun;
+    return PCP_OK;
+}
+
+// pyCudaPolygon.py:674-731 (the reference's Python minimizeFIRE) with its
+// per-step loop (pyCudaPolygon.py:653-672) run on the device: the same calls
+// before the loop, then step graphs launched in chunks without a host round
+// trip per step, stopped on the device by |F|max <= thr or by the energy
+// stagnation rule of pyCudaPolygon.py:723-727.
+}  // extern "C"
+
+// Everything of a device-resident run before its first step.  rule 1: the
+// reference's Python driver (pyCudaPolygon.py:674-700: initForceEnergy,
+// which resets the cell size to 0.5, and the small gradient step; then its
+// loop's start, :658-664) with its stagnation stop rule; rule 0:
+// Model::minimizeFIRE (model.cpp:488-496), stopped only by |F|max and the
+// step limit.  max_steps <= 0 with rule 1 runs only the calls before the loop.
+static int prepare_run(pcp_model* m, int rule, double thr, double dt0, int max_steps,
+                       double dt_max, double alpha_start, double f_alpha, double f_inc,
+                       double f_dec, int n_min, int shake_iter) {
+    int rc = need_topology(m);
+    if (rc) return rc;
+    const bool normal = m->modelType == PCP_MODEL_NORMAL;
+#define RUN(call) do { rc = (call); if (rc) return rc; } while (0)
+    if (rule == 1) {
+        RUN(pcp_model_reset_velocities(m));
+        if (normal) {
+            RUN(pcp_model_initialize_neighbor_cells(m));
+            RUN(pcp_model_set_max_edge_length(m, 0.5));
+            RUN(pcp_model_update_neighbor_cells(m));
+            RUN(pcp_model_update_neighbors(m));
+            RUN(pcp_model_update_outersections(m));
+        }
+        RUN(pcp_model_update_polygon_geometry(m));
+        RUN(pcp_model_update_force_energy(m));
+        if (normal) RUN(pcp_model_project_force(m));
+        if (normal && max_steps > 0) {
+            RUN(pcp_model_update_positions(m, dt0));
+            RUN(pcp_model_update_polygon_geometry(m));
+            RUN(pcp_model_update_neighbor_cells(m));
+            RUN(pcp_model_update_neighbors(m));
+            RUN(pcp_model_update_outersections(m));
+            RUN(pcp_model_update_force_energy(m));
+            RUN(pcp_model_project_force(m));
+            RUN(pcp_model_reset_velocities(m));
+        }
+        if (max_steps <= 0) return PCP_OK;
+    }
+#undef RUN
+    const double tol0 = m->stopTol;
+    const int lim0 = m->stopStagnant;
+    m->stopTol = 1e-15;
+    m->stopStagnant = rule == 1 ? 5 : -1;
+    rc = pcp_model_fire_setup(m, thr, dt0, max_steps, dt_max, alpha_start, f_alpha, f_inc, f_dec,
+                              n_min, shake_iter);
+    m->stopTol = tol0;
+    m->stopStagnant = lim0;
+    return rc;
+}
+
+extern "C" {
+
+// pyCudaPolygon.py:674-731 (the reference's Python minimizeFIRE) with its
+// per-step loop (pyCudaPolygon.py:653-672) run on the device: the same calls
+// before the loop, then step graphs launched in chunks without a host round
+// trip per step, stopped on the device by |F|max <= thr or by the energy
+// stagnation rule of pyCudaPolygon.py:723-727.
+int pcp_model_minimize_fire_driver(pcp_model* m, double thr, double dt0, int max_steps,
+                                   double dt_max, double alpha_start, double f_alpha, double f_inc,
+                                   double f_dec, int n_min, int shake_iter, double out[6]) {
+    CHECK_M(m);
+    const bool normal = m->modelType == PCP_MODEL_NORMAL;
+    int rc = prepare_run(m, 1, thr, dt0, max_steps, dt_max, alpha_start, f_alpha, f_inc, f_dec,
+                         n_min, shake_iter);
+    if (rc) return rc;
+    if (max_steps <= 0) {
+        double e = 0.0;
+        rc = pcp_model_get_energy(m, &e);
+        if (rc) return rc;
+        out[0] = e; out[1] = dt0; out[2] = 0; out[3] = 1e9; out[4] = 0; out[5] = 0;
+        return PCP_OK;
+    }
+    const int chunk = 32;
+    int recoveries = 0;
+    for (;;) {
+        int left = max_steps - m->ctrlHost->stepsDone;
+        int todo = std::min(chunk, left);
+        if (todo <= 0) break;
+        for (int s = 0; s < todo; ++s) CK(cudaGraphLaunch(m->fireExec, m->stream));
+        m->launches += (long long)todo * m->fireKernelNodes;
+        rc = read_ctrl(m);
+        if (rc) return rc;
+        bool redo = false;
+        rc = recover_fire(m, redo);
+        if (rc) return rc;
+        if (redo) {
+            if (++recoveries > 16) return fail(PCP_ERR_CAPACITY, "contact buffers could not be sized");
+            continue;
+        }
+        if (!m->ctrlHost->active) break;
+    }
+    const Ctrl& c = *m->ctrlHost;
+    m->lastShakeIters = c.shakeLast;
+    m->numIntersections = c.numRecords;
+    m->view = pcp_model::VIEW_FINAL;
+    m->invalidate();
+    if (normal && c.stepsDone > 0) {
+        m->geometryStale = true;
+        m->geomFromSnapshot = false;
+    }
+    out[0] = c.outE;
+    out[1] = c.dt;
+    out[2] = c.stepsDone;
+    out[3] = c.stepsDone > 0 ? (double)c.shakeMinRun : 1e9;
+    out[4] = (double)c.shakeSumRun / (double)max_steps;
+    out[5] = (double)c.shakeMaxRun;
+    return PCP_OK;
 }
 
 int pcp_model_fire_continue(pcp_model* m, int n_steps) {
@@ -1339,6 +1525,51 @@ int pcp_model_fire_status(pcp_model* m, double out[8], int* redo_out) {
     m->numIntersections = c.numRecords;
     m->view = pcp_model::VIEW_FINAL;
     m->invalidate();
+    return PCP_OK;
+}
+
+int pcp_model_set_positions_device(pcp_model* m, const double* d_pos, int len) {
+    CHECK_M(m);
+    if (len != 2 * m->V) return fail(PCP_ERR_ARG, "positions must hold 2*numVertices values");
+    if (len > 0 && !d_pos) return fail(PCP_ERR_ARG, "null device buffer");
+    if (len > 0)
+        CK(cudaMemcpyAsync(m->pos, d_pos, (size_t)len * sizeof(double), cudaMemcpyDeviceToDevice,
+                           m->stream));
+    // the same state changes as the host setter
+    m->geometryStale = false;
+    m->geomFromSnapshot = false;
+    m->invalidate();
+    return PCP_OK;
+}
+
+int pcp_model_overlap_energy_gradient(pcp_model* m, int mode, int search, double* energy_out,
+                                      double* d_out) {
+    CHECK_M(m);
+    int rc = need_topology(m);
+    if (rc) return rc;
+    if (mode != kRefForce && mode != kExactGrad) return fail(PCP_ERR_ARG, "unknown mode %d", mode);
+    if (!d_out || !energy_out) return fail(PCP_ERR_ARG, "null output");
+    if (search) {
+        rc = run_contacts(m);
+        if (rc) return rc;
+        m->view = pcp_model::VIEW_COMPACT;
+        m->invalidate();
+    }
+    if (!m->gradEnergy) CK(dalloc(&m->gradEnergy, 1));
+    if (!m->gradBad) CK(dalloc(&m->gradBad, 1));
+    CK(cudaMemsetAsync(d_out, 0, (size_t)m->V * 2 * sizeof(double), m->stream));
+    CK(cudaMemsetAsync(m->gradEnergy, 0, sizeof(double), m->stream));
+    CK(cudaMemsetAsync(m->gradBad, 0, sizeof(int), m->stream));
+    CK(launch_overlap_energy_grad(m->pos, m->start, m->V, m->ws, m->ctrl, mode,
+                                  reinterpret_cast<double2*>(d_out), m->gradEnergy, m->gradBad,
+                                  m->stream));
+    m->launches++;
+    int bad = 0;
+    CK(cudaMemcpyAsync(energy_out, m->gradEnergy, sizeof(double), cudaMemcpyDeviceToHost, m->stream));
+    CK(cudaMemcpyAsync(&bad, m->gradBad, sizeof(int), cudaMemcpyDeviceToHost, m->stream));
+    rc = sync(m);
+    if (rc) return rc;
+    if (bad) return fail(PCP_ERR_NUMERIC, "a crossing record names a vertex outside its polygon");
     return PCP_OK;
 }
 
@@ -1385,6 +1616,13 @@ int pcp_model_get_energy(pcp_model* m, double* out) {
 }
 int pcp_model_get_max_unbalanced_force(pcp_model* m, double* out) {
     CHECK_M(m);
+    if (m->maxFSerial != 0 && m->maxFSerial + 1 == m->callSerial) {
+        // the FIRE step just before read it back with its control block (the
+        // same maximum over the same forces); the reference's per-step loop
+        // (pyCudaPolygon.py:666-668) asks for it after every step
+        *out = m->maxFCached;
+        return PCP_OK;
+    }
     CK(launch_max_abs(reinterpret_cast<const double*>(m->force), 2 * m->V, m->dtmp, m->stream));
     m->launches++;
     CK(cudaMemcpyAsync(out, m->dtmp, sizeof(double), cudaMemcpyDeviceToHost, m->stream));
@@ -1730,6 +1968,296 @@ int pcp_shake_project_noalloc(double* d_pos, const int* d_start, int P, const do
 
 int pcp_update_positions(double* d_pos, const double* d_force, int V, double dt, void* stream) {
     CK(launch_update_positions(d_pos, d_force, V, dt, (cudaStream_t)stream));
+    return PCP_OK;
+}
+
+}  // extern "C"
+
+// ======================================================================
+// Many independent systems minimised together (no reference counterpart;
+// the reference runs one system per Model).  Every system keeps its own
+// model, buffers and step graph; the batch gives each a stream of a pool of
+// streams, launches each system's graph of `chunk` consecutive FIRE steps
+// on its stream, reads all control blocks back once per chunk and drops the
+// systems that have stopped.  Systems on different streams run at the same
+// time, so small systems fill the GPU together.
+// ======================================================================
+struct pcp_batch {
+    std::vector<pcp_model*> models;
+    std::vector<cudaStream_t> streams;
+    int nStreams = 16;
+    int chunk = 8;
+    std::string report;          // the last autotune table (JSON)
+    ~pcp_batch() {
+        for (cudaStream_t s : streams) cudaStreamDestroy(s);
+    }
+};
+
+namespace {
+
+int batch_streams(pcp_batch* b) {
+    while ((int)b->streams.size() < b->nStreams) {
+        cudaStream_t s = nullptr;
+        CK(cudaStreamCreateWithFlags(&s, cudaStreamNonBlocking));
+        b->streams.push_back(s);
+    }
+    return PCP_OK;
+}
+
+struct RunArgs {
+    int rule;
+    double thr, dt0;
+    int maxSteps;
+    double dtMax, alphaStart, fAlpha, fInc, fDec;
+    int nMin, shakeIter;
+};
+
+// Prepare every system (on its own stream), then launch chunks of steps
+// until every system has stopped.  `which` lists the systems to run.
+int batch_run(pcp_batch* b, const std::vector<int>& which, const RunArgs& a) {
+    int rc = batch_streams(b);
+    if (rc) return rc;
+    const int K = b->nStreams;
+    for (size_t q = 0; q < which.size(); ++q) {
+        pcp_model* m = b->models[which[q]];
+        m->stream = b->streams[q % K];
+        rc = prepare_run(m, a.rule, a.thr, a.dt0, a.maxSteps, a.dtMax, a.alphaStart, a.fAlpha,
+                         a.fInc, a.fDec, a.nMin, a.shakeIter);
+        if (rc) return rc;
+        rc = build_fire_graph_multi(m, a.shakeIter, b->chunk);
+        if (rc) return rc;
+    }
+    std::vector<int> active = which;
+    int recoveries = 0;
+    while (!active.empty()) {
+        for (int i : active) {
+            pcp_model* m = b->models[i];
+            CK(cudaGraphLaunch(m->fireExecMulti, m->stream));
+            m->launches += (long long)b->chunk * m->fireKernelNodes;
+            CK(cudaMemcpyAsync(m->ctrlHost, m->ctrl, sizeof(Ctrl), cudaMemcpyDeviceToHost,
+                               m->stream));
+        }
+        for (cudaStream_t s : b->streams) CK(cudaStreamSynchronize(s));
+        std::vector<int> next;
+        for (int i : active) {
+            pcp_model* m = b->models[i];
+            bool redo = false;
+            rc = recover_fire(m, redo);
+            if (rc) return rc;
+            if (redo) {
+                if (++recoveries > 16 * (int)b->models.size())
+                    return fail(PCP_ERR_CAPACITY, "contact buffers could not be sized");
+                rc = build_fire_graph_multi(m, a.shakeIter, b->chunk);
+                if (rc) return rc;
+                next.push_back(i);
+            } else if (m->ctrlHost->active) {
+                next.push_back(i);
+            }
+        }
+        active.swap(next);
+    }
+    for (int i : which) {
+        pcp_model* m = b->models[i];
+        const Ctrl& c = *m->ctrlHost;
+        m->lastShakeIters = c.shakeLast;
+        m->numIntersections = c.numRecords;
+        m->view = pcp_model::VIEW_FINAL;
+        m->invalidate();
+        if (m->modelType == PCP_MODEL_NORMAL && c.stepsDone > 0) {
+            m->geometryStale = true;
+            m->geomFromSnapshot = false;
+        }
+    }
+    return PCP_OK;
+}
+
+}  // namespace
+
+extern "C" {
+
+int pcp_batch_create(pcp_batch** out) {
+    if (!out) return fail(PCP_ERR_ARG, "null output");
+    *out = new pcp_batch();
+    return PCP_OK;
+}
+
+int pcp_batch_destroy(pcp_batch* b) {
+    delete b;
+    return PCP_OK;
+}
+
+int pcp_batch_add(pcp_batch* b, pcp_model* m) {
+    if (!b || !m) return fail(PCP_ERR_ARG, "null batch or model");
+    int rc = need_topology(m);
+    if (rc) return rc;
+    b->models.push_back(m);
+    return PCP_OK;
+}
+
+int pcp_batch_size(pcp_batch* b, int* out) {
+    if (!b || !out) return fail(PCP_ERR_ARG, "null argument");
+    *out = (int)b->models.size();
+    return PCP_OK;
+}
+
+int pcp_batch_set_streams(pcp_batch* b, int n_streams, int chunk_steps) {
+    if (!b) return fail(PCP_ERR_ARG, "null batch");
+    if (n_streams < 1 || n_streams > 256 || chunk_steps < 1 || chunk_steps > 256)
+        return fail(PCP_ERR_ARG, "streams and chunk steps must be in 1..256");
+    b->nStreams = n_streams;
+    b->chunk = chunk_steps;
+    return PCP_OK;
+}
+
+int pcp_model_set_launch_shape(pcp_model* m, int narrow_blocks, int force_blocks) {
+    CHECK_M(m);
+    if (narrow_blocks < 0 || force_blocks < 0) return fail(PCP_ERR_ARG, "negative block count");
+    if (m->ws.narrowBlocks != narrow_blocks || m->ws.forceBlocks != force_blocks) {
+        m->ws.narrowBlocks = narrow_blocks;
+        m->ws.forceBlocks = force_blocks;
+        m->generation++;          // the step graphs bake the grids in: rebuild them
+    }
+    return PCP_OK;
+}
+
+int pcp_model_get_launch_shape(pcp_model* m, int out[2]) {
+    CHECK_M(m);
+    out[0] = m->ws.narrowBlocks > 0 ? m->ws.narrowBlocks : sm_count() * 4;
+    out[1] = m->ws.forceBlocks > 0 ? m->ws.forceBlocks : sm_count() * 4;
+    return PCP_OK;
+}
+
+int pcp_batch_minimize_fire(pcp_batch* b, int rule, double thr, double dt0, int max_steps,
+                            double dt_max, double alpha_start, double f_alpha, double f_inc,
+                            double f_dec, int n_min, int shake_iter, double* out) {
+    if (!b || !out) return fail(PCP_ERR_ARG, "null argument");
+    if (rule != 0 && rule != 1) return fail(PCP_ERR_ARG, "rule must be 0 or 1");
+    if (max_steps <= 0) return fail(PCP_ERR_ARG, "max_steps must be positive");
+    std::vector<int> all(b->models.size());
+    for (size_t i = 0; i < all.size(); ++i) all[i] = (int)i;
+    RunArgs a{rule, thr, dt0, max_steps, dt_max, alpha_start, f_alpha, f_inc, f_dec, n_min,
+              shake_iter};
+    std::vector<cudaStream_t> saved;
+    for (pcp_model* m : b->models) saved.push_back(m->stream);
+    int rc = batch_run(b, all, a);
+    for (size_t i = 0; i < b->models.size(); ++i) b->models[i]->stream = saved[i];
+    if (rc) return rc;
+    for (size_t i = 0; i < b->models.size(); ++i) {
+        const Ctrl& c = *b->models[i]->ctrlHost;
+        out[4 * i + 0] = c.outE;
+        out[4 * i + 1] = c.dt;
+        out[4 * i + 2] = c.stepsDone;
+        out[4 * i + 3] = c.converged ? 1 : (c.stagnated ? 2 : 0);
+    }
+    return PCP_OK;
+}
+
+// Autotuner of the launch shapes: systems are grouped by polygon count
+// (classes [2^k, 2^(k+1))); for each class every candidate grid (SMs x {1/4,
+// 1/2, 1, 2, 4} blocks for both the narrow phase and the force pass) runs
+// `steps` FIRE steps of all the class's systems at once on the batch's
+// streams from the same start positions, and the fastest is kept for the
+// class.  Positions are restored after each trial.  shapes_out (2 per
+// system, may be null) receives the chosen (narrow, force) blocks; the table
+// of timings is kept as JSON for pcp_batch_autotune_report.
+int pcp_batch_autotune(pcp_batch* b, int steps, int* shapes_out) {
+    if (!b) return fail(PCP_ERR_ARG, "null batch");
+    if (steps < 1) return fail(PCP_ERR_ARG, "steps must be positive");
+    const int n = (int)b->models.size();
+    std::map<int, std::vector<int>> classes;
+    for (int i = 0; i < n; ++i) {
+        int p = std::max(1, b->models[i]->P), k = 0;
+        while ((2 << k) <= p) ++k;
+        classes[k].push_back(i);
+    }
+    const int sm = sm_count();
+    const int cand[5] = {std::max(1, sm / 4), std::max(1, sm / 2), sm, 2 * sm, 4 * sm};
+    std::vector<cudaStream_t> saved;
+    for (pcp_model* m : b->models) saved.push_back(m->stream);
+    std::vector<double2*> keep(n, nullptr);
+    int rc = PCP_OK;
+    std::string rep = "{\"candidates_blocks\": [";
+    for (int c = 0; c < 5; ++c) rep += (c ? ", " : "") + std::to_string(cand[c]);
+    rep += "], \"classes\": [";
+    bool firstClass = true;
+    for (int i = 0; i < n && rc == PCP_OK; ++i) {
+        pcp_model* m = b->models[i];
+        if (dalloc(&keep[i], (size_t)m->V) != cudaSuccess) rc = fail(PCP_ERR_CUDA, "autotune buffer");
+        else if (cudaMemcpy(keep[i], m->pos, (size_t)m->V * sizeof(double2),
+                            cudaMemcpyDeviceToDevice) != cudaSuccess)
+            rc = fail(PCP_ERR_CUDA, "autotune copy");
+    }
+    RunArgs a{0, -1.0, 1e-3, steps, 0.1, 0.1, 0.99, 1.1, 0.5, 5, 5};
+    for (auto& kv : classes) {
+        if (rc) break;
+        const std::vector<int>& which = kv.second;
+        double best = 1e300;
+        int bestC = 2;
+        std::string row = "{\"polygons_from\": " + std::to_string(1 << kv.first) +
+                          ", \"systems\": " + std::to_string(which.size()) + ", \"ms\": [";
+        for (int c = 0; c < 5 && rc == PCP_OK; ++c) {
+            for (int i : which) {
+                rc = pcp_model_set_launch_shape(b->models[i], cand[c], cand[c]);
+                if (rc) break;
+                if (cudaMemcpy(b->models[i]->pos, keep[i], (size_t)b->models[i]->V * sizeof(double2),
+                               cudaMemcpyDeviceToDevice) != cudaSuccess)
+                    rc = fail(PCP_ERR_CUDA, "autotune copy");
+                b->models[i]->geometryStale = true;
+                b->models[i]->geomFromSnapshot = false;
+            }
+            if (rc) break;
+            // a first run builds the graphs and warms up; the second is timed
+            rc = batch_run(b, which, a);
+            if (rc) break;
+            for (int i : which)
+                cudaMemcpy(b->models[i]->pos, keep[i], (size_t)b->models[i]->V * sizeof(double2),
+                           cudaMemcpyDeviceToDevice);
+            CK(cudaDeviceSynchronize());
+            auto t0 = std::chrono::steady_clock::now();
+            rc = batch_run(b, which, a);
+            CK(cudaDeviceSynchronize());
+            double ms = std::chrono::duration<double, std::milli>(
+                std::chrono::steady_clock::now() - t0).count();
+            row += (c ? ", " : "") + std::to_string(ms);
+            if (ms < best) { best = ms; bestC = c; }
+        }
+        row += "], \"chosen_blocks\": " + std::to_string(cand[bestC]) + "}";
+        rep += (firstClass ? "" : ", ") + row;
+        firstClass = false;
+        for (int i : which) {
+            if (rc) break;
+            rc = pcp_model_set_launch_shape(b->models[i], cand[bestC], cand[bestC]);
+        }
+    }
+    rep += "], \"steps_per_trial\": " + std::to_string(steps) + "}";
+    for (int i = 0; i < n; ++i) {
+        if (keep[i]) {
+            cudaMemcpy(b->models[i]->pos, keep[i], (size_t)b->models[i]->V * sizeof(double2),
+                       cudaMemcpyDeviceToDevice);
+            b->models[i]->geometryStale = true;
+            b->models[i]->geomFromSnapshot = false;
+            cudaFree(keep[i]);
+        }
+        b->models[i]->stream = saved[i];
+    }
+    if (rc) return rc;
+    b->report = rep;
+    if (shapes_out)
+        for (int i = 0; i < n; ++i) {
+            shapes_out[2 * i] = b->models[i]->ws.narrowBlocks;
+            shapes_out[2 * i + 1] = b->models[i]->ws.forceBlocks;
+        }
+    return PCP_OK;
+}
+
+int pcp_batch_autotune_report(pcp_batch* b, char* buf, int cap, int* len_out) {
+    if (!b) return fail(PCP_ERR_ARG, "null batch");
+    if (len_out) *len_out = (int)b->report.size();
+    if (buf && cap > 0) {
+        int k = std::min(cap - 1, (int)b->report.size());
+        std::memcpy(buf, b->report.data(), (size_t)k);
+        buf[k] = 0;
+    }
     return PCP_OK;
 }
 

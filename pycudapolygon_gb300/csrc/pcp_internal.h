@@ -79,6 +79,16 @@ struct Ctrl {
     // blocks of the step's force pass finished (its last one decides the
     // energy rollback)
     unsigned int forceTicket;
+    // stop rule of the reference's Python driver (pyCudaPolygon.py:719-727):
+    // steps whose returned energy moved by less than stagnantTol are counted
+    // (never reset); the run stops once the count exceeds stagnantLimit
+    // (< 0: rule off)
+    double prevE, stagnantTol;
+    int stagnant, stagnantLimit, stagnated;
+    // per-step SHAKE iterations over the run (min, sum, max), as that driver
+    // reports them
+    int shakeMinRun, shakeMaxRun;
+    long long shakeSumRun;
 };
 
 enum : unsigned int {
@@ -111,6 +121,10 @@ struct ContactWS {
     float2* recUT = nullptr;        // [capRecords]
     int* fixList = nullptr;         // [capFix] records whose partner group is empty
     int* slowList = nullptr;        // [capSlow] pair indices for the block path
+    // launch shapes (0: the default, 4 blocks per SM): blocks of the
+    // warp-per-pair narrow phase and of the overlap-force pass; both kernels
+    // take their work from the record/pair counters, so any grid covers it
+    int narrowBlocks = 0, forceBlocks = 0;
 };
 
 // The Verlet move of a FIRE step, done by the step-start kernel (pos == null:
@@ -226,9 +240,20 @@ cudaError_t launch_xpbd_iteration(double2* pos, const int* start, int P,
 
 // FIRE parameters of a run, written into Ctrl by one thread on the stream
 // (no host round trip)
+// Overlap energy with a per-vertex output (gradient.cu): kRefForce gives
+// the reference's force and energy, kExactGrad the exact gradient of the
+// energy taken at the exact crossing points.  `out` (2V doubles) and
+// `energy` are added to; `bad` is set on a record outside the polygons.
+enum { kRefForce = 0, kExactGrad = 1 };
+cudaError_t launch_overlap_energy_grad(const double2* pos, const int* start, int V,
+                                       const ContactWS& ws, const Ctrl* ctrl, int mode,
+                                       double2* out, double* energy, int* bad, cudaStream_t st);
+
 struct FireScalars {
     double dt, alpha, dtMax, alphaStart, fAlpha, fInc, fDec, threshold;
     int nPos, nMin, shakeIter, stepLimit, resetRun, rbBodyKernels;
+    double stagnantTol;
+    int stagnantLimit;
 };
 cudaError_t launch_set_fire_params(Ctrl* c, const FireScalars& f, cudaStream_t st);
 

@@ -14,6 +14,7 @@
 #include <pybind11/stl.h>
 
 #include <cstdint>
+#include <cstring>
 #include <stdexcept>
 #include <string>
 #include <tuple>
@@ -111,6 +112,40 @@ public:
         return {out[0], out[1], (int)out[2]};
     }
 
+    py::tuple minimizeFIREDevice(double thr, double dt, int maxSteps, double dtMax,
+                                 double alphaStart, double fAlpha, double fInc, double fDec,
+                                 int nMin, int shakeIter) {
+        double out[6];
+        {
+            py::gil_scoped_release nogil;
+            check(pcp_model_minimize_fire_driver(m_, thr, dt, maxSteps, dtMax, alphaStart, fAlpha,
+                                                 fInc, fDec, nMin, shakeIter, out));
+        }
+        if (maxSteps <= 0) return py::make_tuple(out[0], out[1], 0);
+        py::list stats;
+        stats.append(out[3]); stats.append(out[4]); stats.append(out[5]);
+        return py::make_tuple(out[0], out[1], (int)out[2], stats);
+    }
+    void setPositionsDevice(std::uintptr_t ptr, int len) {
+        check(pcp_model_set_positions_device(m_, reinterpret_cast<const double*>(ptr), len));
+    }
+    double overlapEnergyGradient(int mode, bool search, std::uintptr_t outPtr) {
+        double e = 0.0;
+        {
+            py::gil_scoped_release nogil;
+            check(pcp_model_overlap_energy_gradient(m_, mode, search ? 1 : 0, &e,
+                                                    reinterpret_cast<double*>(outPtr)));
+        }
+        return e;
+    }
+    void fireSetStopRule(double tol, int stagnantLimit) {
+        check(pcp_model_fire_set_stop_rule(m_, tol, stagnantLimit));
+    }
+    py::tuple fireRunStats() {
+        double out[4];
+        check(pcp_model_fire_run_stats(m_, out));
+        return py::make_tuple((int)out[0], out[1], out[2], out[3]);
+    }
     void fireSetup(double thr, double dt, int maxSteps, double dtMax, double alphaStart,
                    double fAlpha, double fInc, double fDec, int nMin, int shakeIter) {
         py::gil_scoped_release nogil;
@@ -209,8 +244,71 @@ public:
     uintptr_t handlePtr() { return (uintptr_t)m_; }
     void setStream(uintptr_t s) { check(pcp_model_set_stream(m_, (void*)s)); }
 
+    void setLaunchShape(int narrowBlocks, int forceBlocks) {
+        check(pcp_model_set_launch_shape(m_, narrowBlocks, forceBlocks));
+    }
+    std::tuple<int, int> getLaunchShape() {
+        int out[2];
+        check(pcp_model_get_launch_shape(m_, out));
+        return {out[0], out[1]};
+    }
+    pcp_model* raw() const { return m_; }
+
 private:
     pcp_model* m_ = nullptr;
+};
+
+// Many independent systems minimised together (an addition: the reference
+// has one system per Model).  Holds references to the Model objects so that
+// they outlive the batch's use of them.
+class Batch {
+public:
+    Batch() { check(pcp_batch_create(&b_)); }
+    ~Batch() { pcp_batch_destroy(b_); }
+    Batch(const Batch&) = delete;
+    Batch& operator=(const Batch&) = delete;
+    void add(py::object model) {
+        Model& mm = model.cast<Model&>();
+        check(pcp_batch_add(b_, mm.raw()));
+        keep_.push_back(model);
+    }
+    int size() const { return (int)keep_.size(); }
+    void setStreams(int n, int chunk) { check(pcp_batch_set_streams(b_, n, chunk)); }
+    py::array_t<double> minimizeFIRE(int rule, double thr, double dt, int maxSteps, double dtMax,
+                                     double alphaStart, double fAlpha, double fInc, double fDec,
+                                     int nMin, int shakeIter) {
+        std::vector<double> out(4 * keep_.size());
+        {
+            py::gil_scoped_release nogil;
+            check(pcp_batch_minimize_fire(b_, rule, thr, dt, maxSteps, dtMax, alphaStart, fAlpha,
+                                          fInc, fDec, nMin, shakeIter, out.data()));
+        }
+        py::array_t<double> a({(py::ssize_t)keep_.size(), (py::ssize_t)4});
+        std::memcpy(a.mutable_data(), out.data(), out.size() * sizeof(double));
+        return a;
+    }
+    py::array_t<int> autotune(int steps) {
+        std::vector<int> out(2 * keep_.size());
+        {
+            py::gil_scoped_release nogil;
+            check(pcp_batch_autotune(b_, steps, out.data()));
+        }
+        py::array_t<int> a({(py::ssize_t)keep_.size(), (py::ssize_t)2});
+        std::memcpy(a.mutable_data(), out.data(), out.size() * sizeof(int));
+        return a;
+    }
+    std::string report() {
+        int len = 0;
+        check(pcp_batch_autotune_report(b_, nullptr, 0, &len));
+        std::string s(len + 1, '\0');
+        check(pcp_batch_autotune_report(b_, &s[0], len + 1, &len));
+        s.resize(len);
+        return s;
+    }
+
+private:
+    pcp_batch* b_ = nullptr;
+    std::vector<py::object> keep_;
 };
 
 PYBIND11_MODULE(libpyCudaPolygon, m) {
@@ -313,7 +411,34 @@ PYBIND11_MODULE(libpyCudaPolygon, m) {
              py::arg("maxSteps"), py::arg("dtMax") = 0.1, py::arg("alphaStart") = 0.1,
              py::arg("fAlpha") = 0.99, py::arg("fInc") = 1.1, py::arg("fDec") = 0.5,
              py::arg("nMin") = 5, py::arg("shakeIter") = 5)
+        .def("minimizeFIREDevice", &Model::minimizeFIREDevice,
+             py::arg("maxForceThreshold") = 1e-14, py::arg("dt") = 1e-3,
+             py::arg("maxSteps") = 100000000, py::arg("dtMax") = 0.1,
+             py::arg("alphaStart") = 0.1, py::arg("fAlpha") = 0.99, py::arg("fInc") = 1.1,
+             py::arg("fDec") = 0.5, py::arg("nMin") = 5, py::arg("shakeIter") = 5)
+        .def("fireSetStopRule", &Model::fireSetStopRule, py::arg("energyTol"),
+             py::arg("stagnantLimit"))
+        .def("fireRunStats", &Model::fireRunStats)
+        .def("setPositionsDevice", &Model::setPositionsDevice, py::arg("ptr"), py::arg("len"))
+        .def("overlapEnergyGradient", &Model::overlapEnergyGradient, py::arg("mode"),
+             py::arg("search"), py::arg("outPtr"))
         .def("fireContinue", &Model::fireContinue)
         .def("fireStatus", &Model::fireStatus)
-        .def("contactsStage", &Model::contactsStage);
+        .def("contactsStage", &Model::contactsStage)
+        .def("setLaunchShape", &Model::setLaunchShape, py::arg("narrowBlocks"),
+             py::arg("forceBlocks"))
+        .def("getLaunchShape", &Model::getLaunchShape);
+
+    py::class_<Batch>(m, "Batch")
+        .def(py::init<>())
+        .def("add", &Batch::add)
+        .def("size", &Batch::size)
+        .def("setStreams", &Batch::setStreams, py::arg("streams"), py::arg("chunkSteps"))
+        .def("minimizeFIRE", &Batch::minimizeFIRE, py::arg("rule") = 1,
+             py::arg("maxForceThreshold") = 1e-14, py::arg("dt") = 1e-3,
+             py::arg("maxSteps") = 100000000, py::arg("dtMax") = 0.1,
+             py::arg("alphaStart") = 0.1, py::arg("fAlpha") = 0.99, py::arg("fInc") = 1.1,
+             py::arg("fDec") = 0.5, py::arg("nMin") = 5, py::arg("shakeIter") = 5)
+        .def("autotune", &Batch::autotune, py::arg("steps") = 8)
+        .def("report", &Batch::report);
 }

@@ -4,6 +4,7 @@ Run where the reference tree is available, with PCP_REFERENCE set to its
 root.  The fixtures it writes are committed, so nothing at test time reads the
 reference:
 
+  testSaver/        the reference's saved-state fixture files, byte for byte
   testsaver.json    the reference's own saved two-pentagon state
                     (tests/testSaver/state.npy, scalars.dat) and the neighbour
                     known answer of tests/neighborTesting.ipynb (cells 6, 9,
@@ -211,6 +212,17 @@ def _shape_setter_cases(ref):
     return out
 
 
+def copy_testsaver():
+    """The reference's saved-state fixture itself (tests/testSaver/state.npy and
+    scalars.dat, the format of pyCudaPolygon.py:733-817), copied byte for
+    byte to tests/golden/testSaver/ for the save/load tests."""
+    import shutil
+    out = os.path.join(HERE, "testSaver")
+    os.makedirs(out, exist_ok=True)
+    for f in ("state.npy", "scalars.dat"):
+        shutil.copyfile(os.path.join(REF, "tests", "testSaver", f), os.path.join(out, f))
+
+
 def main():
     ref = _import_reference_model()
     Model = ref.model
@@ -232,6 +244,8 @@ def main():
         "answer_source": "tests/neighborTesting.ipynb cells 6, 9 and 14 ({1: [7, 8]}, "
                          "also after the global shift (pos - mean(pos)) % 1)",
     }, open(os.path.join(HERE, "testsaver.json"), "w"), indent=1)
+
+    copy_testsaver()
 
     # ---- getDf twin ----
     cases = []

@@ -18,7 +18,7 @@ if not torch.cuda.is_available():
 import pycudapolygon_gb300 as pg  # noqa: E402
 
 pg.build()
-from pycudapolygon_gb300.model import model  # noqa: E402
+from refdriver import model  # noqa: E402
 
 FIX = json.load(open(os.path.join(os.path.dirname(__file__), "golden", "shape_setters.json")))
 
