@@ -69,7 +69,8 @@ def lib():
             "orc_minimize_fire": (None, [P, D, D, I, D, D, D, D, D, I, I, dp]),
         }
         for name in ["orc_num_vertices", "orc_num_polygons", "orc_num_intersections",
-                     "orc_max_neighbors", "orc_box_size", "orc_last_shake_iters"]:
+                     "orc_max_neighbors", "orc_box_size", "orc_last_shake_iters",
+                     "orc_fire_first_shake_iters"]:
             sig[name] = (I, [P])
         for name in ["orc_energy", "orc_max_edge_length"]:
             sig[name] = (D, [P])
@@ -284,6 +285,11 @@ class OracleModel:
 
     def getLastShakeIters(self):
         return self._L.orc_last_shake_iters(self._m)
+
+    def getFireFirstShakeIters(self):
+        """Iterations of the first SHAKE call of the last FIRE step (at the
+        step's shakeIter the step retried; test use only)."""
+        return self._L.orc_fire_first_shake_iters(self._m)
 
     def getEnergy(self):
         return self._L.orc_energy(self._m)

@@ -163,6 +163,7 @@ struct orc_model {
     int maxNeighbors;
     int numIntersections;
     int lastShakeIters;
+    int fireFirstShakeIters;   /* first SHAKE call of the last FIRE step (test use) */
     double stiffness, compressibility;
     double energy;
     double maxEdgeLength;
@@ -1395,6 +1396,7 @@ void orc_fire_step(orc_model* m, double dt, double alpha, int nPos, double dtMax
             memcpy(m->positionsTMP, m->positions, nb);
             orc_shake_project(m, shakeIter, 1e-15);
             orc_update_polygon_geometry(m);
+            m->fireFirstShakeIters = m->lastShakeIters;
             if (m->lastShakeIters >= shakeIter) {
                 orc_shake_project(m, shakeIter * 10, 1e-15);
                 orc_update_polygon_geometry(m);
@@ -1480,6 +1482,9 @@ int orc_num_intersections(const orc_model* m) { return m->numIntersections; }
 int orc_max_neighbors(const orc_model* m) { return m->maxNeighbors; }
 int orc_box_size(const orc_model* m) { return m->boxSize; }
 int orc_last_shake_iters(const orc_model* m) { return m->lastShakeIters; }
+/* iterations of the first SHAKE call of the last FIRE step: at the limit,
+ * the step retried (no counterpart in the reference; test use) */
+int orc_fire_first_shake_iters(const orc_model* m) { return m->fireFirstShakeIters; }
 double orc_energy(const orc_model* m) { return m->energy; }
 double orc_max_edge_length(const orc_model* m) { return m->maxEdgeLength; }
 const double* orc_positions(const orc_model* m) { return m->positions; }

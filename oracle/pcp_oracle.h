@@ -102,6 +102,7 @@ int orc_num_intersections(const orc_model* m);
 int orc_max_neighbors(const orc_model* m);
 int orc_box_size(const orc_model* m);
 int orc_last_shake_iters(const orc_model* m);
+int orc_fire_first_shake_iters(const orc_model* m);
 double orc_energy(const orc_model* m);
 double orc_max_edge_length(const orc_model* m);
 const double*   orc_positions(const orc_model* m);

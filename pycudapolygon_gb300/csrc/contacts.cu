@@ -717,10 +717,17 @@ __device__ void narrow_cull(const PairCtx& pc, const float4* ringA, const float4
     // and a candidate pair lies within 0.4 of A's vertex 0, so nothing wraps):
     // A's box was measured in this frame by the prepass (the same FP32
     // operations as the culls below) and B's box is moved from B's frame,
-    // widened by 1e-6 for the rounding of the move.  Otherwise the boxes are
-    // measured from the rings here.
+    // widened by 1e-6 for the rounding of the move.
     float ox0, ox1, oy0, oy1;
-    if (pr.flagA && pr.flagB) {
+    // A polygon that is not well formed (the prepass's flag 0: extent of 0.2
+    // or more, or non-finite) may span more than half the box, and then
+    // coordinates taken relative to A's vertex 0 no longer give every edge
+    // pair its own minimum image (kernels.cuh:778-790 wraps each difference
+    // separately).  Such pairs keep every edge and skip the box tests; the
+    // FP32 crossing filter and the exact test wrap per edge pair.
+    const bool boxes = pr.flagA && pr.flagB;
+    const float kInf = __int_as_float(0x7f800000);
+    if (boxes) {
         const float4 ba = pr.boxA;
         ox0 = ba.x - m; ox1 = ba.y + m; oy0 = ba.z - m; oy1 = ba.w + m;
         if (!pc.self) {
@@ -732,23 +739,7 @@ __device__ void narrow_cull(const PairCtx& pc, const float4* ringA, const float4
             if (ox0 > ox1 || oy0 > oy1) { nLAout = 0; nLBout = 0; return; }
         }
     } else {
-        float ax0 = 3.f, ax1 = -3.f, ay0 = 3.f, ay1 = -3.f;
-        for (int a = lane; a < nA; a += 32) {
-            float x = wrapf(ringA[a].x - f0x), y = wrapf(ringA[a].y - f0y);
-            ax0 = fminf(ax0, x); ax1 = fmaxf(ax1, x); ay0 = fminf(ay0, y); ay1 = fmaxf(ay1, y);
-        }
-        ax0 = warp_minf(ax0); ax1 = warp_maxf(ax1); ay0 = warp_minf(ay0); ay1 = warp_maxf(ay1);
-        ox0 = ax0 - m; ox1 = ax1 + m; oy0 = ay0 - m; oy1 = ay1 + m;
-        if (!pc.self) {
-            float bx0 = 3.f, bx1 = -3.f, by0 = 3.f, by1 = -3.f;
-            for (int b = lane; b < nB; b += 32) {
-                float x = wrapf(ringB[b].x - f0x), y = wrapf(ringB[b].y - f0y);
-                bx0 = fminf(bx0, x); bx1 = fmaxf(bx1, x); by0 = fminf(by0, y); by1 = fmaxf(by1, y);
-            }
-            bx0 = warp_minf(bx0); bx1 = warp_maxf(bx1); by0 = warp_minf(by0); by1 = warp_maxf(by1);
-            ox0 = fmaxf(ax0, bx0) - m; ox1 = fminf(ax1, bx1) + m;
-            oy0 = fmaxf(ay0, by0) - m; oy1 = fminf(ay1, by1) + m;
-        }
+        ox0 = -kInf; ox1 = kInf; oy0 = -kInf; oy1 = kInf;
     }
     // candidate edges of each ring (edge box padded by m meets the overlap box)
     auto collect = [&](const float4* ring, int n, EdgeCand* out, float pad) -> int {
@@ -761,8 +752,9 @@ __device__ void narrow_cull(const PairCtx& pc, const float4* ringA, const float4
                 float4 v0 = ring[e], v1 = ring[(e + 1 == n) ? 0 : e + 1];
                 float x0 = wrapf(v0.x - f0x), y0 = wrapf(v0.y - f0y);
                 float x1 = wrapf(v1.x - f0x), y1 = wrapf(v1.y - f0y);
-                c.box = make_float4(fminf(x0, x1) - pad, fmaxf(x0, x1) + pad,
-                                    fminf(y0, y1) - pad, fmaxf(y0, y1) + pad);
+                c.box = boxes ? make_float4(fminf(x0, x1) - pad, fmaxf(x0, x1) + pad,
+                                            fminf(y0, y1) - pad, fmaxf(y0, y1) + pad)
+                              : make_float4(-kInf, kInf, -kInf, kInf);
                 c.idx = e; c.cx = __float_as_int(v0.z); c.cy = __float_as_int(v0.w); c.pad = 0;
                 // keep unless certainly outside the overlap box (NaN keeps it)
                 ok = !(c.box.x > ox1 || c.box.y < ox0 || c.box.z > oy1 || c.box.w < oy0);

@@ -20,6 +20,7 @@ if not torch.cuda.is_available():
 import pycudapolygon_gb300 as pg  # noqa: E402
 from pycudapolygon_gb300.systems import PolygonSystem, load_into, make_system  # noqa: E402
 from oracle import oracle as orc  # noqa: E402
+from fire_shadow import FireShadow  # noqa: E402
 
 pg.build()
 lib = pg.load_module()
@@ -171,6 +172,48 @@ def test_self_crossing_records_bit_exact(box):
     sj = keys >> np.uint64(48)
     assert np.count_nonzero(si == sj) >= 6      # bow tie 2, pentagram 5 (at least)
     assert_records_equal(g, o)
+
+
+def _scrambled_system():
+    """A 64-polygon system after a FIRE step whose Verlet move flung some
+    polygons' vertices across the box (as a step with huge forces does before
+    SHAKE gives up and puts them back): three polygons with vertices spread
+    over the whole box, one stretched over more than half of it along x, one
+    along the diagonal, the others as generated."""
+    s = make_system(64, 16, 0.85, seed=5)
+    x = s.positions.reshape(-1, 2).copy()
+    rng = np.random.default_rng(11)
+    st = s.start_indices
+    for p in (3, 17, 40):
+        x[st[p]:st[p + 1]] = rng.random((st[p + 1] - st[p], 2))
+    for p, d in ((25, (0.7, 0.0)), (52, (0.45, 0.45))):
+        k = np.arange(st[p + 1] - st[p]) / (st[p + 1] - st[p])
+        spread = np.abs(2.0 * k - 1.0)[:, None] * np.asarray(d)[None, :]
+        x[st[p]:st[p + 1]] = (x[st[p]:st[p + 1]] + spread) % 1.0
+    return PolygonSystem(positions=x.reshape(-1), n_array=s.n_array,
+                         start_indices=s.start_indices, target_areas=s.target_areas,
+                         target_edge_lengths=s.target_edge_lengths,
+                         max_edge_length=s.max_edge_length, phi=s.phi)
+
+
+@pytest.mark.parametrize("box", ["system", 2, 7])
+def test_records_bit_exact_with_polygons_spanning_the_box(box):
+    """Polygons that span more than half the box: the edge pairs the
+    reference tests (kernels.cuh:709-812, each difference wrapped on its
+    own) are all tested, whatever frame the narrow phase's culls use."""
+    system = _scrambled_system()
+    g, o = pair(system)
+    if box != "system":
+        g.setMaxEdgeLength(1.0 / box)
+        o.setMaxEdgeLength(1.0 / box)
+    contacts(g)
+    contacts(o)
+    assert o.getNumIntersections() > 0
+    assert_records_equal(g, o)
+    g.updateForceEnergy()
+    o.updateForceEnergy()
+    assert g.getEnergy() == pytest.approx(o.getEnergy(), rel=ENERGY_RTOL)
+    assert_forces_close(g.getForces(), o.getForces())
 
 
 def test_geometry_parity_odd_shapes():
@@ -337,36 +380,29 @@ def test_fire_steps_parity_general_kernels():
 def test_fire_steps_parity_thread_per_polygon():
     """20000 polygons, more than 128 per SM: inside the step graph the
     projection takes its thread-per-polygon form."""
-    _fire_steps_parity(make_system(20000, 8, 0.85, seed=17), 4)
+    # the SHAKE count is the largest over 20000 polygons, so one polygon at
+    # the rounding floor of the stop test moves it: 3 of 4 steps equal
+    _fire_steps_parity(make_system(20000, 8, 0.85, seed=17), 4, same_frac=0.75)
 
 
-def _fire_steps_parity(s, steps):
+def _fire_steps_parity(s, steps, same_frac=0.9):
+    """Each FIRE step of the CUDA path against one oracle step from the CUDA
+    path's state (tests/fire_shadow.py: energy 1e-12, positions 1e-12,
+    forces and velocities 1e-10 on plain steps).  The velocities read
+    between steps include the step's deferred bend (model.cpp:471-484), and
+    the next step does not bend them again."""
     g, o = pair(s)
     for m in (g, o):
         m.shakeProject(200, 1e-15)
         contacts(m)
         m.updateForceEnergy()
         m.projectForce()
-    st_g = (1e-3, 0.1, 0)
-    st_o = (1e-3, 0.1, 0)
-    for step in range(steps):
-        rg = g.minimizeFIREStep(*st_g)
-        ro = o.minimizeFIREStep(*st_o)
-        assert rg[0] == pytest.approx(ro[0], rel=1e-9, abs=1e-14), step
-        assert rg[1] == pytest.approx(ro[1], rel=1e-12), step
-        assert rg[3] == ro[3], step
-        assert g.getLastShakeIters() == pytest.approx(o.getLastShakeIters(), abs=1)
-        if step % 7 == 3:
-            # the step's velocity bend (model.cpp:471-484) is in the velocities
-            # read between steps, and the next step does not bend them again
-            vg, vo = np.asarray(g.getVelocities()), np.asarray(o.getVelocities())
-            assert np.abs(vg - vo).max() <= 1e-6 * np.abs(vo).max() + 1e-14, step
-        st_g = rg[1:]
-        st_o = ro[1:]
-    d = (np.asarray(g.getPositions()) - o.getPositions() + 0.5) % 1.0 - 0.5
-    assert np.abs(d).max() < 1e-9
-    vg, vo = np.asarray(g.getVelocities()), np.asarray(o.getVelocities())
-    assert np.abs(vg - vo).max() <= 1e-6 * np.abs(vo).max() + 1e-14
+    sh = FireShadow(g, o)
+    st = (1e-3, 0.1, 0)
+    for _ in range(steps):
+        st = sh.step(*st)[1:]
+    sh.check_counts(same_frac=same_frac)
+    assert sh.plain > 0
 
 
 @pytest.mark.parametrize("mt,k,c,dt0", [(3, 1.0, 1.0, 1.0), (5, 1.0, 1.0, 0.1), (1, 2.0, 0.0, 0.3),
@@ -387,19 +423,11 @@ def test_fire_steps_soft_models_parity(mt, k, c, dt0):
         m.setCompressibility(c)
         contacts(m)
         m.updateForceEnergy()
-    st_g = st_o = (dt0, 0.1, 0)
-    for step in range(25):
-        rg = g.minimizeFIREStep(*st_g, 1.0)
-        ro = o.minimizeFIREStep(*st_o, 1.0)
-        assert rg[0] == pytest.approx(ro[0], rel=1e-9, abs=1e-14), step
-        assert rg[1:] == pytest.approx(ro[1:], rel=1e-12), step
-        if step % 6 == 2:
-            vg, vo = np.asarray(g.getVelocities()), np.asarray(o.getVelocities())
-            assert np.abs(vg - vo).max() <= 1e-6 * np.abs(vo).max() + 1e-14, step
-        st_g, st_o = rg[1:], ro[1:]
-    d = (np.asarray(g.getPositions()) - o.getPositions() + 0.5) % 1.0 - 0.5
-    assert np.abs(d).max() < 1e-9
-    assert g.getMaxUnbalancedForce() == pytest.approx(o.getMaxUnbalancedForce(), rel=1e-9)
+    sh = FireShadow(g, o, shake=False)
+    st = (dt0, 0.1, 0)
+    for _ in range(25):
+        st = sh.step(*st, 1.0)[1:]
+    assert sh.plain == 25
 
 
 def test_fire_rollback_state_matches_reference():
@@ -415,31 +443,23 @@ def test_fire_rollback_state_matches_reference():
         contacts(m)
         m.updateForceEnergy()
         m.projectForce()
-    st_g = st_o = (1e-3, 0.1, 0)
+    sh = FireShadow(g, o)
+    st = (1e-3, 0.1, 0)
     rolled = None
     for step in range(60):
-        x_o = np.asarray(o.getPositions()).copy()
         x_g = np.asarray(g.getPositions()).copy()
-        rg = g.minimizeFIREStep(*st_g)
-        ro = o.minimizeFIREStep(*st_o)
-        assert rg[0] == pytest.approx(ro[0], rel=1e-9, abs=1e-14), step
-        assert rg[1:] == pytest.approx(ro[1:], rel=1e-12), step
-        st_g, st_o = rg[1:], ro[1:]
-        if np.array_equal(np.asarray(o.getPositions()), x_o) and o.getLastShakeIters() < 50:
+        rg = sh.step(*st)
+        st = rg[1:]
+        if np.array_equal(np.asarray(g.getPositions()), x_g) and g.getLastShakeIters() < 50:
             rolled = step
-            assert np.array_equal(np.asarray(g.getPositions()), x_g)
             break
-    assert rolled is not None
-    assert g.getEnergy() == pytest.approx(o.getEnergy(), rel=1e-9)
-    assert_forces_close(g.getForces(), o.getForces())
-    assert g.getMaxUnbalancedForce() == pytest.approx(o.getMaxUnbalancedForce(), rel=1e-9)
+    assert rolled is not None and sh.plain == sh.n
+    # the oracle's step from the same state rolled back too and recomputed
+    # the records there
+    assert np.array_equal(np.asarray(o.getPositions()), x_g)
     assert_records_equal(g, o)
     # and the run continues from the restored state
-    rg = g.minimizeFIREStep(*st_g)
-    ro = o.minimizeFIREStep(*st_o)
-    assert rg[0] == pytest.approx(ro[0], rel=1e-9, abs=1e-14)
-    d = (np.asarray(g.getPositions()) - o.getPositions() + 0.5) % 1.0 - 0.5
-    assert np.abs(d).max() < 1e-9
+    sh.step(*st)
 
 
 @pytest.mark.parametrize("seed,dt,shake_iter,fails", [(1, 0.2, 1, False), (1, 1.0, 1, True),
@@ -465,28 +485,29 @@ def test_fire_step_shake_retry_and_failure_match_reference(seed, dt, shake_iter,
     assert g.getLastShakeIters() == pytest.approx(o.getLastShakeIters(), abs=1)
     assert np.array_equal(np.asarray(o.getPositions()), xo0) == fails
     assert np.array_equal(np.asarray(g.getPositions()), xg0) == fails
-    assert rg[0] == pytest.approx(ro[0], rel=1e-9, abs=1e-14)
-    assert rg[1:] == pytest.approx(ro[1:], rel=1e-12)
+    assert rg[1:] == ro[1:]
     d = (np.asarray(g.getPositions()) - o.getPositions() + 0.5) % 1.0 - 0.5
     if fails:
         # back at the step-start state: the usual tolerances.  The force
         # there comes from records of the moved positions (huge), so the
         # next steps are short ones: the first rolls back on an energy
         # increase, the others proceed.
+        assert rg[0] == pytest.approx(ro[0], rel=1e-12)
         assert np.abs(d).max() < 1e-12
         assert_forces_close(g.getForces(), o.getForces())
-        assert g.getMaxUnbalancedForce() == pytest.approx(o.getMaxUnbalancedForce(), rel=1e-9)
+        assert g.getMaxUnbalancedForce() == pytest.approx(o.getMaxUnbalancedForce(), rel=1e-10)
+        sh = FireShadow(g, o)
+        st = (1e-5,) + tuple(rg[2:])
         for _ in range(3):
-            rg = g.minimizeFIREStep(1e-5, *rg[2:])
-            ro = o.minimizeFIREStep(1e-5, *ro[2:])
-            assert rg[0] == pytest.approx(ro[0], rel=1e-9, abs=1e-14)
-            assert rg[1:] == pytest.approx(ro[1:], rel=1e-12)
-        d = (np.asarray(g.getPositions()) - o.getPositions() + 0.5) % 1.0 - 0.5
-        assert np.abs(d).max() < 1e-9
+            st = sh.step(*st)[1:]
+        assert sh.plain == 3
     else:
-        # a step this large ends far from the pre-step shapes, where the two
-        # SHAKE solvers' 1e-15 residuals leave the positions ~1e-10 apart
-        # (not 1e-12), and the force follows them
+        # the retry starts from the first call's unconverged iterate, which
+        # the two SHAKEs reach only up to the rounding of their FP32 Newton
+        # corrections; the retry's end point moves with it along the
+        # constraint manifold (tests/fire_shadow.py), and the energy and
+        # force follow
+        assert rg[0] == pytest.approx(ro[0], rel=1e-9)
         assert np.abs(d).max() < 1e-9
         of = np.asarray(o.getForces())
         assert np.abs(np.asarray(g.getForces()) - of).max() <= 1e-7 * np.abs(of).max()
