@@ -195,9 +195,9 @@ int pcp_model_minimize_fire_driver(pcp_model* m, double max_force_threshold, dou
 /* The contact search (update of the crossing records) split into its stages,
  * enqueued without waiting: 0 = per-polygon prepass and broad phase
  * (bounding circles, grid counting sort, candidate pairs), 1 = narrow phase
- * (warp-per-pair kernel and its block fallback, whose last block also does
- * the exit matching's empty-group fix-up), 2 = nothing left to enqueue (kept
- * for callers that run the three stages).
+ * (warp-per-pair kernel, its block fallback, and the exit matching's
+ * empty-group fix-up), 2 = nothing left to enqueue (kept for callers that
+ * run the three stages).
  * Overflow is only detected by pcp_model_update_neighbors. */
 int pcp_model_contacts_stage(pcp_model* m, int stage);
 

@@ -912,10 +912,34 @@ __device__ __forceinline__ int find_partner(const PairCtx& pc, int R,
     return best;
 }
 
+// The largest key and a record that holds it, over the warp (lanes with no
+// record pass key 0).
+__device__ __forceinline__ void warp_max_key(unsigned long long& k, int& pos) {
+    for (int o = 16; o > 0; o >>= 1) {
+        const unsigned long long tk = __shfl_xor_sync(PCP_FULL, k, o);
+        const int tp = __shfl_xor_sync(PCP_FULL, pos, o);
+        if (tk > k) { k = tk; pos = tp; }
+    }
+}
+
+// Raise ctrl->maxKey to k (held by record pos).  A warp that raised it lists
+// its record, so the record holding the final maximum is in the list (the
+// last raise was made by its writer); k_fixup looks it up there instead of
+// scanning every record.  One call per warp of the narrow phase.
+__device__ __forceinline__ void publish_max_key(Ctrl* __restrict__ ctrl, ContactWS& ws,
+                                                unsigned long long k, int pos) {
+    const unsigned long long old = atomicMax(&ctrl->maxKey, k);
+    if (old < k) {
+        const int c = atomicAdd(&ctrl->numMaxCand, 1);
+        if (c < kMaxCand) ws.maxCand[c] = pos;
+        else atomicOr(&ctrl->flags, kFlagCapacity);
+    }
+}
+
 __device__ unsigned long long match_and_write(const PairCtx& pc, int R,
                                               const unsigned long long* recKey,
                                               const float2* recTU, Ctrl* ctrl, ContactWS& ws,
-                                              bool publishMax = true) {
+                                              int& kmaxPos) {
     const int lane = threadIdx.x & 31;
     // the slot of the pair's records: the atomic's round trip overlaps the
     // matching below, whose results wait in registers (up to 32 records,
@@ -923,6 +947,7 @@ __device__ unsigned long long match_and_write(const PairCtx& pc, int R,
     int base = 0;
     if (lane == 0) base = atomicAdd(&ctrl->numRecords, R);
     unsigned long long kmax = 0;
+    int kpos = -1;
     for (int r0 = 0; r0 < R; r0 += 32) {
         const int r = r0 + lane;
         unsigned long long key = 0, outer = 0;
@@ -941,7 +966,6 @@ __device__ unsigned long long match_and_write(const PairCtx& pc, int R,
                 ut = tu;
                 fix = !groupSeen;
             }
-            kmax = key > kmax ? key : kmax;
         }
         if (r0 == 0) {
             base = __shfl_sync(PCP_FULL, base, 0);
@@ -952,6 +976,7 @@ __device__ unsigned long long match_and_write(const PairCtx& pc, int R,
         }
         if (r < R) {
             int g = base + r;
+            if (key > kmax) { kmax = key; kpos = g; }
             ws.recKey[g] = key;
             ws.recTU[g] = tu;
             ws.recOuter[g] = outer;
@@ -963,13 +988,10 @@ __device__ unsigned long long match_and_write(const PairCtx& pc, int R,
             }
         }
     }
-    for (int o = 16; o > 0; o >>= 1) {
-        unsigned long long t = __shfl_xor_sync(PCP_FULL, kmax, o);
-        kmax = t > kmax ? t : kmax;
-    }
-    // the largest key (fixup_records' partner of last resort): published here, or
-    // gathered by the caller and published once
-    if (publishMax && lane == 0 && R > 0) atomicMax(&ctrl->maxKey, kmax);
+    // the largest key (k_fixup's partner of last resort) and its record,
+    // gathered by the caller and published once per warp
+    warp_max_key(kmax, kpos);
+    kmaxPos = kpos;
     return kmax;
 }
 
@@ -1002,8 +1024,17 @@ struct alignas(16) WarpSmem {
     float2 recTU[kSlots][kSlotRecords];
     int queue[64];
     PairSlot slot[kSlots];
+    int defer[16];     // pairs whose crossings overflowed their slot (see narrow_pair_global)
     unsigned long long bar[2];
 };
+constexpr int kDefer = 16;
+
+// a pair whose crossings overflowed its slot, for k_narrow_over
+__device__ __forceinline__ void push_over(int q, Ctrl* ctrl, ContactWS& ws) {
+    int s = atomicAdd(&ctrl->numOver, 1);
+    if (s < ws.capPairs) ws.overList[s] = q;
+    else atomicOr(&ctrl->flags, kFlagSlowOverflow);
+}
 
 __device__ __forceinline__ void push_slow(int q, Ctrl* ctrl, ContactWS& ws) {
     int s = atomicAdd(&ctrl->numSlow, 1);
@@ -1039,6 +1070,146 @@ __device__ __forceinline__ bool maybe_cross(float4 p, float4 p2, float4 q, float
     return true;
 }
 
+// A pair of the warp path whose crossings overflow its record slot (more
+// than kSlotRecords: dense overlaps, or polygons a huge FIRE move scrambled)
+// is finished by its own warp with the records in global memory: the rings
+// are read from global memory (the staged copies are in use), one pass over
+// the candidate edge pairs counts the crossings, one atomic reserves their
+// range of the record arrays, a second pass writes them, and the partners
+// are matched within that range (find_partner, L2-resident).  The same
+// culls, filters and exact test as the warp path, in the same order, so the
+// two passes find the same crossings.  Needs the warp's queue and candidate
+// buffers free (no edge pair pending).  Returns the largest key written.
+struct GlobalPairBufs {
+    EdgeCand* candA;   // [kFastRing]
+    EdgeCand* candB;   // [kFastRing]
+    int* queue;        // [64]
+};
+__device__ unsigned long long narrow_pair_global(const PairCtx& pc, const GlobalPairBufs& S,
+                                                 int B, const double2* __restrict__ pos,
+                                                 ContactWS& ws, Ctrl* __restrict__ ctrl,
+                                                 int& kmaxPos) {
+    const int lane = threadIdx.x & 31;
+    const unsigned lt = (1u << lane) - 1u;
+    const float4* ringA = ws.vtx + pc.stA;
+    const float4* ringB = pc.self ? ringA : ws.vtx + pc.stB;
+    int nLA = 0, nLB = 0;
+    narrow_cull(pc, ringA, ringB, S.candA, S.candB,
+                load_pair_recs(pc, ws.polyInfo, ws.polyBox, ws.polyFlags), nLA, nLB);
+    if (nLA == 0 || nLB == 0) return 0ull;
+    const EdgeCand* cb = pc.self ? S.candA : S.candB;
+    const bool wrapB = B >= 3;
+    int lb = 0;
+    while ((1 << lb) < nLB && lb < 5) ++lb;
+    const int bw = 1 << lb, aw = 32 >> lb;
+    const int la = lane >> lb, lbb = lane & (bw - 1);
+    int base = 0, R = 0;
+    for (int pass = 0; pass < 2; ++pass) {
+        int found = 0, qn = 0;
+        // exact test of the first cnt queued edge pairs; pass 1 writes the hits
+        auto test = [&](int cnt) {
+            bool hit = false;
+            unsigned long long key = 0;
+            float2 tuf = make_float2(0.f, 0.f);
+            if (lane < cnt) {
+                const int e = S.queue[lane];
+                const int ea = e & 0xFFFF, eb = e >> 16;
+                const int id1 = pc.stA + ea, nid = pc.stB + eb;
+                Crossing c = cross_exact(pos[id1], ws.edgeVec[id1], pos[nid], ws.edgeVec[nid]);
+                if (c.hit) {
+                    hit = true;
+                    if (c.denom > 0) {   // kernels.cuh:796-799, 862-867
+                        key = pack_key(pc.a, pc.b, eb, ea);
+                        tuf = make_float2((float)c.tt, (float)c.uu);
+                    } else {             // kernels.cuh:800-804, 868-873
+                        key = pack_key(pc.b, pc.a, ea, eb);
+                        tuf = make_float2((float)c.uu, (float)c.tt);
+                    }
+                }
+            }
+            const unsigned mk = __ballot_sync(PCP_FULL, hit);
+            if (pass == 1 && hit) {
+                const int g = base + found + __popc(mk & lt);
+                ws.recKey[g] = key;
+                ws.recTU[g] = tuf;
+            }
+            found += __popc(mk);
+            // drop the tested entries from the front of the queue
+            const int rest = qn - cnt;
+            const int v = lane < rest ? S.queue[cnt + lane] : 0;
+            __syncwarp();
+            if (lane < rest) S.queue[lane] = v;
+            qn = rest;
+            __syncwarp();
+        };
+        for (int b0 = 0; b0 < nLB; b0 += bw) {
+            for (int a0 = 0; a0 < nLA; a0 += aw) {
+                const int ia = a0 + la, ib = b0 + lbb;
+                bool ok = ia < nLA && ib < nLB;
+                EdgeCand ea, eb;
+                if (ok) { ea = S.candA[ia]; eb = cb[ib]; }
+                else {
+                    ea.box = eb.box = make_float4(0.f, 0.f, 0.f, 0.f);
+                    ea.idx = eb.idx = 0; ea.cx = eb.cx = 0; ea.cy = eb.cy = 0;
+                }
+                if (pc.self) ok = ok && eb.idx > ea.idx + 1 && !(ea.idx == 0 && eb.idx == pc.nA - 1);
+                ok = ok && !(eb.box.x > ea.box.y || eb.box.y < ea.box.x ||
+                             eb.box.z > ea.box.w || eb.box.w < ea.box.z);
+                if (wrapB) {
+                    const int dx = abs(ea.cx - eb.cx), dy = abs(ea.cy - eb.cy);
+                    ok = ok && (dx <= 1 || dx == B - 1) && (dy <= 1 || dy == B - 1);
+                }
+                if (ok) {
+                    const int an = (ea.idx + 1 == pc.nA) ? 0 : ea.idx + 1;
+                    const int bn = (eb.idx + 1 == pc.nB) ? 0 : eb.idx + 1;
+                    ok = maybe_cross(ringA[ea.idx], ringA[an], ringB[eb.idx], ringB[bn]);
+                }
+                const unsigned mk = __ballot_sync(PCP_FULL, ok);
+                if (mk) {
+                    if (ok) S.queue[qn + __popc(mk & lt)] = ea.idx | (eb.idx << 16);
+                    qn += __popc(mk);
+                    __syncwarp();
+                    if (qn >= 32) test(32);
+                }
+            }
+        }
+        if (qn > 0) test(qn);
+        if (pass == 0) {
+            R = found;
+            if (R == 0) return 0ull;
+            if (lane == 0) base = atomicAdd(&ctrl->numRecords, R);
+            base = __shfl_sync(PCP_FULL, base, 0);
+            if (base + R > ws.capRecords) {
+                if (lane == 0) atomicOr(&ctrl->flags, kFlagRecordOverflow);
+                return 0ull;
+            }
+        }
+    }
+    __syncwarp();   // the warp's record writes before its lanes read them
+    const unsigned long long* keys = ws.recKey + base;
+    const float2* tus = ws.recTU + base;
+    unsigned long long kmax = 0ull;
+    int kpos = -1;
+    for (int r = lane; r < R; r += 32) {
+        const unsigned long long key = keys[r];
+        const float2 tu = tus[r];
+        bool groupSeen = false;
+        const int best = find_partner(pc, R, keys, tus, key, tu, groupSeen);
+        const int g = base + r;
+        ws.recOuter[g] = best >= 0 ? keys[best] : key;
+        ws.recUT[g] = best >= 0 ? tus[best] : tu;
+        if (best < 0 && !groupSeen) {
+            const int f = atomicAdd(&ctrl->numFix, 1);
+            if (f < ws.capFix) ws.fixList[f] = g;
+            else atomicOr(&ctrl->flags, kFlagFixOverflow);
+        }
+        if (key > kmax) { kmax = key; kpos = g; }
+    }
+    warp_max_key(kmax, kpos);
+    kmaxPos = kpos;
+    return kmax;
+}
+
 // Warp per pair (pairs claimed dynamically), rings staged by bulk copies into
 // a double buffer with bounded mbarrier waits.  The FP32 culls and the FP32
 // crossing test run per pair; the edge pairs they cannot reject are queued,
@@ -1065,6 +1236,7 @@ k_narrow(const double2* __restrict__ pos, const int* __restrict__ start, int B,
     uint32_t phase[2] = {0u, 0u};
     int qn_ = 0;   // queued edge pairs
     unsigned long long warpMaxKey = 0ull;
+    int warpMaxPos = -1;
 
     // exact FP64 test of the first cnt queued edge pairs
     auto run_batch = [&](int cnt) {
@@ -1117,22 +1289,29 @@ k_narrow(const double2* __restrict__ pos, const int* __restrict__ start, int B,
         qn_ = rest;
         __syncwarp();
     };
-    // match and write (or hand to the block path) every slot whose pair is
-    // enumerated and fully tested
+    // match and write (or defer, when its records overflowed the slot) every
+    // slot whose pair is enumerated and fully tested
+    int nDefer = 0;
     auto finalize_ready = [&]() {
         for (int k = 0; k < kSlots; ++k) {
             const int st = S.slot[k].state;
             if ((st & kSlotBusy) && (st & kSlotDone) && S.slot[k].outstanding == 0) {
                 const PairSlot sl = S.slot[k];
                 if (sl.state & kSlotOverflow) {
-                    if (lane == 0) push_slow(sl.q, ctrl, ws);
+                    if (nDefer < kDefer) {
+                        if (lane == 0) S.defer[nDefer] = sl.q;
+                        ++nDefer;
+                    } else if (lane == 0) {
+                        push_over(sl.q, ctrl, ws);
+                    }
                 } else if (sl.R > 0) {
                     PairCtx pc;
                     pc.a = sl.a; pc.b = sl.b; pc.stA = sl.stA; pc.stB = sl.stB;
                     pc.nA = sl.nA; pc.nB = sl.nB; pc.self = sl.self != 0;
-                    unsigned long long km =
-                        match_and_write(pc, sl.R, S.recKey[k], S.recTU[k], ctrl, ws, false);
-                    warpMaxKey = km > warpMaxKey ? km : warpMaxKey;
+                    int kp = -1;
+                    const unsigned long long km =
+                        match_and_write(pc, sl.R, S.recKey[k], S.recTU[k], ctrl, ws, kp);
+                    if (km > warpMaxKey) { warpMaxKey = km; warpMaxPos = kp; }
                 }
                 __syncwarp();
                 if (lane == 0) S.slot[k].state = 0;
@@ -1144,6 +1323,22 @@ k_narrow(const double2* __restrict__ pos, const int* __restrict__ start, int B,
         for (int k = 0; k < kSlots; ++k)
             if (!(S.slot[k].state & kSlotBusy)) return k;
         return -1;
+    };
+    // finish every pending edge pair and slot, then the deferred pairs (they
+    // take the queue and candidate buffers, which are then free)
+    auto run_deferred = [&]() {
+        if (qn_ > 0) run_batch(qn_);
+        finalize_ready();
+        for (int d = 0; d < nDefer; ++d) {
+            const int qd = S.defer[d];
+            int kp = -1;
+            const unsigned long long km =
+                narrow_pair_global(make_ctx(ws.pairs[qd], start),
+                                   GlobalPairBufs{S.candA, S.candB, S.queue}, B, pos, ws, ctrl, kp);
+            if (km > warpMaxKey) { warpMaxKey = km; warpMaxPos = kp; }
+        }
+        nDefer = 0;
+        __syncwarp();
     };
 
     // pairs claimed one at a time from a shared cursor, the next one while
@@ -1295,16 +1490,48 @@ k_narrow(const double2* __restrict__ pos, const int* __restrict__ start, int B,
         recCur = recNext;
         q = qn;
     }
-    if (qn_ > 0) run_batch(qn_);
-    finalize_ready();
-    if (lane == 0 && warpMaxKey) atomicMax(&ctrl->maxKey, warpMaxKey);
+    run_deferred();
+    if (lane == 0 && warpMaxKey) publish_max_key(ctrl, ws, warpMaxKey, warpMaxPos);
+}
+
+// Pairs whose crossings overflowed their warp's record slot when that warp's
+// own deferred list was full (a FIRE step that scrambled the polygons makes
+// nearly every pair such a pair): one warp per pair, records straight to
+// the global arrays (narrow_pair_global), pairs claimed from a cursor.
+constexpr int kOverWarps = 4;
+struct alignas(16) OverSmem {
+    EdgeCand candA[kFastRing];
+    EdgeCand candB[kFastRing];
+    int queue[64];
+};
+__global__ void __launch_bounds__(32 * kOverWarps)
+k_narrow_over(const double2* __restrict__ pos, const int* __restrict__ start, int B,
+              ContactWS ws, Ctrl* __restrict__ ctrl, const int* gate) {
+    pdl_enter();
+    if (gate_closed(gate)) return;
+    __shared__ OverSmem sm[kOverWarps];
+    OverSmem& S = sm[threadIdx.x / 32];
+    const int lane = threadIdx.x & 31;
+    const int numOver = min(ctrl->numOver, ws.capPairs);
+    unsigned long long warpMaxKey = 0ull;
+    int warpMaxPos = -1;
+    for (;;) {
+        int i = 0;
+        if (lane == 0) i = atomicAdd(&ctrl->overCursor, 1);
+        i = __shfl_sync(PCP_FULL, i, 0);
+        if (i >= numOver) break;
+        int kp = -1;
+        const unsigned long long km =
+            narrow_pair_global(make_ctx(ws.pairs[ws.overList[i]], start),
+                               GlobalPairBufs{S.candA, S.candB, S.queue}, B, pos, ws, ctrl, kp);
+        if (km > warpMaxKey) { warpMaxKey = km; warpMaxPos = kp; }
+    }
+    if (lane == 0 && warpMaxKey) publish_max_key(ctrl, ws, warpMaxKey, warpMaxPos);
 }
 
 // Block path: one warp per block, rings loaded with plain loads into a large
 // dynamic shared-memory area; for polygons above kFastRing vertices and for
 // pairs with more than kFastRecords crossings.
-__device__ void fixup_records(ContactWS& ws, Ctrl* __restrict__ ctrl);
-
 __global__ void __launch_bounds__(32)
 k_narrow_slow(const double2* __restrict__ pos, const int* __restrict__ start, int B,
               ContactWS ws, Ctrl* __restrict__ ctrl, const int* gate) {
@@ -1321,6 +1548,8 @@ k_narrow_slow(const double2* __restrict__ pos, const int* __restrict__ start, in
     int* queue = reinterpret_cast<int*>(recTU + kSlowRecords);
     const int lane = threadIdx.x & 31;
     int numSlow = min(ctrl->numSlow, ws.capSlow);
+    unsigned long long warpMaxKey = 0ull;
+    int warpMaxPos = -1;
     for (;;) {
         int s = 0;
         if (lane == 0) s = atomicAdd(&ctrl->slowCursor, 1);
@@ -1346,53 +1575,50 @@ k_narrow_slow(const double2* __restrict__ pos, const int* __restrict__ start, in
         if (R < 0) {
             if (lane == 0) atomicOr(&ctrl->flags, kFlagCapacity);
         } else if (R > 0) {
-            match_and_write(pc, R, recKey, recTU, ctrl, ws);
+            int kp = -1;
+            const unsigned long long km = match_and_write(pc, R, recKey, recTU, ctrl, ws, kp);
+            if (km > warpMaxKey) { warpMaxKey = km; warpMaxPos = kp; }
         }
         __syncwarp();
     }
-    // every record is written once the last block gets here (the fast
-    // path's before this kernel started): it fixes the empty-group records
-    if (lane == 0) __threadfence();
-    __syncwarp();
-    unsigned int t = 0;
-    if (lane == 0) t = atomicAdd(&ctrl->slowDone, 1u);
-    t = __shfl_sync(PCP_FULL, t, 0);
-    if (t == gridDim.x - 1) {
-        __threadfence();
-        fixup_records(ws, ctrl);
-    }
+    if (lane == 0 && warpMaxKey) publish_max_key(ctrl, ws, warpMaxKey, warpMaxPos);
 }
 
 // A crossing whose reverse group is empty: the reference's binary search
 // (kernels.cuh:993-1000) stops at the last record when every key is below
-// sij, and that record is then tried as the partner.  Reproduced here.
-// Run by one warp once every record is written (the last block of the block
-// path); the records of other blocks are read past L1.
-__device__ void fixup_records(ContactWS& ws, Ctrl* __restrict__ ctrl) {
-    const int lane = threadIdx.x & 31;
-    const int nf = min((int)__ldcg(&ctrl->numFix), ws.capFix);
+// sij, and that record is then tried as the partner.  Reproduced here, once
+// every record is written (the kernel after the narrow phase): each block
+// finds the record holding the largest key among the few that raised it
+// (publish_max_key), then the fix list is dealt out over the grid.
+__global__ void __launch_bounds__(256)
+k_fixup(ContactWS ws, Ctrl* __restrict__ ctrl, const int* gate) {
+    pdl_enter();
+    if (gate_closed(gate)) return;
+    const int nf = min(ctrl->numFix, ws.capFix);
     if (nf == 0) return;
-    const int I = min((int)__ldcg(&ctrl->numRecords), ws.capRecords);
-    const unsigned long long kmax = __ldcg(&ctrl->maxKey);
-    // locate the record holding the largest key (keys are unique)
-    int mi = -1;
-    for (int g0 = 0; g0 < I; g0 += 32) {
-        const int g = g0 + lane;
-        const unsigned hit = __ballot_sync(PCP_FULL, g < I && __ldcg(&ws.recKey[g]) == kmax);
-        if (hit) { mi = g0 + __ffs(hit) - 1; break; }
+    const int I = min(ctrl->numRecords, ws.capRecords);
+    const int nc = min(ctrl->numMaxCand, kMaxCand);
+    const unsigned long long kmax = ctrl->maxKey;
+    __shared__ int s_mi;
+    if (threadIdx.x == 0) s_mi = -1;
+    __syncthreads();
+    for (int c = threadIdx.x; c < nc; c += blockDim.x) {
+        const int g = ws.maxCand[c];
+        if (g >= 0 && g < I && ws.recKey[g] == kmax) s_mi = g;   // keys are unique
     }
+    __syncthreads();
+    const int mi = s_mi;
     if (mi < 0) return;
-    const float2 tuMax = __ldcg(&ws.recTU[mi]);
-    for (int f = lane; f < nf; f += 32) {
-        const int g = __ldcg(&ws.fixList[f]);
-        const unsigned long long key = __ldcg(&ws.recKey[g]);
+    const float2 tuMax = ws.recTU[mi];
+    const int l = (int)(kmax & 0xFFFF);
+    for (int f = blockIdx.x * blockDim.x + threadIdx.x; f < nf; f += gridDim.x * blockDim.x) {
+        const int g = ws.fixList[f];
+        const unsigned long long key = ws.recKey[g];
         const int sj = (int)(key >> 48), si = (int)((key >> 32) & 0xFFFF);
         const int i = (int)((key >> 16) & 0xFFFF);
         const unsigned long long sij = ((unsigned long long)si << 48) | ((unsigned long long)sj << 32);
         if (!(sij > kmax)) continue;
-        const int l = (int)(kmax & 0xFFFF);
-        const float tVal = __ldcg(&ws.recTU[g]).y;
-        if (l == i && tVal >= tuMax.x) continue;
+        if (l == i && ws.recTU[g].y >= tuMax.x) continue;
         ws.recOuter[g] = kmax;
         ws.recUT[g] = tuMax;
     }
@@ -1669,8 +1895,11 @@ cudaError_t launch_contacts(const double2* pos, const int* start, const int* sha
         size_t smem = sizeof(WarpSmem) * kNarrowWarps;
         int grid = ws.narrowBlocks > 0 ? ws.narrowBlocks : sm_count() * 4;
         launch_k(k_narrow, dim3(grid), dim3(32 * kNarrowWarps), smem, st, pos, start, B, ws, ctrl, gate);
+        launch_k(k_narrow_over, dim3(sm_count() * 4), dim3(32 * kOverWarps), 0, st, pos, start, B,
+                 ws, ctrl, gate);
         // pairs for the block path are rare: a few blocks take them in turn
         launch_k(k_narrow_slow, dim3(16), dim3(32), kSlowSmem, st, pos, start, B, ws, ctrl, gate);
+        launch_k(k_fixup, dim3(sm_count()), dim3(256), 0, st, ws, ctrl, gate);
     }
     return cudaGetLastError();
 }

@@ -169,6 +169,7 @@ struct pcp_model {
         dfree(&ws.gridCount); dfree(&ws.gridStart); dfree(&ws.gridFill); dfree(&ws.sortedPoly);
         dfree(&ws.unsafeList); dfree(&ws.pairs); dfree(&ws.recKey); dfree(&ws.recOuter);
         dfree(&ws.recTU); dfree(&ws.recUT); dfree(&ws.fixList); dfree(&ws.slowList);
+        dfree(&ws.maxCand); dfree(&ws.overList);
     }
     void invalidate() {
         recordsCached = false;
@@ -210,6 +211,8 @@ int alloc_ws(pcp_model* m, int capPairs, int capRecords) {
     CK(dalloc(&w.recKey, (size_t)capRecords)); CK(dalloc(&w.recOuter, (size_t)capRecords));
     CK(dalloc(&w.recTU, (size_t)capRecords)); CK(dalloc(&w.recUT, (size_t)capRecords));
     CK(dalloc(&w.fixList, (size_t)w.capFix)); CK(dalloc(&w.slowList, (size_t)w.capSlow));
+    if (!w.maxCand) CK(dalloc(&w.maxCand, (size_t)kMaxCand));
+    CK(dalloc(&w.overList, (size_t)capPairs));
     m->generation++;
     return PCP_OK;
 }
@@ -237,7 +240,7 @@ int run_contacts(pcp_model* m) {
     for (int attempt = 0; attempt < 8; ++attempt) {
         CK(launch_contacts(m->pos, m->start, m->shapeId, m->cellLocation, m->P, m->V, m->boxSize,
                            m->ws, m->ctrl, nullptr, m->stream));
-        m->launches += 8;
+        m->launches += 10;
         int rc = read_ctrl(m);
         if (rc) return rc;
         unsigned fl = m->ctrlHost->flags;
@@ -1083,8 +1086,8 @@ int pcp_model_update_outersections(pcp_model* m) {
     CHECK_M(m);
     int rc = need_topology(m);
     if (rc) return rc;
-    // (the narrow phase matched the partners, and the last block of its
-    // block path did the empty-group fixup)
+    // (the narrow phase matched the partners, and k_fixup after it did the
+    // empty-group fixup)
     rc = read_ctrl(m);
     if (rc) return rc;
     m->numIntersections = m->ctrlHost->numRecords;
@@ -1580,7 +1583,7 @@ int pcp_model_contacts_stage(pcp_model* m, int stage) {
     if (stage == 0 || stage == 1) {
         CK(launch_contacts(m->pos, m->start, m->shapeId, m->cellLocation, m->P, m->V, m->boxSize,
                            m->ws, m->ctrl, nullptr, m->stream, stage == 0 ? 1 : 2));
-        m->launches += stage == 0 ? 6 : 2;
+        m->launches += stage == 0 ? 6 : 4;
     } else if (stage == 2) {
         // nothing left to launch: the fixup runs at the end of stage 1
     } else {
@@ -2112,6 +2115,8 @@ int pcp_batch_set_streams(pcp_batch* b, int n_streams, int chunk_steps) {
 int pcp_model_set_launch_shape(pcp_model* m, int narrow_blocks, int force_blocks) {
     CHECK_M(m);
     if (narrow_blocks < 0 || force_blocks < 0) return fail(PCP_ERR_ARG, "negative block count");
+    if (narrow_blocks > kMaxNarrowBlocks)
+        return fail(PCP_ERR_ARG, "at most %d narrow-phase blocks", kMaxNarrowBlocks);
     if (m->ws.narrowBlocks != narrow_blocks || m->ws.forceBlocks != force_blocks) {
         m->ws.narrowBlocks = narrow_blocks;
         m->ws.forceBlocks = force_blocks;

@@ -18,6 +18,12 @@ constexpr int kSlowRing = 2048;
 constexpr int kSlowRecords = 2048;
 // Largest polygon the thread-per-polygon projection / SHAKE kernels accept.
 constexpr int kMaxPolyN = 256;
+// Largest narrow-phase grid (blocks) a launch shape may ask for; every warp
+// of the narrow phase publishes its largest key once, so kMaxCand covers
+// them all (4 warps per block, plus the overflow kernel's 4 per block on
+// 4 blocks per SM and the block path's 16).
+constexpr int kMaxNarrowBlocks = 16384;
+constexpr int kMaxCand = 4 * kMaxNarrowBlocks + 4096;
 // Broad-phase grid cap per axis.
 constexpr int kGridMax = 256;
 
@@ -32,10 +38,12 @@ struct Ctrl {
     int slowCursor;
     int numUnsafe;
     int numSelf;           // self pairs among the candidate pairs
+    int numMaxCand;        // entries of ContactWS::maxCand
+    int numOver;           // entries of ContactWS::overList
+    int overCursor;
     int G;                 // broad-phase grid cells per axis
     unsigned int flags;    // kFlag* bits
     float Rmax;            // largest bounding radius of a well-formed polygon
-    unsigned int slowDone; // blocks of the narrow phase's block path finished
     unsigned long long maxKey;
     // ---- energy / force ----
     double energy;
@@ -121,6 +129,8 @@ struct ContactWS {
     float2* recUT = nullptr;        // [capRecords]
     int* fixList = nullptr;         // [capFix] records whose partner group is empty
     int* slowList = nullptr;        // [capSlow] pair indices for the block path
+    int* maxCand = nullptr;         // [kMaxCand] records that raised maxKey when written
+    int* overList = nullptr;        // [capPairs] pairs whose crossings overflowed a warp slot
     // launch shapes (0: the default, 4 blocks per SM): blocks of the
     // warp-per-pair narrow phase and of the overlap-force pass; both kernels
     // take their work from the record/pair counters, so any grid covers it

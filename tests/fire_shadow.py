@@ -14,14 +14,16 @@ takes the same box size).
 Every step: dt, alpha and nPos exact (the branch the step took,
 model.cpp:405-486).  A plain step (SHAKE converged within shakeIter
 iterations, or no SHAKE) and a step whose SHAKE failed on both sides
-(positions put back exactly, model.cpp:430-434): energy 1e-12 relative,
-positions 1e-12 (minimum image), forces 1e-10 of their largest component,
+(positions put back exactly, model.cpp:430-434): energy 1e-12 relative
+plus 2 (d + 1e-16) sum |F| for a position difference d (the first-order
+change d can make; the energy, a sum of signed chain terms, can be far
+smaller than its terms), positions 1e-12 (minimum image), forces 1e-10 of their largest component,
 velocities 1e-10 of their largest component or 1e-14/dt, whichever is
 larger: a step rederives v from its displacement (x_SHAKE - x_Verlet)/dt,
 model.cpp:436, so a position difference d becomes d/dt of velocity, and the
 SHAKE kernels take their last, small updates in an FP32 form whose error
 is below 6e-15 (1e-14/dt of velocity: 1e-11 at dt = 1e-3).  The SHAKE iteration counts of plain steps
-are counted as equal or not: SHAKE's stop test (max |s_k|/L, |A - A0| <
+must be equal in at least 80% of them (the tests may ask for more): SHAKE's stop test (max |s_k|/L, |A - A0| <
 1e-15) sits at the FP64 rounding floor of its residuals, so a count can
 follow the rounding.
 
@@ -106,7 +108,12 @@ class FireShadow:
             assert xd <= RETRY_TOL, ("x retry",) + info
             self.retry_steps.append((k, xd))
             return rg
-        assert rg[0] == pytest.approx(ro[0], rel=E_RTOL, abs=1e-300), ("E",) + info
+        # 1e-12 relative, plus the first-order change the measured position
+        # difference xd can make: sum |F| * xd (the energy is a sum of signed
+        # chain terms and can be far smaller than the terms themselves)
+        fo = np.asarray(o.getForces())
+        e_tol = E_RTOL * abs(ro[0]) + 2.0 * (xd + 1e-16) * np.abs(fo).sum()
+        assert abs(rg[0] - ro[0]) <= e_tol, ("E", e_tol) + info
         assert xd <= X_ATOL, ("x",) + info
         self.plain += 1
         if self.shake:
@@ -119,7 +126,7 @@ class FireShadow:
         self.kinds.add("reset" if rg[3] == 0 and rg[2] == full[4] else "advance")
         return rg
 
-    def check_counts(self, floor_frac=0.05, retry_frac=0.1, same_frac=0.9):
+    def check_counts(self, floor_frac=0.05, retry_frac=0.1, same_frac=0.8):
         assert len(self.floor_steps) <= floor_frac * self.n, self.floor_steps
         assert len(self.retry_steps) <= retry_frac * self.n, self.retry_steps
         if self.shake:

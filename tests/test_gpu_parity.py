@@ -385,7 +385,7 @@ def test_fire_steps_parity_thread_per_polygon():
     _fire_steps_parity(make_system(20000, 8, 0.85, seed=17), 4, same_frac=0.75)
 
 
-def _fire_steps_parity(s, steps, same_frac=0.9):
+def _fire_steps_parity(s, steps, same_frac=0.8):
     """Each FIRE step of the CUDA path against one oracle step from the CUDA
     path's state (tests/fire_shadow.py: energy 1e-12, positions 1e-12,
     forces and velocities 1e-10 on plain steps).  The velocities read
