@@ -8,9 +8,9 @@ step: Verlet update, edge-midpoint cells, contact search (broad phase, narrow
 phase, exit matching), SHAKE (5 iterations, retry x10), overlap energy and
 force, constraint projection, energy-rollback test and FIRE velocity update.
 
-metric  pair evals/s: candidate polygon pairs (a < b, overlapping bounding
-        circles) taken through the narrow phase, exit matching and force per
-        second.  `value` is measured with the system resident in HBM, L2 flushed
+metric  pair evals/s: polygon pairs (a < b) taken through the narrow phase,
+        exit matching and force per second (the pairs whose bounding circles
+        and crossing-margin boxes meet).  `value` is measured with the system resident in HBM, L2 flushed
         (256 MiB write) before every timed step, CUDA events around each step.
 e2e     the same metric through the C ABI with host buffers: positions copied
         from pinned host memory in, the step, positions copied back, per step.
@@ -45,8 +45,11 @@ CONFIG = {"workload": WORKLOAD, "polygons": N_POLY, "vertices_per_polygon": N_VE
           "l2": "flushed before every timed step (256 MiB write)",
           "fire": "dt0 1e-3, dtMax 0.1, alpha0 0.1, fAlpha 0.99, fInc 1.1, fDec 0.5, "
                   "nMin 5, shakeIter 5"}
-PAIR_RULE = ("pair evals are polygon pairs a < b with overlapping bounding circles; the "
-             "narrow phase receives the subset whose padded boxes also meet")
+PAIR_RULE = ("a pair eval is a polygon pair a < b handed to the narrow phase (bounding "
+             "circles meet and boxes padded by the crossing margin meet), counted on the "
+             "device over the timed steps, rollback searches included; the CPU arms count "
+             "the same rule in numpy at both ends of their runs; circle_pairs_per_step is "
+             "the looser count of pairs whose bounding circles meet")
 
 
 def dist_env():
@@ -196,11 +199,14 @@ def make_workload(seed):
 
 
 def candidate_pairs(positions, start):
-    """Pairs (a < b) with overlapping bounding circles: the pair count of the
-    narrow phase (same circle rule and padding as the broad phase)."""
+    """Pair evaluations of one contact search, counted with the broad phase's
+    rules: (narrow, circle), where circle counts the pairs a < b whose
+    bounding circles meet and narrow the subset whose boxes, padded by the
+    crossing margin, also meet (the pairs the narrow phase tests)."""
     xy = positions.reshape(-1, 2)
     P = len(start) - 1
-    cx, cy, R = np.zeros(P), np.zeros(P), np.zeros(P)
+    cx, cy, R, L = np.zeros(P), np.zeros(P), np.zeros(P), np.zeros(P)
+    bw, bh = np.zeros(P), np.zeros(P)
     for p in range(P):
         ring = xy[start[p]:start[p + 1]]
         rel = (ring - ring[0] + 0.5) % 1.0 - 0.5
@@ -208,13 +214,21 @@ def candidate_pairs(positions, start):
         c = (ring[0] + 0.5 * (lo + hi)) % 1.0
         cx[p], cy[p] = c
         R[p] = 0.5 * np.hypot(*(hi - lo)) * 1.0001 + 4e-6
-    count = 0
+        bw[p], bh[p] = hi - lo
+        e = (np.roll(ring, -1, axis=0) - ring + 0.5) % 1.0 - 0.5
+        L[p] = np.sqrt((e * e).sum(axis=1)).max()
+    circle = narrow = 0
     for p in range(P - 1):
         dx = (cx[p + 1:] - cx[p] + 0.5) % 1.0 - 0.5
         dy = (cy[p + 1:] - cy[p] + 0.5) % 1.0 - 0.5
         rr = R[p] + R[p + 1:] + 1e-5
-        count += int(np.count_nonzero(dx * dx + dy * dy <= rr * rr))
-    return count
+        near = dx * dx + dy * dy <= rr * rr
+        m = 2.0 * (4e-6 + 1e-3 * L[p] * L[p + 1:]) + 2e-6
+        box = (np.abs(dx) <= 0.5 * (bw[p] + bw[p + 1:]) + m) & \
+              (np.abs(dy) <= 0.5 * (bh[p] + bh[p + 1:]) + m)
+        circle += int(np.count_nonzero(near))
+        narrow += int(np.count_nonzero(near & box))
+    return narrow, circle
 
 
 def prepare_gpu(seed):
@@ -251,7 +265,8 @@ def run_gpu(args, ws, rank, local):
         raise RuntimeError("contact buffers grew during warm-up; rerun")
     ev = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True))
           for _ in range(args.steps)]
-    pairs0 = m.getPairCount()
+    pairs0 = m.getNarrowPairTotal()
+    circle0 = m.getPairCount()
     launches0 = m.getLaunchCount()
     torch.cuda.synchronize()
     if dist:
@@ -272,7 +287,8 @@ def run_gpu(args, ws, rank, local):
     if st[8]:
         raise RuntimeError("contact buffers grew inside the timed region; rerun")
     ms = sum(a.elapsed_time(b) for a, b in ev)
-    pairs = m.getPairCount() - pairs0
+    pairs = m.getNarrowPairTotal() - pairs0
+    circle = m.getPairCount() - circle0
     narrow_last = m.getNarrowPairCount()
     launches = m.getLaunchCount() - launches0
     ms, pairs = reduce_over_ranks(ms, pairs, dist, "cuda")
@@ -284,7 +300,8 @@ def run_gpu(args, ws, rank, local):
         "data": "synthetic (seeded bidisperse star polygons; the reference publishes no inputs)",
         "config": dict(CONFIG, parallelism="replicas" if ws > 1 else "single"),
         "pairs": {"rule": PAIR_RULE, "pair_evals_per_step": pairs / max(1, args.steps) / ws,
-                  "narrow_pairs_last_step": narrow_last[0] + narrow_last[1]},
+                  "circle_pairs_per_step": circle / max(1, args.steps),
+                  "self_pairs_last_step": narrow_last[1]},
         "clocks": clk.summary(),
         "gpu_launches": int(launches),
         "fire_state": {"energy": st[0], "dt": st[1], "max_force": st[4], "steps": st[5]},
@@ -391,7 +408,7 @@ def e2e(args, s):
     for _ in range(args.warmup):
         _, dt, alpha, npos = c.fire_step(dt, alpha, npos)
     c.get_positions_into(host)
-    p0 = c.pair_count()
+    p0 = c.narrow_pair_total()
     total = 0.0
     steps = args.steps          # same trajectory as the device-timed steps
     for i in range(steps):
@@ -402,8 +419,8 @@ def e2e(args, s):
         _, dt, alpha, npos = c.fire_step(dt, alpha, npos)
         c.get_positions_into(host)
         total += time.perf_counter() - t0
-    pairs = c.pair_count() - p0
-    ctrl_bytes = 304            # the control block read back after the step
+    pairs = c.narrow_pair_total() - p0
+    ctrl_bytes = c.L.pcp_control_block_bytes()   # read back after the step
     c.close()
     return {"value": pairs / total, "unit": UNIT,
             "h2d_bytes_per_step": 16 * s.num_vertices,
@@ -636,13 +653,13 @@ def run_cpu_steps(s, steps, warmup, threads):
     for _ in range(warmup):
         _, dt, alpha, npos = o.minimizeFIREStep(dt, alpha, npos)
     # the pair count moves slowly along a FIRE run: count it at both ends
-    first = candidate_pairs(o.getPositions(), s.start_indices)
+    first = candidate_pairs(o.getPositions(), s.start_indices)[0]
     total = 0.0
     for _ in range(steps):
         t0 = time.perf_counter()
         _, dt, alpha, npos = o.minimizeFIREStep(dt, alpha, npos)
         total += time.perf_counter() - t0
-    last = candidate_pairs(o.getPositions(), s.start_indices)
+    last = candidate_pairs(o.getPositions(), s.start_indices)[0]
     return total, 0.5 * (first + last) * steps, steps
 
 

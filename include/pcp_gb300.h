@@ -272,10 +272,17 @@ int pcp_model_device_forces(pcp_model* m, double** out);
 /* Pair evaluations since creation: polygon pairs a < b with overlapping
  * bounding circles taken through the contact search. */
 int pcp_model_get_pair_count(pcp_model* m, long long* out);
+/* No reference counterpart: pairs a < b handed to the narrow phase since
+ * creation (bounding circles meet and boxes within the crossing margin meet;
+ * self pairs not counted) -- the pair evaluations a benchmark counts. */
+int pcp_model_get_narrow_pair_total(pcp_model* m, long long* out);
 /* Pairs the last contact search handed to the narrow phase: polygon pairs
  * a < b whose bounding boxes are within the crossing margin, and self pairs
  * (polygons not certified simple). */
 int pcp_model_get_narrow_pair_count(pcp_model* m, int* pairs_out, int* self_out);
+/* No reference counterpart: bytes of the per-model control block that a
+ * FIRE step reads back to the host (counters and FIRE scalars). */
+int pcp_control_block_bytes(void);
 /* Kernel launches issued by the model since creation (for accounting). */
 int pcp_model_get_launch_count(pcp_model* m, long long* out);
 

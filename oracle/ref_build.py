@@ -6,9 +6,12 @@ come from the reference's own kernels, rebuilt for sm_103a and run on a GPU.
 
   stage   copy the reference's sources (src/kernels.cuh, model.cu, model.cpp,
           model.hpp, cuda_check.h, enumTypes.h) from the reference checkout
-          named by PCP_REFERENCE into oracle/_ref/src/.  oracle/_ref/ is git-ignored: the copies are
-          build inputs for the GPU machine, which has no reference checkout,
-          and are never committed.
+          named by PCP_REFERENCE into oracle/_ref/src/, and its unchanged
+          Python layer (pyCudaPolygon/*.py with polygonMixins/) into
+          oracle/_ref/py/pyCudaPolygon/, which the drop-in test imports on
+          top of this build's module.  oracle/_ref/ is git-ignored: the
+          copies are inputs for the GPU machine, which has no reference
+          checkout, and are never committed.
   build   compile oracle/_ref/src with the shims in oracle/ref_shim/ (CUDA 13
           removed cub::TransformInputIterator, src/model.cu:12,92; the
           reference does not ship src/FIRE.h and src/shake.h, model.cu:15-16)
@@ -33,6 +36,10 @@ BIN = os.path.join(REF_DIR, "ref_golden")
 CUDA_HOME = os.environ.get("CUDA_HOME", "/usr/local/cuda")
 NVCC = os.path.join(CUDA_HOME, "bin", "nvcc")
 SOURCES = ["kernels.cuh", "model.cu", "model.cpp", "model.hpp", "cuda_check.h", "enumTypes.h"]
+PY_STAGED = os.path.join(REF_DIR, "py", "pyCudaPolygon")
+PY_SOURCES = ["__init__.py", "enums.py", "pyCudaPolygon.py", "pyCudaPolygonLink.py",
+              os.path.join("polygonMixins", "polygonDraw.py"),
+              os.path.join("polygonMixins", "polygonUtils.py")]
 
 
 def reference_root():
@@ -50,7 +57,17 @@ def stage(ref=None):
     os.makedirs(STAGED, exist_ok=True)
     for f in SOURCES:
         shutil.copyfile(os.path.join(src, f), os.path.join(STAGED, f))
+    pysrc = os.path.join(ref or reference_root(), "pyCudaPolygon")
+    os.makedirs(os.path.join(PY_STAGED, "polygonMixins"), exist_ok=True)
+    for f in PY_SOURCES:
+        shutil.copyfile(os.path.join(pysrc, f), os.path.join(PY_STAGED, f))
     return STAGED
+
+
+def python_staged():
+    """The staged Python layer's package directory, or None."""
+    ok = all(os.path.exists(os.path.join(PY_STAGED, f)) for f in PY_SOURCES)
+    return PY_STAGED if ok else None
 
 
 def staged():

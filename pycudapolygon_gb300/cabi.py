@@ -170,6 +170,9 @@ class CModel:
     def pair_count(self):
         return self._scalar("get_pair_count", ctypes.c_longlong)
 
+    def narrow_pair_total(self):
+        return self._scalar("get_narrow_pair_total", ctypes.c_longlong)
+
     def launch_count(self):
         return self._scalar("get_launch_count", ctypes.c_longlong)
 

@@ -561,7 +561,10 @@ k_candidates(const float4* __restrict__ polyInfo, const float4* __restrict__ pol
             // polygon simple (kernels.cuh:766-775 records s1 == s2 crossings)
             if (n >= 4 && !(flags[i] & 2)) {
                 put(lane == 0, i, i);
-                if (pass == 0 && lane == 0) atomicAdd(&ctrl->numSelf, 1);
+                if (pass == 0 && lane == 0) {
+                    atomicAdd(&ctrl->numSelf, 1);
+                    atomicAdd(&ctrl->selfEvals, 1ull);
+                }
             }
             if (!safe) {
                 // not well formed: paired with everyone (safe partners below i, all above)
@@ -600,6 +603,7 @@ k_candidates(const float4* __restrict__ polyInfo, const float4* __restrict__ pol
                 int b0 = tot ? atomicAdd(&ctrl->numPairs, tot) : 0;
                 if (b0 + tot > capPairs) atomicOr(&ctrl->flags, kFlagPairOverflow);
                 if (ev) atomicAdd(&ctrl->pairEvals, ev);
+                if (tot) atomicAdd(&ctrl->narrowEvals, (unsigned long long)tot);
                 s_base = b0;
             }
             __syncthreads();
@@ -1895,8 +1899,10 @@ cudaError_t launch_contacts(const double2* pos, const int* start, const int* sha
         size_t smem = sizeof(WarpSmem) * kNarrowWarps;
         int grid = ws.narrowBlocks > 0 ? ws.narrowBlocks : sm_count() * 4;
         launch_k(k_narrow, dim3(grid), dim3(32 * kNarrowWarps), smem, st, pos, start, B, ws, ctrl, gate);
-        launch_k(k_narrow_over, dim3(sm_count() * 4), dim3(32 * kOverWarps), 0, st, pos, start, B,
-                 ws, ctrl, gate);
+        // usually empty: launched after the narrow phase has finished, so that
+        // its blocks do not sit on the SMs beside it (and beside SHAKE)
+        launch_k_serial(k_narrow_over, dim3(sm_count() * 4), dim3(32 * kOverWarps), 0, st, pos,
+                        start, B, ws, ctrl, gate);
         // pairs for the block path are rare: a few blocks take them in turn
         launch_k(k_narrow_slow, dim3(16), dim3(32), kSlowSmem, st, pos, start, B, ws, ctrl, gate);
         launch_k(k_fixup, dim3(sm_count()), dim3(256), 0, st, ws, ctrl, gate);

@@ -1837,6 +1837,14 @@ int pcp_model_get_pair_count(pcp_model* m, long long* out) {
     *out = (long long)m->ctrlHost->pairEvals;
     return PCP_OK;
 }
+int pcp_control_block_bytes(void) { return (int)sizeof(Ctrl); }
+int pcp_model_get_narrow_pair_total(pcp_model* m, long long* out) {
+    CHECK_M(m);
+    int rc = read_ctrl(m);
+    if (rc) return rc;
+    *out = (long long)(m->ctrlHost->narrowEvals - m->ctrlHost->selfEvals);
+    return PCP_OK;
+}
 int pcp_model_get_narrow_pair_count(pcp_model* m, int* pairs_out, int* self_out) {
     CHECK_M(m);
     int rc = read_ctrl(m);

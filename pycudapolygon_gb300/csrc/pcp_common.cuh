@@ -45,6 +45,21 @@ inline cudaError_t launch_k(void (*kernel)(KArgs...), dim3 grid, dim3 block, siz
     return cudaLaunchKernelEx(&cfg, kernel, args...);
 }
 
+// The same launch without programmatic dependent launch: the kernel's blocks
+// are scheduled only once the previous kernel on the stream has finished, so
+// none wait on an SM beside it (for wide grids that are usually empty).
+template <typename... KArgs, typename... Args>
+inline cudaError_t launch_k_serial(void (*kernel)(KArgs...), dim3 grid, dim3 block, size_t smem,
+                                   cudaStream_t st, Args... args) {
+    cudaLaunchConfig_t cfg = {};
+    cfg.gridDim = grid;
+    cfg.blockDim = block;
+    cfg.dynamicSmemBytes = smem;
+    cfg.stream = st;
+    cfg.numAttrs = 0;
+    return cudaLaunchKernelEx(&cfg, kernel, args...);
+}
+
 // ---------------------------------------------------------------- wraps ----
 
 // wrap (kernels.cuh:115-119): minimum image into [-0.5, 0.5),

@@ -73,6 +73,8 @@ struct Ctrl {
     int snapNPos;
     double snapDt, snapAlpha;   // FIRE scalars at the start of the step
     unsigned long long pairEvals;   // cumulative candidate pairs (a < b) examined
+    unsigned long long narrowEvals; // cumulative pairs handed to the narrow phase (self pairs too)
+    unsigned long long selfEvals;   // cumulative self pairs among them
     // last-block tickets of the FIRE step's SHAKE and velocity-mixing kernels
     // (zeroed by k_fire_begin) and the kernels run inside the step graph's
     // conditional bodies (the host counts the unconditional ones)

@@ -176,6 +176,11 @@ public:
     double getMaxEdgeLength() { double v; check(pcp_model_get_max_edge_length(m_, &v)); return v; }
     double getOverlapArea() { double v; check(pcp_model_get_overlap_area(m_, &v)); return v; }
     long long getPairCount() { long long v; check(pcp_model_get_pair_count(m_, &v)); return v; }
+    long long getNarrowPairTotal() {
+        long long v;
+        check(pcp_model_get_narrow_pair_total(m_, &v));
+        return v;
+    }
     long long getLaunchCount() { long long v; check(pcp_model_get_launch_count(m_, &v)); return v; }
     std::tuple<int, int> getNarrowPairCount() {
         int a = 0, b = 0;
@@ -401,6 +406,7 @@ PYBIND11_MODULE(libpyCudaPolygon, m) {
         .def("getMaxNeighbors", &Model::getMaxNeighbors)
         .def("getBoxSize", &Model::getBoxSize)
         .def("getPairCount", &Model::getPairCount)
+        .def("getNarrowPairTotal", &Model::getNarrowPairTotal)
         .def("getLaunchCount", &Model::getLaunchCount)
         .def("getNarrowPairCount", &Model::getNarrowPairCount)
         .def("devicePositions", &Model::devicePositions)
