@@ -364,7 +364,7 @@ def roofline(m, s, torch, flush, args):
             traffic = None
     roof = {"bound": "hbm", "achieved": achieved, "peak": hbm, "unit": "GB/s",
             "frac": achieved / hbm, "traffic": traffic, "peak_source": src + " (MEASURED_PEAKS.json hbm_gbs)",
-            "kernel": "k_narrow + k_narrow_slow (contact stage 1)",
+            "kernel": "k_narrow (+ k_narrow_over, k_narrow_slow, k_fixup: contact stage 1)",
             "launch_ms": ms, "algorithmic_bytes": bytes_launch, "pairs": pairs,
             "self_pairs": selfs}
     # the projection, SHAKE and force kernels are bound by the FP64 pipe, not

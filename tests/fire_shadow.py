@@ -14,13 +14,13 @@ takes the same box size).
 Every step: dt, alpha and nPos exact (the branch the step took,
 model.cpp:405-486).  A plain step (SHAKE converged within shakeIter
 iterations, or no SHAKE) and a step whose SHAKE failed on both sides
-(positions put back exactly, model.cpp:430-434): energy 1e-12 relative
+(positions put back exactly, model.cpp:431-435): energy 1e-12 relative
 plus 2 (d + 1e-16) sum |F| for a position difference d (the first-order
 change d can make; the energy, a sum of signed chain terms, can be far
 smaller than its terms), positions 1e-12 (minimum image), forces 1e-10 of their largest component,
 velocities 1e-10 of their largest component or 1e-14/dt, whichever is
 larger: a step rederives v from its displacement (x_SHAKE - x_Verlet)/dt,
-model.cpp:436, so a position difference d becomes d/dt of velocity, and the
+model.cpp:437, so a position difference d becomes d/dt of velocity, and the
 SHAKE kernels take their last, small updates in an FP32 form whose error
 is below 6e-15 (1e-14/dt of velocity: 1e-11 at dt = 1e-3).  The SHAKE iteration counts of plain steps
 must be equal in at least 80% of them (the tests may ask for more): SHAKE's stop test (max |s_k|/L, |A - A0| <
@@ -28,7 +28,7 @@ must be equal in at least 80% of them (the tests may ask for more): SHAKE's stop
 follow the rounding.
 
 A step whose first SHAKE call reached its limit and retried with ten times
-the iterations (model.cpp:421-428) mostly meets the same bounds; where it
+the iterations (model.cpp:423-430) mostly meets the same bounds; where it
 does not, it is compared within 1e-6 (energy relative, positions absolute)
 and counted: the retry starts from the first call's unconverged
 iterate, which the two implementations reach only up to the rounding of
