@@ -280,6 +280,27 @@ int pcp_model_get_narrow_pair_total(pcp_model* m, long long* out);
  * a < b whose bounding boxes are within the crossing margin, and self pairs
  * (polygons not certified simple). */
 int pcp_model_get_narrow_pair_count(pcp_model* m, int* pairs_out, int* self_out);
+/* ======================================================================
+ * Learned warm start (no counterpart in the reference): the dense products
+ * and the neighbour sums of a small message-passing network over the
+ * contact graph.  FIRE remains the minimiser; the network only proposes a
+ * starting point.
+ * ====================================================================== */
+/* C[m,n] = A[m,k] B[n,k]^T (+ bias[n]) (then ReLU when relu != 0) on the
+ * tensor cores: A and B BF16, row-major, k a multiple of 8, 16-byte aligned;
+ * C FP32, row-major.  splits > 1 divides k over blocks that add into C
+ * (which the caller zeroes; bias added once, no ReLU).  Asynchronous on the
+ * stream. */
+int pcp_gemm_bf16(const void* d_a, const void* d_b, float* d_c, int m, int n, int k,
+                  const float* d_bias, int relu, int splits, void* stream);
+/* 1 in *out when a wait inside a GEMM launched since the last call ran out
+ * (its results are then not to be used); clears the flag.  Synchronises. */
+int pcp_gemm_status(int* out);
+/* out[i,:] = scale * sum over j in col[rowptr[i]..rowptr[i+1]) of h[j,:],
+ * BF16 rows of f (even) values, FP32 sums. */
+int pcp_graph_sum_bf16(const int* d_rowptr, const int* d_col, const void* d_h, void* d_out,
+                       int v, int f, float scale, void* stream);
+
 /* No reference counterpart: bytes of the per-model control block that a
  * FIRE step reads back to the host (counters and FIRE scalars). */
 int pcp_control_block_bytes(void);

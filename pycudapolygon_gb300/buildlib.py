@@ -28,7 +28,7 @@ MODULE = os.path.join(OUT, "libpyCudaPolygon" + EXT)
 CUDA_HOME = os.environ.get("CUDA_HOME", "/usr/local/cuda")
 NVCC = os.path.join(CUDA_HOME, "bin", "nvcc")
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
-CU_SOURCES = ["geometry.cu", "contacts.cu", "constraints.cu", "gradient.cu"]
+CU_SOURCES = ["geometry.cu", "contacts.cu", "constraints.cu", "gradient.cu", "warmstart.cu"]
 CPP_SOURCES = ["model.cpp"]
 HEADERS = ["pcp_common.cuh", "pcp_internal.h", "pcp_fire.cuh"]
 

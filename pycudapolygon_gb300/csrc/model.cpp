@@ -1837,6 +1837,45 @@ int pcp_model_get_pair_count(pcp_model* m, long long* out) {
     *out = (long long)m->ctrlHost->pairEvals;
     return PCP_OK;
 }
+// ---- tensor-core kernels of the learned warm start (warmstart.cu) ----
+int pcp_gemm_bf16(const void* d_a, const void* d_b, float* d_c, int m, int n, int k,
+                  const float* d_bias, int relu, int splits, void* stream) {
+    if (m < 0 || n < 0 || k < 0 || splits < 1)
+        return fail(PCP_ERR_ARG, "pcp_gemm_bf16: negative size or splits < 1");
+    if (m == 0 || n == 0) return PCP_OK;
+    if (!d_a || !d_b || !d_c) return fail(PCP_ERR_ARG, "pcp_gemm_bf16: null buffer");
+    if (k == 0 || k % 8 != 0)
+        return fail(PCP_ERR_ARG, "pcp_gemm_bf16: K must be a positive multiple of 8");
+    if ((reinterpret_cast<uintptr_t>(d_a) | reinterpret_cast<uintptr_t>(d_b)) % 16 != 0)
+        return fail(PCP_ERR_ARG, "pcp_gemm_bf16: A and B must be 16-byte aligned");
+    if (splits > 1 && relu)
+        return fail(PCP_ERR_ARG, "pcp_gemm_bf16: ReLU needs the whole K sum (splits = 1)");
+    int rc = launch_gemm_bf16(d_a, d_b, d_c, m, n, k, d_bias, relu, splits,
+                              static_cast<cudaStream_t>(stream));
+    if (rc == -1) return fail(PCP_ERR_CUDA, "pcp_gemm_bf16: tensor map encoding failed");
+    if (rc != 0)
+        return fail(PCP_ERR_CUDA, "pcp_gemm_bf16: %s", cudaGetErrorString((cudaError_t)rc));
+    return PCP_OK;
+}
+
+int pcp_gemm_status(int* out) {
+    if (!out) return fail(PCP_ERR_ARG, "pcp_gemm_status: null output");
+    CK(gemm_error_flag(out));
+    return PCP_OK;
+}
+
+int pcp_graph_sum_bf16(const int* d_rowptr, const int* d_col, const void* d_h, void* d_out, int v,
+                       int f, float scale, void* stream) {
+    if (v < 0 || f <= 0 || f % 2 != 0)
+        return fail(PCP_ERR_ARG, "pcp_graph_sum_bf16: bad sizes (f must be positive and even)");
+    if (v == 0) return PCP_OK;
+    if (!d_rowptr || !d_col || !d_h || !d_out)
+        return fail(PCP_ERR_ARG, "pcp_graph_sum_bf16: null buffer");
+    CK(launch_graph_sum_bf16(d_rowptr, d_col, d_h, d_out, v, f, scale,
+                             static_cast<cudaStream_t>(stream)));
+    return PCP_OK;
+}
+
 int pcp_control_block_bytes(void) { return (int)sizeof(Ctrl); }
 int pcp_model_get_narrow_pair_total(pcp_model* m, long long* out) {
     CHECK_M(m);

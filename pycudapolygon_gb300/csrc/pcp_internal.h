@@ -289,4 +289,14 @@ cudaError_t launch_fire_settle(double2* vel, const double2* force, int V, Ctrl* 
 
 int sm_count();
 
+// ---- warmstart.cu: tensor-core kernels of the learned warm start ----
+// C[m,n] = A[m,k] B[n,k]^T (+ bias, ReLU), BF16 in, FP32 out; 0, -1 when a
+// tensor map could not be encoded, else a cudaError_t
+int launch_gemm_bf16(const void* a, const void* b, float* c, int m, int n, int k,
+                     const float* bias, int relu, int splits, cudaStream_t st);
+// reads and clears the flag a timed-out wait of the GEMM sets
+cudaError_t gemm_error_flag(int* out);
+cudaError_t launch_graph_sum_bf16(const int* rowptr, const int* col, const void* h, void* out,
+                                  int v, int f, float scale, cudaStream_t st);
+
 }  // namespace pcp
