@@ -316,6 +316,11 @@ def run_gpu(args, ws, rank, local):
         result["time_to_stop"] = time_to_stop(args, torch)
     if rank == 0 and args.batch_systems > 0:
         result["batched"] = batched(args, torch)
+    if rank == 0 and args.warm_start_train > 0:
+        from pycudapolygon_gb300 import warmstart
+        result["warm_start"] = warmstart.experiment(
+            n_train=args.warm_start_train, n_test=max(1, args.warm_start_train // 4),
+            epochs=10, physics=0.1)
     if dist:
         dist.destroy_process_group()
     if rank == 0:
@@ -727,6 +732,9 @@ def main():
     ap.add_argument("--no-cpu", action="store_true")
     ap.add_argument("--no-roofline", action="store_true")
     ap.add_argument("--no-stop", action="store_true")
+    ap.add_argument("--warm-start-train", type=int, default=16,
+                    help="training pairs of the learned warm start (0: skip it); a quarter "
+                         "as many held-out seeds")
     ap.add_argument("--batch-systems", type=int, default=BATCH_SYSTEMS,
                     help="systems of the many-systems leg (0: skip it)")
     ap.add_argument("--stages", type=int, default=0,

@@ -214,16 +214,28 @@ k_gemm_bf16(const __grid_constant__ CUtensorMap mapA, const __grid_constant__ CU
         uint32_t r[16];
         ld_16cols(tmem + ((uint32_t)(warp * 32) << 16) + (uint32_t)cc, r);
         if (ok && row < M) {
+            const int col0 = n0 + cc;
+            float v[16];
 #pragma unroll
             for (int j = 0; j < 16; ++j) {
-                const int col = n0 + cc + j;
-                if (col < N) {
-                    float v = __uint_as_float(r[j]);
-                    if (addBias) v += bias[col];
-                    if (relu) v = fmaxf(v, 0.f);
-                    float* dst = C + (size_t)row * N + col;
-                    if (atomic) atomicAdd(dst, v);
-                    else *dst = v;
+                v[j] = __uint_as_float(r[j]);
+                if (addBias && col0 + j < N) v[j] += bias[col0 + j];
+                if (relu) v[j] = fmaxf(v[j], 0.f);
+            }
+            float* dst = C + (size_t)row * N + col0;
+            if (!atomic && col0 + 16 <= N && (N & 3) == 0) {
+                // the 16 columns of this row: four 16-byte stores
+                float4* d4 = reinterpret_cast<float4*>(dst);
+#pragma unroll
+                for (int q = 0; q < 4; ++q)
+                    d4[q] = make_float4(v[4 * q], v[4 * q + 1], v[4 * q + 2], v[4 * q + 3]);
+            } else {
+#pragma unroll
+                for (int j = 0; j < 16; ++j) {
+                    if (col0 + j < N) {
+                        if (atomic) atomicAdd(dst + j, v[j]);
+                        else dst[j] = v[j];
+                    }
                 }
             }
         }

@@ -345,11 +345,11 @@ def make_sample(lib, seed, P, n, phi0, phi1, max_steps):
                 target=_wrap(np.asarray(m.getPositions()) - x), cold=(secs, e, steps, fmax))
 
 
-def train(net, samples, epochs, dscale, lr=1e-3, physics=0.0, seed=0):
-    """Adam on the mean squared error of the displacement (in units of
-    dscale) over every vertex; with physics > 0, plus physics * E(x + d) /
-    E(x) from the overlap energy's autograd Function (its backward is the
-    exact-gradient kernel).  Returns the loss per epoch."""
+def train(net, samples, epochs, dscale, lr=1e-3, physics=0.0, seed=0, mse=1.0):
+    """Adam on mse times the mean squared error of the displacement (in
+    units of dscale) over every vertex; with physics > 0, plus physics *
+    E(x + d) / E(x) from the overlap energy's autograd Function (its
+    backward is the exact-gradient kernel).  Returns the loss per epoch."""
     from .autograd import OverlapSystem, overlap_energy
     rng = np.random.default_rng(seed)
     osys = {}
@@ -366,8 +366,8 @@ def train(net, samples, epochs, dscale, lr=1e-3, physics=0.0, seed=0):
             y = net.forward(smp["feats"], smp["rowptr"], smp["col"], keep=True)
             diff = (y - t)
             diff[V:] = 0.0
-            loss = float((diff[:V] ** 2).sum()) / V
-            dy = 2.0 * diff / V
+            loss = mse * float((diff[:V] ** 2).sum()) / V
+            dy = (2.0 * mse / V) * diff
             if physics > 0.0:
                 key = id(smp["system"])
                 if key not in osys:
@@ -407,7 +407,7 @@ def warm_minimise(lib, net, smp, dscale, max_steps):
 
 
 def experiment(n_train=32, n_test=8, P=1024, n=24, phi0=0.84, phi1=0.86, epochs=8,
-               max_steps=100000, seed=9000, physics=0.1):
+               max_steps=100000, seed=9000, physics=0.1, mse=1.0, lr=1e-3):
     """Generate pairs with the plain method, train, and compare warm-started
     with cold FIRE on held-out seeds.  Returns a JSON-ready dict."""
     from . import load_module
@@ -420,7 +420,7 @@ def experiment(n_train=32, n_test=8, P=1024, n=24, phi0=0.84, phi1=0.86, epochs=
     dscale = float(np.sqrt(np.mean([np.mean(s["target"] ** 2) for s in train_s])))
     net = WarmStartNet(seed=seed)
     t0 = time.perf_counter()
-    hist = train(net, train_s, epochs, dscale, physics=physics, seed=seed)
+    hist = train(net, train_s, epochs, dscale, lr=lr, physics=physics, seed=seed, mse=mse)
     torch.cuda.synchronize()
     t_train = time.perf_counter() - t0
     ok = gemm_status()
@@ -438,7 +438,8 @@ def experiment(n_train=32, n_test=8, P=1024, n=24, phi0=0.84, phi1=0.86, epochs=
                     "seeds" % (P, n, phi0, phi1, n_train, n_test),
         "network": "3 message-passing layers, hidden 128, BF16 operands with FP32 "
                    "accumulation (tcgen05 GEMM), neighbour sums over ring and contact edges",
-        "loss": "displacement MSE + %.2g x overlap energy (autograd Function)" % physics,
+        "loss": "%.2g x displacement MSE + %.2g x overlap energy (autograd Function)" % (
+            mse, physics),
         "train_loss_per_epoch": [float(h) for h in hist],
         "gemm_waits_ok": bool(ok),
         "data_generation_s": t_data, "training_s": t_train,
