@@ -62,6 +62,39 @@ void dfree(T** p) {
     if (*p) { cudaFree(*p); *p = nullptr; }
 }
 
+// Stream-ordered allocation for the contact workspace, which grows inside
+// FIRE runs (the reference's resize-and-retry): cudaMalloc and cudaFree wait
+// for the whole device, which stalled every other system of a batch each time
+// one system's buffers grew.  The device's default pool keeps up to 8 GiB of
+// freed memory for reuse.
+void keep_pool_memory() {
+    static bool done = false;
+    if (done) return;
+    int dev = 0;
+    cudaMemPool_t pool;
+    if (cudaGetDevice(&dev) == cudaSuccess && cudaDeviceGetDefaultMemPool(&pool, dev) == cudaSuccess) {
+        unsigned long long keep = 8ull << 30;
+        cudaMemPoolSetAttribute(pool, cudaMemPoolAttrReleaseThreshold, &keep);
+    }
+    done = true;
+}
+template <typename T>
+cudaError_t dalloc_async(T** p, size_t n, cudaStream_t st) {
+    if (*p) {
+        cudaError_t e = cudaFreeAsync(*p, st);
+        *p = nullptr;
+        if (e != cudaSuccess) return e;
+    }
+    if (n == 0) n = 1;
+    cudaError_t e = cudaMallocAsync((void**)p, n * sizeof(T), st);
+    if (e == cudaSuccess) e = cudaMemsetAsync(*p, 0, n * sizeof(T), st);
+    return e;
+}
+template <typename T>
+void dfree_async(T** p, cudaStream_t st) {
+    if (*p) { cudaFreeAsync(*p, st); *p = nullptr; }
+}
+
 }  // namespace
 
 struct pcp_model {
@@ -165,11 +198,18 @@ struct pcp_model {
         free_ws();
     }
     void free_ws() {
-        dfree(&ws.edgeVec); dfree(&ws.vtx); dfree(&ws.polyInfo); dfree(&ws.polyBox); dfree(&ws.polyFlags);
-        dfree(&ws.gridCount); dfree(&ws.gridStart); dfree(&ws.gridFill); dfree(&ws.sortedPoly);
-        dfree(&ws.unsafeList); dfree(&ws.pairs); dfree(&ws.recKey); dfree(&ws.recOuter);
-        dfree(&ws.recTU); dfree(&ws.recUT); dfree(&ws.fixList); dfree(&ws.slowList);
-        dfree(&ws.maxCand); dfree(&ws.overList);
+        // stream-ordered, like their allocation (alloc_ws)
+        cudaStream_t st = stream;
+        dfree_async(&ws.edgeVec, st); dfree_async(&ws.vtx, st); dfree_async(&ws.polyInfo, st);
+        dfree_async(&ws.polyBox, st); dfree_async(&ws.polyFlags, st);
+        dfree_async(&ws.gridCount, st); dfree_async(&ws.gridStart, st);
+        dfree_async(&ws.gridFill, st); dfree_async(&ws.sortedPoly, st);
+        dfree_async(&ws.unsafeList, st); dfree_async(&ws.pairs, st); dfree_async(&ws.recKey, st);
+        dfree_async(&ws.recOuter, st); dfree_async(&ws.recTU, st); dfree_async(&ws.recUT, st);
+        dfree_async(&ws.fixList, st); dfree_async(&ws.slowList, st);
+        dfree_async(&ws.maxCand, st); dfree_async(&ws.overList, st);
+        if (st) cudaStreamSynchronize(st);
+        else cudaDeviceSynchronize();
     }
     void invalidate() {
         recordsCached = false;
@@ -201,18 +241,20 @@ int alloc_ws(pcp_model* m, int capPairs, int capRecords) {
     w.capFix = std::max(1024, capRecords / 16);
     w.capSlow = std::max(1024, capPairs / 4);
     size_t V = (size_t)m->V, P = (size_t)std::max(m->P, 1);
-    CK(dalloc(&w.edgeVec, V)); CK(dalloc(&w.vtx, V));
-    CK(dalloc(&w.polyInfo, P)); CK(dalloc(&w.polyBox, P)); CK(dalloc(&w.polyFlags, P));
-    CK(dalloc(&w.gridCount, (size_t)kGridMax * kGridMax));
-    CK(dalloc(&w.gridStart, (size_t)kGridMax * kGridMax + 1));
-    CK(dalloc(&w.gridFill, (size_t)kGridMax * kGridMax));
-    CK(dalloc(&w.sortedPoly, P)); CK(dalloc(&w.unsafeList, P));
-    CK(dalloc(&w.pairs, (size_t)capPairs));
-    CK(dalloc(&w.recKey, (size_t)capRecords)); CK(dalloc(&w.recOuter, (size_t)capRecords));
-    CK(dalloc(&w.recTU, (size_t)capRecords)); CK(dalloc(&w.recUT, (size_t)capRecords));
-    CK(dalloc(&w.fixList, (size_t)w.capFix)); CK(dalloc(&w.slowList, (size_t)w.capSlow));
-    if (!w.maxCand) CK(dalloc(&w.maxCand, (size_t)kMaxCand));
-    CK(dalloc(&w.overList, (size_t)capPairs));
+    cudaStream_t st = m->stream;
+    keep_pool_memory();
+    CK(dalloc_async(&w.edgeVec, V, st)); CK(dalloc_async(&w.vtx, V, st));
+    CK(dalloc_async(&w.polyInfo, P, st)); CK(dalloc_async(&w.polyBox, P, st)); CK(dalloc_async(&w.polyFlags, P, st));
+    CK(dalloc_async(&w.gridCount, (size_t)kGridMax * kGridMax, st));
+    CK(dalloc_async(&w.gridStart, (size_t)kGridMax * kGridMax + 1, st));
+    CK(dalloc_async(&w.gridFill, (size_t)kGridMax * kGridMax, st));
+    CK(dalloc_async(&w.sortedPoly, P, st)); CK(dalloc_async(&w.unsafeList, P, st));
+    CK(dalloc_async(&w.pairs, (size_t)capPairs, st));
+    CK(dalloc_async(&w.recKey, (size_t)capRecords, st)); CK(dalloc_async(&w.recOuter, (size_t)capRecords, st));
+    CK(dalloc_async(&w.recTU, (size_t)capRecords, st)); CK(dalloc_async(&w.recUT, (size_t)capRecords, st));
+    CK(dalloc_async(&w.fixList, (size_t)w.capFix, st)); CK(dalloc_async(&w.slowList, (size_t)w.capSlow, st));
+    if (!w.maxCand) CK(dalloc_async(&w.maxCand, (size_t)kMaxCand, st));
+    CK(dalloc_async(&w.overList, (size_t)capPairs, st));
     m->generation++;
     return PCP_OK;
 }
