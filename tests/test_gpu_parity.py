@@ -216,6 +216,38 @@ def test_records_bit_exact_with_polygons_spanning_the_box(box):
     assert_forces_close(g.getForces(), o.getForces())
 
 
+def test_records_bit_exact_when_most_pairs_overflow():
+    """Every polygon scrambled (random vertices over the whole box, as after a
+    FIRE step with a huge force): 400 polygons of 24 vertices at box size 2
+    give about 80,000 candidate pairs with dozens of crossings each, more
+    than the warps of the narrow phase can finish themselves, so the
+    overflow kernel (k_narrow_over) and the grid-wide fixup take most of the
+    work.  Records, outersections, energy and force against the oracle."""
+    s = make_system(400, 24, 0.85, seed=21)
+    x = np.random.default_rng(5).random(s.positions.size)
+    system = PolygonSystem(positions=x, n_array=s.n_array, start_indices=s.start_indices,
+                           target_areas=s.target_areas, target_edge_lengths=s.target_edge_lengths,
+                           max_edge_length=s.max_edge_length, phi=s.phi)
+    g, o = pair(system)
+    g.setMaxEdgeLength(0.5)
+    o.setMaxEdgeLength(0.5)
+    contacts(g)
+    contacts(o)
+    keys = o.getIntersections().astype(np.uint64)
+    a = (keys >> np.uint64(48)).astype(np.int64)
+    b = ((keys >> np.uint64(32)) & np.uint64(0xFFFF)).astype(np.int64)
+    _, per_pair = np.unique(np.minimum(a, b) * 65536 + np.maximum(a, b), return_counts=True)
+    # more pairs over a warp's 32-record slot than the warps finish
+    # themselves: 16 per warp, 4 warps per block of the default grid
+    blocks = lib.Model(8).getLaunchShape()[0]
+    assert np.count_nonzero(per_pair > 32) > 16 * 4 * blocks
+    assert_records_equal(g, o)
+    g.updateForceEnergy()
+    o.updateForceEnergy()
+    assert g.getEnergy() == pytest.approx(o.getEnergy(), rel=ENERGY_RTOL)
+    assert_forces_close(g.getForces(), o.getForces())
+
+
 def test_geometry_parity_odd_shapes():
     """Geometry of the odd shapes: a repeated vertex (a zero-length edge,
     whose unit tangent the reference computes as 0/0), a bow tie, a sliver,
