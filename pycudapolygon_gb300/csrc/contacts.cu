@@ -1050,7 +1050,11 @@ __device__ __forceinline__ void push_slow(int q, Ctrl* ctrl, ContactWS& ws) {
 // false only when the FP64 test of cross_exact certainly rejects the pair.
 // The FP32 coordinates are within 6e-8 of the FP64 ones, so every component
 // of r = p2 - p, s = q2 - q, g = q - p is within d = 1.5e-7 of the FP64
-// vector (same minimum image while all components stay below 0.45), and
+// vector.  Both take the same minimum image while every FP32 component stays
+// below 0.4999: the unwrapped difference is then within 0.4999 + 1.3e-7 of
+// the integer the FP32 wrap removed, so that integer is its unique nearest
+// one, which the FP64 wrap removes too (edges of polygons a large FIRE move
+// scrambled reach lengths near 0.5 and still get the filter).  And
 // each of denom, g x s, g x r is within E = 4 M d + 2 d^2 + 4 2^-24 M^2 of
 // its FP64 value (M bounds the components).  With |denom| > E + 1e-12 the
 // FP64 denominator has the same sign and passes the 1e-12 test; t <= 0 is
@@ -1062,7 +1066,7 @@ __device__ __forceinline__ bool maybe_cross(float4 p, float4 p2, float4 q, float
     const float gx = wrapf(q.x - p.x), gy = wrapf(q.y - p.y);
     const float M = fmaxf(fmaxf(fmaxf(fabsf(rx), fabsf(ry)), fmaxf(fabsf(sx), fabsf(sy))),
                           fmaxf(fabsf(gx), fabsf(gy)));
-    if (!(M < 0.45f)) return true;                      // (NaN too)
+    if (!(M < 0.4999f)) return true;                    // (NaN too)
     const float d = 1.5e-7f, Mb = M + d;
     const float E = 4.f * Mb * d + 2.f * d * d + 2.4e-7f * Mb * Mb;
     const float den = rx * sy - ry * sx;
