@@ -720,6 +720,32 @@ def run_stages(args):
                       "launches": m.getLaunchCount()}))
 
 
+def run_scrambled(args):
+    """Profiling mode: one system of the many-systems workload (by rank in
+    polygon count) with every vertex placed at random in the box, as a FIRE
+    step whose Verlet move scrambled the polygons leaves it, and one contact
+    search and overlap-force evaluation at cell size 0.5."""
+    import torch
+    import pycudapolygon_gb300 as pg
+    from pycudapolygon_gb300.systems import batched_specs, load_into, make_system
+    lib = pg.load_module()
+    specs = batched_specs(BATCH_SYSTEMS, BATCH_SEED)
+    order = sorted(range(len(specs)), key=lambda i: specs[i][0])
+    P, nv, phi, sd = specs[order[args.scrambled]]
+    s = make_system(P, nv, phi, seed=sd)
+    m = load_into(lib.Model(s.num_vertices), s)
+    m.setMaxEdgeLength(0.5)
+    m.setPositions(np.random.default_rng(0).random(s.positions.size))
+    m.updatePolygonGeometry()
+    m.updateNeighborCells()
+    m.updateNeighbors()
+    m.updateOutersections()
+    m.updateForceEnergy()
+    torch.cuda.synchronize()
+    print(json.dumps({"polygons": P, "vertices": s.num_vertices,
+                      "records": m.getNumIntersections(), "pairs": m.getNarrowPairCount()}))
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
@@ -739,6 +765,9 @@ def main():
                     help="systems of the many-systems leg (0: skip it)")
     ap.add_argument("--stages", type=int, default=0,
                     help="profiling mode: run every stage this many times, no timing")
+    ap.add_argument("--scrambled", type=int, default=-1,
+                    help="profiling mode: one contact search and force on the scrambled state "
+                         "of the many-systems workload's system of this rank in size")
     args = ap.parse_args()
     if args.warmup < 3:
         args.warmup = 3
@@ -748,6 +777,9 @@ def main():
         return
     if args.stages > 0:
         run_stages(args)
+        return
+    if args.scrambled >= 0:
+        run_scrambled(args)
         return
     run_gpu(args, ws, rank, local)
 
