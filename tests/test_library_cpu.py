@@ -52,3 +52,23 @@ def test_unbound_reference_methods_stay_unbound(built):
     mod = pg.load_module()
     for n in ["initializeRandomSeed", "getRandomSeed", "getAreaPerOverlap"]:
         assert not hasattr(mod.Model, n)
+
+
+def test_warm_start_kernels_check_arguments_first(built):
+    """The warm start's entry points refuse bad arguments before touching
+    the device (no GPU needed): K not a multiple of 8, misaligned operands,
+    ReLU with a split K, an odd row width."""
+    lib = cabi.lib(built[0])
+    fake = ctypes.c_void_p(1 << 20)          # never dereferenced: the checks come first
+    odd = ctypes.c_void_p((1 << 20) + 8)
+    assert lib.pcp_gemm_bf16(fake, fake, fake, 128, 128, 7, None, 0, 1, None) == 1
+    assert b"multiple of 8" in lib.pcp_last_error()
+    assert lib.pcp_gemm_bf16(odd, fake, fake, 128, 128, 64, None, 0, 1, None) == 1
+    assert b"aligned" in lib.pcp_last_error()
+    assert lib.pcp_gemm_bf16(fake, fake, fake, 128, 128, 64, None, 1, 4, None) == 1
+    assert b"ReLU" in lib.pcp_last_error()
+    assert lib.pcp_gemm_bf16(fake, fake, fake, 128, 128, 64, None, 0, 0, None) == 1
+    assert lib.pcp_gemm_bf16(None, fake, fake, 128, 128, 64, None, 0, 1, None) == 1
+    assert lib.pcp_gemm_bf16(fake, fake, fake, 0, 128, 64, None, 0, 1, None) == 0   # empty
+    assert lib.pcp_graph_sum_bf16(fake, fake, fake, fake, 10, 7, ctypes.c_float(1.0), None) == 1
+    assert b"even" in lib.pcp_last_error()
