@@ -58,6 +58,8 @@ enum { PCP_MODEL_NORMAL = 0, PCP_MODEL_EDGE_ONLY = 1, PCP_MODEL_AREA_ONLY = 2,
 /* minimizerEnum (src/enumTypes.h:9) */
 enum { PCP_MINIMIZER_GD = 0, PCP_MINIMIZER_FIRE = 1 };
 
+/* Output pointers of the scalar getters must not be NULL (PCP_ERR_ARG);
+ * the array getters take the capacity of their output. */
 /* Message of the last failed call on this thread ("" if none). */
 const char* pcp_last_error(void);
 /* Library version string. */
@@ -287,17 +289,19 @@ int pcp_model_get_narrow_pair_count(pcp_model* m, int* pairs_out, int* self_out)
  * starting point.
  * ====================================================================== */
 /* C[m,n] = A[m,k] B[n,k]^T (+ bias[n]) (then ReLU when relu != 0) on the
- * tensor cores: A and B BF16, row-major, k a multiple of 8, 16-byte aligned;
- * C FP32, row-major.  splits > 1 divides k over blocks that add into C
- * (which the caller zeroes; bias added once, no ReLU).  Asynchronous on the
- * stream. */
+ * tensor cores: A and B BF16, row-major, k a multiple of 8; C FP32,
+ * row-major; A, B and C 16-byte aligned.  splits > 1 divides k over blocks
+ * that add into C (which the caller zeroes; bias added once, no ReLU).
+ * Asynchronous on the stream. */
 int pcp_gemm_bf16(const void* d_a, const void* d_b, float* d_c, int m, int n, int k,
                   const float* d_bias, int relu, int splits, void* stream);
 /* 1 in *out when a wait inside a GEMM launched since the last call ran out
  * (its results are then not to be used); clears the flag.  Synchronises. */
 int pcp_gemm_status(int* out);
 /* out[i,:] = scale * sum over j in col[rowptr[i]..rowptr[i+1]) of h[j,:],
- * BF16 rows of f (even) values, FP32 sums. */
+ * BF16 rows of f (even) values, FP32 sums; h and out 4-byte aligned.  The
+ * device arrays are not read on the host: rowptr[0..v] must be
+ * non-decreasing and every col entry a row of h. */
 int pcp_graph_sum_bf16(const int* d_rowptr, const int* d_col, const void* d_h, void* d_out,
                        int v, int f, float scale, void* stream);
 

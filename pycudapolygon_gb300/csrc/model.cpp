@@ -907,6 +907,8 @@ const char* pcp_last_error(void) { return g_err.c_str(); }
 const char* pcp_version(void) { return "pcp_gb300 0.1 (sm_103a)"; }
 
 #define CHECK_M(m) do { if (!(m)) return fail(PCP_ERR_ARG, "null model"); ++(m)->callSerial; } while (0)
+// a model call with one scalar output
+#define CHECK_MO(m, o) do { CHECK_M(m); if (!(o)) return fail(PCP_ERR_ARG, "null output"); } while (0)
 
 int pcp_model_create(int size, pcp_model** out) {
     if (!out) return fail(PCP_ERR_ARG, "null output");
@@ -1040,8 +1042,8 @@ int pcp_model_set_model_enum(pcp_model* m, int e) {
 
 int pcp_model_set_stiffness(pcp_model* m, double k) { CHECK_M(m); m->stiffness = k; return PCP_OK; }
 int pcp_model_set_compressibility(pcp_model* m, double c) { CHECK_M(m); m->compressibility = c; return PCP_OK; }
-int pcp_model_get_stiffness(pcp_model* m, double* out) { CHECK_M(m); *out = m->stiffness; return PCP_OK; }
-int pcp_model_get_compressibility(pcp_model* m, double* out) { CHECK_M(m); *out = m->compressibility; return PCP_OK; }
+int pcp_model_get_stiffness(pcp_model* m, double* out) { CHECK_MO(m, out); *out = m->stiffness; return PCP_OK; }
+int pcp_model_get_compressibility(pcp_model* m, double* out) { CHECK_MO(m, out); *out = m->compressibility; return PCP_OK; }
 
 int pcp_model_initialize_neighbor_cells(pcp_model* m) {
     CHECK_M(m);
@@ -1238,7 +1240,7 @@ int pcp_model_save_tentative_positions(pcp_model* m) {
 }
 
 int pcp_model_get_max_effective_force(pcp_model* m, double dt, int minimizer, double* out) {
-    CHECK_M(m);
+    CHECK_MO(m, out);
     double scale = (minimizer == PCP_MINIMIZER_GD) ? (1.0 / dt) : (2.0 / (dt * dt));
     CK(launch_max_effective_force(reinterpret_cast<const double*>(m->pos),
                                   reinterpret_cast<const double*>(m->posTent),
@@ -1555,7 +1557,7 @@ int pcp_model_fire_continue(pcp_model* m, int n_steps) {
 }
 
 int pcp_model_fire_status(pcp_model* m, double out[8], int* redo_out) {
-    CHECK_M(m);
+    CHECK_MO(m, out);
     int rc = read_ctrl(m);
     if (rc) return rc;
     bool redo = false;
@@ -1637,11 +1639,11 @@ int pcp_model_contacts_stage(pcp_model* m, int stage) {
 }
 
 // ---- scalar getters ----
-int pcp_model_get_num_vertices(pcp_model* m, int* out) { CHECK_M(m); *out = m->V; return PCP_OK; }
-int pcp_model_get_num_polygons(pcp_model* m, int* out) { CHECK_M(m); *out = m->P; return PCP_OK; }
-int pcp_model_get_num_intersections(pcp_model* m, int* out) { CHECK_M(m); *out = m->numIntersections; return PCP_OK; }
+int pcp_model_get_num_vertices(pcp_model* m, int* out) { CHECK_MO(m, out); *out = m->V; return PCP_OK; }
+int pcp_model_get_num_polygons(pcp_model* m, int* out) { CHECK_MO(m, out); *out = m->P; return PCP_OK; }
+int pcp_model_get_num_intersections(pcp_model* m, int* out) { CHECK_MO(m, out); *out = m->numIntersections; return PCP_OK; }
 int pcp_model_get_max_neighbors(pcp_model* m, int* out) {
-    CHECK_M(m);
+    CHECK_MO(m, out);
     if (m->topology && m->view != pcp_model::VIEW_NONE) {
         int rc = ensure_neighbors(m);
         if (rc) return rc;
@@ -1649,18 +1651,18 @@ int pcp_model_get_max_neighbors(pcp_model* m, int* out) {
     *out = m->maxNeighbors;
     return PCP_OK;
 }
-int pcp_model_get_box_size(pcp_model* m, int* out) { CHECK_M(m); *out = m->boxSize; return PCP_OK; }
-int pcp_model_get_model_enum(pcp_model* m, int* out) { CHECK_M(m); *out = m->modelType; return PCP_OK; }
-int pcp_model_get_last_shake_iters(pcp_model* m, int* out) { CHECK_M(m); *out = m->lastShakeIters; return PCP_OK; }
+int pcp_model_get_box_size(pcp_model* m, int* out) { CHECK_MO(m, out); *out = m->boxSize; return PCP_OK; }
+int pcp_model_get_model_enum(pcp_model* m, int* out) { CHECK_MO(m, out); *out = m->modelType; return PCP_OK; }
+int pcp_model_get_last_shake_iters(pcp_model* m, int* out) { CHECK_MO(m, out); *out = m->lastShakeIters; return PCP_OK; }
 int pcp_model_get_energy(pcp_model* m, double* out) {
-    CHECK_M(m);
+    CHECK_MO(m, out);
     int rc = read_ctrl(m);
     if (rc) return rc;
     *out = m->ctrlHost->energy;
     return PCP_OK;
 }
 int pcp_model_get_max_unbalanced_force(pcp_model* m, double* out) {
-    CHECK_M(m);
+    CHECK_MO(m, out);
     if (m->maxFSerial != 0 && m->maxFSerial + 1 == m->callSerial) {
         // the FIRE step just before read it back with its control block (the
         // same maximum over the same forces); the reference's per-step loop
@@ -1675,11 +1677,11 @@ int pcp_model_get_max_unbalanced_force(pcp_model* m, double* out) {
 }
 int pcp_model_get_max_edge_length(pcp_model* m, double* out) {
     if (m && m->geometryStale) { int grc = ensure_geometry(m); if (grc) return grc; }
-    CHECK_M(m);
+    CHECK_MO(m, out);
     CK(cudaMemcpyAsync(out, m->maxEdge, sizeof(double), cudaMemcpyDeviceToHost, m->stream));
     return sync(m);
 }
-int pcp_model_get_overlap_area(pcp_model* m, double* out) { CHECK_M(m); *out = m->overlapArea; return PCP_OK; }
+int pcp_model_get_overlap_area(pcp_model* m, double* out) { CHECK_MO(m, out); *out = m->overlapArea; return PCP_OK; }
 
 // ---- array getters ----
 int pcp_model_get_positions(pcp_model* m, double* out, int cap, int* len) {
@@ -1867,13 +1869,13 @@ int pcp_model_get_intersections_counter(pcp_model* m, int* out, int cap, int* le
 }
 
 int pcp_model_device_positions(pcp_model* m, double** out) {
-    CHECK_M(m); *out = reinterpret_cast<double*>(m->pos); return PCP_OK;
+    CHECK_MO(m, out); *out = reinterpret_cast<double*>(m->pos); return PCP_OK;
 }
 int pcp_model_device_forces(pcp_model* m, double** out) {
-    CHECK_M(m); *out = reinterpret_cast<double*>(m->force); return PCP_OK;
+    CHECK_MO(m, out); *out = reinterpret_cast<double*>(m->force); return PCP_OK;
 }
 int pcp_model_get_pair_count(pcp_model* m, long long* out) {
-    CHECK_M(m);
+    CHECK_MO(m, out);
     int rc = read_ctrl(m);
     if (rc) return rc;
     *out = (long long)m->ctrlHost->pairEvals;
@@ -1888,8 +1890,11 @@ int pcp_gemm_bf16(const void* d_a, const void* d_b, float* d_c, int m, int n, in
     if (!d_a || !d_b || !d_c) return fail(PCP_ERR_ARG, "pcp_gemm_bf16: null buffer");
     if (k == 0 || k % 8 != 0)
         return fail(PCP_ERR_ARG, "pcp_gemm_bf16: K must be a positive multiple of 8");
-    if ((reinterpret_cast<uintptr_t>(d_a) | reinterpret_cast<uintptr_t>(d_b)) % 16 != 0)
-        return fail(PCP_ERR_ARG, "pcp_gemm_bf16: A and B must be 16-byte aligned");
+    // A and B: the tensor maps' base addresses; C: the epilogue's 16-byte
+    // row stores
+    if ((reinterpret_cast<uintptr_t>(d_a) | reinterpret_cast<uintptr_t>(d_b) |
+         reinterpret_cast<uintptr_t>(d_c)) % 16 != 0)
+        return fail(PCP_ERR_ARG, "pcp_gemm_bf16: A, B and C must be 16-byte aligned");
     if (splits > 1 && relu)
         return fail(PCP_ERR_ARG, "pcp_gemm_bf16: ReLU needs the whole K sum (splits = 1)");
     int rc = launch_gemm_bf16(d_a, d_b, d_c, m, n, k, d_bias, relu, splits,
@@ -1913,6 +1918,8 @@ int pcp_graph_sum_bf16(const int* d_rowptr, const int* d_col, const void* d_h, v
     if (v == 0) return PCP_OK;
     if (!d_rowptr || !d_col || !d_h || !d_out)
         return fail(PCP_ERR_ARG, "pcp_graph_sum_bf16: null buffer");
+    if ((reinterpret_cast<uintptr_t>(d_h) | reinterpret_cast<uintptr_t>(d_out)) % 4 != 0)
+        return fail(PCP_ERR_ARG, "pcp_graph_sum_bf16: h and out must be 4-byte aligned");
     CK(launch_graph_sum_bf16(d_rowptr, d_col, d_h, d_out, v, f, scale,
                              static_cast<cudaStream_t>(stream)));
     return PCP_OK;
@@ -1920,7 +1927,7 @@ int pcp_graph_sum_bf16(const int* d_rowptr, const int* d_col, const void* d_h, v
 
 int pcp_control_block_bytes(void) { return (int)sizeof(Ctrl); }
 int pcp_model_get_narrow_pair_total(pcp_model* m, long long* out) {
-    CHECK_M(m);
+    CHECK_MO(m, out);
     int rc = read_ctrl(m);
     if (rc) return rc;
     *out = (long long)(m->ctrlHost->narrowEvals - m->ctrlHost->selfEvals);
@@ -1935,7 +1942,7 @@ int pcp_model_get_narrow_pair_count(pcp_model* m, int* pairs_out, int* self_out)
     return PCP_OK;
 }
 int pcp_model_get_launch_count(pcp_model* m, long long* out) {
-    CHECK_M(m);
+    CHECK_MO(m, out);
     int rc = read_ctrl(m);
     if (rc) return rc;
     *out = m->launches + (long long)m->ctrlHost->condLaunches;

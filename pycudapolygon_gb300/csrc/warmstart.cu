@@ -174,7 +174,7 @@ k_gemm_bf16(const __grid_constant__ CUtensorMap mapA, const __grid_constant__ CU
             tma_2d(st + S::kA, &mapB, (c0 + c) * kBK, n0, &full[s]);
         };
         bool ok = true;
-        int issued = 0;
+        int issued = 0, landed = 0;   // loads issued; loads whose wait succeeded
         load(0, 0);
         ++issued;
         for (int c = 0; c < nc && ok; ++c) {
@@ -188,6 +188,7 @@ k_gemm_bf16(const __grid_constant__ CUtensorMap mapA, const __grid_constant__ CU
             }
             ok = bar_wait(&full[s], (c >> 1) & 1);
             if (!ok) break;
+            ++landed;
             asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
             const uint32_t a = saddr(smem + s * S::kStage), b = a + S::kA;
 #pragma unroll
@@ -197,10 +198,13 @@ k_gemm_bf16(const __grid_constant__ CUtensorMap mapA, const __grid_constant__ CU
             mma_commit(&empty[s]);
         }
         if (!ok) {
-            // a wait ran out: let the copies already issued land (bounded)
+            // a wait ran out: let the copies still in flight land (bounded)
             // before the block leaves, so none writes into a later block's
-            // shared memory
-            for (int c = 0; c < issued; ++c) bar_wait(&full[c & 1], (c >> 1) & 1);
+            // shared memory.  Those are the loads landed..issued-1, at most
+            // one per stage and each the latest use of its stage, so the
+            // parity of its own phase names it (an older phase's parity
+            // would alias a newer one).
+            for (int c = landed; c < issued; ++c) bar_wait(&full[c & 1], (c >> 1) & 1);
         }
         mma_commit(&done);   // arrives once every MMA issued above has completed
     }

@@ -56,14 +56,17 @@ def test_unbound_reference_methods_stay_unbound(built):
 
 def test_warm_start_kernels_check_arguments_first(built):
     """The warm start's entry points refuse bad arguments before touching
-    the device (no GPU needed): K not a multiple of 8, misaligned operands,
-    ReLU with a split K, an odd row width."""
+    the device (no GPU needed): K not a multiple of 8, misaligned operands
+    or outputs, ReLU with a split K, an odd row width."""
     lib = cabi.lib(built[0])
     fake = ctypes.c_void_p(1 << 20)          # never dereferenced: the checks come first
     odd = ctypes.c_void_p((1 << 20) + 8)
     assert lib.pcp_gemm_bf16(fake, fake, fake, 128, 128, 7, None, 0, 1, None) == 1
     assert b"multiple of 8" in lib.pcp_last_error()
     assert lib.pcp_gemm_bf16(odd, fake, fake, 128, 128, 64, None, 0, 1, None) == 1
+    assert b"aligned" in lib.pcp_last_error()
+    # C takes 16-byte row stores
+    assert lib.pcp_gemm_bf16(fake, fake, odd, 128, 128, 64, None, 0, 1, None) == 1
     assert b"aligned" in lib.pcp_last_error()
     assert lib.pcp_gemm_bf16(fake, fake, fake, 128, 128, 64, None, 1, 4, None) == 1
     assert b"ReLU" in lib.pcp_last_error()
@@ -72,3 +75,6 @@ def test_warm_start_kernels_check_arguments_first(built):
     assert lib.pcp_gemm_bf16(fake, fake, fake, 0, 128, 64, None, 0, 1, None) == 0   # empty
     assert lib.pcp_graph_sum_bf16(fake, fake, fake, fake, 10, 7, ctypes.c_float(1.0), None) == 1
     assert b"even" in lib.pcp_last_error()
+    half = ctypes.c_void_p((1 << 20) + 2)     # BF16 pairs are read and written as 4-byte words
+    assert lib.pcp_graph_sum_bf16(fake, fake, half, fake, 10, 8, ctypes.c_float(1.0), None) == 1
+    assert b"4-byte" in lib.pcp_last_error()
