@@ -354,6 +354,11 @@ int pcp_batch_autotune_report(pcp_batch* b, char* buf, int cap, int* len_out);
 /* ======================================================================
  * 2. Stateless kernels on caller-owned device buffers (stream = cudaStream_t)
  * ====================================================================== */
+/* A negative size, a NULL buffer for a non-empty input, or box_size < 1
+ * returns PCP_ERR_ARG before any launch.  pcp_project_force and
+ * pcp_shake_project read d_start back (they size their scratch from it)
+ * and return PCP_ERR_ARG unless it is CSR offsets: start[0] == 0, never
+ * decreasing.  The other launchers do not read device arrays on the host. */
 
 /* topology: updateShapeIdKernel + computeNextPrevKernel
  * (model.cu:77-81, 387-391; kernels.cuh:127-135, 652-659) */

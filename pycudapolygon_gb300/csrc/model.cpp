@@ -1952,6 +1952,9 @@ int pcp_model_get_launch_count(pcp_model* m, long long* out) {
 // ---- stateless launchers ----
 int pcp_topology(const int* d_start, int P, int V, int* d_shape_id, int* d_next, int* d_prev,
                  void* stream) {
+    if (P < 0 || V < 0) return fail(PCP_ERR_ARG, "pcp_topology: negative size");
+    if (P > 0 && (!d_start || !d_shape_id || !d_next || !d_prev))
+        return fail(PCP_ERR_ARG, "pcp_topology: null device buffer");
     CK(launch_topology(d_start, P, V, d_shape_id, d_next, d_prev, (cudaStream_t)stream));
     return PCP_OK;
 }
@@ -1960,6 +1963,10 @@ int pcp_polygon_geometry(const double* d_pos, const int* d_start, int P, int V,
                          double* d_edge_lengths, double* d_areas, double* d_com_x, double* d_com_y,
                          double* d_perimeters, double* d_constraints, double* d_max_edge,
                          void* stream) {
+    if (P < 0 || V < 0) return fail(PCP_ERR_ARG, "pcp_polygon_geometry: negative size");
+    if (P > 0 && (!d_pos || !d_start || !d_edge_lengths || !d_areas || !d_com_x || !d_com_y ||
+                  !d_perimeters || !d_constraints || !d_max_edge))
+        return fail(PCP_ERR_ARG, "pcp_polygon_geometry: null device buffer");
     CK(launch_geometry(reinterpret_cast<const double2*>(d_pos), d_start, P, V, d_edge_lengths,
                        d_areas, d_com_x, d_com_y, d_perimeters, d_constraints, d_max_edge, nullptr,
                        (cudaStream_t)stream));
@@ -1968,6 +1975,10 @@ int pcp_polygon_geometry(const double* d_pos, const int* d_start, int P, int V,
 
 int pcp_neighbor_cells(const double* d_pos, const int* d_start, const int* d_shape_id, int V,
                        int B, int* d_cell, void* stream) {
+    if (V < 0 || B < 1)
+        return fail(PCP_ERR_ARG, "pcp_neighbor_cells: negative size or box_size < 1");
+    if (V > 0 && (!d_pos || !d_start || !d_shape_id || !d_cell))
+        return fail(PCP_ERR_ARG, "pcp_neighbor_cells: null device buffer");
     CK(launch_neighbor_cells(reinterpret_cast<const double2*>(d_pos), d_start, d_shape_id, V, B,
                              d_cell, nullptr, (cudaStream_t)stream));
     return PCP_OK;
@@ -1989,17 +2000,27 @@ static double* stateless_scratch(int V) {
     return buf;
 }
 
+// Reads the CSR offsets back and checks them: the kernels index positions
+// and scratch by them, and the scratch is sized from start[P].
 static int start_info(const int* d_start, int P, int& V, int& nmax) {
+    if (P < 0) return fail(PCP_ERR_ARG, "negative polygon count");
+    if (P > 0 && !d_start) return fail(PCP_ERR_ARG, "null start array");
     std::vector<int> h(P + 1, 0);
     if (P > 0) CK(cudaMemcpy(h.data(), d_start, (P + 1) * sizeof(int), cudaMemcpyDeviceToHost));
+    if (h[0] != 0) return fail(PCP_ERR_ARG, "start must begin at 0 and never decrease");
     V = h[P];
     nmax = 0;
-    for (int p = 0; p < P; ++p) nmax = std::max(nmax, h[p + 1] - h[p]);
+    for (int p = 0; p < P; ++p) {
+        if (h[p + 1] < h[p]) return fail(PCP_ERR_ARG, "start must begin at 0 and never decrease");
+        nmax = std::max(nmax, h[p + 1] - h[p]);
+    }
     return PCP_OK;
 }
 
 int pcp_project_force(const double* d_pos, const int* d_start, int P, const double* d_constraints,
                       double* d_force, void* stream) {
+    if (P > 0 && (!d_pos || !d_constraints || !d_force))
+        return fail(PCP_ERR_ARG, "pcp_project_force: null device buffer");
     int V = 0, nmax = 0;
     int rc = start_info(d_start, P, V, nmax);
     if (rc) return rc;
@@ -2014,6 +2035,9 @@ int pcp_project_force(const double* d_pos, const int* d_start, int P, const doub
 
 int pcp_shake_project(double* d_pos, const int* d_start, int P, const double* d_tl,
                       const double* d_ta, int max_iter, double tol, int* d_max_iters, void* stream) {
+    if (!d_max_iters) return fail(PCP_ERR_ARG, "pcp_shake_project: null d_max_iters");
+    if (P > 0 && (!d_pos || !d_tl || !d_ta))
+        return fail(PCP_ERR_ARG, "pcp_shake_project: null device buffer");
     int V = 0, nmax = 0;
     int rc = start_info(d_start, P, V, nmax);
     if (rc) return rc;
@@ -2066,6 +2090,9 @@ int pcp_shake_project_noalloc(double* d_pos, const int* d_start, int P, const do
 }
 
 int pcp_update_positions(double* d_pos, const double* d_force, int V, double dt, void* stream) {
+    if (V < 0) return fail(PCP_ERR_ARG, "pcp_update_positions: negative size");
+    if (V > 0 && (!d_pos || !d_force))
+        return fail(PCP_ERR_ARG, "pcp_update_positions: null device buffer");
     CK(launch_update_positions(d_pos, d_force, V, dt, (cudaStream_t)stream));
     return PCP_OK;
 }

@@ -78,3 +78,25 @@ def test_warm_start_kernels_check_arguments_first(built):
     half = ctypes.c_void_p((1 << 20) + 2)     # BF16 pairs are read and written as 4-byte words
     assert lib.pcp_graph_sum_bf16(fake, fake, half, fake, 10, 8, ctypes.c_float(1.0), None) == 1
     assert b"4-byte" in lib.pcp_last_error()
+
+
+def test_stateless_launchers_check_arguments_first(built):
+    """The stateless launchers refuse negative sizes, NULL buffers and a
+    box size below one before any launch (no GPU needed)."""
+    lib = cabi.lib(built[0])
+    fake = ctypes.c_void_p(1 << 20)          # never dereferenced: the checks come first
+    d = ctypes.c_double
+    assert lib.pcp_topology(fake, -1, 10, fake, fake, fake, None) == 1
+    assert lib.pcp_topology(fake, 4, 10, None, fake, fake, None) == 1
+    assert b"null" in lib.pcp_last_error()
+    assert lib.pcp_topology(None, 0, 0, None, None, None, None) == 0   # empty: nothing to do
+    assert lib.pcp_polygon_geometry(fake, fake, 4, 40, fake, fake, fake, fake, fake, fake, None,
+                                    None) == 1
+    assert lib.pcp_neighbor_cells(fake, fake, fake, 40, 0, fake, None) == 1
+    assert b"box_size" in lib.pcp_last_error()
+    assert lib.pcp_project_force(fake, fake, -2, fake, fake, None) == 1
+    assert lib.pcp_project_force(fake, None, 3, fake, fake, None) == 1
+    assert lib.pcp_shake_project(fake, fake, 3, fake, fake, 5, d(1e-15), None, None) == 1
+    assert lib.pcp_shake_project(None, fake, 3, fake, fake, 5, d(1e-15), fake, None) == 1
+    assert lib.pcp_update_positions(fake, None, 10, d(1e-3), None) == 1
+    assert lib.pcp_update_positions(fake, fake, -1, d(1e-3), None) == 1
