@@ -1673,7 +1673,7 @@ k_overlap_force(const double2* __restrict__ pos, const int* __restrict__ start,
          base += warpsTotal * kForceRecs) {
         const int r = base + (lane >> 1);
         bool valid = r < I;
-        // round 1: the record (keys and both crossing parameters)
+        // load 1: the record (keys and both crossing parameters)
         unsigned long long inter = 0, outer = 0;
         float tRec = 0.f, uRec = 0.f;
         if (valid) {
@@ -1681,7 +1681,7 @@ k_overlap_force(const double2* __restrict__ pos, const int* __restrict__ start,
             tRec = ws.recTU[r].y; uRec = ws.recUT[r].y;
         }
         valid = valid && inter != outer;
-        // round 2: both polygons' vertex ranges.  The topology is the CSR
+        // load 2: both polygons' vertex ranges.  The topology is the CSR
         // one (next = the following vertex of the polygon, cyclic), so every
         // vertex index below is formed without reading `next`.
         int start1 = 0, n1 = 0, iLoc = 0, lLoc = 0, lDist = 0;
@@ -1722,7 +1722,7 @@ k_overlap_force(const double2* __restrict__ pos, const int* __restrict__ start,
                 else { v2 = l; v3 = nx1(lLoc); }
             }
         }
-        // round 3: the vertices.  The crossing points: the even lane of the
+        // load 3: the vertices.  The crossing points: the even lane of the
         // pair takes f_ij on edge (i, zi), the odd one f_kl on edge (k, zk),
         // and they swap them.
         double2 pa = make_double2(0.0, 0.0), pza = pa, ra = pa, fa = pa, q2 = pa, d3 = pa;
