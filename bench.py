@@ -198,11 +198,12 @@ def make_workload(seed):
     return make_system(N_POLY, N_VERT, PHI, seed=seed)
 
 
-def candidate_pairs(positions, start):
+def candidate_pairs(positions, start, pairs_out=None):
     """Pair evaluations of one contact search, counted with the broad phase's
     rules: (narrow, circle), where circle counts the pairs a < b whose
     bounding circles meet and narrow the subset whose boxes, padded by the
-    crossing margin, also meet (the pairs the narrow phase tests)."""
+    crossing margin, also meet (the pairs the narrow phase tests).  A list
+    given as pairs_out receives the narrow pairs (a, b)."""
     xy = positions.reshape(-1, 2)
     P = len(start) - 1
     cx, cy, R, L = np.zeros(P), np.zeros(P), np.zeros(P), np.zeros(P)
@@ -219,16 +220,25 @@ def candidate_pairs(positions, start):
         L[p] = np.sqrt((e * e).sum(axis=1)).max()
     circle = narrow = 0
     for p in range(P - 1):
-        dx = (cx[p + 1:] - cx[p] + 0.5) % 1.0 - 0.5
-        dy = (cy[p + 1:] - cy[p] + 0.5) % 1.0 - 0.5
-        rr = R[p] + R[p + 1:] + 1e-5
-        near = dx * dx + dy * dy <= rr * rr
-        m = 2.0 * (4e-6 + 1e-3 * L[p] * L[p + 1:]) + 2e-6
-        box = (np.abs(dx) <= 0.5 * (bw[p] + bw[p + 1:]) + m) & \
-              (np.abs(dy) <= 0.5 * (bh[p] + bh[p + 1:]) + m)
+        near, both = _pair_masks(p, cx, cy, R, L, bw, bh)
         circle += int(np.count_nonzero(near))
-        narrow += int(np.count_nonzero(near & box))
+        narrow += int(np.count_nonzero(both))
+        if pairs_out is not None:
+            pairs_out.extend((p, p + 1 + int(q)) for q in np.flatnonzero(both))
     return narrow, circle
+
+
+def _pair_masks(p, cx, cy, R, L, bw, bh):
+    """Polygons q > p whose bounding circles meet p's (near), and the subset
+    whose boxes, padded by the crossing margin, meet too (both)."""
+    dx = (cx[p + 1:] - cx[p] + 0.5) % 1.0 - 0.5
+    dy = (cy[p + 1:] - cy[p] + 0.5) % 1.0 - 0.5
+    rr = R[p] + R[p + 1:] + 1e-5
+    near = dx * dx + dy * dy <= rr * rr
+    m = 2.0 * (4e-6 + 1e-3 * L[p] * L[p + 1:]) + 2e-6
+    box = (np.abs(dx) <= 0.5 * (bw[p] + bw[p + 1:]) + m) & \
+          (np.abs(dy) <= 0.5 * (bh[p] + bh[p + 1:]) + m)
+    return near, near & box
 
 
 def prepare_gpu(seed):
