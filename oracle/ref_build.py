@@ -9,7 +9,7 @@ come from the reference's own kernels, rebuilt for sm_103a and run on a GPU.
           named by PCP_REFERENCE into oracle/_ref/src/, and its unchanged
           Python layer (pyCudaPolygon/*.py with polygonMixins/) into
           oracle/_ref/py/pyCudaPolygon/, which the drop-in test imports on
-          top of this build's module.  oracle/_ref/ is git-ignored: the
+          top of this repository's module.  oracle/_ref/ is git-ignored: the
           copies are inputs for the GPU machine, which has no reference
           checkout, and are never committed.
   build   compile oracle/_ref/src with the shims in oracle/ref_shim/ (CUDA 13

@@ -1,9 +1,9 @@
 """Learned FIRE warm start: a message-passing network over the contact graph.
 
-The reference has no counterpart: this is the benchmark spec's learned warm
-start.  A system compressed to a higher packing fraction is minimised by
-plain FIRE from a starting point the network proposes (per-vertex
-displacements), instead of from the compressed state itself.  FIRE with the
+The reference has no counterpart.  A system compressed to a higher packing
+fraction is minimised by plain FIRE from a starting point the network
+proposes (per-vertex displacements), instead of from the compressed state
+itself.  FIRE with the
 reference's rules still runs to the same stop, so the network can only move
 the starting point; the result is always FIRE's.
 

@@ -1,5 +1,5 @@
 """The reference's own, unchanged Python layer (pyCudaPolygon/pyCudaPolygon.py,
-its mixins, enums.py, pyCudaPolygonLink.py) on top of this build's
+its mixins, enums.py, pyCudaPolygonLink.py) on top of this repository's
 libpyCudaPolygon module.
 
 The reference's checkout is needed (PCP_REFERENCE names its root); without

@@ -1,5 +1,5 @@
 """The reference's own, unchanged Python layer (pyCudaPolygon/pyCudaPolygon.py,
-its mixins, enums.py, pyCudaPolygonLink.py) driving this build's
+its mixins, enums.py, pyCudaPolygonLink.py) driving this repository's
 libpyCudaPolygon module on the GPU.
 
 `python oracle/ref_build.py stage` (PCP_REFERENCE naming a reference
@@ -80,7 +80,7 @@ def _stand_ins():
 def _reference_package():
     _stand_ins()
     pg.build()
-    lib = pg.load_module()                 # this build's module, first on sys.path
+    lib = pg.load_module()                 # this repository's module, first on sys.path
     if PKG not in sys.path:
         sys.path.insert(1, PKG)
     for name in ("pyCudaPolygon", "enums", "pyCudaPolygonLink", "polygonMixins"):
