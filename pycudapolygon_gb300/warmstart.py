@@ -3,9 +3,8 @@
 The reference has no counterpart.  A system compressed to a higher packing
 fraction is minimised by plain FIRE from a starting point the network
 proposes (per-vertex displacements), instead of from the compressed state
-itself.  FIRE with the
-reference's rules still runs to the same stop, so the network can only move
-the starting point; the result is always FIRE's.
+itself.  FIRE with the reference's rules still runs to the same stop, so
+the network can only move the starting point; the result is always FIRE's.
 
 Graph: one node per polygon vertex; edges join each vertex to its two ring
 neighbours and the end vertices of every pair of crossing edges (the contact
