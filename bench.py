@@ -713,8 +713,8 @@ def run_reference(args, ws, rank):
 
 def run_stages(args):
     """Each stage of one overlap evaluation, constraint projection and SHAKE
-    run once per round through the Model API (no graph, no gates), so that a
-    profiler captures exactly one launch of every kernel per round."""
+    run once per pass through the Model API (no graph, no gates), so that a
+    profiler captures exactly one launch of every kernel per pass."""
     import torch
     lib, m, s = prepare_gpu(args.seed)
     for _ in range(args.stages):
