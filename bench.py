@@ -318,6 +318,8 @@ def run_gpu(args, ws, rank, local):
     }
     if rank == 0 and not args.no_roofline:
         result["roofline"], result["fp64"] = roofline(m, s, torch, flush, args)
+    if rank == 0 and reference_kernels_record() is not None:
+        result["reference_kernels_gb300"] = reference_kernels_record()
     if rank == 0 and not args.no_e2e:
         result["e2e"] = e2e(args, s)
     if rank == 0 and not args.no_cpu:
@@ -392,6 +394,23 @@ def roofline(m, s, torch, flush, args):
         except (OSError, ValueError):
             fp64 = None
     return roof, fp64
+
+
+def reference_kernels_record():
+    """The reference's own kernels, rebuilt for sm_103a, against this
+    repository's on one evaluation of a 4096 x 32 system on a GB300: the
+    committed result of oracle/ref_time.py (this benchmark does not run the
+    reference's code)."""
+    path = os.path.join(ROOT, "profiles", "reference_kernels_4096x32.json")
+    try:
+        d = json.load(open(path))
+        return {"source": "profiles/reference_kernels_4096x32.json (oracle/ref_time.py)",
+                "workload": d["workload"], "timing": d["timing"],
+                "evaluation_ms": d["evaluation_ms"], "speedup": d["speedup"],
+                "stage_ms": {"reference": d["reference_kernels_sm103a"]["stage_ms"],
+                             "this_repository": d["this_repository"]["stage_ms"]}}
+    except (OSError, ValueError, KeyError, TypeError):
+        return None
 
 
 def e2e(args, s):

@@ -20,6 +20,17 @@
 //        4 grid overlap estimate, 8 softBody energy/force, 16 hybrid.
 // Output: records {int32 name length, name, int32 type (0 f64, 1 i32, 2 u64,
 //         3 u8), int64 count, raw data}.
+//
+// Timing mode, `ref_golden --time <input.bin> <reps> <output.json>`: after
+// one warm-up evaluation, <reps> evaluations of the same path (geometry,
+// cells, neighbours, outersections, and with flag 1 the overlap force, with
+// flag 2 the projection), each method timed on the host around the call and
+// a device synchronisation; the mean milliseconds per stage go to a JSON
+// object.  The reference's methods allocate, copy and synchronise inside,
+// so the host clock is the honest one for them.
+#include <cuda_runtime.h>
+
+#include <chrono>
 #include <cstdint>
 #include <cstdio>
 #include <cstdlib>
@@ -64,15 +75,55 @@ void read_into(FILE* f, T* dst, size_t n) {
     }
 }
 
+int time_stages(Model& m, int reps, int flags, const char* path) {
+    static const char* kNames[6] = {"updatePolygonGeometry", "updateNeighborCells",
+                                    "updateNeighbors", "updateOutersections",
+                                    "updateForceEnergy", "projectForce"};
+    const int stages = (flags & 1) ? ((flags & 2) ? 6 : 5) : 4;
+    auto run = [&m](int s) {
+        switch (s) {
+            case 0: m.updatePolygonGeometry(); break;
+            case 1: m.updateNeighborCells(); break;
+            case 2: m.updateNeighbors(); break;
+            case 3: m.updateOutersections(); break;
+            case 4: m.updateForceEnergy(); break;
+            default: m.projectForce(); break;
+        }
+    };
+    for (int s = 0; s < stages; ++s) run(s);
+    if (cudaDeviceSynchronize() != cudaSuccess) return 3;
+    double total[6] = {0, 0, 0, 0, 0, 0};
+    for (int r = 0; r < reps; ++r) {
+        for (int s = 0; s < stages; ++s) {
+            auto t0 = std::chrono::steady_clock::now();
+            run(s);
+            if (cudaDeviceSynchronize() != cudaSuccess) return 3;
+            total[s] += std::chrono::duration<double>(std::chrono::steady_clock::now() - t0).count();
+        }
+    }
+    FILE* f = std::fopen(path, "w");
+    if (!f) { std::perror(path); return 2; }
+    std::fprintf(f, "{\"reps\": %d, \"records\": %d, \"energy\": %.17g, \"stage_ms\": {",
+                 reps, m.getNumIntersections(), (flags & 1) ? m.getEnergy() : 0.0);
+    for (int s = 0; s < stages; ++s)
+        std::fprintf(f, "%s\"%s\": %.6f", s ? ", " : "", kNames[s], 1e3 * total[s] / reps);
+    std::fprintf(f, "}}\n");
+    std::fclose(f);
+    return 0;
+}
+
 }  // namespace
 
 int main(int argc, char** argv) {
-    if (argc != 3) {
-        std::fprintf(stderr, "usage: ref_golden <input.bin> <output.bin>\n");
+    const bool timing = argc == 5 && std::string(argv[1]) == "--time";
+    if (argc != 3 && !timing) {
+        std::fprintf(stderr, "usage: ref_golden <input.bin> <output.bin>\n"
+                             "       ref_golden --time <input.bin> <reps> <output.json>\n");
         return 2;
     }
-    FILE* in = std::fopen(argv[1], "rb");
-    if (!in) { std::perror(argv[1]); return 2; }
+    const char* inPath = timing ? argv[2] : argv[1];
+    FILE* in = std::fopen(inPath, "rb");
+    if (!in) { std::perror(inPath); return 2; }
     int32_t hdr[6];
     read_into(in, hdr, 6);
     if (hdr[0] != 0x47504350 || hdr[1] != 1) {
@@ -93,9 +144,6 @@ int main(int argc, char** argv) {
         std::fprintf(stderr, "ref_golden: inconsistent sizes\n");
         return 2;
     }
-    g_out = std::fopen(argv[2], "wb");
-    if (!g_out) { std::perror(argv[2]); return 2; }
-
     Model m(V);
     // The constructor leaves the model type unset (model.cpp:99 passes the
     // member's own indeterminate value); the Python model sets it right after
@@ -110,6 +158,13 @@ int main(int argc, char** argv) {
     // it, pyCudaPolygon.py:54-57, and would leave a 2x2 grid).
     m.setMaxEdgeLength(scal[0]);
     m.initializeNeighborCells();
+    if (timing) {
+        const int reps = std::atoi(argv[3]);
+        if (reps < 1) { std::fprintf(stderr, "ref_golden: reps must be positive\n"); return 2; }
+        return time_stages(m, reps, flags, argv[4]);
+    }
+    g_out = std::fopen(argv[2], "wb");
+    if (!g_out) { std::perror(argv[2]); return 2; }
 
     m.updatePolygonGeometry();
     emit("areas", m.getAreas());
