@@ -100,3 +100,13 @@ def test_stateless_launchers_check_arguments_first(built):
     assert lib.pcp_shake_project(None, fake, 3, fake, fake, 5, d(1e-15), fake, None) == 1
     assert lib.pcp_update_positions(fake, None, 10, d(1e-3), None) == 1
     assert lib.pcp_update_positions(fake, fake, -1, d(1e-3), None) == 1
+
+
+def test_integration_notes_list_every_extra_method(built, golden_dir):
+    """Every method the module adds to the reference's table is named in
+    INTEGRATION.md's list of deliberate differences."""
+    mod = pg.load_module()
+    ref = set(json.load(open(os.path.join(golden_dir, "pybind_methods.json")))["methods"])
+    extra = sorted(n for n in dir(mod.Model) if not n.startswith("_") and n not in ref)
+    doc = open(os.path.join(os.path.dirname(golden_dir), "..", "INTEGRATION.md")).read()
+    assert [n for n in extra if n not in doc] == []
