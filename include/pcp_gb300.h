@@ -26,6 +26,11 @@
  *     replaces an `extern "C"` wrapper of src/model.cu that the reference's
  *     C++ host code declares at src/model.cpp:17-56.
  *
+ * One device per process: the library serves the device that is current
+ * when it is first used (its SM count sizes the grids, and kernel launch
+ * attributes are set once), as one process per GPU does; pcp_shake_project_
+ * noalloc's first call on a device looks up that device's static workspace.
+ *
  * Data layout (identical to the reference): positions and forces are
  * interleaved FP64 [x0, y0, x1, y1, ...] in the unit periodic box; polygon p
  * owns vertices [startIndices[p], startIndices[p+1]) in counter-clockwise
