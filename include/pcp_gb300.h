@@ -28,8 +28,7 @@
  *
  * One device per process: the library serves the device that is current
  * when it is first used (its SM count sizes the grids, and kernel launch
- * attributes are set once), as one process per GPU does; pcp_shake_project_
- * noalloc's first call on a device looks up that device's static workspace.
+ * attributes are set once), as one process per GPU does.
  *
  * Data layout (identical to the reference): positions and forces are
  * interleaved FP64 [x0, y0, x1, y1, ...] in the unit periodic box; polygon p
