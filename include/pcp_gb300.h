@@ -226,7 +226,8 @@ int pcp_model_set_positions_device(pcp_model* m, const double* d_pos, int len);
 int pcp_model_overlap_energy_gradient(pcp_model* m, int mode, int search, double* energy_out,
                                       double* d_out);
 
-/* ---- getters (model.cpp:654-893); arrays are copied into caller memory ---- */
+/* ---- getters (model.cpp:654-893; bound among pybindWrapper.cpp:35-104);
+ * arrays are copied into caller memory ---- */
 int pcp_model_get_num_vertices(pcp_model* m, int* out);
 int pcp_model_get_num_polygons(pcp_model* m, int* out);
 int pcp_model_get_num_intersections(pcp_model* m, int* out);
@@ -271,18 +272,19 @@ int pcp_model_get_ut(pcp_model* m, double* out, int cap, int* len_out);
 int pcp_model_get_keys(pcp_model* m, uint32_t* out, int cap, int* len_out);
 int pcp_model_get_intersections_counter(pcp_model* m, int* out, int cap, int* len_out);
 
-/* Device views of the model's state (valid until the next resize); for
- * zero-copy use from CUDA-aware callers.  Interleaved FP64 [2*numVertices]. */
+/* No reference counterpart: device views of the model's state (valid until
+ * the next resize); for zero-copy use from CUDA-aware callers.  Interleaved FP64 [2*numVertices]. */
 int pcp_model_device_positions(pcp_model* m, double** out);
 int pcp_model_device_forces(pcp_model* m, double** out);
-/* Pair evaluations since creation: polygon pairs a < b with overlapping
- * bounding circles taken through the contact search. */
+/* No reference counterpart: pair evaluations since creation, polygon pairs
+ * a < b with overlapping bounding circles taken through the contact search. */
 int pcp_model_get_pair_count(pcp_model* m, long long* out);
 /* No reference counterpart: pairs a < b handed to the narrow phase since
  * creation (bounding circles meet and boxes within the crossing margin meet;
  * self pairs not counted) -- the pair evaluations a benchmark counts. */
 int pcp_model_get_narrow_pair_total(pcp_model* m, long long* out);
-/* Pairs the last contact search handed to the narrow phase: polygon pairs
+/* No reference counterpart: pairs the last contact search handed to the
+ * narrow phase, polygon pairs
  * a < b whose bounding boxes are within the crossing margin, and self pairs
  * (polygons not certified simple). */
 int pcp_model_get_narrow_pair_count(pcp_model* m, int* pairs_out, int* self_out);
